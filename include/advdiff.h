@@ -1,0 +1,171 @@
+/*
+ * advdiff.h -- native C ABI of the GB300 (sm_103a) advection-diffusion library.
+ *
+ * Plain C types only: raw device pointers, sizes, a cudaStream_t passed as void*. Buffers are
+ * dense, x fastest, then y, then z: node (i,j,k) lives at i + nx*j + nx*ny*k, the layout of the
+ * reference (SingleGPU/Diffusion3d_baselineCode/kernels.cu:113, SingleGPU/Burgers3d_WENO5/
+ * kernels.cu:305). The caller owns every state buffer; the library allocates only what a plan
+ * or run needs for itself (graphs, tensor maps, device scalars) and frees it on destroy.
+ * Every entry point returns an adv_status and never exits the process
+ * (the reference's wrappers return void and its drivers exit on CUDA errors,
+ * SingleGPU/Burgers3d_WENO5/main.cpp:13-24).
+ *
+ * Reference interfaces this ABI replaces:
+ *   adv_heat_stage / adv_heat_run   <- Call_Lu3d + Call_RK3d (SingleGPU/Diffusion3d_baselineCode/
+ *                                      acoustics3d.h:57-59), Call_Lu2d + Call_RK2d
+ *                                      (SingleGPU/Diffusion2d/diffusion2d.h:57-59), fused into one
+ *                                      launch per stage; the host loop of main.cpp:106-122.
+ *   adv_burgers_stage / _run        <- Call_Adv_x/y/z + Call_Diff_ + Call_sspRK
+ *                                      (SingleGPU/Burgers3d_WENO5/Burgers.h:72-82), fused into one
+ *                                      launch per SSP-RK3 stage; the host loop of main.cpp:127-150.
+ *   adv_ic_* / adv_write_result_bin <- Call_Init3D / Call_Init3d / SaveBinary3D
+ *                                      (SingleGPU/Diffusion3d_baselineCode/tools.cpp:59-143,
+ *                                      SingleGPU/Burgers3d_WENO5/tools.cpp:241-322).
+ * The reference's own extern "C" names are exported by the compatibility libraries declared
+ * in advdiff_compat_heat2d.h, advdiff_compat_heat3d.h and advdiff_compat_burgers3d.h.
+ */
+#ifndef ADVDIFF_H
+#define ADVDIFF_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ADV_ABI_VERSION 1
+
+typedef enum adv_status {
+  ADV_OK = 0,
+  ADV_ERR_INVALID_ARG = 1, /* bad descriptor, size, pointer alignment or enum */
+  ADV_ERR_CUDA = 2,        /* a CUDA runtime/driver call failed; see adv_last_error_string() */
+  ADV_ERR_TIMEOUT = 3,     /* a bounded device-side wait gave up (status word) */
+  ADV_ERR_NONFINITE = 4,   /* a NaN/Inf was seen in the state (max|u| reduction) */
+  ADV_ERR_CFL = 5,         /* dt rule produced a non-positive or non-finite step */
+  ADV_ERR_UNSUPPORTED = 6, /* valid request this build does not implement */
+  ADV_ERR_ALLOC = 7        /* host or device allocation failed */
+} adv_status;
+
+typedef enum adv_dtype { ADV_F32 = 0, ADV_F64 = 1 } adv_dtype;
+typedef enum adv_time { ADV_EULER = 0, ADV_SSPRK3 = 1 } adv_time;
+typedef enum adv_weno { ADV_WENO5_JS = 0, ADV_WENO5_Z = 1 } adv_weno;
+typedef enum adv_lf { ADV_LF_LOCAL = 0, ADV_LF_GLOBAL = 1 } adv_lf;
+typedef enum adv_bc { ADV_BC_FROZEN = 0, ADV_BC_PERIODIC = 1 } adv_bc;
+/* Precision of the WENO weight divisions when the state is FP32. */
+typedef enum adv_div { ADV_DIV_F32 = 0, ADV_DIV_F64 = 1 } adv_div;
+/* Burgers time-step rule. FIXED: dt = min(CFL*dx/1, 0.9/(2C sum 1/h^2)) as the reference driver
+ * (SingleGPU/Burgers3d_WENO5/main.cpp:130-133); MAXU: dt = CFL*dx/max|u^n| computed on the
+ * device each step (Matlab_Prototipes/InviscidBurgersNd/LFWENO5FDM3d.m:71). Both trim the last
+ * step to land on tEnd and accumulate t in FP64. */
+typedef enum adv_dt_rule { ADV_DT_FIXED = 0, ADV_DT_MAXU = 1 } adv_dt_rule;
+
+/* ---------------------------------------------------------------------------- heat
+ * One fused stage computes u_out = combine(u_n, u_in + dt * L(u_in)) on the updated nodes,
+ * with L = kx*Sx + ky*Sy (+ kz*Sz) and per axis
+ *   order 2: S = u[+1] - 2u + u[-1]                  (kernels.cu:37-64, the O2 7-pt kernel)
+ *   order 4: S = -u[+2] + 16u[+1] - 30u + 16u[-1] - u[-2]  (kernels.cu:66-99, the 13-pt kernel)
+ * The reference sets k = C/(12 h^2) for order 4 (main.cpp:62-64); order 2 takes k = C/h^2.
+ * stage 1 (= forward Euler): u_n + dt L; stage 2: 3/4 u_n + 1/4 (u_in + dt L);
+ * stage 3: (u_n + 2 (u_in + dt L)) / 3 (kernels.cu:104-142).
+ * Nodes closer than `frozen` layers to any face are not updated: they are copied from u_in, or
+ * written as 0 on the outermost layer when zero_boundary is set (Dirichlet u = 0).
+ * The reference freezes 2 layers in 3D (kernels.cu:127) and 3 in 2D (Diffusion2d/kernels.cu:53).
+ */
+typedef struct adv_heat_desc {
+  int32_t ndim;          /* 2 or 3 */
+  int32_t nx, ny, nz;    /* nodes per axis; nz = 1 when ndim == 2 */
+  int32_t dtype;         /* adv_dtype */
+  int32_t order;         /* 2 or 4 */
+  int32_t frozen;        /* >= order/2 */
+  int32_t zero_boundary; /* 0 or 1 */
+  double kx, ky, kz;     /* per-axis coefficients (kz ignored in 2D) */
+  double dt;
+} adv_heat_desc;
+
+/* u_in and u_out must not alias; u_n may alias u_out (it is read at the written node only). */
+adv_status adv_heat_stage(const adv_heat_desc* d, int stage, const void* u_in, const void* u_n,
+                          void* u_out, void* stream);
+/* Bytes of caller-provided workspace adv_heat_run needs: one state array for Euler, two for
+ * SSP-RK3. */
+adv_status adv_heat_workspace_bytes(const adv_heat_desc* d, int time_scheme, size_t* bytes);
+/* nsteps time steps of the chosen scheme; the result is left in u. */
+adv_status adv_heat_run(const adv_heat_desc* d, int time_scheme, int64_t nsteps, void* u,
+                        void* workspace, void* stream);
+
+/* --------------------------------------------------------------------------- Burgers
+ * u_t + (u^2/2)_x + (u^2/2)_y + (u^2/2)_z = nu * Lap(u). One fused launch per SSP-RK3 stage:
+ * Lax-Friedrichs split f+- = (u^2/2 +- a u)/2 with a = |u| per node (local, the reference's
+ * kernels.cu:224-238) or a = max|u_in| (global); WENO5-JS (kernels.cu:92-140) or WENO5-Z
+ * (kernels.cu:142-192) face fluxes along x, y, z; RHS L = -(dF)/dx - (dG)/dy - (dH)/dz
+ * (+ the O4 viscous term with coefficients kx,ky,kz when nonzero, kernels.cu:444-494);
+ * stage update as for heat. BC FROZEN leaves the outer 3 layers untouched (kernels.cu:518);
+ * PERIODIC wraps every neighbour index. The same launch also reduces max|u_out| for the next
+ * stage's Lax-Friedrichs constant and time step.
+ */
+typedef struct adv_burgers_desc {
+  int32_t nx, ny, nz;
+  int32_t dtype;  /* adv_dtype: state and flux precision */
+  int32_t weno;   /* adv_weno */
+  int32_t lf;     /* adv_lf */
+  int32_t bc;     /* adv_bc */
+  int32_t div;    /* adv_div (FP32 state only) */
+  int32_t bug_b2; /* 1: add the viscous term twice on slabs 16..18 as the reference does */
+  int32_t pad0;
+  double dx, dy, dz;
+  double kx, ky, kz; /* viscous O4 coefficients C/(12 h^2); all 0 = inviscid */
+} adv_burgers_desc;
+
+/* One stage. alpha is the global Lax-Friedrichs constant (ignored for local LF).
+ * maxabs_out, if non-NULL, is a device float (FP32 state) or double (FP64 state) that receives
+ * max(|u_out|) via atomicMax; the caller zeroes it first. */
+adv_status adv_burgers_stage(const adv_burgers_desc* d, int stage, const void* u_in,
+                             const void* u_n, void* u_out, double dt, double alpha,
+                             void* maxabs_out, void* stream);
+adv_status adv_burgers_workspace_bytes(const adv_burgers_desc* d, size_t* bytes);
+/* Full time loop to tEnd (at most max_steps steps). dt and the global-LF constant are computed
+ * on the device; the loop runs as one CUDA graph (a while-conditional node when the driver
+ * supports it, else fixed-size predicated chunks). C is the viscous coefficient used only by
+ * ADV_DT_FIXED's diffusive bound (0 drops it). t_out / steps_out may be NULL. */
+adv_status adv_burgers_run(const adv_burgers_desc* d, void* u, void* workspace, double tEnd,
+                           double cfl, int dt_rule, double C, int64_t max_steps, double* t_out,
+                           int64_t* steps_out, void* stream);
+
+/* ------------------------------------------------------------------ reductions
+ * max|u| over n values into *out (host double). Synchronises the stream. */
+adv_status adv_max_abs(int dtype, const void* u, int64_t n, double* out, void* stream);
+
+/* ----------------------------------------------------------- initial conditions (host)
+ * Seeded inputs use Philox4x32-10 (counter-based) so every consumer regenerates them exactly. */
+/* Reference heat IC 3 (tools.cpp:128-139): exp(-|x-5|^2/(4*0.1)) at nodes (i dx, j dy, k dz),
+ * faces zeroed; ndim 2 or 3. */
+adv_status adv_ic_heat_ref(int ndim, int nx, int ny, int nz, double dx, double dy, double dz,
+                           double* u);
+/* 2D: Gaussian bump exp(-((x-.5)^2+(y-.5)^2)/0.01) + N(0, sigma^2) noise on [0,1]^2, edges 0. */
+adv_status adv_ic_heat2d_gauss_noise(int nx, int ny, uint32_t seed, double sigma, double* u);
+/* 3D: sum of nblobs Gaussians, centres U[0.2,0.8]^3, widths U[0.02,0.08], on [0,1]^3, faces 0. */
+adv_status adv_ic_heat3d_blobs(int nx, int ny, int nz, uint32_t seed, int nblobs, double* u);
+/* Burgers: 0.5 + sum of nmodes a cos(pi n.x + phi), |n| <= 4, a ~ U[0,amax], on the periodic
+ * cell centres of [0,L)^3. */
+adv_status adv_ic_burgers_fourier(int nx, int ny, int nz, double L, uint32_t seed, int nmodes,
+                                  double amax, double* u);
+/* Reference Burgers IC 3 (tools.cpp:126-137): exp(-|x-1|^2/0.1) at (i dx, j dy, k dz). */
+adv_status adv_ic_burgers_ref(int nx, int ny, int nz, double dx, double dy, double dz, double* u);
+
+/* ---------------------------------------------------------------------- output (host)
+ * result.bin as the reference writes it: float32, x fastest, no header
+ * (SingleGPU/Diffusion3d_baselineCode/tools.cpp:59-87). */
+adv_status adv_write_result_bin(const char* path, int dtype, const void* host_u, int64_t n);
+
+/* ------------------------------------------------------------------------- misc */
+const char* adv_last_error_string(void);
+const char* adv_status_string(adv_status s);
+int adv_abi_version(void);
+/* Kernels this library launched since load (for launch-count accounting). */
+int64_t adv_kernel_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ADVDIFF_H */

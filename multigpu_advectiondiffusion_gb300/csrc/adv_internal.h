@@ -1,0 +1,100 @@
+// adv_internal.h -- declarations shared by the library's translation units (not installed).
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+
+#include "../../include/advdiff.h"
+
+namespace adv {
+
+// Records a message for adv_last_error_string() and returns `s`.
+adv_status set_error(adv_status s, const std::string& msg);
+adv_status cuda_error(cudaError_t e, const char* what);
+void count_launches(int64_t n);
+
+#define ADV_CUDA_TRY(call)                                    \
+  do {                                                        \
+    cudaError_t e_ = (call);                                  \
+    if (e_ != cudaSuccess) return ::adv::cuda_error(e_, #call); \
+  } while (0)
+
+// Device properties used for launch sizing, cached per device.
+struct DeviceInfo {
+  int device = -1;
+  int sms = 0;
+  int cc_major = 0, cc_minor = 0;
+  size_t smem_optin = 0;
+};
+adv_status device_info(DeviceInfo* out);
+
+// cuTensorMapEncodeTiled resolved through the runtime (no -lcuda link needed).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled_fn();
+
+// Device status word (per device): 0 = OK, else an adv_status raised by a kernel.
+adv_status read_and_clear_device_status(cudaStream_t s);
+int* device_status_ptr();
+
+// ------------------------------------------------------------------ heat launchers
+struct HeatLaunch {
+  // resolved per plan: whether the TMA path applies and the chosen z-chunk
+  bool tma = false;
+  int zchunk = 0;
+  dim3 grid, block;
+  size_t smem = 0;
+  CUtensorMap tmap_in;  // tensor map of u_in (re-encoded when the pointer changes)
+};
+adv_status heat_prepare(const adv_heat_desc& d, const void* u_in, HeatLaunch* L);
+adv_status heat_launch(const adv_heat_desc& d, const HeatLaunch& L, int stage, const void* u_in,
+                       const void* u_n, void* u_out, cudaStream_t s);
+adv_status heat_validate(const adv_heat_desc* d);
+
+// --------------------------------------------------------------- Burgers launchers
+struct BurgersLaunch {
+  bool tma = false;
+  int zchunk = 0;
+  dim3 grid, block;
+  size_t smem = 0;
+  CUtensorMap tmap_in;
+};
+adv_status burgers_validate(const adv_burgers_desc* d);
+adv_status burgers_prepare(const adv_burgers_desc& d, const void* u_in, BurgersLaunch* L);
+// Stage launch arguments. The Lax-Friedrichs constant and dt come from the host values unless
+// a device source is given (used by the graph-resident time loop).
+struct BurgersStageArgs {
+  int stage;
+  const void* u_in;
+  const void* u_n;
+  void* u_out;
+  double dt_host;
+  double alpha_host;
+  const double* dt_dev;     // nullable: dt as FP64
+  const double* alpha_dev;  // nullable: LF constant as FP64
+  const void* alpha_key;    // nullable: max|u| key of the previous stage (FP32/FP64 bits)
+  void* maxabs_key;         // nullable: accumulator key for max|u_out|
+  const int* active;        // nullable: kernel returns at once when *active == 0
+};
+adv_status burgers_launch(const adv_burgers_desc& d, const BurgersLaunch& L,
+                          const BurgersStageArgs& a, cudaStream_t s);
+
+// Loop-control state for adv_burgers_run (device resident; see api_device.cu).
+struct BurgersLoopState {
+  double t, tEnd, cfl, dx, dt_fixed, dt, alpha0;
+  int64_t step, max_steps;
+  int dt_rule, active;
+  unsigned maxbits[3];              // rotating FP32 max|u| accumulators (stage s writes s % 3)
+  unsigned long long maxbits64[3];  // the same for FP64 state
+};
+adv_status burgers_loop_begin_step(BurgersLoopState* st, int dtype, unsigned long long cond_handle,
+                                   int use_cond, cudaStream_t s);
+adv_status max_abs_launch(int dtype, const void* u, int64_t n, void* accum_bits, cudaStream_t s);
+
+}  // namespace adv

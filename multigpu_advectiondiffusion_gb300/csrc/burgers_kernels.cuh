@@ -1,0 +1,342 @@
+// burgers_kernels.cuh -- fused WENO5 / WENO5-Z Burgers SSP-RK3 stage for sm_103a.
+//
+// One launch per stage replaces the reference's five (Compute_dF, Compute_dG, Compute_dH,
+// Compute_Laplace_Async, Compute_RK: SingleGPU/Burgers3d_WENO5/kernels.cu:197-530, driven by
+// main.cpp:143-149) and its per-step device copy.
+//
+// Work layout: a CTA owns a 32 x 16 tile of x-y columns (256 threads, two rows per thread) and
+// marches through a chunk of z planes. Each plane of the tile plus a 3-cell halo is staged in a
+// 6-slot shared-memory ring by TMA (x start rounded down to a 16-byte boundary; periodic tiles
+// at a domain edge patch their wrapped halo after the copy lands). For the output plane k:
+//   * f+- of the staged plane go to shared memory once (Lax-Friedrichs split);
+//   * the 33x16 x-faces and 32x17 y-faces are reconstructed by all threads in a flat loop;
+//   * each thread's z-faces come from per-column register windows of f+- sliding along z;
+//   * L = -(dF/dx + dG/dy + dH/dz) (+ viscous O4 term), the SSP-RK3 combine, the store and a
+//     warp-shuffle max|u_out| reduction (one atomicMax per warp) for the next stage's
+//     Lax-Friedrichs constant and time step all happen in the same pass.
+// Every node is read from HBM once per stage and written once.
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include "adv_device.cuh"
+#include "adv_math.cuh"
+#include "weno.cuh"
+
+namespace adv {
+
+template <class T>
+struct BurgersParams {
+  const T* uin;
+  const T* un;
+  T* out;
+  int nx, ny, nz;
+  int stage;
+  int periodic;  // 1: periodic wrap; 0: the reference's frozen outer 3 layers
+  int bug_b2;
+  int zchunk;
+  int tma;
+  int un_is_uin;
+  int lf_global;
+  double dx, dy, dz;
+  T kx, ky, kz;
+  double dt_host, alpha_host;
+  const double* dt_dev;
+  const double* alpha_dev;
+  const void* alpha_key;
+  void* maxabs_key;
+  const int* active;
+  int* status;
+};
+
+struct BurgersTile {
+  static constexpr int BX = 32, BY = 16, NT = 256;
+  static constexpr int R = 3;
+  static constexpr int PADX = 4;  // shared column 0 holds x0 - 4 (16-byte aligned for FP32 and FP64)
+  static constexpr int SW = BX + 2 * PADX;  // 40
+  static constexpr int SH = BY + 2 * R;     // 22
+  static constexpr int PLANE = SW * SH;     // 880
+  static constexpr int NS = 6;              // ring: planes k .. k+5 (k+3 consumed, 2 prefetched)
+  static constexpr int P = 2;
+  static constexpr int NXF = (BX + 1) * BY;  // x-faces
+  static constexpr int NYF = BX * (BY + 1);  // y-faces
+};
+
+template <class T>
+struct BurgersSmem {
+  static constexpr int SLOT_ELEMS = ((BurgersTile::PLANE * (int)sizeof(T) + 127) / 128 * 128) / (int)sizeof(T);
+  static constexpr size_t RING = (size_t)BurgersTile::NS * SLOT_ELEMS * sizeof(T);
+  static constexpr size_t FPM = (size_t)BurgersTile::PLANE * sizeof(T);
+  static constexpr size_t FACES = (size_t)(BurgersTile::NXF + BurgersTile::NYF) * sizeof(T);
+  static constexpr size_t TOTAL = RING + 2 * FPM + FACES;
+};
+
+template <class T> __device__ __forceinline__ T absval(T v) { return fabs(v); }
+template <> __device__ __forceinline__ float absval<float>(float v) { return fabsf(v); }
+
+__device__ __forceinline__ int wrapi(int i, int n) {
+  i %= n;
+  return i < 0 ? i + n : i;
+}
+
+// Face reconstruction for state type T: FP32 takes the fast form with divisions in D,
+// FP64 the reference literal form.
+template <class T, bool Z, class D>
+struct Face;
+template <bool Z, class D>
+struct Face<float, Z, D> {
+  __device__ __forceinline__ static float f(float p0, float p1, float p2, float p3, float p4, float m0, float m1,
+                                            float m2, float m3, float m4) {
+    return weno_face_fast<Z, D>(p0, p1, p2, p3, p4, m0, m1, m2, m3, m4);
+  }
+};
+template <bool Z, class D>
+struct Face<double, Z, D> {
+  __device__ __forceinline__ static double f(double p0, double p1, double p2, double p3, double p4, double m0,
+                                             double m1, double m2, double m3, double m4) {
+    return weno_face_ref<Z, double>(p0, p1, p2, p3, p4, m0, m1, m2, m3, m4);
+  }
+};
+
+template <class T, bool Z, class D, bool VISC>
+__global__ void __launch_bounds__(256, 2)
+burgers_stage_kernel(const __grid_constant__ CUtensorMap tmap, const BurgersParams<T> p) {
+  using TL = BurgersTile;
+  using SM = BurgersSmem<T>;
+  using K = typename KeyOf<T>::type;
+  constexpr bool EXACT = sizeof(T) == 8;  // FP64: reference operand order, correctly rounded
+
+  if (p.active && *p.active == 0) return;
+
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  T* ring = reinterpret_cast<T*>(smem_raw);
+  T* fpS = reinterpret_cast<T*>(smem_raw + SM::RING);
+  T* fmS = fpS + TL::PLANE;
+  T* fxS = fmS + TL::PLANE;   // [BY][BX+1]
+  T* fyS = fxS + TL::NXF;     // [BY+1][BX]
+  __shared__ uint64_t bars[TL::NS];
+  __shared__ int abort_flag;
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nx = p.nx, ny = p.ny, nz = p.nz;
+  const int x0 = blockIdx.x * TL::BX, y0 = blockIdx.y * TL::BY;
+  const int zs = blockIdx.z * p.zchunk;
+  const int ze = min(nz, zs + p.zchunk);
+  const int Q = (ze - zs) + 2 * TL::R;
+  const int p0 = zs - TL::R;
+  const size_t sxy = (size_t)nx * ny;
+  const bool per = p.periodic != 0;
+  const bool edge = per && (x0 - TL::PADX < 0 || x0 + TL::BX + TL::PADX > nx || y0 - TL::R < 0 || y0 + TL::BY + TL::R > ny);
+
+  // Lax-Friedrichs constant and dt for this stage.
+  T alpha;
+  if (p.alpha_dev) alpha = (T)*p.alpha_dev;
+  else if (p.alpha_key) alpha = (T)key_to_value(*static_cast<const K*>(p.alpha_key));
+  else alpha = (T)p.alpha_host;
+  const T dt = (T)(p.dt_dev ? *p.dt_dev : p.dt_host);
+  const bool glob = p.lf_global != 0;
+
+  if (tid == 0) {
+    if (p.tma) {
+      for (int s = 0; s < TL::NS; ++s) mbar_init(&bars[s], 1);
+      mbar_fence_init();
+      tma_prefetch_desc(&tmap);
+    }
+    abort_flag = 0;
+  }
+  __syncthreads();
+
+  auto plane_z = [&](int q) { return per ? wrapi(p0 + q, nz) : p0 + q; };
+  auto issue = [&](int q) {
+    T* dst = ring + (q % TL::NS) * SM::SLOT_ELEMS;
+    const int z = plane_z(q);
+    if (p.tma) {
+      if (tid == 0) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        uint64_t* bar = &bars[q % TL::NS];
+        mbar_arrive_expect_tx(bar, TL::PLANE * (unsigned)sizeof(T));
+        tma_load_3d(dst, &tmap, x0 - TL::PADX, y0 - TL::R, z, bar);
+      }
+    } else {
+      const bool zok = z >= 0 && z < nz;
+      for (int e = tid; e < TL::PLANE; e += TL::NT) {
+        const int r = e / TL::SW, c = e - r * TL::SW;
+        int gx = x0 - TL::PADX + c, gy = y0 - TL::R + r;
+        if (per) { gx = wrapi(gx, nx); gy = wrapi(gy, ny); }
+        const bool ok = zok && gx >= 0 && gx < nx && gy >= 0 && gy < ny;
+        const T* src = ok ? p.uin + (size_t)z * sxy + (size_t)gy * nx + gx : p.uin;
+        cp_async_zfill<sizeof(T)>(dst + e, src, ok);
+      }
+    }
+  };
+
+  for (int q = 0; q <= TL::P && q < Q; ++q) {
+    issue(q);
+    if (!p.tma) cp_async_commit();
+  }
+  if (!p.tma)
+    for (int q = Q; q <= TL::P; ++q) cp_async_commit();
+
+  // Per-thread columns: (lane, warp) and (lane, warp + 8).
+  const int cx = lane;
+  const int cy0 = warp, cy1 = warp + 8;
+  // z windows per column: f+ at k-2..k+2, f- at k-1..k+3, the f+ of the newest plane held back
+  // one step, u at k-3..k+3 (viscous term and the stage input at k).
+  T fpw[2][5], fmw[2][5], fpn[2], uw[2][7];
+  T fz_prev[2] = {T(0), T(0)};
+#pragma unroll
+  for (int c = 0; c < 2; ++c) {
+    fpn[c] = T(0);
+#pragma unroll
+    for (int s = 0; s < 5; ++s) { fpw[c][s] = T(0); fmw[c][s] = T(0); }
+#pragma unroll
+    for (int s = 0; s < 7; ++s) uw[c][s] = T(0);
+  }
+  K kmax = 0;
+  const T rdx = T(1.0 / p.dx), rdy = T(1.0 / p.dy), rdz = T(1.0 / p.dz);
+  const int F = per ? 0 : 3;
+
+  for (int q = 0; q < Q; ++q) {
+    T* plq = ring + (q % TL::NS) * SM::SLOT_ELEMS;
+    if (p.tma) {
+      if (!mbar_wait_bounded(&bars[q % TL::NS], (q / TL::NS) & 1, p.status)) abort_flag = 1;
+      if (edge) {
+        // Periodic edge tile: the TMA box zero-filled what lies outside the domain; fill it with
+        // the wrapped neighbours. Written here, read only after the next barrier.
+        const int z = plane_z(q);
+        for (int e = tid; e < TL::PLANE; e += TL::NT) {
+          const int r = e / TL::SW, c = e - r * TL::SW;
+          const int gx = x0 - TL::PADX + c, gy = y0 - TL::R + r;
+          if (gx < 0 || gx >= nx || gy < 0 || gy >= ny)
+            plq[e] = p.uin[(size_t)z * sxy + (size_t)wrapi(gy, ny) * nx + wrapi(gx, nx)];
+        }
+      }
+    } else {
+      cp_async_wait<TL::P>();
+    }
+    __syncthreads();  // plane q visible to all threads; abort_flag now uniform
+    const bool aborted = abort_flag != 0;
+    // ---- z windows: push plane q for this thread's two columns
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      const int cy = c ? cy1 : cy0;
+      const T u = plq[(cy + TL::R) * TL::SW + TL::PADX + cx];
+      T fp, fm;
+      lf_split<T>(u, glob ? alpha : absval(u), fp, fm);
+#pragma unroll
+      for (int s = 0; s < 4; ++s) { fpw[c][s] = fpw[c][s + 1]; fmw[c][s] = fmw[c][s + 1]; }
+      fpw[c][4] = fpn[c];
+      fpn[c] = fp;
+      fmw[c][4] = fm;
+#pragma unroll
+      for (int s = 0; s < 6; ++s) uw[c][s] = uw[c][s + 1];
+      uw[c][6] = u;
+    }
+    // z-face at (newest plane - 3) + 1/2 once the windows hold planes newest-5 .. newest.
+    T fz_new[2] = {T(0), T(0)};
+    if (q >= 5) {
+#pragma unroll
+      for (int c = 0; c < 2; ++c)
+        fz_new[c] = Face<T, Z, D>::f(fpw[c][0], fpw[c][1], fpw[c][2], fpw[c][3], fpw[c][4], fmw[c][0], fmw[c][1],
+                                    fmw[c][2], fmw[c][3], fmw[c][4]);
+    }
+    if (q >= 6) {
+      const int k = zs + q - 6;  // output plane; its staged copy is stream entry q - 3
+      const T* plc = ring + ((q - 3) % TL::NS) * SM::SLOT_ELEMS;
+      const bool kin = per || (k >= F && k < nz - F);
+      const bool any_upd = kin && !aborted;
+      if (any_upd) {
+        // f+- of the output plane into shared memory
+        for (int e = tid; e < TL::PLANE; e += TL::NT) {
+          const T u = plc[e];
+          T fp, fm;
+          lf_split<T>(u, glob ? alpha : absval(u), fp, fm);
+          fpS[e] = fp;
+          fmS[e] = fm;
+        }
+        __syncthreads();
+        // x-faces: face fi of row r sits between x0+fi-1 and x0+fi; y-faces likewise.
+        for (int f = tid; f < TL::NXF + TL::NYF; f += TL::NT) {
+          if (f < TL::NXF) {
+            const int r = f / (TL::BX + 1), fi = f - r * (TL::BX + 1);
+            const int base = (r + TL::R) * TL::SW + fi + 1;  // column of x0+fi-3
+            fxS[f] = Face<T, Z, D>::f(fpS[base], fpS[base + 1], fpS[base + 2], fpS[base + 3], fpS[base + 4],
+                                      fmS[base + 1], fmS[base + 2], fmS[base + 3], fmS[base + 4], fmS[base + 5]);
+          } else {
+            const int g = f - TL::NXF;
+            const int fj = g / TL::BX, c = g - fj * TL::BX;
+            const int base = fj * TL::SW + TL::PADX + c;  // row of y0+fj-3
+            constexpr int W = TL::SW;
+            fyS[g] = Face<T, Z, D>::f(fpS[base], fpS[base + W], fpS[base + 2 * W], fpS[base + 3 * W],
+                                      fpS[base + 4 * W], fmS[base + W], fmS[base + 2 * W], fmS[base + 3 * W],
+                                      fmS[base + 4 * W], fmS[base + 5 * W]);
+          }
+        }
+        __syncthreads();
+      }
+      // ---- RHS, stage combine, store, max|u_out|
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        const int cy = c ? cy1 : cy0;
+        const int x = x0 + cx, y = y0 + cy;
+        const T uo = uw[c][3];
+        T res = uo;
+        const bool upd = any_upd && (per || (x >= F && x < nx - F && y >= F && y < ny - F));
+        if (upd) {
+          const T fxp = fxS[cy * (TL::BX + 1) + cx + 1], fxm = fxS[cy * (TL::BX + 1) + cx];
+          const T fyp = fyS[(cy + 1) * TL::BX + cx], fym = fyS[cy * TL::BX + cx];
+          T L;
+          if (EXACT) {
+            L = div_rn(-sub_rn(fxp, fxm), T(p.dx));
+            L = sub_rn(L, div_rn(sub_rn(fyp, fym), T(p.dy)));
+            L = sub_rn(L, div_rn(sub_rn(fz_new[c], fz_prev[c]), T(p.dz)));
+          } else {
+            L = -(fxp - fxm) * rdx - (fyp - fym) * rdy - (fz_new[c] - fz_prev[c]) * rdz;
+          }
+          if (VISC) {
+            const T* row = plc + (cy + TL::R) * TL::SW + TL::PADX + cx;
+            constexpr int W = TL::SW;
+            const T vx = sub_rn(add_rn(sub_rn(add_rn(-row[-2], mul_rn(T(16), row[-1])), mul_rn(T(30), uo)),
+                                       mul_rn(T(16), row[1])), row[2]);
+            const T vy = sub_rn(add_rn(sub_rn(add_rn(-row[-2 * W], mul_rn(T(16), row[-W])), mul_rn(T(30), uo)),
+                                       mul_rn(T(16), row[W])), row[2 * W]);
+            const T vz = sub_rn(add_rn(sub_rn(add_rn(-uw[c][1], mul_rn(T(16), uw[c][2])), mul_rn(T(30), uo)),
+                                       mul_rn(T(16), uw[c][4])), uw[c][5]);
+            const T v = add_rn(add_rn(mul_rn(p.kx, vx), mul_rn(p.ky, vy)), mul_rn(p.kz, vz));
+            L = add_rn(L, v);
+            // The reference's first viscous z-block starts at slab 3 yet runs 16 slabs, adding
+            // slabs 16..18 twice (kernels.cu:464-491); reproduced only on request.
+            if (p.bug_b2 && !per && k >= 16 && k <= 18 && k <= nz - 3) L = add_rn(L, v);
+          }
+          T un;
+          if (p.un_is_uin) un = uo;
+          else un = p.un[(size_t)k * sxy + (size_t)y * nx + x];
+          res = stage_combine<T>(p.stage, un, uo, dt, L);
+        }
+        if (x < nx && y < ny) {
+          p.out[(size_t)k * sxy + (size_t)y * nx + x] = res;
+          const K kk = abs_key(res);
+          kmax = kk > kmax ? kk : kmax;
+        }
+      }
+    }
+    if (q >= 5) {
+      fz_prev[0] = fz_new[0];
+      fz_prev[1] = fz_new[1];
+    }
+    __syncthreads();  // stream entry q - 3 fully consumed
+    if (aborted) {
+      if (p.tma && tid == 0)
+        for (int m = q; m < Q && m <= q + TL::P; ++m) mbar_wait_bounded(&bars[m % TL::NS], (m / TL::NS) & 1, p.status);
+      return;
+    }
+    if (q + TL::P + 1 < Q) issue(q + TL::P + 1);
+    if (!p.tma) cp_async_commit();
+  }
+  if (p.maxabs_key) {
+    kmax = warp_max(kmax);
+    if (lane == 0 && kmax) atomicMax(static_cast<K*>(p.maxabs_key), kmax);
+  }
+}
+
+}  // namespace adv

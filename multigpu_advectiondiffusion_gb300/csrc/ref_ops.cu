@@ -1,0 +1,229 @@
+// ref_ops.cu -- the reference's unfused operators (include/advdiff_ref_ops.h) as sm_103a kernels.
+//
+// One thread per node, grid-stride over a flat index, so the launch never depends on the
+// caller's block shape (the reference's wrappers take dim3 arguments; the compatibility
+// libraries ignore them). Arithmetic uses correctly rounded intrinsics in the reference's
+// operand order, so FP64 results equal the reference's own kernels' and the CPU oracle's.
+#include <algorithm>
+
+#include "../../include/advdiff_ref_ops.h"
+#include "adv_internal.h"
+#include "adv_math.cuh"
+#include "weno.cuh"
+
+namespace adv {
+
+struct Grid3 {
+  int nx, ny, nz;
+  int64_t pitch;
+  __device__ __forceinline__ int64_t count() const { return (int64_t)nx * ny * nz; }
+  __device__ __forceinline__ void ijk(int64_t f, int& i, int& j, int& k) const {
+    i = (int)(f % nx);
+    const int64_t r = f / nx;
+    j = (int)(r % ny);
+    k = (int)(r / ny);
+  }
+  __device__ __forceinline__ int64_t at(int i, int j, int k) const { return i + pitch * j + pitch * ny * (int64_t)k; }
+};
+
+template <class T>
+__global__ void ref_laplace_kernel(Grid3 g, int ndim, int order, int lo, int zero_outside, T kx, T ky, T kz,
+                                   const T* __restrict__ u, T* __restrict__ Lu) {
+  for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < g.count(); f += (int64_t)gridDim.x * blockDim.x) {
+    int i, j, k;
+    g.ijk(f, i, j, k);
+    const int64_t o = g.at(i, j, k);
+    bool in = i >= lo && i < g.nx - lo && j >= lo && j < g.ny - lo;
+    if (ndim == 3) in = in && k >= lo && k < g.nz - lo;
+    if (!in) {
+      if (zero_outside) Lu[o] = T(0);
+      continue;
+    }
+    const int64_t sy = g.pitch, sz = g.pitch * g.ny;
+    const T c = u[o];
+    T L;
+    if (order == 4) {
+      if (ndim == 3) {  // east first (Diffusion3d_baselineCode/kernels.cu:95-97)
+        const T Sx = sub_rn(add_rn(sub_rn(add_rn(-u[o + 2], mul_rn(T(16), u[o + 1])), mul_rn(T(30), c)), mul_rn(T(16), u[o - 1])), u[o - 2]);
+        const T Sy = sub_rn(add_rn(sub_rn(add_rn(-u[o + 2 * sy], mul_rn(T(16), u[o + sy])), mul_rn(T(30), c)), mul_rn(T(16), u[o - sy])), u[o - 2 * sy]);
+        const T Sz = sub_rn(add_rn(sub_rn(add_rn(-u[o + 2 * sz], mul_rn(T(16), u[o + sz])), mul_rn(T(30), c)), mul_rn(T(16), u[o - sz])), u[o - 2 * sz]);
+        L = add_rn(add_rn(mul_rn(kx, Sx), mul_rn(ky, Sy)), mul_rn(kz, Sz));
+      } else {  // west first (Diffusion2d/kernels.cu:82-83)
+        const T Sx = sub_rn(add_rn(sub_rn(add_rn(-u[o - 2], mul_rn(T(16), u[o - 1])), mul_rn(T(30), c)), mul_rn(T(16), u[o + 1])), u[o + 2]);
+        const T Sy = sub_rn(add_rn(sub_rn(add_rn(-u[o - 2 * sy], mul_rn(T(16), u[o - sy])), mul_rn(T(30), c)), mul_rn(T(16), u[o + sy])), u[o + 2 * sy]);
+        L = add_rn(mul_rn(kx, Sx), mul_rn(ky, Sy));
+      }
+    } else {  // 12*k*(e - 2o + w) per axis (kernels.cu:58-60)
+      const T Sx = add_rn(sub_rn(u[o + 1], mul_rn(T(2), c)), u[o - 1]);
+      const T Sy = add_rn(sub_rn(u[o + sy], mul_rn(T(2), c)), u[o - sy]);
+      L = add_rn(mul_rn(mul_rn(T(12), kx), Sx), mul_rn(mul_rn(T(12), ky), Sy));
+      if (ndim == 3) {
+        const T Sz = add_rn(sub_rn(u[o + sz], mul_rn(T(2), c)), u[o - sz]);
+        L = add_rn(L, mul_rn(mul_rn(T(12), kz), Sz));
+      }
+    }
+    Lu[o] = L;
+  }
+}
+
+template <class T>
+__global__ void ref_rk_kernel(Grid3 g, int ndim, int lo, int step, T dt, T* __restrict__ u, const T* __restrict__ uo,
+                              const T* __restrict__ Lu) {
+  for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < g.count(); f += (int64_t)gridDim.x * blockDim.x) {
+    int i, j, k;
+    g.ijk(f, i, j, k);
+    bool in = i >= lo && i < g.nx - lo && j >= lo && j < g.ny - lo;
+    if (ndim == 3) in = in && k >= lo && k < g.nz - lo;
+    if (!in || step < 1 || step > 3) continue;
+    const int64_t o = g.at(i, j, k);
+    u[o] = stage_combine<T>(step, uo[o], u[o], dt, Lu[o]);
+  }
+}
+
+template <class T, bool Z>
+__device__ __forceinline__ T sweep_face(const T* __restrict__ u, int64_t o, int64_t s) {
+  // face at o + 1/2 along stride s: f+ at o-2s..o+2s, f- at o-s..o+3s (local LF)
+  T fp[6], fm[6];
+#pragma unroll
+  for (int q = 0; q < 6; ++q) {
+    const T v = u[o + (q - 2) * s];
+    lf_split<T>(v, fabs(v), fp[q], fm[q]);
+  }
+  return weno_face_ref<Z, T>(fp[0], fp[1], fp[2], fp[3], fp[4], fm[1], fm[2], fm[3], fm[4], fm[5]);
+}
+
+template <class T, bool Z>
+__global__ void ref_sweep_kernel(Grid3 g, int axis, T h, const T* __restrict__ u, T* __restrict__ Lu) {
+  for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < g.count(); f += (int64_t)gridDim.x * blockDim.x) {
+    int i, j, k;
+    g.ijk(f, i, j, k);
+    const int a = axis == 0 ? i : axis == 1 ? j : k;
+    const int na = axis == 0 ? g.nx : axis == 1 ? g.ny : g.nz;
+    const int b = axis == 0 ? j : i, nb = axis == 0 ? g.ny : g.nx;
+    const int c = axis == 2 ? j : k, nc = axis == 2 ? g.ny : g.nz;
+    if (a < 2 || a > na - 4 || b < 3 || b > nb - 4 || c < 3 || c > nc - 4) continue;
+    const int64_t o = g.at(i, j, k);
+    const int64_t s = axis == 0 ? 1 : axis == 1 ? g.pitch : g.pitch * g.ny;
+    const T fu = sweep_face<T, Z>(u, o, s);
+    const T fu_old = a == 2 ? T(0) : sweep_face<T, Z>(u, o - s, s);
+    if (axis == 0) Lu[o] = div_rn(-sub_rn(fu, fu_old), h);
+    else Lu[o] = sub_rn(Lu[o], div_rn(sub_rn(fu, fu_old), h));
+  }
+}
+
+template <class T>
+__global__ void ref_viscous_kernel(Grid3 g, T kx, T ky, T kz, int bug_b2, const T* __restrict__ u, T* __restrict__ Lu) {
+  for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < g.count(); f += (int64_t)gridDim.x * blockDim.x) {
+    int i, j, k;
+    g.ijk(f, i, j, k);
+    if (i < 3 || i > g.nx - 4 || j < 3 || j > g.ny - 4 || k < 3 || k > g.nz - 3) continue;
+    const int64_t o = g.at(i, j, k), sy = g.pitch, sz = g.pitch * g.ny;
+    const T c = u[o];
+    const T vx = sub_rn(add_rn(sub_rn(add_rn(-u[o - 2], mul_rn(T(16), u[o - 1])), mul_rn(T(30), c)), mul_rn(T(16), u[o + 1])), u[o + 2]);
+    const T vy = sub_rn(add_rn(sub_rn(add_rn(-u[o - 2 * sy], mul_rn(T(16), u[o - sy])), mul_rn(T(30), c)), mul_rn(T(16), u[o + sy])), u[o + 2 * sy]);
+    const T vz = sub_rn(add_rn(sub_rn(add_rn(-u[o - 2 * sz], mul_rn(T(16), u[o - sz])), mul_rn(T(30), c)), mul_rn(T(16), u[o + sz])), u[o + 2 * sz]);
+    const T v = add_rn(add_rn(mul_rn(kx, vx), mul_rn(ky, vy)), mul_rn(kz, vz));
+    T L = add_rn(Lu[o], v);
+    if (bug_b2 && k >= 16 && k <= 18) L = add_rn(L, v);
+    Lu[o] = L;
+  }
+}
+
+static adv_status check_grid(int dtype, int64_t pitch, int nx, int ny, int nz, const void* a, const void* b) {
+  if (dtype != ADV_F32 && dtype != ADV_F64) return set_error(ADV_ERR_INVALID_ARG, "ref op: bad dtype");
+  if (nx < 1 || ny < 1 || nz < 1 || pitch < nx) return set_error(ADV_ERR_INVALID_ARG, "ref op: bad sizes or pitch");
+  if (!a || !b) return set_error(ADV_ERR_INVALID_ARG, "ref op: null buffer");
+  return ADV_OK;
+}
+
+static dim3 flat_grid(int64_t n) {
+  DeviceInfo di;
+  int sms = 148;
+  if (device_info(&di) == ADV_OK) sms = di.sms;
+  return dim3((unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)sms * 16)));
+}
+
+}  // namespace adv
+
+using namespace adv;
+
+extern "C" {
+
+adv_status adv_ref_laplace(int dtype, int ndim, int order, int lo, int zero_outside, int64_t pitch, int nx, int ny, int nz,
+                           double kx, double ky, double kz, const void* u, void* Lu, void* stream) {
+  if (ndim == 2) nz = 1;
+  adv_status st = check_grid(dtype, pitch, nx, ny, nz, u, Lu);
+  if (st != ADV_OK) return st;
+  if ((ndim != 2 && ndim != 3) || (order != 2 && order != 4) || lo < order / 2)
+    return set_error(ADV_ERR_INVALID_ARG, "ref_laplace: bad ndim/order/lo");
+  Grid3 g{nx, ny, nz, pitch};
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const dim3 grid = flat_grid((int64_t)nx * ny * nz);
+  if (dtype == ADV_F64)
+    ref_laplace_kernel<double><<<grid, 256, 0, s>>>(g, ndim, order, lo, zero_outside, kx, ky, kz, (const double*)u, (double*)Lu);
+  else
+    ref_laplace_kernel<float><<<grid, 256, 0, s>>>(g, ndim, order, lo, zero_outside, (float)kx, (float)ky, (float)kz,
+                                                   (const float*)u, (float*)Lu);
+  ADV_CUDA_TRY(cudaGetLastError());
+  count_launches(1);
+  return ADV_OK;
+}
+
+adv_status adv_ref_rk(int dtype, int ndim, int lo, int64_t pitch, int nx, int ny, int nz, int step, double dt, void* u,
+                      const void* uo, const void* Lu, void* stream) {
+  if (ndim == 2) nz = 1;
+  adv_status st = check_grid(dtype, pitch, nx, ny, nz, u, uo);
+  if (st != ADV_OK) return st;
+  if (!Lu || (ndim != 2 && ndim != 3) || lo < 0 || step < 1 || step > 3)
+    return set_error(ADV_ERR_INVALID_ARG, "ref_rk: bad arguments");
+  Grid3 g{nx, ny, nz, pitch};
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const dim3 grid = flat_grid((int64_t)nx * ny * nz);
+  if (dtype == ADV_F64)
+    ref_rk_kernel<double><<<grid, 256, 0, s>>>(g, ndim, lo, step, dt, (double*)u, (const double*)uo, (const double*)Lu);
+  else
+    ref_rk_kernel<float><<<grid, 256, 0, s>>>(g, ndim, lo, step, (float)dt, (float*)u, (const float*)uo, (const float*)Lu);
+  ADV_CUDA_TRY(cudaGetLastError());
+  count_launches(1);
+  return ADV_OK;
+}
+
+adv_status adv_ref_burgers_sweep(int dtype, int axis, int weno, int64_t pitch, int nx, int ny, int nz, double h,
+                                 const void* u, void* Lu, void* stream) {
+  adv_status st = check_grid(dtype, pitch, nx, ny, nz, u, Lu);
+  if (st != ADV_OK) return st;
+  if (axis < 0 || axis > 2 || (weno != ADV_WENO5_JS && weno != ADV_WENO5_Z) || !(h != 0.0))
+    return set_error(ADV_ERR_INVALID_ARG, "ref_burgers_sweep: bad arguments");
+  Grid3 g{nx, ny, nz, pitch};
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const dim3 grid = flat_grid((int64_t)nx * ny * nz);
+  const bool z = weno == ADV_WENO5_Z;
+  if (dtype == ADV_F64) {
+    if (z) ref_sweep_kernel<double, true><<<grid, 256, 0, s>>>(g, axis, h, (const double*)u, (double*)Lu);
+    else ref_sweep_kernel<double, false><<<grid, 256, 0, s>>>(g, axis, h, (const double*)u, (double*)Lu);
+  } else {
+    if (z) ref_sweep_kernel<float, true><<<grid, 256, 0, s>>>(g, axis, (float)h, (const float*)u, (float*)Lu);
+    else ref_sweep_kernel<float, false><<<grid, 256, 0, s>>>(g, axis, (float)h, (const float*)u, (float*)Lu);
+  }
+  ADV_CUDA_TRY(cudaGetLastError());
+  count_launches(1);
+  return ADV_OK;
+}
+
+adv_status adv_ref_burgers_viscous(int dtype, int64_t pitch, int nx, int ny, int nz, double kx, double ky, double kz,
+                                   int bug_b2, const void* u, void* Lu, void* stream) {
+  adv_status st = check_grid(dtype, pitch, nx, ny, nz, u, Lu);
+  if (st != ADV_OK) return st;
+  Grid3 g{nx, ny, nz, pitch};
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const dim3 grid = flat_grid((int64_t)nx * ny * nz);
+  if (dtype == ADV_F64)
+    ref_viscous_kernel<double><<<grid, 256, 0, s>>>(g, kx, ky, kz, bug_b2, (const double*)u, (double*)Lu);
+  else
+    ref_viscous_kernel<float><<<grid, 256, 0, s>>>(g, (float)kx, (float)ky, (float)kz, bug_b2, (const float*)u, (float*)Lu);
+  ADV_CUDA_TRY(cudaGetLastError());
+  count_launches(1);
+  return ADV_OK;
+}
+
+}  // extern "C"

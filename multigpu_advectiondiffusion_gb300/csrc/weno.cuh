@@ -1,0 +1,112 @@
+// weno.cuh -- WENO5-JS / WENO5-Z face reconstruction for the Lax-Friedrichs split Burgers flux.
+//
+// Face flux at i+1/2:  F = R(f+_{i-2..i+2}) + R(f-_{i+3..i-1} reversed), where R is the
+// left-biased 5-point reconstruction of SingleGPU/Burgers3d_WENO5/kernels.cu:142-192 (WENO5-Z)
+// and :92-140 (WENO5-JS); the right-biased half of those functions is R applied to the
+// mirrored stencil (same smoothness indicators, linear weights 0.1/0.6/0.3 reversed).
+//
+// Two forms:
+//  * weno_face_ref<double>: the reference's own expression, operand for operand, with
+//    correctly rounded intrinsics -> equal to the FP64 oracle bit for bit.
+//  * weno_side_fast<D>: the same weights with the common denominator b0*b1*b2 (WENO5-Z) or
+//    (b0*b1*b2)^2 (WENO5-JS) multiplied through, leaving ONE division per side instead of four;
+//    that division runs in type D (FP32 or FP64). Used for the FP32 state.
+#pragma once
+#include "adv_math.cuh"
+
+namespace adv {
+
+// Lax-Friedrichs split of f(u) = u^2/2 (kernels.cu:224-238): f+- = (f +- a u)/2.
+template <class T>
+__device__ __forceinline__ void lf_split(T u, T a, T& fp, T& fm) {
+  const T f = mul_rn(mul_rn(T(0.5), u), u);
+  const T au = mul_rn(a, u);
+  fp = mul_rn(T(0.5), add_rn(f, au));
+  fm = mul_rn(T(0.5), sub_rn(f, au));
+}
+
+// ---------------------------------------------------------------- fast FP32 form
+template <bool Z, class D>
+__device__ __forceinline__ float weno_side_fast(float a, float b, float c, float d, float e) {
+  const float t0 = a - 2.f * b + c, t1 = b - 2.f * c + d, t2 = c - 2.f * d + e;
+  const float s0 = a - 4.f * b + 3.f * c, s1 = b - d, s2 = 3.f * c - 4.f * d + e;
+  const float k13 = 13.f / 12.f;
+  const float B0 = k13 * t0 * t0 + 0.25f * s0 * s0;
+  const float B1 = k13 * t1 * t1 + 0.25f * s1 * s1;
+  const float B2 = k13 * t2 * t2 + 0.25f * s2 * s2;
+  const float q0 = 2.f * a - 7.f * b + 11.f * c;
+  const float q1 = -b + 5.f * c + 2.f * d;
+  const float q2 = 2.f * c + 5.f * d - e;
+  const float b0 = B0 + 1e-6f, b1 = B1 + 1e-6f, b2 = B2 + 1e-6f;
+  float w0, w1, w2;
+  if (Z) {  // alpha_k = d_k (1 + tau/b_k), times b0 b1 b2
+    const float tau = fabsf(B0 - B2);
+    w0 = 0.1f * (b0 + tau) * (b1 * b2);
+    w1 = 0.6f * (b1 + tau) * (b0 * b2);
+    w2 = 0.3f * (b2 + tau) * (b0 * b1);
+  } else {  // alpha_k = d_k / b_k^2, times (b0 b1 b2)^2
+    const float p12 = b1 * b2, p02 = b0 * b2, p01 = b0 * b1;
+    w0 = 0.1f * p12 * p12;
+    w1 = 0.6f * p02 * p02;
+    w2 = 0.3f * p01 * p01;
+  }
+  const float num = w0 * q0 + w1 * q1 + w2 * q2;
+  const float den = 6.f * (w0 + w1 + w2);
+  return (float)((D)num / (D)den);
+}
+
+// f+ at i-2..i+2 (p0..p4) and f- at i-1..i+3 (m0..m4).
+template <bool Z, class D>
+__device__ __forceinline__ float weno_face_fast(float p0, float p1, float p2, float p3, float p4, float m0, float m1,
+                                                float m2, float m3, float m4) {
+  return weno_side_fast<Z, D>(p0, p1, p2, p3, p4) + weno_side_fast<Z, D>(m4, m3, m2, m1, m0);
+}
+
+// ---------------------------------------------------------- reference literal form
+// Operand order of kernels.cu:142-192 / :92-140 (and of the CPU oracle), correctly rounded.
+template <bool Z, class T>
+__device__ __forceinline__ T weno_face_ref(T vmm, T vm, T v, T vp, T vpp, T umm, T um, T u, T up, T upp) {
+  const T c1312 = T(13. / 12.), c14 = T(1. / 4.), eps = T(1e-6);
+  auto beta = [&](T a, T b, T c, T d, T e, T& B0, T& B1, T& B2) {
+    const T A0 = add_rn(sub_rn(a, mul_rn(T(2), b)), c);
+    const T C0 = add_rn(sub_rn(a, mul_rn(T(4), b)), mul_rn(T(3), c));
+    B0 = add_rn(mul_rn(mul_rn(c1312, A0), A0), mul_rn(mul_rn(c14, C0), C0));
+    const T A1 = add_rn(sub_rn(b, mul_rn(T(2), c)), d);
+    const T C1 = sub_rn(b, d);
+    B1 = add_rn(mul_rn(mul_rn(c1312, A1), A1), mul_rn(mul_rn(c14, C1), C1));
+    const T A2 = add_rn(sub_rn(c, mul_rn(T(2), d)), e);
+    const T C2 = add_rn(sub_rn(mul_rn(T(3), c), mul_rn(T(4), d)), e);
+    B2 = add_rn(mul_rn(mul_rn(c1312, A2), A2), mul_rn(mul_rn(c14, C2), C2));
+  };
+  auto weights = [&](T B0, T B1, T B2, T d0, T d1, T d2, T& a0, T& a1, T& a2) {
+    if (Z) {
+      const T tau5 = fabs(sub_rn(B0, B2));
+      a0 = mul_rn(d0, add_rn(T(1), div_rn(tau5, add_rn(B0, eps))));
+      a1 = mul_rn(d1, add_rn(T(1), div_rn(tau5, add_rn(B1, eps))));
+      a2 = mul_rn(d2, add_rn(T(1), div_rn(tau5, add_rn(B2, eps))));
+    } else {
+      a0 = div_rn(d0, mul_rn(add_rn(eps, B0), add_rn(eps, B0)));
+      a1 = div_rn(d1, mul_rn(add_rn(eps, B1), add_rn(eps, B1)));
+      a2 = div_rn(d2, mul_rn(add_rn(eps, B2), add_rn(eps, B2)));
+    }
+  };
+  T B0, B1, B2, a0, a1, a2;
+  beta(vmm, vm, v, vp, vpp, B0, B1, B2);
+  weights(B0, B1, B2, T(1. / 10.), T(6. / 10.), T(3. / 10.), a0, a1, a2);
+  T asum = add_rn(add_rn(a0, a1), a2);
+  const T q0m = add_rn(sub_rn(mul_rn(T(2), vmm), mul_rn(T(7), vm)), mul_rn(T(11), v));
+  const T q1m = add_rn(add_rn(-vm, mul_rn(T(5), v)), mul_rn(T(2), vp));
+  const T q2m = sub_rn(add_rn(mul_rn(T(2), v), mul_rn(T(5), vp)), vpp);
+  const T fm = div_rn(add_rn(add_rn(mul_rn(a0, q0m), mul_rn(a1, q1m)), mul_rn(a2, q2m)), mul_rn(T(6), asum));
+
+  beta(umm, um, u, up, upp, B0, B1, B2);
+  weights(B0, B1, B2, T(3. / 10.), T(6. / 10.), T(1. / 10.), a0, a1, a2);
+  asum = add_rn(add_rn(a0, a1), a2);
+  const T q0p = add_rn(add_rn(-umm, mul_rn(T(5), um)), mul_rn(T(2), u));
+  const T q1p = sub_rn(add_rn(mul_rn(T(2), um), mul_rn(T(5), u)), up);
+  const T q2p = add_rn(sub_rn(mul_rn(T(11), u), mul_rn(T(7), up)), mul_rn(T(2), upp));
+  const T fp = div_rn(add_rn(add_rn(mul_rn(a0, q0p), mul_rn(a1, q1p)), mul_rn(a2, q2p)), mul_rn(T(6), asum));
+  return add_rn(fm, fp);
+}
+
+}  // namespace adv

@@ -1,0 +1,195 @@
+"""Host-side mirror of the reference's solver surface over the CUDA library.
+
+The reference drives its kernels from main.cpp time loops (SingleGPU/Diffusion3d_baselineCode/
+main.cpp:55-122, SingleGPU/Diffusion2d/main.cpp:52-125, SingleGPU/Burgers3d_WENO5/
+main.cpp:53-150). This module keeps those constants and dt rules and calls the fused stage
+kernels through the C ABI on torch CUDA tensors (torch supplies device memory and streams only).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass
+
+from . import _native as N
+
+
+def _ptr(t) -> int:
+    if not t.is_cuda or not t.is_contiguous():
+        raise ValueError("expected a contiguous CUDA tensor")
+    return t.data_ptr()
+
+
+def _dtype_code(t) -> int:
+    import torch
+    if t.dtype == torch.float32:
+        return N.ADV_F32
+    if t.dtype == torch.float64:
+        return N.ADV_F64
+    raise ValueError(f"unsupported dtype {t.dtype}")
+
+
+@dataclass
+class HeatConfig:
+    """Heat-equation scheme (fields as adv_heat_desc in include/advdiff.h)."""
+    ndim: int
+    nx: int
+    ny: int
+    nz: int
+    order: int = 4
+    frozen: int = 2
+    zero_boundary: bool = False
+    kx: float = 0.0
+    ky: float = 0.0
+    kz: float = 0.0
+    dt: float = 0.0
+    time: int = N.ADV_SSPRK3
+
+    @classmethod
+    def reference_3d(cls, C: float, L: int, W: int, H: int, nx: int, ny: int, nz: int) -> "HeatConfig":
+        """The reference 3D scheme: O4 + SSP-RK3, dt = 0.9/(2C sum 1/h^2), k = C/(12 h^2), two
+        frozen layers (SingleGPU/Diffusion3d_baselineCode/main.cpp:55-62, kernels.cu:127)."""
+        dx, dy, dz = L / (nx - 1), W / (ny - 1), H / (nz - 1)
+        dt = 1 / (2 * C * (1 / dx / dx + 1 / dy / dy + 1 / dz / dz)) * 0.9
+        return cls(3, nx, ny, nz, 4, 2, False, C / (12 * dx * dx), C / (12 * dy * dy), C / (12 * dz * dz), dt)
+
+    @classmethod
+    def reference_2d(cls, C: float, L: int, W: int, nx: int, ny: int) -> "HeatConfig":
+        """The reference 2D scheme: O4 + SSP-RK3, three frozen layers
+        (SingleGPU/Diffusion2d/main.cpp:52-57, kernels.cu:53)."""
+        dx, dy = L / (nx - 1), W / (ny - 1)
+        dt = 1 / (2 * C * (1 / dx / dx + 1 / dy / dy)) * 0.9
+        return cls(2, nx, ny, 1, 4, 3, False, C / (12 * dx * dx), C / (12 * dy * dy), 0.0, dt)
+
+    @classmethod
+    def dirichlet_o2(cls, ndim: int, n: int, k: float = 1.0, r: float | None = None, L: float = 1.0) -> "HeatConfig":
+        """O2 (5/7-point) forward Euler with r = k dt/h^2 on the node grid of [0,L]^d, u = 0 on the
+        boundary nodes. Default r: 0.2 in 2D, 1/8 in 3D."""
+        r = (0.2 if ndim == 2 else 0.125) if r is None else r
+        h = L / (n - 1)
+        c = k / (h * h)
+        return cls(ndim, n, n, n if ndim == 3 else 1, 2, 1, True, c, c, c if ndim == 3 else 0.0, r * h * h / k,
+                   N.ADV_EULER)
+
+    def desc(self, dtype: int) -> N.HeatDesc:
+        return N.HeatDesc(self.ndim, self.nx, self.ny, self.nz if self.ndim == 3 else 1, dtype, self.order,
+                          self.frozen, int(self.zero_boundary), self.kx, self.ky, self.kz, self.dt)
+
+    @property
+    def numel(self) -> int:
+        return self.nx * self.ny * (self.nz if self.ndim == 3 else 1)
+
+
+def heat_stage(cfg: HeatConfig, stage: int, u_in, u_n, u_out, stream=None) -> None:
+    """One fused stage u_out = combine(u_n, u_in + dt L(u_in)) (adv_heat_stage)."""
+    d = cfg.desc(_dtype_code(u_in))
+    N.check(N.load().adv_heat_stage(C.byref(d), stage, _ptr(u_in), _ptr(u_n), _ptr(u_out), N.stream_handle(stream)),
+            "adv_heat_stage")
+
+
+def heat_workspace(cfg: HeatConfig, like):
+    import torch
+    d = cfg.desc(_dtype_code(like))
+    nb = C.c_size_t(0)
+    N.check(N.load().adv_heat_workspace_bytes(C.byref(d), cfg.time, C.byref(nb)), "adv_heat_workspace_bytes")
+    return torch.empty(nb.value, dtype=torch.uint8, device=like.device)
+
+
+def heat_run(cfg: HeatConfig, u, nsteps: int, workspace=None, stream=None):
+    """nsteps time steps in place on u (adv_heat_run); returns u."""
+    ws = heat_workspace(cfg, u) if workspace is None else workspace
+    d = cfg.desc(_dtype_code(u))
+    N.check(N.load().adv_heat_run(C.byref(d), cfg.time, int(nsteps), _ptr(u), _ptr(ws), N.stream_handle(stream)),
+            "adv_heat_run")
+    return u
+
+
+@dataclass
+class BurgersConfig:
+    """Burgers scheme (fields as adv_burgers_desc in include/advdiff.h)."""
+    nx: int
+    ny: int
+    nz: int
+    dx: float
+    dy: float
+    dz: float
+    weno: int = N.ADV_WENO5_Z
+    lf: int = N.ADV_LF_LOCAL
+    bc: int = N.ADV_BC_FROZEN
+    div: int = N.ADV_DIV_F32
+    bug_b2: bool = False
+    C: float = 0.0
+
+    @classmethod
+    def reference(cls, L: float, W: float, H: float, nx: int, ny: int, nz: int, C: float = 1e-5,
+                  bug_b2: bool = False) -> "BurgersConfig":
+        """The reference scheme: node grid dx = L/(N-1), local LF, WENO5-Z, viscous term C = 1e-5,
+        frozen 3 layers (SingleGPU/Burgers3d_WENO5/main.cpp:53-59)."""
+        return cls(nx, ny, nz, L / (nx - 1), W / (ny - 1), H / (nz - 1), N.ADV_WENO5_Z, N.ADV_LF_LOCAL,
+                   N.ADV_BC_FROZEN, N.ADV_DIV_F32, bug_b2, C)
+
+    @classmethod
+    def periodic(cls, n: int, L: float = 2.0, weno: str = "z", lf: str = "global", div: str = "f32") -> "BurgersConfig":
+        """Inviscid periodic [0,L)^3 on n^3 cell centres, dx = L/n."""
+        h = L / n
+        return cls(n, n, n, h, h, h, N.ADV_WENO5_Z if weno == "z" else N.ADV_WENO5_JS,
+                   N.ADV_LF_GLOBAL if lf == "global" else N.ADV_LF_LOCAL, N.ADV_BC_PERIODIC,
+                   N.ADV_DIV_F64 if div == "f64" else N.ADV_DIV_F32, False, 0.0)
+
+    def desc(self, dtype: int) -> N.BurgersDesc:
+        k = [self.C / (12 * h * h) if self.C else 0.0 for h in (self.dx, self.dy, self.dz)]
+        return N.BurgersDesc(self.nx, self.ny, self.nz, dtype, self.weno, self.lf, self.bc, self.div,
+                             int(self.bug_b2), 0, self.dx, self.dy, self.dz, *k)
+
+    @property
+    def numel(self) -> int:
+        return self.nx * self.ny * self.nz
+
+
+def burgers_stage(cfg: BurgersConfig, stage: int, u_in, u_n, u_out, dt: float, alpha: float = 0.0,
+                  maxabs_key=None, stream=None) -> None:
+    """One fused SSP-RK3 stage (adv_burgers_stage). maxabs_key: optional device tensor of one
+    int32 (FP32 state) / int64 (FP64 state), zeroed by the caller, receiving max|u_out| bits."""
+    d = cfg.desc(_dtype_code(u_in))
+    key = None if maxabs_key is None else maxabs_key.data_ptr()
+    N.check(N.load().adv_burgers_stage(C.byref(d), stage, _ptr(u_in), _ptr(u_n), _ptr(u_out), float(dt), float(alpha),
+                                       key, N.stream_handle(stream)), "adv_burgers_stage")
+
+
+def burgers_workspace(cfg: BurgersConfig, like):
+    import torch
+    d = cfg.desc(_dtype_code(like))
+    nb = C.c_size_t(0)
+    N.check(N.load().adv_burgers_workspace_bytes(C.byref(d), C.byref(nb)), "adv_burgers_workspace_bytes")
+    return torch.empty(nb.value, dtype=torch.uint8, device=like.device)
+
+
+def burgers_run(cfg: BurgersConfig, u, tEnd: float, cfl: float, dt_rule: int = N.ADV_DT_MAXU,
+                max_steps: int = 1 << 40, workspace=None, stream=None) -> tuple[float, int]:
+    """Time loop to tEnd in place on u (adv_burgers_run); returns (t, steps)."""
+    ws = burgers_workspace(cfg, u) if workspace is None else workspace
+    d = cfg.desc(_dtype_code(u))
+    t = C.c_double(0.0)
+    steps = C.c_int64(0)
+    N.check(N.load().adv_burgers_run(C.byref(d), _ptr(u), _ptr(ws), float(tEnd), float(cfl), int(dt_rule),
+                                     float(cfg.C), int(max_steps), C.byref(t), C.byref(steps),
+                                     N.stream_handle(stream)), "adv_burgers_run")
+    return t.value, steps.value
+
+
+def max_abs(u, stream=None) -> float:
+    out = C.c_double(0.0)
+    N.check(N.load().adv_max_abs(_dtype_code(u), _ptr(u), u.numel(), C.byref(out), N.stream_handle(stream)),
+            "adv_max_abs")
+    return out.value
+
+
+def reference_heat_final_time(dt: float, iters: int, t0: float = 0.1) -> float:
+    """tFinal = t0 + dt*iters as the reference prints it (main.cpp:63)."""
+    return t0 + dt * iters
+
+
+def reference_burgers_fixed_dt(cfl: float, dx: float, dy: float, dz: float, C: float) -> float:
+    """dt = min(CFL dx / 1, 0.9/(2C sum 1/h^2)) (SingleGPU/Burgers3d_WENO5/main.cpp:130-132)."""
+    dt2 = 1.0 / (2 * C * (1 / dx / dx + 1 / dy / dy + 1 / dz / dz)) * 0.9 if C > 0 else math.inf
+    return min(cfl * dx / 1.0, dt2)

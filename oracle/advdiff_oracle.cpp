@@ -1,0 +1,681 @@
+// advdiff_oracle.cpp -- TEST INFRASTRUCTURE ONLY.
+//
+// CPU restatement of the reference's numerical schemes for the two explicit solvers
+// (heat-equation stencil + time update, 3D Burgers WENO5/WENO5-Z + Lax-Friedrichs + SSP-RK3).
+// It is the parity oracle for the CUDA path and the timed CPU baseline. Only the tests,
+// the smoke check and the CPU-baseline leg of the benchmark load this library; the product
+// library never links, calls or falls back to it.
+//
+// FP64 is the reference's own precision (SingleGPU/Burgers3d_WENO5/Burgers.h:47-54,
+// SingleGPU/Diffusion3d_baselineCode/acoustics3d.h:35-42). Every routine is templated on the
+// arithmetic type so an FP32 variant can measure the single-precision error floor on the CPU.
+//
+// Parity pins (checked by tests/test_oracle_golden.py):
+//   * Matlab_Prototipes/DiffusionNd/TestingAccuracy.log:53-72 (O4 + SSP-RK3 heat 1D/2D/3D),
+//     reproduced by orc_heat_accuracy() which follows diffusion{1,2,3}dTest.m literally;
+//   * recorded "Final Time" 0.325 / 0.329157 (SingleGPU/Diffusion2d/Run.m:11,
+//     SingleGPU/Diffusion3d_baselineCode/Run.m:11) via the reference dt rule;
+//   * recorded iteration counts 86 / 167 / 267 of the Burgers dt loop
+//     (SingleGPU/Burgers3d_WENO5/Run.m:24,36; SingleGPU/Burgers3d_WENO5_Hybrid2/Run.m:12).
+//
+// Built with -ffp-contract=off so x86 and Arm hosts give bitwise identical results.
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+// ------------------------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy as 1, 2, 3",
+// SC'11). Counter-based; used for every seeded synthetic input.
+// ------------------------------------------------------------------------------------------
+inline void philox4x32_10(const uint32_t ctr_in[4], const uint32_t key_in[2], uint32_t out[4]) {
+  uint32_t c0 = ctr_in[0], c1 = ctr_in[1], c2 = ctr_in[2], c3 = ctr_in[3];
+  uint32_t k0 = key_in[0], k1 = key_in[1];
+  for (int r = 0; r < 10; ++r) {
+    uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+    uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+    uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    uint32_t n0 = hi1 ^ c1 ^ k0;
+    uint32_t n2 = hi0 ^ c3 ^ k1;
+    c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+    k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+  }
+  out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+// Two uniforms in [0,1) with 53-bit resolution from draw `idx` of stream `stream`.
+inline void philox_u01x2(uint32_t seed, uint32_t stream, uint64_t idx, double* a, double* b) {
+  uint32_t ctr[4] = {(uint32_t)idx, (uint32_t)(idx >> 32), 0u, 0u};
+  uint32_t key[2] = {seed, stream};
+  uint32_t o[4];
+  philox4x32_10(ctr, key, o);
+  const double s = 1.0 / 9007199254740992.0;  // 2^-53
+  *a = (double)(((uint64_t)o[0] << 21) ^ (uint64_t)(o[1] >> 11)) * s;
+  *b = (double)(((uint64_t)o[2] << 21) ^ (uint64_t)(o[3] >> 11)) * s;
+}
+
+inline int64_t wrap(int64_t i, int64_t n) { i %= n; return i < 0 ? i + n : i; }
+
+// ------------------------------------------------------------------------------------------
+// Heat: one fused stage. Laplacian as SingleGPU/Diffusion3d_baselineCode/kernels.cu:37-99
+// (O2 7-pt / O4 13-pt, same operand order), 2D as SingleGPU/Diffusion2d/kernels.cu:70-88,
+// stage update as kernels.cu:104-142 (stage 1 == forward Euler).
+//   order:   2 -> k*(e - 2o + w) per axis; 4 -> k*(-ee + 16e - 30o + 16w - ww) per axis.
+//   frozen:  outer layers that are never updated (copied through); the reference freezes
+//            2 layers in 3D (kernels.cu:127) and 3 in 2D (Diffusion2d/kernels.cu:53).
+//   zero_boundary: the outermost layer is written as 0 (Dirichlet u=0).
+//   periodic: every node is updated and neighbours wrap.
+// ------------------------------------------------------------------------------------------
+struct HeatCfg {
+  int ndim, nx, ny, nz, order, frozen, zero_boundary, periodic;
+  double kx, ky, kz, dt;
+};
+
+template <class T>
+inline T stage_combine(int stage, T un, T uin, T dt, T L) {
+  switch (stage) {
+    case 2: return (T)0.75 * un + (T)0.25 * (uin + dt * L);
+    case 3: return (un + (T)2 * (uin + dt * L)) / (T)3;
+    default: return un + dt * L;
+  }
+}
+
+template <class T>
+void heat_stage(const HeatCfg& c, int stage, const T* uin, const T* un, T* out) {
+  const int64_t nx = c.nx, ny = c.ny, nz = (c.ndim == 3) ? c.nz : 1;
+  const int64_t sx = 1, sy = nx, sz = nx * ny;
+  const T kx = (T)c.kx, ky = (T)c.ky, kz = (T)c.kz, dt = (T)c.dt;
+  const int F = c.periodic ? 0 : c.frozen;
+#pragma omp parallel for collapse(2) schedule(static)
+  for (int64_t k = 0; k < nz; ++k)
+    for (int64_t j = 0; j < ny; ++j)
+      for (int64_t i = 0; i < nx; ++i) {
+        const int64_t o = i + nx * j + sz * k;
+        bool interior = i >= F && i < nx - F && j >= F && j < ny - F;
+        if (c.ndim == 3) interior = interior && k >= F && k < nz - F;
+        if (!interior) {
+          bool outer = i == 0 || i == nx - 1 || j == 0 || j == ny - 1;
+          if (c.ndim == 3) outer = outer || k == 0 || k == nz - 1;
+          out[o] = (c.zero_boundary && outer) ? (T)0 : uin[o];
+          continue;
+        }
+        auto at = [&](int64_t di, int64_t dj, int64_t dk) -> T {
+          if (c.periodic)
+            return uin[wrap(i + di, nx) + nx * wrap(j + dj, ny) + sz * wrap(k + dk, nz)];
+          return uin[o + di * sx + dj * sy + dk * sz];
+        };
+        const T uo = uin[o];
+        T L;
+        if (c.order == 4 && c.ndim == 2) {
+          // 2D operand order is west/south first (SingleGPU/Diffusion2d/kernels.cu:82-83).
+          T Sx = -at(-2, 0, 0) + (T)16 * at(-1, 0, 0) - (T)30 * uo + (T)16 * at(1, 0, 0) - at(2, 0, 0);
+          T Sy = -at(0, -2, 0) + (T)16 * at(0, -1, 0) - (T)30 * uo + (T)16 * at(0, 1, 0) - at(0, 2, 0);
+          L = kx * Sx + ky * Sy;
+        } else if (c.order == 4) {
+          // 3D operand order is east/north/top first (Diffusion3d_baselineCode/kernels.cu:95-97).
+          T Sx = -at(2, 0, 0) + (T)16 * at(1, 0, 0) - (T)30 * uo + (T)16 * at(-1, 0, 0) - at(-2, 0, 0);
+          T Sy = -at(0, 2, 0) + (T)16 * at(0, 1, 0) - (T)30 * uo + (T)16 * at(0, -1, 0) - at(0, -2, 0);
+          L = kx * Sx + ky * Sy;
+          if (c.ndim == 3) {
+            T Sz = -at(0, 0, 2) + (T)16 * at(0, 0, 1) - (T)30 * uo + (T)16 * at(0, 0, -1) - at(0, 0, -2);
+            L = L + kz * Sz;
+          }
+        } else {
+          T Sx = at(1, 0, 0) - (T)2 * uo + at(-1, 0, 0);
+          T Sy = at(0, 1, 0) - (T)2 * uo + at(0, -1, 0);
+          L = kx * Sx + ky * Sy;
+          if (c.ndim == 3) {
+            T Sz = at(0, 0, 1) - (T)2 * uo + at(0, 0, -1);
+            L = L + kz * Sz;
+          }
+        }
+        out[o] = stage_combine<T>(stage, un[o], uo, dt, L);
+      }
+}
+
+// Fixed-step run: `time`==0 forward Euler, `time`==1 SSP-RK3 (the reference's heat loop,
+// SingleGPU/Diffusion3d_baselineCode/main.cpp:106-122). Result left in u.
+template <class T>
+void heat_run(const HeatCfg& c, int time, int64_t nsteps, T* u) {
+  const size_t n = (size_t)c.nx * c.ny * (c.ndim == 3 ? c.nz : 1);
+  std::vector<T> a(n), b(n);
+  for (int64_t s = 0; s < nsteps; ++s) {
+    if (time == 0) {
+      heat_stage<T>(c, 1, u, u, a.data());
+      std::memcpy(u, a.data(), n * sizeof(T));
+    } else {
+      heat_stage<T>(c, 1, u, u, a.data());
+      heat_stage<T>(c, 2, a.data(), u, b.data());
+      heat_stage<T>(c, 3, b.data(), u, a.data());
+      std::memcpy(u, a.data(), n * sizeof(T));
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// Burgers. Flux f = u^2/2 (SingleGPU/Burgers3d_WENO5/kernels.cu:37-40), Lax-Friedrichs split
+// f+- = (f +- a u)/2 (kernels.cu:224-238; a = |u| local, or a = max|u| global as in
+// Matlab_Prototipes/InviscidBurgersNd/LFWENO5FDM3d.m:71 with a scalar). Face flux
+// F_{i+1/2} = WENO(f+ at i-2..i+2) + WENO(f- at i-1..i+3): WENO5-Z as kernels.cu:142-192,
+// WENO5-JS as kernels.cu:92-140 (= MultiGPU/Burgers3d_Baseline/Kernels.cu:112-222).
+// The divisions of the smoothness-indicator weights run in type D.
+// ------------------------------------------------------------------------------------------
+template <class T, class D>
+inline T weno_face(int z, T vmm, T vm, T v, T vp, T vpp, T umm, T um, T u, T up, T upp) {
+  const T c1312 = (T)(13. / 12.), c14 = (T)(1. / 4.);
+  const D eps = (D)1e-6;
+  T B0 = c1312 * (vmm - (T)2 * vm + v) * (vmm - (T)2 * vm + v) + c14 * (vmm - (T)4 * vm + (T)3 * v) * (vmm - (T)4 * vm + (T)3 * v);
+  T B1 = c1312 * (vm - (T)2 * v + vp) * (vm - (T)2 * v + vp) + c14 * (vm - vp) * (vm - vp);
+  T B2 = c1312 * (v - (T)2 * vp + vpp) * (v - (T)2 * vp + vpp) + c14 * ((T)3 * v - (T)4 * vp + vpp) * ((T)3 * v - (T)4 * vp + vpp);
+  D a0, a1, a2;
+  if (z) {
+    D tau5 = std::fabs((D)B0 - (D)B2);
+    a0 = (D)(1. / 10.) * ((D)1 + tau5 / ((D)B0 + eps));
+    a1 = (D)(6. / 10.) * ((D)1 + tau5 / ((D)B1 + eps));
+    a2 = (D)(3. / 10.) * ((D)1 + tau5 / ((D)B2 + eps));
+  } else {
+    a0 = (D)(1. / 10.) / ((eps + (D)B0) * (eps + (D)B0));
+    a1 = (D)(6. / 10.) / ((eps + (D)B1) * (eps + (D)B1));
+    a2 = (D)(3. / 10.) / ((eps + (D)B2) * (eps + (D)B2));
+  }
+  D asum = a0 + a1 + a2;
+  D fm = (a0 * (D)((T)2 * vmm - (T)7 * vm + (T)11 * v) + a1 * (D)(-vm + (T)5 * v + (T)2 * vp) +
+          a2 * (D)((T)2 * v + (T)5 * vp - vpp)) / ((D)6 * asum);
+
+  B0 = c1312 * (umm - (T)2 * um + u) * (umm - (T)2 * um + u) + c14 * (umm - (T)4 * um + (T)3 * u) * (umm - (T)4 * um + (T)3 * u);
+  B1 = c1312 * (um - (T)2 * u + up) * (um - (T)2 * u + up) + c14 * (um - up) * (um - up);
+  B2 = c1312 * (u - (T)2 * up + upp) * (u - (T)2 * up + upp) + c14 * ((T)3 * u - (T)4 * up + upp) * ((T)3 * u - (T)4 * up + upp);
+  if (z) {
+    D tau5 = std::fabs((D)B0 - (D)B2);
+    a0 = (D)(3. / 10.) * ((D)1 + tau5 / ((D)B0 + eps));
+    a1 = (D)(6. / 10.) * ((D)1 + tau5 / ((D)B1 + eps));
+    a2 = (D)(1. / 10.) * ((D)1 + tau5 / ((D)B2 + eps));
+  } else {
+    a0 = (D)(3. / 10.) / ((eps + (D)B0) * (eps + (D)B0));
+    a1 = (D)(6. / 10.) / ((eps + (D)B1) * (eps + (D)B1));
+    a2 = (D)(1. / 10.) / ((eps + (D)B2) * (eps + (D)B2));
+  }
+  asum = a0 + a1 + a2;
+  D fp = (a0 * (D)(-umm + (T)5 * um + (T)2 * u) + a1 * (D)((T)2 * um + (T)5 * u - up) +
+          a2 * (D)((T)11 * u - (T)7 * up + (T)2 * upp)) / ((D)6 * asum);
+  return (T)fm + (T)fp;
+}
+
+struct BurgersCfg {
+  int nx, ny, nz;
+  int weno_z;     // 1: WENO5-Z, 0: WENO5-JS
+  int lf_global;  // 1: a = max|u| of the stage input, 0: a = |u| per node
+  int periodic;   // 1: periodic wrap; 0: reference frozen boundary (3 layers)
+  int bug_b2;     // reproduce the doubled viscous slabs 16..18 of the reference
+  double dx, dy, dz;
+  double kx, ky, kz;  // viscous O4 coefficients C/(12 h^2); 0 disables the term
+};
+
+template <class T>
+inline void lf_split(T u, T a_glob, int global, T* fp, T* fm) {
+  T f = (T)0.5 * u * u;
+  T a = global ? a_glob : std::fabs(u);
+  *fp = (T)0.5 * (f + a * u);
+  *fm = (T)0.5 * (f - a * u);
+}
+
+// Face flux at +1/2 of position p along an axis: cells p-2..p+3 given by `get`.
+template <class T, class D, class G>
+inline T face_flux(const BurgersCfg& c, T a_glob, G get) {
+  T fp[6], fm[6];
+  for (int q = 0; q < 6; ++q) lf_split<T>(get(q - 2), a_glob, c.lf_global, &fp[q], &fm[q]);
+  return weno_face<T, D>(c.weno_z, fp[0], fp[1], fp[2], fp[3], fp[4], fm[1], fm[2], fm[3], fm[4], fm[5]);
+}
+
+// Right-hand side Lu at every updated cell (others untouched). Accumulation order follows
+// the reference's sweeps: Lu = -(dF)/dx; Lu -= dG/dy; Lu -= dH/dz; Lu += viscous
+// (SingleGPU/Burgers3d_WENO5/main.cpp:143-149; kernels.cu:197-494).
+template <class T, class D>
+void burgers_rhs(const BurgersCfg& c, const T* u, T a_glob, T* Lu) {
+  const int64_t nx = c.nx, ny = c.ny, nz = c.nz, sz = nx * ny;
+  const int F = c.periodic ? 0 : 3;
+  const T dx = (T)c.dx, dy = (T)c.dy, dz = (T)c.dz;
+  const T kx = (T)c.kx, ky = (T)c.ky, kz = (T)c.kz;
+  const bool visc = c.kx != 0.0 || c.ky != 0.0 || c.kz != 0.0;
+#pragma omp parallel for collapse(2) schedule(static)
+  for (int64_t k = F; k < nz - F; ++k)
+    for (int64_t j = F; j < ny - F; ++j)
+      for (int64_t i = F; i < nx - F; ++i) {
+        const int64_t o = i + nx * j + sz * k;
+        auto U = [&](int64_t ii, int64_t jj, int64_t kk) -> T {
+          if (c.periodic) return u[wrap(ii, nx) + nx * wrap(jj, ny) + sz * wrap(kk, nz)];
+          return u[ii + nx * jj + sz * kk];
+        };
+        T fxp = face_flux<T, D>(c, a_glob, [&](int q) { return U(i + q, j, k); });
+        T fxm = face_flux<T, D>(c, a_glob, [&](int q) { return U(i - 1 + q, j, k); });
+        T fyp = face_flux<T, D>(c, a_glob, [&](int q) { return U(i, j + q, k); });
+        T fym = face_flux<T, D>(c, a_glob, [&](int q) { return U(i, j - 1 + q, k); });
+        T fzp = face_flux<T, D>(c, a_glob, [&](int q) { return U(i, j, k + q); });
+        T fzm = face_flux<T, D>(c, a_glob, [&](int q) { return U(i, j, k - 1 + q); });
+        T L = -(fxp - fxm) / dx;
+        L = L - (fyp - fym) / dy;
+        L = L - (fzp - fzm) / dz;
+        if (visc) {
+          const T ce = u[o];
+          T v = kx * (-U(i - 2, j, k) + (T)16 * U(i - 1, j, k) - (T)30 * ce + (T)16 * U(i + 1, j, k) - U(i + 2, j, k)) +
+                ky * (-U(i, j - 2, k) + (T)16 * U(i, j - 1, k) - (T)30 * ce + (T)16 * U(i, j + 1, k) - U(i, j + 2, k)) +
+                kz * (-U(i, j, k - 2) + (T)16 * U(i, j, k - 1) - (T)30 * ce + (T)16 * U(i, j, k + 1) - U(i, j, k + 2));
+          L = L + v;
+          // Reference bug B2: Compute_Laplace_Async's first z-block starts at max(kstart,0)=3 but
+          // still runs LOOP=16 slabs, so slabs 16..18 are added twice (kernels.cu:464-491).
+          if (c.bug_b2 && !c.periodic && k >= 16 && k <= 18 && k <= nz - 3) L = L + v;
+        }
+        Lu[o] = L;
+      }
+}
+
+template <class T>
+T max_abs(const T* u, size_t n) {
+  T m = 0;
+#pragma omp parallel for reduction(max : m) schedule(static)
+  for (size_t i = 0; i < n; ++i) m = std::max(m, (T)std::fabs(u[i]));
+  return m;
+}
+
+// One SSP-RK3 stage: out = combine(un, uin, dt, Lu) on updated cells, uin elsewhere.
+template <class T>
+void burgers_combine(const BurgersCfg& c, int stage, const T* uin, const T* un, const T* Lu, T dt, T* out) {
+  const int64_t nx = c.nx, ny = c.ny, nz = c.nz;
+  const int F = c.periodic ? 0 : 3;
+#pragma omp parallel for collapse(2) schedule(static)
+  for (int64_t k = 0; k < nz; ++k)
+    for (int64_t j = 0; j < ny; ++j)
+      for (int64_t i = 0; i < nx; ++i) {
+        const int64_t o = i + nx * j + nx * ny * k;
+        bool interior = i >= F && i < nx - F && j >= F && j < ny - F && k >= F && k < nz - F;
+        out[o] = interior ? stage_combine<T>(stage, un[o], uin[o], dt, Lu[o]) : uin[o];
+      }
+}
+
+template <class T, class D>
+void burgers_stage(const BurgersCfg& c, int stage, const T* uin, const T* un, double dt, T* out, T* Lu_scratch) {
+  const size_t n = (size_t)c.nx * c.ny * c.nz;
+  T a = c.lf_global ? max_abs<T>(uin, n) : (T)0;
+  burgers_rhs<T, D>(c, uin, a, Lu_scratch);
+  burgers_combine<T>(c, stage, uin, un, Lu_scratch, (T)dt, out);
+}
+
+// Time loop. dt_rule 0: reference fixed dt = min(CFL*dx/1.0, 0.9/(2C sum 1/h^2))
+// (SingleGPU/Burgers3d_WENO5/main.cpp:127-136; C from the viscous coefficient, the second
+// bound dropped when C == 0). dt_rule 1: dt = CFL*dx/max|u^n| (LFWENO5FDM3d.m:71).
+// Both trim the last step to hit tEnd and accumulate t in FP64.
+template <class T, class D>
+int64_t burgers_run(const BurgersCfg& c, T* u, double tEnd, double CFL, int dt_rule, double C,
+                    int64_t max_steps, double* t_out) {
+  const size_t n = (size_t)c.nx * c.ny * c.nz;
+  std::vector<T> a(n), b(n), Lu(n, (T)0);
+  double t = 0.0;
+  int64_t it = 0;
+  while (t < tEnd && it < max_steps) {
+    double dt;
+    if (dt_rule == 0) {
+      double dt1 = CFL * c.dx / 1.0;
+      double dt2 = (C > 0) ? 1. / (2 * C * (1 / c.dx / c.dx + 1 / c.dy / c.dy + 1 / c.dz / c.dz)) * 0.9
+                           : std::numeric_limits<double>::infinity();
+      dt = dt1 < dt2 ? dt1 : dt2;
+    } else {
+      dt = CFL * c.dx / (double)max_abs<T>(u, n);
+    }
+    if ((t + dt) > tEnd) dt = tEnd - t;
+    t += dt;
+    it += 1;
+    burgers_stage<T, D>(c, 1, u, u, dt, a.data(), Lu.data());
+    burgers_stage<T, D>(c, 2, a.data(), u, dt, b.data(), Lu.data());
+    burgers_stage<T, D>(c, 3, b.data(), u, dt, a.data(), Lu.data());
+    std::memcpy(u, a.data(), n * sizeof(T));
+  }
+  if (t_out) *t_out = t;
+  return it;
+}
+
+}  // namespace
+
+extern "C" {
+
+// ----------------------------------------------------------------------------- RNG
+void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+  philox4x32_10(ctr, key, out);
+}
+void orc_philox_u01x2(uint32_t seed, uint32_t stream, uint64_t idx, double* a, double* b) {
+  philox_u01x2(seed, stream, idx, a, b);
+}
+
+int orc_num_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+void orc_set_num_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
+
+// ----------------------------------------------------------------------------- heat
+#define HEAT_CFG                                                                             \
+  HeatCfg c{ndim, nx, ny, nz, order, frozen, zero_boundary, periodic, kx, ky, kz, dt};
+
+void orc_heat_stage_f64(int ndim, int nx, int ny, int nz, int order, int frozen, int zero_boundary,
+                        int periodic, double kx, double ky, double kz, double dt, int stage,
+                        const double* uin, const double* un, double* out) {
+  HEAT_CFG heat_stage<double>(c, stage, uin, un, out);
+}
+void orc_heat_stage_f32(int ndim, int nx, int ny, int nz, int order, int frozen, int zero_boundary,
+                        int periodic, double kx, double ky, double kz, double dt, int stage,
+                        const float* uin, const float* un, float* out) {
+  HEAT_CFG heat_stage<float>(c, stage, uin, un, out);
+}
+void orc_heat_run_f64(int ndim, int nx, int ny, int nz, int order, int frozen, int zero_boundary,
+                      int periodic, double kx, double ky, double kz, double dt, int time,
+                      int64_t nsteps, double* u) {
+  HEAT_CFG heat_run<double>(c, time, nsteps, u);
+}
+void orc_heat_run_f32(int ndim, int nx, int ny, int nz, int order, int frozen, int zero_boundary,
+                      int periodic, double kx, double ky, double kz, double dt, int time,
+                      int64_t nsteps, float* u) {
+  HEAT_CFG heat_run<float>(c, time, nsteps, u);
+}
+
+// Reference heat dt and final time (SingleGPU/Diffusion3d_baselineCode/main.cpp:55-63,
+// SingleGPU/Diffusion2d/main.cpp:52-58). L/W/H are integers there (parsed with atoi).
+void orc_heat_ref_constants(int ndim, double C, int L, int W, int H, int nx, int ny, int nz,
+                            int iters, double* dx, double* dy, double* dz, double* dt,
+                            double* k_x, double* k_y, double* k_z, double* tFinal) {
+  *dx = (double)L / (nx - 1);
+  *dy = (double)W / (ny - 1);
+  *dz = (ndim == 3) ? (double)H / (nz - 1) : 0.0;
+  if (ndim == 3)
+    *dt = 1 / (2 * C * (1 / *dx / *dx + 1 / *dy / *dy + 1 / *dz / *dz)) * 0.9;
+  else
+    *dt = 1 / (2 * C * (1 / *dx / *dx + 1 / *dy / *dy)) * 0.9;
+  *k_x = C / (12 * *dx * *dx);
+  *k_y = C / (12 * *dy * *dy);
+  *k_z = (ndim == 3) ? C / (12 * *dz * *dz) : 0.0;
+  *tFinal = 0.1 + *dt * iters;
+}
+
+// Reference heat initial condition 3 (SingleGPU/Diffusion3d_baselineCode/tools.cpp:128-139 with
+// EXP_DISTRIBUTION of acoustics3d.h:29; 2D: SingleGPU/Diffusion2d/tools.cpp:109-119).
+void orc_ic_heat_ref(int ndim, int nx, int ny, int nz, double dx, double dy, double dz, double* u) {
+  const int NZ = ndim == 3 ? nz : 1;
+  for (int k = 0; k < NZ; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        size_t o = (size_t)i + (size_t)nx * j + (size_t)nx * ny * k;
+        double r2 = (-5 + i * dx) * (-5 + i * dx) + (-5 + j * dy) * (-5 + j * dy);
+        if (ndim == 3) r2 += (-5 + k * dz) * (-5 + k * dz);
+        u[o] = std::exp(-(r2) / (4 * 1.0 * 0.1));
+        bool face = i == 0 || i == nx - 1 || j == 0 || j == ny - 1;
+        if (ndim == 3) face = face || k == 0 || k == nz - 1;
+        if (face) u[o] = 0.0;
+      }
+}
+
+// MATLAB accuracy study, literal: Matlab_Prototipes/DiffusionNd/diffusion{1,2,3}dTest.m with
+// Laplace{1,2,3}d.m ("OMP" index range in 3D, Laplace3d.m:38-53). O4 + SSP-RK3, outermost layer
+// reset to 0 after each step, dt trimmed AFTER the step and t advanced by the trimmed dt
+// (diffusion3dTest.m:55-68). Returns the number of steps; L1/L2/Linf as the .m files print them.
+int orc_heat_accuracy(int dim, int nc, double tFinal, double param, double* L1, double* L2,
+                      double* Linf) {
+  const double D = 1.0, t0 = 0.1, L = 10.0;
+  const double dx = L / (nc - 1);
+  const double Dx = D / (dx * dx);
+  const int nx = nc, ny = dim >= 2 ? nc : 1, nz = dim == 3 ? nc : 1;
+  const size_t n = (size_t)nx * ny * nz;
+  std::vector<double> u(n), uo(n), dF(n), uE(n);
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        double x = -L / 2 + i * dx, y = -L / 2 + j * dx, z = -L / 2 + k * dx;
+        double r2 = x * x;
+        if (dim >= 2) r2 += y * y;
+        if (dim == 3) r2 += z * z;
+        size_t o = (size_t)i + (size_t)nx * j + (size_t)nx * ny * k;
+        u[o] = std::exp(-r2 / (4 * 1.0 * t0));
+        double amp = dim == 1 ? std::sqrt(t0 / tFinal) : dim == 2 ? t0 / tFinal : std::pow(t0 / tFinal, 1.5);
+        uE[o] = amp * std::exp(-r2 / (4 * 1.0 * tFinal));
+      }
+  double dt;
+  if (dim == 1) dt = 1 / (2 * D * (1 / (dx * dx))) * param;
+  else if (dim == 2) dt = 1 / (2 * D * (1 / (dx * dx) + 1 / (dx * dx))) * param;
+  else dt = 1 / (2 * D * (1 / (dx * dx) + 1 / (dx * dx) + 1 / (dx * dx))) * param;
+
+  auto lap = [&](const std::vector<double>& w) {
+    std::fill(dF.begin(), dF.end(), 0.0);
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+          bool in = i >= 2 && i <= nx - 3;
+          if (dim >= 2) in = in && j >= 2 && j <= ny - 3;
+          if (dim == 3) in = in && k >= 2 && k <= nz - 3;
+          if (!in) continue;
+          size_t o = (size_t)i + (size_t)nx * j + (size_t)nx * ny * k;
+          size_t sy = nx, sz = (size_t)nx * ny;
+          double v = Dx / 12 * (-w[o + 2] + 16 * w[o + 1] - 30 * w[o] + 16 * w[o - 1] - w[o - 2]);
+          if (dim >= 2) v = v + Dx / 12 * (-w[o + 2 * sy] + 16 * w[o + sy] - 30 * w[o] + 16 * w[o - sy] - w[o - 2 * sy]);
+          if (dim == 3) v = v + Dx / 12 * (-w[o + 2 * sz] + 16 * w[o + sz] - 30 * w[o] + 16 * w[o - sz] - w[o - 2 * sz]);
+          dF[o] = v;
+        }
+  };
+  double t = t0;
+  int it = 0;
+  while (t < tFinal) {
+    uo = u;
+    lap(u);
+    for (size_t o = 0; o < n; ++o) u[o] = uo[o] + dt * dF[o];
+    lap(u);
+    for (size_t o = 0; o < n; ++o) u[o] = 0.75 * uo[o] + 0.25 * (u[o] + dt * dF[o]);
+    lap(u);
+    for (size_t o = 0; o < n; ++o) u[o] = (uo[o] + 2 * (u[o] + dt * dF[o])) / 3;
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+          bool b = i == 0 || i == nx - 1;
+          if (dim >= 2) b = b || j == 0 || j == ny - 1;
+          if (dim == 3) b = b || k == 0 || k == nz - 1;
+          if (b) u[(size_t)i + (size_t)nx * j + (size_t)nx * ny * k] = 0.0;
+        }
+    if (t + dt > tFinal) dt = tFinal - t;
+    it = it + 1;
+    t = t + dt;
+  }
+  const double vol = dim == 1 ? dx : dim == 2 ? dx * dx : dx * dx * dx;
+  double s1 = 0, s2 = 0, mx = 0;
+  for (size_t o = 0; o < n; ++o) {
+    double e = std::fabs(uE[o] - u[o]);
+    s1 += e;
+    s2 += e * e;
+    mx = std::max(mx, e);
+  }
+  *L1 = vol * s1;
+  *L2 = std::sqrt(vol * s2);
+  *Linf = mx;
+  return it;
+}
+
+// Seeded configuration initial conditions (all draws from Philox4x32-10).
+// 2D: exp(-((x-.5)^2+(y-.5)^2)/0.01) + N(0, sigma^2) on nodes x_i = i/(n-1); boundary = 0.
+// Noise draw for node o uses stream 1, index o (Box-Muller on the two uniforms).
+void orc_ic_heat2d_gauss_noise(int nx, int ny, uint32_t seed, double sigma, double* u) {
+  const double hx = 1.0 / (nx - 1), hy = 1.0 / (ny - 1);
+  const double two_pi = 6.283185307179586476925286766559;
+  for (int j = 0; j < ny; ++j)
+    for (int i = 0; i < nx; ++i) {
+      size_t o = (size_t)i + (size_t)nx * j;
+      double x = i * hx, y = j * hy;
+      double g = std::exp(-((x - 0.5) * (x - 0.5) + (y - 0.5) * (y - 0.5)) / 0.01);
+      double a, b;
+      philox_u01x2(seed, 1u, (uint64_t)o, &a, &b);
+      double z = std::sqrt(-2.0 * std::log(1.0 - a)) * std::cos(two_pi * b);
+      u[o] = g + sigma * z;
+      if (i == 0 || i == nx - 1 || j == 0 || j == ny - 1) u[o] = 0.0;
+    }
+}
+
+// Blob parameters: blob m uses stream 2, draws 2m and 2m+1 -> (cx, cy), (cz, sigma).
+void orc_heat3d_blob_params(uint32_t seed, int nblobs, double* params /* 4*nblobs */) {
+  for (int m = 0; m < nblobs; ++m) {
+    double a, b, c, d;
+    philox_u01x2(seed, 2u, (uint64_t)(2 * m), &a, &b);
+    philox_u01x2(seed, 2u, (uint64_t)(2 * m + 1), &c, &d);
+    params[4 * m + 0] = 0.2 + 0.6 * a;
+    params[4 * m + 1] = 0.2 + 0.6 * b;
+    params[4 * m + 2] = 0.2 + 0.6 * c;
+    params[4 * m + 3] = 0.02 + 0.06 * d;
+  }
+}
+
+// 3D: sum of blobs exp(-|x-c|^2/(2 sigma^2)) on nodes x_i = i/(n-1) of [0,1]^3; boundary = 0.
+void orc_ic_heat3d_blobs(int nx, int ny, int nz, uint32_t seed, int nblobs, double* u) {
+  std::vector<double> p(4 * (size_t)nblobs);
+  orc_heat3d_blob_params(seed, nblobs, p.data());
+  const double hx = 1.0 / (nx - 1), hy = 1.0 / (ny - 1), hz = 1.0 / (nz - 1);
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        size_t o = (size_t)i + (size_t)nx * j + (size_t)nx * ny * k;
+        double x = i * hx, y = j * hy, z = k * hz, s = 0.0;
+        for (int m = 0; m < nblobs; ++m) {
+          double ddx = x - p[4 * m], ddy = y - p[4 * m + 1], ddz = z - p[4 * m + 2], sg = p[4 * m + 3];
+          s += std::exp(-(ddx * ddx + ddy * ddy + ddz * ddz) / (2 * sg * sg));
+        }
+        bool face = i == 0 || i == nx - 1 || j == 0 || j == ny - 1 || k == 0 || k == nz - 1;
+        u[o] = face ? 0.0 : s;
+      }
+}
+
+// Fourier-mode parameters: mode m draws (stream 3) wave vectors n in [-4,4]^3 \ {0} with
+// |n| <= 4 by rejection (draw index advanced per attempt), then amplitude a ~ U[0, amax]
+// and phase ~ U[0, 2 pi) from stream 4, index m. params = (n1, n2, n3, a, phi) per mode.
+void orc_burgers_fourier_params(uint32_t seed, int nmodes, double amax, double* params) {
+  const double two_pi = 6.283185307179586476925286766559;
+  uint64_t idx = 0;
+  for (int m = 0; m < nmodes; ++m) {
+    int n1, n2, n3;
+    for (;;) {
+      double a, b, c, d;
+      philox_u01x2(seed, 3u, idx++, &a, &b);
+      philox_u01x2(seed, 3u, idx++, &c, &d);
+      n1 = (int)std::floor(a * 9.0) - 4;
+      n2 = (int)std::floor(b * 9.0) - 4;
+      n3 = (int)std::floor(c * 9.0) - 4;
+      int r2 = n1 * n1 + n2 * n2 + n3 * n3;
+      if (r2 > 0 && r2 <= 16) break;
+    }
+    double a, b;
+    philox_u01x2(seed, 4u, (uint64_t)m, &a, &b);
+    params[5 * m + 0] = n1;
+    params[5 * m + 1] = n2;
+    params[5 * m + 2] = n3;
+    params[5 * m + 3] = amax * a;
+    params[5 * m + 4] = two_pi * b;
+  }
+}
+
+// u0 = 0.5 + sum_m a_m cos(pi n_m . x + phi_m) on the periodic cell centres
+// x_i = (i + 1/2) L/N of [0, L)^3 (L = 2).
+void orc_ic_burgers_fourier(int nx, int ny, int nz, double L, uint32_t seed, int nmodes,
+                            double amax, double* u) {
+  std::vector<double> p(5 * (size_t)nmodes);
+  orc_burgers_fourier_params(seed, nmodes, amax, p.data());
+  const double pi = 3.14159265358979323846264338327950288;
+  const double hx = L / nx, hy = L / ny, hz = L / nz;
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        double x = (i + 0.5) * hx, y = (j + 0.5) * hy, z = (k + 0.5) * hz, s = 0.5;
+        for (int m = 0; m < nmodes; ++m)
+          s += p[5 * m + 3] * std::cos(pi * (p[5 * m] * x + p[5 * m + 1] * y + p[5 * m + 2] * z) + p[5 * m + 4]);
+        u[(size_t)i + (size_t)nx * j + (size_t)nx * ny * k] = s;
+      }
+}
+
+// Reference Burgers initial condition 3 (SingleGPU/Burgers3d_WENO5/tools.cpp:126-137,
+// GAUSSIAN_DISTRIBUTION of Burgers.h:41) at nodes (i dx, j dy, k dz).
+void orc_ic_burgers_ref(int nx, int ny, int nz, double dx, double dy, double dz, double* u) {
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        double x = i * dx, y = j * dy, z = k * dz;
+        u[(size_t)i + (size_t)nx * j + (size_t)nx * ny * k] =
+            1.0 * std::exp(-((x - 1.0) * (x - 1.0) + (y - 1.0) * (y - 1.0) + (z - 1.0) * (z - 1.0)) / 0.1);
+      }
+}
+
+// ----------------------------------------------------------------------------- Burgers
+#define BURG_CFG                                                                               \
+  BurgersCfg c{nx, ny, nz, weno_z, lf_global, periodic, bug_b2, dx, dy, dz, kx, ky, kz};
+#define BURG_ARGS                                                                              \
+  int nx, int ny, int nz, int weno_z, int lf_global, int periodic, int bug_b2, double dx,      \
+      double dy, double dz, double kx, double ky, double kz
+
+void orc_burgers_rhs_f64(BURG_ARGS, const double* u, double a_glob, double* Lu) {
+  BURG_CFG burgers_rhs<double, double>(c, u, a_glob, Lu);
+}
+// FP32 state with `div64` selecting FP64 (1) or FP32 (0) weight divisions.
+void orc_burgers_rhs_f32(BURG_ARGS, int div64, const float* u, float a_glob, float* Lu) {
+  BURG_CFG if (div64) burgers_rhs<float, double>(c, u, a_glob, Lu);
+  else burgers_rhs<float, float>(c, u, a_glob, Lu);
+}
+void orc_burgers_stage_f64(BURG_ARGS, int stage, const double* uin, const double* un, double dt,
+                           double* out, double* Lu) {
+  BURG_CFG burgers_stage<double, double>(c, stage, uin, un, dt, out, Lu);
+}
+void orc_burgers_stage_f32(BURG_ARGS, int div64, int stage, const float* uin, const float* un,
+                           double dt, float* out, float* Lu) {
+  BURG_CFG if (div64) burgers_stage<float, double>(c, stage, uin, un, dt, out, Lu);
+  else burgers_stage<float, float>(c, stage, uin, un, dt, out, Lu);
+}
+int64_t orc_burgers_run_f64(BURG_ARGS, double* u, double tEnd, double CFL, int dt_rule, double C,
+                            int64_t max_steps, double* t_out) {
+  BURG_CFG return burgers_run<double, double>(c, u, tEnd, CFL, dt_rule, C, max_steps, t_out);
+}
+int64_t orc_burgers_run_f32(BURG_ARGS, int div64, float* u, double tEnd, double CFL, int dt_rule,
+                            double C, int64_t max_steps, double* t_out) {
+  BURG_CFG if (div64) return burgers_run<float, double>(c, u, tEnd, CFL, dt_rule, C, max_steps, t_out);
+  return burgers_run<float, float>(c, u, tEnd, CFL, dt_rule, C, max_steps, t_out);
+}
+
+// Reference Burgers dt loop alone (no field update): number of steps and final t
+// (SingleGPU/Burgers3d_WENO5/main.cpp:127-136).
+int64_t orc_burgers_ref_steps(double tEnd, double CFL, double L, double W, double H, int nx, int ny,
+                              int nz, double C, double* t_out) {
+  double dx = L / (nx - 1), dy = W / (ny - 1), dz = H / (nz - 1);
+  double t = 0, dt;
+  int64_t it = 0;
+  while (t < tEnd) {
+    double dt1 = CFL * dx / 1.0;
+    double dt2 = 1. / (2 * C * (1 / dx / dx + 1 / dy / dy + 1 / dz / dz)) * 0.9;
+    dt = dt1 < dt2 ? dt1 : dt2;
+    if ((t + dt) > tEnd) dt = tEnd - t;
+    t += dt;
+    it += 1;
+  }
+  *t_out = t;
+  return it;
+}
+
+double orc_max_abs_f64(const double* u, int64_t n) { return max_abs<double>(u, (size_t)n); }
+float orc_max_abs_f32(const float* u, int64_t n) { return max_abs<float>(u, (size_t)n); }
+
+}  // extern "C"

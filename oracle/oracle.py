@@ -1,0 +1,203 @@
+"""Python handle on the CPU oracle (advdiff_oracle.cpp) -- TEST INFRASTRUCTURE ONLY.
+
+The oracle restates the reference's schemes in FP64 (and FP32 for error-floor studies). Only the
+tests, the smoke check and the benchmark's CPU-baseline leg use it; the product never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+SO = HERE / "_build" / "liboracle.so"
+SRC = HERE / "advdiff_oracle.cpp"
+
+_lib = None
+_D, _I, _I64, _U32 = C.c_double, C.c_int, C.c_int64, C.c_uint32
+_PD = C.POINTER(C.c_double)
+_HEAT = [_I, _I, _I, _I, _I, _I, _I, _I, _D, _D, _D, _D]
+_BURG = [_I, _I, _I, _I, _I, _I, _I, _D, _D, _D, _D, _D, _D]
+
+
+def build() -> Path:
+    """Compiles liboracle.so with g++ (the same flags as oracle/Makefile)."""
+    if not SO.exists() or SO.stat().st_mtime < SRC.stat().st_mtime:
+        SO.parent.mkdir(parents=True, exist_ok=True)
+        cxx = os.environ.get("CXX", "g++")
+        subprocess.run([cxx, "-O3", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
+                        "-o", str(SO), str(SRC)], check=True)
+    return SO
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(str(SO))
+        sig = {
+            "orc_heat_stage_f64": (None, _HEAT + [_I, C.c_void_p, C.c_void_p, C.c_void_p]),
+            "orc_heat_stage_f32": (None, _HEAT + [_I, C.c_void_p, C.c_void_p, C.c_void_p]),
+            "orc_heat_run_f64": (None, _HEAT + [_I, _I64, C.c_void_p]),
+            "orc_heat_run_f32": (None, _HEAT + [_I, _I64, C.c_void_p]),
+            "orc_heat_ref_constants": (None, [_I, _D, _I, _I, _I, _I, _I, _I, _I] + [_PD] * 8),
+            "orc_ic_heat_ref": (None, [_I, _I, _I, _I, _D, _D, _D, C.c_void_p]),
+            "orc_heat_accuracy": (_I, [_I, _I, _D, _D, _PD, _PD, _PD]),
+            "orc_ic_heat2d_gauss_noise": (None, [_I, _I, _U32, _D, C.c_void_p]),
+            "orc_heat3d_blob_params": (None, [_U32, _I, C.c_void_p]),
+            "orc_ic_heat3d_blobs": (None, [_I, _I, _I, _U32, _I, C.c_void_p]),
+            "orc_burgers_fourier_params": (None, [_U32, _I, _D, C.c_void_p]),
+            "orc_ic_burgers_fourier": (None, [_I, _I, _I, _D, _U32, _I, _D, C.c_void_p]),
+            "orc_ic_burgers_ref": (None, [_I, _I, _I, _D, _D, _D, C.c_void_p]),
+            "orc_burgers_rhs_f64": (None, _BURG + [C.c_void_p, _D, C.c_void_p]),
+            "orc_burgers_rhs_f32": (None, _BURG + [_I, C.c_void_p, C.c_float, C.c_void_p]),
+            "orc_burgers_stage_f64": (None, _BURG + [_I, C.c_void_p, C.c_void_p, _D, C.c_void_p, C.c_void_p]),
+            "orc_burgers_stage_f32": (None, _BURG + [_I, _I, C.c_void_p, C.c_void_p, _D, C.c_void_p, C.c_void_p]),
+            "orc_burgers_run_f64": (_I64, _BURG + [C.c_void_p, _D, _D, _I, _D, _I64, _PD]),
+            "orc_burgers_run_f32": (_I64, _BURG + [_I, C.c_void_p, _D, _D, _I, _D, _I64, _PD]),
+            "orc_burgers_ref_steps": (_I64, [_D, _D, _D, _D, _D, _I, _I, _I, _D, _PD]),
+            "orc_max_abs_f64": (_D, [C.c_void_p, _I64]),
+            "orc_philox_u01x2": (None, [_U32, _U32, C.c_uint64, _PD, _PD]),
+            "orc_num_threads": (_I, []),
+            "orc_set_num_threads": (None, [_I]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _p(a: np.ndarray) -> int:
+    assert a.flags.c_contiguous
+    return a.ctypes.data
+
+
+def _heat_args(ndim, nx, ny, nz, order, frozen, zero_boundary, periodic, kx, ky, kz, dt):
+    return [ndim, nx, ny, nz if ndim == 3 else 1, order, frozen, int(zero_boundary), int(periodic), kx, ky, kz, dt]
+
+
+def heat_stage(cfg, stage: int, uin: np.ndarray, un: np.ndarray, periodic: bool = False) -> np.ndarray:
+    """One stage with the scheme of a solvers.HeatConfig-like object (ndim, nx.., order, ...)."""
+    out = np.empty_like(uin)
+    f = lib().orc_heat_stage_f64 if uin.dtype == np.float64 else lib().orc_heat_stage_f32
+    f(*_heat_args(cfg.ndim, cfg.nx, cfg.ny, cfg.nz, cfg.order, cfg.frozen, cfg.zero_boundary, periodic,
+                  cfg.kx, cfg.ky, cfg.kz, cfg.dt), stage, _p(uin), _p(un), _p(out))
+    return out
+
+
+def heat_run(cfg, u: np.ndarray, nsteps: int, time: int) -> np.ndarray:
+    u = np.ascontiguousarray(u).copy()
+    f = lib().orc_heat_run_f64 if u.dtype == np.float64 else lib().orc_heat_run_f32
+    f(*_heat_args(cfg.ndim, cfg.nx, cfg.ny, cfg.nz, cfg.order, cfg.frozen, cfg.zero_boundary, False,
+                  cfg.kx, cfg.ky, cfg.kz, cfg.dt), time, nsteps, _p(u))
+    return u
+
+
+def heat_accuracy(dim: int, nc: int, tEnd: float, factor: float):
+    L1, L2, Li = C.c_double(), C.c_double(), C.c_double()
+    it = lib().orc_heat_accuracy(dim, nc, tEnd, factor, C.byref(L1), C.byref(L2), C.byref(Li))
+    return it, L1.value, L2.value, Li.value
+
+
+def heat_ref_constants(ndim, Cc, L, W, H, nx, ny, nz, iters):
+    out = [C.c_double() for _ in range(8)]
+    lib().orc_heat_ref_constants(ndim, Cc, L, W, H, nx, ny, nz, iters, *[C.byref(o) for o in out])
+    return dict(zip(["dx", "dy", "dz", "dt", "kx", "ky", "kz", "tFinal"], [o.value for o in out]))
+
+
+def ic_heat_ref(ndim, nx, ny, nz, dx, dy, dz) -> np.ndarray:
+    u = np.empty(nx * ny * (nz if ndim == 3 else 1))
+    lib().orc_ic_heat_ref(ndim, nx, ny, nz, dx, dy, dz, _p(u))
+    return u
+
+
+def ic_heat2d_gauss_noise(nx, ny, seed, sigma) -> np.ndarray:
+    u = np.empty(nx * ny)
+    lib().orc_ic_heat2d_gauss_noise(nx, ny, seed, sigma, _p(u))
+    return u
+
+
+def ic_heat3d_blobs(nx, ny, nz, seed, nblobs=8) -> np.ndarray:
+    u = np.empty(nx * ny * nz)
+    lib().orc_ic_heat3d_blobs(nx, ny, nz, seed, nblobs, _p(u))
+    return u
+
+
+def heat3d_blob_params(seed, nblobs=8) -> np.ndarray:
+    p = np.empty(4 * nblobs)
+    lib().orc_heat3d_blob_params(seed, nblobs, _p(p))
+    return p.reshape(nblobs, 4)
+
+
+def burgers_fourier_params(seed, nmodes=16, amax=0.1) -> np.ndarray:
+    p = np.empty(5 * nmodes)
+    lib().orc_burgers_fourier_params(seed, nmodes, amax, _p(p))
+    return p.reshape(nmodes, 5)
+
+
+def ic_burgers_fourier(nx, ny, nz, L, seed, nmodes=16, amax=0.1) -> np.ndarray:
+    u = np.empty(nx * ny * nz)
+    lib().orc_ic_burgers_fourier(nx, ny, nz, L, seed, nmodes, amax, _p(u))
+    return u
+
+
+def ic_burgers_ref(nx, ny, nz, dx, dy, dz) -> np.ndarray:
+    u = np.empty(nx * ny * nz)
+    lib().orc_ic_burgers_ref(nx, ny, nz, dx, dy, dz, _p(u))
+    return u
+
+
+def _burg_args(cfg):
+    k = [cfg.C / (12 * h * h) if cfg.C else 0.0 for h in (cfg.dx, cfg.dy, cfg.dz)]
+    return [cfg.nx, cfg.ny, cfg.nz, int(cfg.weno == 1), int(cfg.lf == 1), int(cfg.bc == 1), int(cfg.bug_b2),
+            cfg.dx, cfg.dy, cfg.dz, *k]
+
+
+def burgers_stage(cfg, stage, uin, un, dt, div64=True):
+    """One SSP-RK3 stage with the scheme of a solvers.BurgersConfig-like object."""
+    out = np.empty_like(uin)
+    Lu = np.zeros_like(uin)
+    if uin.dtype == np.float64:
+        lib().orc_burgers_stage_f64(*_burg_args(cfg), stage, _p(uin), _p(un), dt, _p(out), _p(Lu))
+    else:
+        lib().orc_burgers_stage_f32(*_burg_args(cfg), int(div64), stage, _p(uin), _p(un), dt, _p(out), _p(Lu))
+    return out
+
+
+def burgers_rhs(cfg, u, alpha):
+    Lu = np.zeros_like(u)
+    if u.dtype == np.float64:
+        lib().orc_burgers_rhs_f64(*_burg_args(cfg), _p(u), alpha, _p(Lu))
+    else:
+        lib().orc_burgers_rhs_f32(*_burg_args(cfg), 1, _p(u), alpha, _p(Lu))
+    return Lu
+
+
+def burgers_run(cfg, u, tEnd, cfl, dt_rule, C_visc=0.0, max_steps=1 << 40, div64=True):
+    u = np.ascontiguousarray(u).copy()
+    t = C.c_double()
+    if u.dtype == np.float64:
+        it = lib().orc_burgers_run_f64(*_burg_args(cfg), _p(u), tEnd, cfl, dt_rule, C_visc, max_steps, C.byref(t))
+    else:
+        it = lib().orc_burgers_run_f32(*_burg_args(cfg), int(div64), _p(u), tEnd, cfl, dt_rule, C_visc, max_steps,
+                                       C.byref(t))
+    return u, t.value, it
+
+
+def burgers_ref_steps(tEnd, cfl, L, W, H, nx, ny, nz, Cv=1e-5):
+    t = C.c_double()
+    it = lib().orc_burgers_ref_steps(tEnd, cfl, L, W, H, nx, ny, nz, Cv, C.byref(t))
+    return it, t.value
+
+
+def set_threads(n: int) -> None:
+    lib().orc_set_num_threads(n)
+
+
+def num_threads() -> int:
+    return lib().orc_num_threads()

@@ -1,0 +1,108 @@
+"""The C-ABI libraries load and export every declared symbol; host-side entry points agree
+with the oracle. No GPU calls."""
+import ctypes as C
+import re
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from multigpu_advectiondiffusion_gb300 import _native as N
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def _declared(header: Path, define_pitched: bool = False) -> set[str]:
+    txt = header.read_text()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    names = set(re.findall(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_ \*]*?\b([A-Za-z_][A-Za-z0-9_]*)\s*\(", txt, flags=re.M))
+    return {n for n in names if n not in {"defined", "if", "ifdef", "ifndef"}}
+
+
+def _exports(so: Path) -> set[str]:
+    out = subprocess.run(["nm", "-D", "--defined-only", str(so)], capture_output=True, text=True, check=True).stdout
+    return {l.split()[-1] for l in out.splitlines() if " T " in l}
+
+
+def test_native_exports_every_declared_symbol(native):
+    exp = _exports(N.lib_path())
+    for h in ("advdiff.h", "advdiff_ref_ops.h"):
+        missing = _declared(ROOT / "include" / h) - exp
+        assert not missing, (h, missing)
+    for name, _, _ in N.SIGNATURES:
+        assert name in exp
+
+
+@pytest.mark.parametrize("lib,header,names", [
+    ("libadvdiff_compat_heat3d.so", "advdiff_compat_heat3d.h", {"CopyToConstantMemory", "Call_Lu3d", "Call_RK3d"}),
+    ("libadvdiff_compat_heat2d.so", "advdiff_compat_heat2d.h", {"CopyToConstantMemory", "Call_Lu2d", "Call_RK2d"}),
+    ("libadvdiff_compat_burgers3d.so", "advdiff_compat_burgers3d.h",
+     {"CopyToConstantMemory", "Call_Adv_x", "Call_Adv_y", "Call_Adv_z", "Call_Diff_", "Call_sspRK"}),
+])
+@pytest.mark.parametrize("pitched", [False, True])
+def test_compat_exports_reference_names(native, lib, header, names, pitched):
+    so = N.LIBDIR / (lib.replace(".so", "_pitched.so") if pitched else lib)
+    C.CDLL(str(so))
+    exp = _exports(so)
+    assert names | {"adv_compat_last_status"} <= exp
+    assert _declared(ROOT / "include" / header) <= exp
+
+
+def test_abi_version_and_strings(native):
+    assert native.adv_abi_version() == 1
+    assert native.adv_status_string(N.ADV_ERR_TIMEOUT) == b"ADV_ERR_TIMEOUT"
+
+
+def test_invalid_descriptors_rejected_without_gpu(native):
+    nb = C.c_size_t(0)
+    bad = N.HeatDesc(4, 8, 8, 8, N.ADV_F32, 2, 1, 1, 1.0, 1.0, 1.0, 0.1)
+    assert native.adv_heat_workspace_bytes(C.byref(bad), N.ADV_EULER, C.byref(nb)) == N.ADV_ERR_INVALID_ARG
+    assert b"ndim" in native.adv_last_error_string()
+    thin = N.HeatDesc(3, 8, 8, 8, N.ADV_F32, 4, 1, 0, 1.0, 1.0, 1.0, 0.1)  # frozen < radius
+    assert native.adv_heat_workspace_bytes(C.byref(thin), N.ADV_EULER, C.byref(nb)) == N.ADV_ERR_INVALID_ARG
+    empty = N.HeatDesc(3, 0, 8, 8, N.ADV_F32, 2, 1, 0, 1.0, 1.0, 1.0, 0.1)
+    assert native.adv_heat_workspace_bytes(C.byref(empty), N.ADV_EULER, C.byref(nb)) == N.ADV_ERR_INVALID_ARG
+    ok = N.HeatDesc(3, 9, 8, 7, N.ADV_F64, 2, 1, 1, 1.0, 1.0, 1.0, 0.1)
+    assert native.adv_heat_workspace_bytes(C.byref(ok), N.ADV_SSPRK3, C.byref(nb)) == N.ADV_OK
+    assert nb.value == 2 * ((9 * 8 * 7 * 8 + 255) // 256 * 256)
+    bd = N.BurgersDesc(4, 8, 8, N.ADV_F32, 1, 1, N.ADV_BC_PERIODIC, 0, 0, 0, 1.0, 1.0, 1.0, 0, 0, 0)
+    assert native.adv_burgers_workspace_bytes(C.byref(bd), C.byref(nb)) == N.ADV_ERR_INVALID_ARG
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def test_host_initial_conditions_equal_oracle(native, oracle):
+    u = np.empty(33 * 31 * 29)
+    assert native.adv_ic_heat3d_blobs(33, 31, 29, 2, 8, _dp(u)) == 0
+    np.testing.assert_array_equal(u, oracle.ic_heat3d_blobs(33, 31, 29, 2, 8))
+    v = np.empty(40 * 36)
+    assert native.adv_ic_heat2d_gauss_noise(40, 36, 1, 1e-3, _dp(v)) == 0
+    np.testing.assert_array_equal(v, oracle.ic_heat2d_gauss_noise(40, 36, 1, 1e-3))
+    w = np.empty(20 * 18 * 16)
+    assert native.adv_ic_burgers_fourier(20, 18, 16, 2.0, 3, 16, 0.1, _dp(w)) == 0
+    np.testing.assert_array_equal(w, oracle.ic_burgers_fourier(20, 18, 16, 2.0, 3, 16, 0.1))
+    r = np.empty(21 * 19 * 17)
+    assert native.adv_ic_heat_ref(3, 21, 19, 17, 0.5, 0.55, 0.6, _dp(r)) == 0
+    np.testing.assert_array_equal(r, oracle.ic_heat_ref(3, 21, 19, 17, 0.5, 0.55, 0.6))
+    b = np.empty(12 * 11 * 10)
+    assert native.adv_ic_burgers_ref(12, 11, 10, 0.2, 0.2, 0.2, _dp(b)) == 0
+    np.testing.assert_array_equal(b, oracle.ic_burgers_ref(12, 11, 10, 0.2, 0.2, 0.2))
+
+
+def test_result_bin_layout(native, tmp_path):
+    """result.bin: float32, x fastest, no header (SingleGPU/Diffusion3d_baselineCode/tools.cpp:59-87)."""
+    u = np.arange(4 * 3 * 2, dtype=np.float64) / 7.0
+    p = tmp_path / "result.bin"
+    assert native.adv_write_result_bin(str(p).encode(), N.ADV_F64, u.ctypes.data, u.size) == 0
+    got = np.fromfile(p, dtype=np.float32)
+    np.testing.assert_array_equal(got, u.astype(np.float32))
+    assert p.stat().st_size == 4 * u.size
+
+
+def test_drivers_print_usage_without_gpu(native):
+    for drv in ("heat2d", "heat3d", "burgers3d"):
+        r = subprocess.run([str(N.LIBDIR / drv)], capture_output=True, text=True)
+        assert r.returncode == 1 and "Usage" in r.stdout

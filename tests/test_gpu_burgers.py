@@ -1,0 +1,175 @@
+"""Fused Burgers WENO stage and the graph-resident time loop on the GPU against the oracle.
+FP64 state (reference operand order) is bit-exact; FP32 state (one division per WENO side) is
+held to a stated tolerance against the FP32 and FP64 oracles."""
+import numpy as np
+import pytest
+
+from multigpu_advectiondiffusion_gb300 import _native as N
+from multigpu_advectiondiffusion_gb300.solvers import BurgersConfig, burgers_run, burgers_stage
+
+pytestmark = pytest.mark.gpu
+
+
+def _t(a, cuda):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).to(cuda)
+
+
+def _cases():
+    out = []
+    for size in [(32, 32, 24), (37, 35, 23), (64, 16, 40)]:
+        for weno in (N.ADV_WENO5_Z, N.ADV_WENO5_JS):
+            out.append(("periodic-global", size, weno))
+            out.append(("periodic-local", size, weno))
+            out.append(("frozen-visc", size, weno))
+    out.append(("frozen-visc-b2", (24, 22, 40), N.ADV_WENO5_Z))
+    out.append(("frozen-local", (40, 20, 12), N.ADV_WENO5_Z))
+    return out
+
+
+def _cfg(kind, size, weno):
+    nx, ny, nz = size
+    if kind.startswith("periodic"):
+        c = BurgersConfig(nx, ny, nz, 2.0 / nx, 2.0 / ny, 2.0 / nz, weno,
+                          N.ADV_LF_GLOBAL if kind.endswith("global") else N.ADV_LF_LOCAL, N.ADV_BC_PERIODIC)
+    else:
+        c = BurgersConfig.reference(2.0, 2.0, 2.0, nx, ny, nz, C=1e-2 if "visc" in kind else 0.0,
+                                    bug_b2="b2" in kind)
+        c.weno = weno
+    return c
+
+
+def _field(cfg, seed):
+    rng = np.random.default_rng(seed)
+    x = np.linspace(0, 2, cfg.nx, endpoint=False)[None, None, :]
+    y = np.linspace(0, 2, cfg.ny, endpoint=False)[None, :, None]
+    z = np.linspace(0, 2, cfg.nz, endpoint=False)[:, None, None]
+    u = 0.5 + 0.4 * np.sin(np.pi * x + 1) * np.cos(np.pi * y) + 0.3 * np.sin(np.pi * z + 0.5)
+    return (u + 0.05 * rng.standard_normal(u.shape)).ravel()
+
+
+@pytest.mark.parametrize("kind,size,weno", _cases())
+@pytest.mark.parametrize("stage", [1, 2, 3])
+def test_burgers_stage_fp64_bitwise(cuda, oracle, kind, size, weno, stage):
+    cfg = _cfg(kind, size, weno)
+    uin = _field(cfg, stage)
+    un = uin if stage == 1 else _field(cfg, 100 + stage)
+    dt = 1e-3
+    want = oracle.burgers_stage(cfg, stage, uin, un, dt)
+    a = _t(uin, cuda)
+    b = a if stage == 1 else _t(un, cuda)
+    out = a.new_full(a.shape, np.nan)
+    alpha = float(np.abs(uin).max())
+    burgers_stage(cfg, stage, a, b, out, dt, alpha)
+    np.testing.assert_array_equal(out.cpu().numpy(), want)
+
+
+@pytest.mark.parametrize("kind,size,weno", _cases()[:6])
+@pytest.mark.parametrize("div", [N.ADV_DIV_F32, N.ADV_DIV_F64])
+def test_burgers_stage_fp32(cuda, oracle, kind, size, weno, div):
+    """FP32 stage vs the FP32 oracle: max |diff| <= 4e-7 * max|u| (a few ulps of the state)."""
+    cfg = _cfg(kind, size, weno)
+    cfg.div = div
+    uin = _field(cfg, 7).astype(np.float32)
+    un = _field(cfg, 8).astype(np.float32)
+    want = oracle.burgers_stage(cfg, 2, uin, un, 2e-3)
+    a, b = _t(uin, cuda), _t(un, cuda)
+    out = a.new_full(a.shape, np.nan)
+    burgers_stage(cfg, 2, a, b, out, 2e-3, float(np.abs(uin).max()))
+    got = out.cpu().numpy()
+    assert np.isfinite(got).all()
+    assert np.abs(got - want).max() <= 4e-7 * np.abs(want).max()
+
+
+def test_burgers_stage_reports_max_abs(cuda, oracle):
+    import torch
+    cfg = _cfg("periodic-global", (32, 32, 24), N.ADV_WENO5_Z)
+    u = _field(cfg, 3)
+    a = _t(u, cuda)
+    out = torch.empty_like(a)
+    key = torch.zeros(1, dtype=torch.int64, device=cuda)
+    burgers_stage(cfg, 1, a, a, out, 1e-3, float(np.abs(u).max()), maxabs_key=key)
+    assert key.view(torch.float64).item() == out.abs().max().item()
+
+
+@pytest.mark.parametrize("weno", [N.ADV_WENO5_Z, N.ADV_WENO5_JS])
+def test_burgers_run_periodic_fp64_bitwise(cuda, oracle, weno):
+    """Device-driven loop (dt = CFL dx / max|u^n|, global LF from the fused max|u| reduction, t in
+    FP64, while-conditional CUDA graph) reproduces the oracle's loop exactly."""
+    cfg = BurgersConfig.periodic(24, weno="z" if weno == N.ADV_WENO5_Z else "js")
+    u0 = oracle.ic_burgers_fourier(24, 24, 24, 2.0, 3)
+    want, t_w, it_w = oracle.burgers_run(cfg, u0, 0.3, 0.4, 1)
+    u = _t(u0, cuda)
+    t, it = burgers_run(cfg, u, 0.3, 0.4, N.ADV_DT_MAXU)
+    assert it == it_w and t == t_w
+    np.testing.assert_array_equal(u.cpu().numpy(), want)
+
+
+def test_burgers_run_reference_scheme_fp64_bitwise(cuda, oracle):
+    """Reference scheme (node grid, local LF, WENO5-Z, C = 1e-5 viscosity with the doubled slabs,
+    fixed dt = CFL dx) at 40^3 to t = 0.02."""
+    cfg = BurgersConfig.reference(2.0, 2.0, 2.0, 40, 40, 40, C=1e-5, bug_b2=True)
+    u0 = oracle.ic_burgers_ref(40, 40, 40, cfg.dx, cfg.dy, cfg.dz)
+    want, t_w, it_w = oracle.burgers_run(cfg, u0, 0.02, 0.3, 0, C_visc=1e-5)
+    u = _t(u0, cuda)
+    t, it = burgers_run(cfg, u, 0.02, 0.3, N.ADV_DT_FIXED)
+    assert it == it_w and t == t_w
+    np.testing.assert_array_equal(u.cpu().numpy(), want)
+
+
+@pytest.mark.parametrize("div", [N.ADV_DIV_F32, N.ADV_DIV_F64])
+def test_burgers_run_fp32_vs_fp64_oracle(cuda, oracle, div):
+    """FP32 state to t = 0.5 (past shock formation) within 1e-5 relative L2 of the FP64 oracle."""
+    cfg = BurgersConfig.periodic(48, weno="z")
+    cfg.div = div
+    u0 = oracle.ic_burgers_fourier(48, 48, 48, 2.0, 3)
+    want, _, it_w = oracle.burgers_run(cfg, u0, 0.5, 0.4, 1)
+    u = _t(u0.astype(np.float32), cuda)
+    _, it = burgers_run(cfg, u, 0.5, 0.4, N.ADV_DT_MAXU)
+    assert abs(it - it_w) <= 1
+    got = u.cpu().numpy().astype(np.float64)
+    rel = np.linalg.norm(got - want) / np.linalg.norm(want)
+    assert rel <= 1e-5, rel
+
+
+def test_burgers_config_c3_full_size_invariants(cuda, oracle):
+    """256^3 periodic WENO5-Z, global LF, CFL 0.4, t = 0.5 in FP32: conserves sum(u) to 1e-6 relative,
+    stays finite and bounded by the initial extremes (1e-3 slack for WENO overshoot), and its first
+    stage is within 1e-6 of the oracle."""
+    import torch
+    n = 256
+    cfg = BurgersConfig.periodic(n, weno="z")
+    u0 = oracle.ic_burgers_fourier(n, n, n, 2.0, 3)
+    first = oracle.burgers_stage(cfg, 1, u0.astype(np.float32), u0.astype(np.float32), 1e-3)
+    a = _t(u0.astype(np.float32), cuda)
+    out = torch.empty_like(a)
+    burgers_stage(cfg, 1, a, a, out, 1e-3, float(np.abs(u0.astype(np.float32)).max()))
+    assert (out.cpu().numpy() - first).__abs__().max() <= 1e-6 * np.abs(first).max()
+    u = _t(u0.astype(np.float32), cuda)
+    s0 = u.double().sum().item()
+    t, it = burgers_run(cfg, u, 0.5, 0.4, N.ADV_DT_MAXU)
+    assert t == pytest.approx(0.5, abs=1e-12) and it > 0
+    assert torch.isfinite(u).all().item()
+    assert abs(u.double().sum().item() - s0) <= 1e-6 * abs(s0)
+    assert u.max().item() <= u0.max() + 1e-3 and u.min().item() >= u0.min() - 1e-3
+
+
+def test_burgers_run_honours_max_steps(cuda, oracle):
+    cfg = BurgersConfig.periodic(16, weno="z")
+    u0 = oracle.ic_burgers_fourier(16, 16, 16, 2.0, 3)
+    want, t_w, it_w = oracle.burgers_run(cfg, u0, 1.0, 0.4, 1, max_steps=5)
+    u = _t(u0, cuda)
+    t, it = burgers_run(cfg, u, 1.0, 0.4, N.ADV_DT_MAXU, max_steps=5)
+    assert it == 5 == it_w and t == t_w
+    np.testing.assert_array_equal(u.cpu().numpy(), want)
+
+
+def test_burgers_nonfinite_detected(cuda, oracle):
+    """A NaN in the state stops the device loop with ADV_ERR_NONFINITE (host-made failure)."""
+    cfg = BurgersConfig.periodic(16, weno="z")
+    u0 = oracle.ic_burgers_fourier(16, 16, 16, 2.0, 3)
+    u0[123] = np.nan
+    u = _t(u0, cuda)
+    with pytest.raises(N.AdvError) as e:
+        burgers_run(cfg, u, 0.1, 0.4, N.ADV_DT_MAXU)
+    assert e.value.status == N.ADV_ERR_NONFINITE

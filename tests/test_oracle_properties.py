@@ -1,0 +1,77 @@
+"""Size-independent properties of the oracle's schemes (CPU only)."""
+import numpy as np
+import pytest
+
+from multigpu_advectiondiffusion_gb300.solvers import BurgersConfig, HeatConfig
+
+
+def test_heat_o2_euler_matches_numpy(oracle):
+    cfg = HeatConfig.dirichlet_o2(3, 12)
+    rng = np.random.default_rng(0)
+    u = rng.random(12 ** 3)
+    u3 = u.reshape(12, 12, 12)
+    out = oracle.heat_stage(cfg, 1, u, u).reshape(12, 12, 12)
+    ref = u3.copy()
+    c = u3[1:-1, 1:-1, 1:-1]
+    lap = (cfg.kx * ((u3[1:-1, 1:-1, 2:] - 2 * c) + u3[1:-1, 1:-1, :-2])
+           + cfg.ky * ((u3[1:-1, 2:, 1:-1] - 2 * c) + u3[1:-1, :-2, 1:-1]))
+    lap = lap + cfg.kz * ((u3[2:, 1:-1, 1:-1] - 2 * c) + u3[:-2, 1:-1, 1:-1])
+    ref[1:-1, 1:-1, 1:-1] = c + cfg.dt * lap
+    for face in (ref[0], ref[-1], ref[:, 0], ref[:, -1], ref[:, :, 0], ref[:, :, -1]):
+        face[...] = 0
+    np.testing.assert_array_equal(out, ref)
+
+
+def test_heat_euler_max_principle(oracle):
+    cfg = HeatConfig.dirichlet_o2(3, 24)
+    u = oracle.ic_heat3d_blobs(24, 24, 24, 2)
+    v = oracle.heat_run(cfg, u, 50, 0)
+    assert v.max() <= u.max() + 1e-15 and v.min() >= -1e-15
+
+
+def test_heat_rk3_stage_in_place_equivalence(oracle):
+    """Stage 3 may write into u_n: each node reads u_n only where it writes."""
+    cfg = HeatConfig.reference_3d(1.0, 10, 10, 10, 14, 13, 12)
+    u = oracle.ic_heat_ref(3, 14, 13, 12, 10 / 13, 10 / 12, 10 / 11)
+    a = oracle.heat_stage(cfg, 1, u, u)
+    b = oracle.heat_stage(cfg, 2, a, u)
+    c = oracle.heat_stage(cfg, 3, b, u)
+    r = oracle.heat_run(cfg, u, 1, 1)
+    np.testing.assert_array_equal(c, r)
+
+
+@pytest.mark.parametrize("weno", [0, 1])
+def test_burgers_constant_state_has_zero_rhs(oracle, weno):
+    cfg = BurgersConfig.periodic(16, weno="z" if weno else "js")
+    u = np.full(16 ** 3, 0.7)
+    assert np.abs(oracle.burgers_rhs(cfg, u, 0.7)).max() == 0.0
+
+
+@pytest.mark.parametrize("weno", ["z", "js"])
+def test_burgers_periodic_conserves_mass(oracle, weno):
+    cfg = BurgersConfig.periodic(16, weno=weno)
+    u0 = oracle.ic_burgers_fourier(16, 16, 16, 2.0, 3)
+    u, t, it = oracle.burgers_run(cfg, u0, 0.2, 0.4, 1)
+    assert it > 0 and t == pytest.approx(0.2, abs=1e-15)
+    assert abs(u.sum() - u0.sum()) <= 1e-10 * abs(u0.sum())
+
+
+def test_burgers_1d_reduction(oracle):
+    """A field constant in y and z evolves as the 1D scheme: identical across y-z."""
+    cfg = BurgersConfig.periodic(16, weno="z")
+    x = (np.arange(16) + 0.5) * cfg.dx
+    u = np.broadcast_to(0.5 + 0.3 * np.sin(np.pi * x), (16, 16, 16)).copy().ravel()
+    v, _, _ = oracle.burgers_run(cfg, u, 0.3, 0.4, 1)
+    v = v.reshape(16, 16, 16)
+    assert np.abs(v - v[:1, :1, :]).max() == 0.0
+
+
+def test_burgers_fp32_error_floor_small(oracle):
+    """FP32 state stays within 1e-5 relative L2 of FP64 before and after the shock forms (n=32)."""
+    cfg = BurgersConfig.periodic(32, weno="z")
+    u0 = oracle.ic_burgers_fourier(32, 32, 32, 2.0, 3)
+    a, ta, ia = oracle.burgers_run(cfg, u0, 0.5, 0.4, 1)
+    b, tb, ib = oracle.burgers_run(cfg, u0.astype(np.float32), 0.5, 0.4, 1)
+    assert ia == ib
+    rel = np.linalg.norm(b.astype(np.float64) - a) / np.linalg.norm(a)
+    assert rel < 1e-5
