@@ -183,6 +183,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="heat3d", choices=["heat3d", "burgers3d"])
     ap.add_argument("--cpu-budget", type=float, default=10.0, help="seconds of CPU-baseline work")
+    ap.add_argument("--div", default="fast", choices=["fast", "f32", "f64"],
+                    help="Burgers WENO weight division (FP32 state)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -230,7 +232,7 @@ def main():
     else:
         from oracle import oracle
         n = 256
-        cfg = BurgersConfig.periodic(n, weno="z")
+        cfg = BurgersConfig.periodic(n, weno="z", div=args.div)
         u0 = torch.from_numpy(oracle.ic_burgers_fourier(n, n, n, 2.0, 3).astype(np.float32)).to(dev)
         u = u0.clone()
         ws = burgers_workspace(cfg, u)
@@ -241,8 +243,8 @@ def main():
 
         def one_step(uu):
             burgers_run(cfg, uu, 1e9, 0.4, N.ADV_DT_MAXU, max_steps=inner, workspace=ws, stream=sh)
-        workload_name = "burgers3d 256^3 f32 weno5-z global-lf periodic cfl 0.4 x 20 steps"
-        kernel = "burgers_stage_kernel<float,Z,float>"
+        workload_name = f"burgers3d 256^3 f32 weno5-z global-lf periodic cfl 0.4 x 20 steps, div {args.div}"
+        kernel = f"burgers_stage_kernel<float,Z,{args.div}>"
 
     def timed(fn, K):
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

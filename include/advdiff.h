@@ -52,8 +52,10 @@ typedef enum adv_time { ADV_EULER = 0, ADV_SSPRK3 = 1 } adv_time;
 typedef enum adv_weno { ADV_WENO5_JS = 0, ADV_WENO5_Z = 1 } adv_weno;
 typedef enum adv_lf { ADV_LF_LOCAL = 0, ADV_LF_GLOBAL = 1 } adv_lf;
 typedef enum adv_bc { ADV_BC_FROZEN = 0, ADV_BC_PERIODIC = 1 } adv_bc;
-/* Precision of the WENO weight divisions when the state is FP32. */
-typedef enum adv_div { ADV_DIV_F32 = 0, ADV_DIV_F64 = 1 } adv_div;
+/* Division of the WENO weights when the state is FP32 (one division per face side):
+ * F32 = IEEE FP32 division, F64 = the division in FP64, FAST = FP32 reciprocal-based division
+ * (at most 2 ulp). The FP64 state always uses the reference's own FP64 divisions. */
+typedef enum adv_div { ADV_DIV_F32 = 0, ADV_DIV_F64 = 1, ADV_DIV_FAST = 2 } adv_div;
 /* Burgers time-step rule. FIXED: dt = min(CFL*dx/1, 0.9/(2C sum 1/h^2)) as the reference driver
  * (SingleGPU/Burgers3d_WENO5/main.cpp:130-133); MAXU: dt = CFL*dx/max|u^n| computed on the
  * device each step (Matlab_Prototipes/InviscidBurgersNd/LFWENO5FDM3d.m:71). Both trim the last

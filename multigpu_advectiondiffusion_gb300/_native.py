@@ -18,7 +18,7 @@ ADV_EULER, ADV_SSPRK3 = 0, 1
 ADV_WENO5_JS, ADV_WENO5_Z = 0, 1
 ADV_LF_LOCAL, ADV_LF_GLOBAL = 0, 1
 ADV_BC_FROZEN, ADV_BC_PERIODIC = 0, 1
-ADV_DIV_F32, ADV_DIV_F64 = 0, 1
+ADV_DIV_F32, ADV_DIV_F64, ADV_DIV_FAST = 0, 1, 2
 ADV_DT_FIXED, ADV_DT_MAXU = 0, 1
 
 

@@ -62,6 +62,17 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity
   return true;
 }
 
+// Warp-convergent bounded wait: lane 0 polls, the other lanes wait at the shuffle instead of
+// spinning (no divergent spin loops eating issue slots), then every lane performs its own
+// (immediately successful) try_wait so it acquires the completed phase itself.
+__device__ __forceinline__ bool mbar_wait_warp(uint64_t* bar, unsigned parity, int* status, int lane) {
+  int ok = 1;
+  if (lane == 0) ok = mbar_wait_bounded(bar, parity, status) ? 1 : 0;
+  ok = __shfl_sync(0xffffffffu, ok, 0);
+  if (ok) (void)mbar_try_wait(bar, parity);
+  return ok != 0;
+}
+
 // ----------------------------------------------------------------------------- TMA
 // 3D tiled load of one box into shared memory, completion signalled on `bar` (complete_tx).
 __device__ __forceinline__ void tma_load_3d(void* smem_dst, const CUtensorMap* tmap, int x, int y,

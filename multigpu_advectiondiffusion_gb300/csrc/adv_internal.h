@@ -47,7 +47,7 @@ int* device_status_ptr();
 struct HeatLaunch {
   // resolved per plan: whether the TMA path applies and the chosen z-chunk
   bool tma = false;
-  int zchunk = 0;
+  int tiles_x = 0, tiles_y = 0;  // x-y tiles; the grid is one wave of CTAs sharing the tile-planes
   dim3 grid, block;
   size_t smem = 0;
   CUtensorMap tmap_in;  // tensor map of u_in (re-encoded when the pointer changes)
@@ -60,7 +60,7 @@ adv_status heat_validate(const adv_heat_desc* d);
 // --------------------------------------------------------------- Burgers launchers
 struct BurgersLaunch {
   bool tma = false;
-  int zchunk = 0;
+  int tiles_x = 0, tiles_y = 0;  // 32 x 16 column tiles; the grid is one wave sharing the tile-planes
   dim3 grid, block;
   size_t smem = 0;
   CUtensorMap tmap_in;

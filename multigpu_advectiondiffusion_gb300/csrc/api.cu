@@ -79,7 +79,8 @@ adv_status burgers_validate(const adv_burgers_desc* d) {
   if (d->weno != ADV_WENO5_JS && d->weno != ADV_WENO5_Z) return set_error(ADV_ERR_INVALID_ARG, "burgers: bad weno");
   if (d->lf != ADV_LF_LOCAL && d->lf != ADV_LF_GLOBAL) return set_error(ADV_ERR_INVALID_ARG, "burgers: bad lf");
   if (d->bc != ADV_BC_FROZEN && d->bc != ADV_BC_PERIODIC) return set_error(ADV_ERR_INVALID_ARG, "burgers: bad bc");
-  if (d->div != ADV_DIV_F32 && d->div != ADV_DIV_F64) return set_error(ADV_ERR_INVALID_ARG, "burgers: bad div");
+  if (d->div != ADV_DIV_F32 && d->div != ADV_DIV_F64 && d->div != ADV_DIV_FAST)
+    return set_error(ADV_ERR_INVALID_ARG, "burgers: bad div");
   if (d->nx < 1 || d->ny < 1 || d->nz < 1) return set_error(ADV_ERR_INVALID_ARG, "burgers: empty grid");
   if (d->nx > (1 << 30) || d->ny > (1 << 30) || d->nz > (1 << 30))
     return set_error(ADV_ERR_INVALID_ARG, "burgers: dimension too large");
@@ -99,15 +100,19 @@ adv_status burgers_prepare(const adv_burgers_desc& d, const void* u_in, BurgersL
   L->tma = aligned;
   L->block = dim3(256, 1, 1);
   const int tiles_x = (d.nx + 31) / 32, tiles_y = (d.ny + 15) / 16;
-  const int64_t want = (int64_t)di.sms * 6;
-  int64_t chunks = (want + (int64_t)tiles_x * tiles_y - 1) / ((int64_t)tiles_x * tiles_y);
-  chunks = std::max<int64_t>(1, std::min<int64_t>(chunks, (d.nz + 15) / 16));
-  L->zchunk = (int)((d.nz + chunks - 1) / chunks);
-  L->grid = dim3(tiles_x, tiles_y, (d.nz + L->zchunk - 1) / L->zchunk);
   L->smem = d.dtype == ADV_F32 ? burgers_smem_f32() : burgers_smem_f64();
   void* k = d.dtype == ADV_F32 ? burgers_kernel_for<float>(d) : burgers_kernel_for<double>(d);
   if (!k) return set_error(ADV_ERR_UNSUPPORTED, "burgers: no kernel for this configuration");
   ADV_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L->smem));
+  int occ = 0;
+  ADV_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, 256, L->smem));
+  occ = std::max(occ, 1);
+  // One wave of CTAs, each with an equal share of the (tile, plane) pairs (at least 8 planes).
+  const int64_t total = (int64_t)tiles_x * tiles_y * d.nz;
+  const int64_t ctas = std::max<int64_t>(1, std::min<int64_t>((int64_t)di.sms * occ, total / 8));
+  L->tiles_x = tiles_x;
+  L->tiles_y = tiles_y;
+  L->grid = dim3((unsigned)ctas, 1, 1);
   std::memset(&L->tmap_in, 0, sizeof(L->tmap_in));
   if (L->tma) {
     EncodeTiledFn enc = encode_tiled_fn();

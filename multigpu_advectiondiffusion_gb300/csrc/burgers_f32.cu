@@ -6,15 +6,20 @@ namespace adv {
 template <>
 void* burgers_kernel_for<float>(const adv_burgers_desc& d) {
   const bool z = d.weno == ADV_WENO5_Z;
-  const bool d64 = d.div == ADV_DIV_F64;
   const bool visc = d.kx != 0.0 || d.ky != 0.0 || d.kz != 0.0;
 #define K(Z, D, V) reinterpret_cast<void*>(&burgers_stage_kernel<float, Z, D, V>)
-  if (z) {
-    if (d64) return visc ? K(true, double, true) : K(true, double, false);
-    return visc ? K(true, float, true) : K(true, float, false);
+#define KD(Z, V)                                          \
+  switch (d.div) {                                        \
+    case ADV_DIV_F64: return K(Z, double, V);             \
+    case ADV_DIV_FAST: return K(Z, FastDiv, V);           \
+    default: return K(Z, float, V);                       \
   }
-  if (d64) return visc ? K(false, double, true) : K(false, double, false);
-  return visc ? K(false, float, true) : K(false, float, false);
+  if (z) {
+    if (visc) { KD(true, true) } else { KD(true, false) }
+  } else {
+    if (visc) { KD(false, true) } else { KD(false, false) }
+  }
+#undef KD
 #undef K
 }
 

@@ -34,7 +34,7 @@ struct BurgersParams {
   int stage;
   int periodic;  // 1: periodic wrap; 0: the reference's frozen outer 3 layers
   int bug_b2;
-  int zchunk;
+  int tiles_x, tiles_y;
   int tma;
   int un_is_uin;
   int lf_global;
@@ -79,8 +79,8 @@ __device__ __forceinline__ int wrapi(int i, int n) {
   return i < 0 ? i + n : i;
 }
 
-// Face reconstruction for state type T: FP32 takes the fast form with divisions in D,
-// FP64 the reference literal form.
+// Face reconstruction and Lax-Friedrichs split for state type T: FP32 takes the fast forms (one
+// division per side, of kind D), FP64 the reference's literal operand order.
 template <class T, bool Z, class D>
 struct Face;
 template <bool Z, class D>
@@ -89,6 +89,7 @@ struct Face<float, Z, D> {
                                             float m2, float m3, float m4) {
     return weno_face_fast<Z, D>(p0, p1, p2, p3, p4, m0, m1, m2, m3, m4);
   }
+  __device__ __forceinline__ static void split(float u, float a, float& fp, float& fm) { lf_split_fast(u, a, fp, fm); }
 };
 template <bool Z, class D>
 struct Face<double, Z, D> {
@@ -96,10 +97,12 @@ struct Face<double, Z, D> {
                                              double m1, double m2, double m3, double m4) {
     return weno_face_ref<Z, double>(p0, p1, p2, p3, p4, m0, m1, m2, m3, m4);
   }
+  __device__ __forceinline__ static void split(double u, double a, double& fp, double& fm) { lf_split<double>(u, a, fp, fm); }
 };
 
+// FP32: at most 80 registers so three CTAs (24 warps) fit per SM; FP64: two CTAs.
 template <class T, bool Z, class D, bool VISC>
-__global__ void __launch_bounds__(256, 2)
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2)
 burgers_stage_kernel(const __grid_constant__ CUtensorMap tmap, const BurgersParams<T> p) {
   using TL = BurgersTile;
   using SM = BurgersSmem<T>;
@@ -113,20 +116,18 @@ burgers_stage_kernel(const __grid_constant__ CUtensorMap tmap, const BurgersPara
   T* fpS = reinterpret_cast<T*>(smem_raw + SM::RING);
   T* fmS = fpS + TL::PLANE;
   T* fxS = fmS + TL::PLANE;   // [BY][BX+1]
-  T* fyS = fxS + TL::NXF;     // [BY+1][BX]
+  // fxS[f] for f < NXF: x-faces [BY][BX+1]; fxS[NXF + g]: y-faces [BY+1][BX]
   __shared__ uint64_t bars[TL::NS];
   __shared__ int abort_flag;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nx = p.nx, ny = p.ny, nz = p.nz;
-  const int x0 = blockIdx.x * TL::BX, y0 = blockIdx.y * TL::BY;
-  const int zs = blockIdx.z * p.zchunk;
-  const int ze = min(nz, zs + p.zchunk);
-  const int Q = (ze - zs) + 2 * TL::R;
-  const int p0 = zs - TL::R;
   const size_t sxy = (size_t)nx * ny;
   const bool per = p.periodic != 0;
-  const bool edge = per && (x0 - TL::PADX < 0 || x0 + TL::BX + TL::PADX > nx || y0 - TL::R < 0 || y0 + TL::BY + TL::R > ny);
+  // Balanced split: the (tile, z-plane) pairs, tile-major, are cut into gridDim.x equal
+  // contiguous ranges (one wave of CTAs); a range crossing a tile boundary becomes segments.
+  const int64_t total = (int64_t)p.tiles_x * p.tiles_y * nz;
+  const int64_t seg_a = total * blockIdx.x / gridDim.x, seg_b = total * (blockIdx.x + 1) / gridDim.x;
 
   // Lax-Friedrichs constant and dt for this stage.
   T alpha;
@@ -146,43 +147,78 @@ burgers_stage_kernel(const __grid_constant__ CUtensorMap tmap, const BurgersPara
   }
   __syncthreads();
 
-  auto plane_z = [&](int q) { return per ? wrapi(p0 + q, nz) : p0 + q; };
-  auto issue = [&](int q) {
-    T* dst = ring + (q % TL::NS) * SM::SLOT_ELEMS;
-    const int z = plane_z(q);
-    if (p.tma) {
-      if (tid == 0) {
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        uint64_t* bar = &bars[q % TL::NS];
-        mbar_arrive_expect_tx(bar, TL::PLANE * (unsigned)sizeof(T));
-        tma_load_3d(dst, &tmap, x0 - TL::PADX, y0 - TL::R, z, bar);
-      }
+  // This thread's share of the 1072 x/y faces of a plane, fixed for the whole kernel: face f
+  // (f = tid + 256 r) is x-face f when f < NXF (row f / 33, face f % 33) or y-face g = f - NXF
+  // (face row g / 32, column g % 32). base: shared-memory index of the face's first stencil
+  // value; the other values follow at stride 1 (x) or SW (y).
+  int fbase[5];
+  bool fisx[5], fact[5];
+#pragma unroll
+  for (int r = 0; r < 5; ++r) {
+    const int f = tid + TL::NT * r;
+    fact[r] = f < TL::NXF + TL::NYF;
+    fisx[r] = f < TL::NXF;
+    if (fisx[r]) {
+      const int row = f / (TL::BX + 1), fi = f - row * (TL::BX + 1);
+      fbase[r] = (row + TL::R) * TL::SW + fi + 1;  // column of x0+fi-3
     } else {
-      const bool zok = z >= 0 && z < nz;
-      for (int e = tid; e < TL::PLANE; e += TL::NT) {
-        const int r = e / TL::SW, c = e - r * TL::SW;
-        int gx = x0 - TL::PADX + c, gy = y0 - TL::R + r;
-        if (per) { gx = wrapi(gx, nx); gy = wrapi(gy, ny); }
-        const bool ok = zok && gx >= 0 && gx < nx && gy >= 0 && gy < ny;
-        const T* src = ok ? p.uin + (size_t)z * sxy + (size_t)gy * nx + gx : p.uin;
-        cp_async_zfill<sizeof(T)>(dst + e, src, ok);
-      }
+      const int g = f - TL::NXF, fj = g / TL::BX, c = g - fj * TL::BX;
+      fbase[r] = fj * TL::SW + TL::PADX + c;  // row of y0+fj-3
     }
-  };
-
-  for (int q = 0; q <= TL::P && q < Q; ++q) {
-    issue(q);
-    if (!p.tma) cp_async_commit();
   }
-  if (!p.tma)
-    for (int q = Q; q <= TL::P; ++q) cp_async_commit();
-
   // Per-thread columns: (lane, warp) and (lane, warp + 8).
   const int cx = lane;
   const int cy0 = warp, cy1 = warp + 8;
+  K kmax = 0;
+  const T rdx = T(1.0 / p.dx), rdy = T(1.0 / p.dy), rdz = T(1.0 / p.dz);
+  const int F = per ? 0 : 3;
+
+  int s_issue = 0, s_wait = 0;  // ring slots of the next plane to issue / to wait for
+  unsigned parity = 0;          // per-slot phase parity of the next wait
   // z windows per column: f+ at k-2..k+2, f- at k-1..k+3, the f+ of the newest plane held back
-  // one step, u at k-3..k+3 (viscous term and the stage input at k).
-  T fpw[2][5], fmw[2][5], fpn[2], uw[2][7];
+  // one step, u at k-3..k+3 (viscous variant only); reset for every segment.
+  T fpw[2][5], fmw[2][5], fpn[2], uw[2][VISC ? 7 : 1];
+
+  for (int64_t pos = seg_a; pos < seg_b;) {
+  const int64_t tile = pos / nz;
+  const int zs = (int)(pos - tile * nz);
+  const int ze = (int)min((int64_t)nz, zs + (seg_b - pos));
+  pos += ze - zs;
+  const int x0 = (int)(tile % p.tiles_x) * TL::BX, y0 = (int)(tile / p.tiles_x) * TL::BY;
+  const int Q = (ze - zs) + 2 * TL::R;
+  const int p0 = zs - TL::R;
+  const bool edge = per && (x0 - TL::PADX < 0 || x0 + TL::BX + TL::PADX > nx || y0 - TL::R < 0 || y0 + TL::BY + TL::R > ny);
+    auto plane_z = [&](int q) { return per ? wrapi(p0 + q, nz) : p0 + q; };
+    auto issue = [&](int q) {
+      T* dst = ring + s_issue * SM::SLOT_ELEMS;
+      const int z = plane_z(q);
+      if (p.tma) {
+        if (tid == 0) {
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          uint64_t* bar = &bars[s_issue];
+          mbar_arrive_expect_tx(bar, TL::PLANE * (unsigned)sizeof(T));
+          tma_load_3d(dst, &tmap, x0 - TL::PADX, y0 - TL::R, z, bar);
+        }
+      } else {
+        const bool zok = z >= 0 && z < nz;
+        for (int e = tid; e < TL::PLANE; e += TL::NT) {
+          const int r = e / TL::SW, c = e - r * TL::SW;
+          int gx = x0 - TL::PADX + c, gy = y0 - TL::R + r;
+          if (per) { gx = wrapi(gx, nx); gy = wrapi(gy, ny); }
+          const bool ok = zok && gx >= 0 && gx < nx && gy >= 0 && gy < ny;
+          const T* src = ok ? p.uin + (size_t)z * sxy + (size_t)gy * nx + gx : p.uin;
+          cp_async_zfill<sizeof(T)>(dst + e, src, ok);
+        }
+        cp_async_commit();
+      }
+      s_issue = s_issue + 1 == TL::NS ? 0 : s_issue + 1;
+    };
+
+    for (int q = 0; q <= TL::P && q < Q; ++q) issue(q);
+    if (!p.tma)
+      for (int q = Q; q <= TL::P; ++q) cp_async_commit();
+
+
   T fz_prev[2] = {T(0), T(0)};
 #pragma unroll
   for (int c = 0; c < 2; ++c) {
@@ -190,16 +226,13 @@ burgers_stage_kernel(const __grid_constant__ CUtensorMap tmap, const BurgersPara
 #pragma unroll
     for (int s = 0; s < 5; ++s) { fpw[c][s] = T(0); fmw[c][s] = T(0); }
 #pragma unroll
-    for (int s = 0; s < 7; ++s) uw[c][s] = T(0);
+    for (int s = 0; s < (VISC ? 7 : 1); ++s) uw[c][s] = T(0);
   }
-  K kmax = 0;
-  const T rdx = T(1.0 / p.dx), rdy = T(1.0 / p.dy), rdz = T(1.0 / p.dz);
-  const int F = per ? 0 : 3;
-
   for (int q = 0; q < Q; ++q) {
-    T* plq = ring + (q % TL::NS) * SM::SLOT_ELEMS;
+    T* plq = ring + s_wait * SM::SLOT_ELEMS;
+    const int s_cent = s_wait >= 3 ? s_wait - 3 : s_wait - 3 + TL::NS;  // slot of stream entry q - 3
     if (p.tma) {
-      if (!mbar_wait_bounded(&bars[q % TL::NS], (q / TL::NS) & 1, p.status)) abort_flag = 1;
+      if (!mbar_wait_warp(&bars[s_wait], (parity >> s_wait) & 1u, p.status, lane)) abort_flag = 1;
       if (edge) {
         // Periodic edge tile: the TMA box zero-filled what lies outside the domain; fill it with
         // the wrapped neighbours. Written here, read only after the next barrier.
@@ -216,21 +249,25 @@ burgers_stage_kernel(const __grid_constant__ CUtensorMap tmap, const BurgersPara
     }
     __syncthreads();  // plane q visible to all threads; abort_flag now uniform
     const bool aborted = abort_flag != 0;
+    parity ^= 1u << s_wait;
+    s_wait = s_wait + 1 == TL::NS ? 0 : s_wait + 1;
     // ---- z windows: push plane q for this thread's two columns
 #pragma unroll
     for (int c = 0; c < 2; ++c) {
       const int cy = c ? cy1 : cy0;
       const T u = plq[(cy + TL::R) * TL::SW + TL::PADX + cx];
       T fp, fm;
-      lf_split<T>(u, glob ? alpha : absval(u), fp, fm);
+      Face<T, Z, D>::split(u, glob ? alpha : absval(u), fp, fm);
 #pragma unroll
       for (int s = 0; s < 4; ++s) { fpw[c][s] = fpw[c][s + 1]; fmw[c][s] = fmw[c][s + 1]; }
       fpw[c][4] = fpn[c];
       fpn[c] = fp;
       fmw[c][4] = fm;
+      if (VISC) {
 #pragma unroll
-      for (int s = 0; s < 6; ++s) uw[c][s] = uw[c][s + 1];
-      uw[c][6] = u;
+        for (int s = 0; s < 6; ++s) uw[c][s] = uw[c][s + 1];
+        uw[c][VISC ? 6 : 0] = u;
+      }
     }
     // z-face at (newest plane - 3) + 1/2 once the windows hold planes newest-5 .. newest.
     T fz_new[2] = {T(0), T(0)};
@@ -242,7 +279,7 @@ burgers_stage_kernel(const __grid_constant__ CUtensorMap tmap, const BurgersPara
     }
     if (q >= 6) {
       const int k = zs + q - 6;  // output plane; its staged copy is stream entry q - 3
-      const T* plc = ring + ((q - 3) % TL::NS) * SM::SLOT_ELEMS;
+      const T* plc = ring + s_cent * SM::SLOT_ELEMS;
       const bool kin = per || (k >= F && k < nz - F);
       const bool any_upd = kin && !aborted;
       if (any_upd) {
@@ -250,27 +287,20 @@ burgers_stage_kernel(const __grid_constant__ CUtensorMap tmap, const BurgersPara
         for (int e = tid; e < TL::PLANE; e += TL::NT) {
           const T u = plc[e];
           T fp, fm;
-          lf_split<T>(u, glob ? alpha : absval(u), fp, fm);
+          Face<T, Z, D>::split(u, glob ? alpha : absval(u), fp, fm);
           fpS[e] = fp;
           fmS[e] = fm;
         }
         __syncthreads();
-        // x-faces: face fi of row r sits between x0+fi-1 and x0+fi; y-faces likewise.
-        for (int f = tid; f < TL::NXF + TL::NYF; f += TL::NT) {
-          if (f < TL::NXF) {
-            const int r = f / (TL::BX + 1), fi = f - r * (TL::BX + 1);
-            const int base = (r + TL::R) * TL::SW + fi + 1;  // column of x0+fi-3
-            fxS[f] = Face<T, Z, D>::f(fpS[base], fpS[base + 1], fpS[base + 2], fpS[base + 3], fpS[base + 4],
-                                      fmS[base + 1], fmS[base + 2], fmS[base + 3], fmS[base + 4], fmS[base + 5]);
-          } else {
-            const int g = f - TL::NXF;
-            const int fj = g / TL::BX, c = g - fj * TL::BX;
-            const int base = fj * TL::SW + TL::PADX + c;  // row of y0+fj-3
-            constexpr int W = TL::SW;
-            fyS[g] = Face<T, Z, D>::f(fpS[base], fpS[base + W], fpS[base + 2 * W], fpS[base + 3 * W],
-                                      fpS[base + 4 * W], fmS[base + W], fmS[base + 2 * W], fmS[base + 3 * W],
-                                      fmS[base + 4 * W], fmS[base + 5 * W]);
-          }
+        // x- and y-faces of the plane, this thread's precomputed share
+#pragma unroll
+        for (int r = 0; r < 5; ++r) {
+          if (!fact[r]) continue;
+          const int b = fbase[r];
+          const int st = fisx[r] ? 1 : TL::SW;
+          fxS[tid + TL::NT * r] = Face<T, Z, D>::f(fpS[b], fpS[b + st], fpS[b + 2 * st], fpS[b + 3 * st], fpS[b + 4 * st],
+                                                   fmS[b + st], fmS[b + 2 * st], fmS[b + 3 * st], fmS[b + 4 * st],
+                                                   fmS[b + 5 * st]);
         }
         __syncthreads();
       }
@@ -279,12 +309,13 @@ burgers_stage_kernel(const __grid_constant__ CUtensorMap tmap, const BurgersPara
       for (int c = 0; c < 2; ++c) {
         const int cy = c ? cy1 : cy0;
         const int x = x0 + cx, y = y0 + cy;
-        const T uo = uw[c][3];
+        const T uo = VISC ? uw[c][VISC ? 3 : 0] : plc[(cy + TL::R) * TL::SW + TL::PADX + cx];
         T res = uo;
-        const bool upd = any_upd && (per || (x >= F && x < nx - F && y >= F && y < ny - F));
+        const bool inside = x < nx && y < ny;  // partial tiles extend past the domain
+        const bool upd = any_upd && inside && (per || (x >= F && x < nx - F && y >= F && y < ny - F));
         if (upd) {
           const T fxp = fxS[cy * (TL::BX + 1) + cx + 1], fxm = fxS[cy * (TL::BX + 1) + cx];
-          const T fyp = fyS[(cy + 1) * TL::BX + cx], fym = fyS[cy * TL::BX + cx];
+          const T fyp = fxS[TL::NXF + (cy + 1) * TL::BX + cx], fym = fxS[TL::NXF + cy * TL::BX + cx];
           T L;
           if (EXACT) {
             L = div_rn(-sub_rn(fxp, fxm), T(p.dx));
@@ -300,8 +331,9 @@ burgers_stage_kernel(const __grid_constant__ CUtensorMap tmap, const BurgersPara
                                        mul_rn(T(16), row[1])), row[2]);
             const T vy = sub_rn(add_rn(sub_rn(add_rn(-row[-2 * W], mul_rn(T(16), row[-W])), mul_rn(T(30), uo)),
                                        mul_rn(T(16), row[W])), row[2 * W]);
-            const T vz = sub_rn(add_rn(sub_rn(add_rn(-uw[c][1], mul_rn(T(16), uw[c][2])), mul_rn(T(30), uo)),
-                                       mul_rn(T(16), uw[c][4])), uw[c][5]);
+            constexpr int Z1 = VISC ? 1 : 0, Z2 = VISC ? 2 : 0, Z4 = VISC ? 4 : 0, Z5 = VISC ? 5 : 0;
+            const T vz = sub_rn(add_rn(sub_rn(add_rn(-uw[c][Z1], mul_rn(T(16), uw[c][Z2])), mul_rn(T(30), uo)),
+                                       mul_rn(T(16), uw[c][Z4])), uw[c][Z5]);
             const T v = add_rn(add_rn(mul_rn(p.kx, vx), mul_rn(p.ky, vy)), mul_rn(p.kz, vz));
             L = add_rn(L, v);
             // The reference's first viscous z-block starts at slab 3 yet runs 16 slabs, adding
@@ -313,7 +345,7 @@ burgers_stage_kernel(const __grid_constant__ CUtensorMap tmap, const BurgersPara
           else un = p.un[(size_t)k * sxy + (size_t)y * nx + x];
           res = stage_combine<T>(p.stage, un, uo, dt, L);
         }
-        if (x < nx && y < ny) {
+        if (inside) {
           p.out[(size_t)k * sxy + (size_t)y * nx + x] = res;
           const K kk = abs_key(res);
           kmax = kk > kmax ? kk : kmax;
@@ -326,13 +358,19 @@ burgers_stage_kernel(const __grid_constant__ CUtensorMap tmap, const BurgersPara
     }
     __syncthreads();  // stream entry q - 3 fully consumed
     if (aborted) {
-      if (p.tma && tid == 0)
-        for (int m = q; m < Q && m <= q + TL::P; ++m) mbar_wait_bounded(&bars[m % TL::NS], (m / TL::NS) & 1, p.status);
+      if (p.tma && tid == 0) {
+        int sl = s_wait;
+        for (int m = q + 1; m < Q && m <= q + TL::P; ++m) {
+          mbar_wait_bounded(&bars[sl], (parity >> sl) & 1u, p.status);
+          sl = sl + 1 == TL::NS ? 0 : sl + 1;
+        }
+      }
       return;
     }
     if (q + TL::P + 1 < Q) issue(q + TL::P + 1);
-    if (!p.tma) cp_async_commit();
+    else if (!p.tma) cp_async_commit();
   }
+  }  // segments
   if (p.maxabs_key) {
     kmax = warp_max(kmax);
     if (lane == 0 && kmax) atomicMax(static_cast<K*>(p.maxabs_key), kmax);

@@ -20,7 +20,8 @@ adv_status burgers_launch_t(const adv_burgers_desc& d, const BurgersLaunch& L, c
   p.stage = a.stage;
   p.periodic = d.bc == ADV_BC_PERIODIC ? 1 : 0;
   p.bug_b2 = d.bug_b2;
-  p.zchunk = L.zchunk;
+  p.tiles_x = L.tiles_x;
+  p.tiles_y = L.tiles_y;
   p.tma = L.tma ? 1 : 0;
   p.un_is_uin = a.u_n == a.u_in ? 1 : 0;
   p.lf_global = d.lf == ADV_LF_GLOBAL ? 1 : 0;

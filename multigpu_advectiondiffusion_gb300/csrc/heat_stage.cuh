@@ -1,0 +1,364 @@
+// heat_stage.cuh -- fused heat-equation stage for sm_103a (kernel template).
+//
+// One launch computes a whole stage u_out = combine(u_n, u_in + dt*L(u_in)), replacing the
+// reference's separate Laplacian and RK launches plus its per-step device copy
+// (SingleGPU/Diffusion3d_baselineCode/kernels.cu:37-142, main.cpp:106-122;
+// SingleGPU/Diffusion2d/kernels.cu:36-88).
+//
+// Work layout. A tile is BX x 16 nodes of an x-y plane (BX = 32 lanes x one 16-byte vector);
+// each thread owns one vector in each of two adjacent rows. The grid is one wave of CTAs; the
+// (tile, z-plane) pairs, tile-major, are split into equal contiguous ranges, one per CTA, so every
+// SM gets the same work. A CTA streams its planes through a shared-memory ring: each plane of the
+// tile plus its stencil halo is copied by TMA (cp.async.bulk.tensor.3d, one mbarrier per slot;
+// the x start is rounded down to a 16-byte boundary, so the box is one vector wider per side).
+// z neighbours come from a per-thread register window sliding along z, y neighbours from 16-byte
+// shared-memory rows (the thread's own second row serves the first and vice versa), x neighbours
+// from the thread's own vector plus warp shuffles (lanes 0 and 31 read the halo from shared
+// memory). Each node is read from HBM once per stage and written once, with 16-byte stores.
+// Row pitches TMA cannot describe (not a multiple of 16 bytes, e.g. the reference's 201-node rows)
+// take the same pipeline with cp.async element copies.
+//
+// Arithmetic. FP64 evaluates the reference's expressions operand for operand with correctly
+// rounded intrinsics (no contraction). FP32 evaluates the same stencil with explicit fused
+// multiply-adds in a fixed pattern (fewer instructions; the stencil is memory-bound only when the
+// instruction count is low). Both are reproduced bit for bit by the CPU oracle.
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include "adv_device.cuh"
+#include "adv_math.cuh"
+
+namespace adv {
+
+template <class T> struct Vec16;
+template <> struct Vec16<float> { using type = float4; };
+template <> struct Vec16<double> { using type = double2; };
+
+__device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
+
+template <class T, int ORDER, int NDIM>
+struct HeatTile {
+  static constexpr int VX = 16 / (int)sizeof(T);  // nodes per thread along x (one 16-byte vector)
+  static constexpr int TX = 32, TY = 8, NT = TX * TY;
+  static constexpr int RY = 2;  // rows per thread
+  static constexpr int BX = TX * VX, BY = TY * RY;
+  static constexpr int R = ORDER / 2;
+  static constexpr int RZ = NDIM == 3 ? R : 0;
+  static constexpr int PADX = VX;  // shared column 0 holds x0 - PADX (16-byte aligned start)
+  static constexpr int SW = BX + 2 * PADX;
+  static constexpr int SH = BY + 2 * R;
+  static constexpr int PLANE = SW * SH;
+  static constexpr int PLANE_BYTES = PLANE * (int)sizeof(T);
+  static constexpr int SLOT_ELEMS = ((PLANE_BYTES + 127) / 128 * 128) / (int)sizeof(T);
+  static constexpr int P = NDIM == 3 ? 3 : 0;  // planes prefetched ahead of the one consumed
+  static constexpr int NS = RZ + 1 + P;         // ring slots
+  static constexpr size_t SMEM = (size_t)NS * SLOT_ELEMS * sizeof(T);
+};
+
+template <class T>
+struct HeatParams {
+  const T* uin;
+  const T* un;
+  T* out;
+  int nx, ny, nz;
+  int frozen, zero_boundary, stage;
+  int tiles_x, tiles_y;
+  int vec_ok;  // output rows 16-byte aligned: vector stores
+  T kx, ky, kz, dt;
+  int* status;  // device status word
+};
+
+// Laplacian at one node from its neighbours along each axis (m2, m1, centre, p1, p2).
+// EXACT: the reference's operand order (3D east first, kernels.cu:95-97; 2D west first,
+// Diffusion2d/kernels.cu:82-83; O2 e - 2o + w, kernels.cu:58-60), correctly rounded.
+// FAST (FP32): O2 fma(-2, c, p1) + m1 per axis; O4 fma(16, far-side neighbour,
+// fma(-30, c, fma(16, near-side neighbour, -near-side outer))) - far-side outer with the same
+// near/far sides as the reference; L = fma(kz, Sz, fma(ky, Sy, kx * Sx)).
+template <class T, int ORDER, int NDIM, bool FAST>
+__device__ __forceinline__ T lap(T xm2, T xm1, T c, T xp1, T xp2, T ym2, T ym1, T yp1, T yp2, T zm2, T zm1, T zp1,
+                                 T zp2, T kx, T ky, T kz) {
+  T Sx, Sy, Sz = T(0);
+  if (ORDER == 2) {
+    if (FAST) {
+      Sx = add_rn(fma_rn(T(-2), c, xp1), xm1);
+      Sy = add_rn(fma_rn(T(-2), c, yp1), ym1);
+      if (NDIM == 3) Sz = add_rn(fma_rn(T(-2), c, zp1), zm1);
+    } else {
+      Sx = add_rn(sub_rn(xp1, mul_rn(T(2), c)), xm1);
+      Sy = add_rn(sub_rn(yp1, mul_rn(T(2), c)), ym1);
+      if (NDIM == 3) Sz = add_rn(sub_rn(zp1, mul_rn(T(2), c)), zm1);
+    }
+  } else {
+    // near side first: +1 in 3D, -1 in 2D
+    const T ax2 = NDIM == 3 ? xp2 : xm2, ax1 = NDIM == 3 ? xp1 : xm1, bx1 = NDIM == 3 ? xm1 : xp1, bx2 = NDIM == 3 ? xm2 : xp2;
+    const T ay2 = NDIM == 3 ? yp2 : ym2, ay1 = NDIM == 3 ? yp1 : ym1, by1 = NDIM == 3 ? ym1 : yp1, by2 = NDIM == 3 ? ym2 : yp2;
+    if (FAST) {
+      Sx = sub_rn(fma_rn(T(16), bx1, fma_rn(T(-30), c, fma_rn(T(16), ax1, -ax2))), bx2);
+      Sy = sub_rn(fma_rn(T(16), by1, fma_rn(T(-30), c, fma_rn(T(16), ay1, -ay2))), by2);
+      if (NDIM == 3) Sz = sub_rn(fma_rn(T(16), zm1, fma_rn(T(-30), c, fma_rn(T(16), zp1, -zp2))), zm2);
+    } else {
+      Sx = sub_rn(add_rn(sub_rn(add_rn(-ax2, mul_rn(T(16), ax1)), mul_rn(T(30), c)), mul_rn(T(16), bx1)), bx2);
+      Sy = sub_rn(add_rn(sub_rn(add_rn(-ay2, mul_rn(T(16), ay1)), mul_rn(T(30), c)), mul_rn(T(16), by1)), by2);
+      if (NDIM == 3) Sz = sub_rn(add_rn(sub_rn(add_rn(-zp2, mul_rn(T(16), zp1)), mul_rn(T(30), c)), mul_rn(T(16), zm1)), zm2);
+    }
+  }
+  if (FAST) {
+    T L = fma_rn(ky, Sy, mul_rn(kx, Sx));
+    if (NDIM == 3) L = fma_rn(kz, Sz, L);
+    return L;
+  }
+  T L = add_rn(mul_rn(kx, Sx), mul_rn(ky, Sy));
+  if (NDIM == 3) L = add_rn(L, mul_rn(kz, Sz));
+  return L;
+}
+
+// Stage combination. EXACT: reference operand order (kernels.cu:130-138). FAST (FP32):
+// 1: fma(dt, L, un); 2: fma(0.25, fma(dt, L, uin), 0.75 * un); 3: (fma(2, fma(dt, L, uin), un)) / 3.
+template <class T, bool FAST>
+__device__ __forceinline__ T combine(int stage, T un, T uin, T dt, T L) {
+  if (!FAST) return stage_combine<T>(stage, un, uin, dt, L);
+  if (stage == 2) return fma_rn(T(0.25), fma_rn(dt, L, uin), mul_rn(T(0.75), un));
+  if (stage == 3) return div_rn(fma_rn(T(2), fma_rn(dt, L, uin), un), T(3));
+  return fma_rn(dt, L, un);
+}
+
+// STAGE: 1 = stage 1 / forward Euler with u_n == u_in (u_n not read); 2, 3 = RK stages;
+// 0 = stage taken at run time with a separate u_n.
+template <class T, int ORDER, int NDIM, bool TMA, int STAGE>
+__global__ void __launch_bounds__(256, ORDER == 2 ? 4 : (sizeof(T) == 4 ? 3 : 2))
+heat_stage_kernel(const __grid_constant__ CUtensorMap tmap, const HeatParams<T> p) {
+  using C = HeatTile<T, ORDER, NDIM>;
+  using V = typename Vec16<T>::type;
+  constexpr bool FAST = sizeof(T) == 4;
+  constexpr int R = C::R, RZ = C::RZ, VX = C::VX, SW = C::SW;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  T* ring = reinterpret_cast<T*>(smem_raw);
+  __shared__ uint64_t bars[C::NS];
+  __shared__ int abort_flag;
+
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * C::TX + tx;
+  const int nx = p.nx, ny = p.ny, nz = p.nz;
+  const size_t sxy = (size_t)nx * ny;
+  const int stage = STAGE == 0 ? p.stage : STAGE;
+  // Balanced split: the (tile, z-plane) pairs, tile-major, are cut into gridDim.x equal
+  // contiguous ranges; a range that crosses a tile boundary becomes several segments.
+  const int64_t total = (int64_t)p.tiles_x * p.tiles_y * nz;
+  const int64_t seg_a = total * blockIdx.x / gridDim.x, seg_b = total * (blockIdx.x + 1) / gridDim.x;
+
+  if (tid == 0) {
+    if (TMA) {
+      for (int s = 0; s < C::NS; ++s) mbar_init(&bars[s], 1);
+      mbar_fence_init();
+      tma_prefetch_desc(&tmap);
+    }
+    abort_flag = 0;
+  }
+  __syncthreads();
+
+  const T kx = p.kx, ky = p.ky, kz = p.kz, dt = p.dt;
+  const int F = p.frozen;
+  T w[2 * RZ + 1][2][VX];  // register window along z (w[RZ] = centre plane), two rows
+  int s_issue = 0, s_wait = 0;  // ring slots of the next plane to issue / to wait for
+  unsigned parity = 0;          // per-slot phase parity of the next wait
+
+  for (int64_t pos = seg_a; pos < seg_b;) {
+    const int64_t tile = pos / nz;
+    const int zs = (int)(pos - tile * nz);
+    const int ze = (int)min((int64_t)nz, zs + (seg_b - pos));
+    pos += ze - zs;
+    const int x0 = (int)(tile % p.tiles_x) * C::BX, y0 = (int)(tile / p.tiles_x) * C::BY;
+    const int Q = (ze - zs) + 2 * RZ;  // planes streamed for this segment
+    const int p0 = zs - RZ;            // z of stream entry 0
+
+    auto issue = [&](int q) {
+      T* dst = ring + s_issue * C::SLOT_ELEMS;
+      const int z = p0 + q;
+      if (TMA) {
+        if (tid == 0) {
+          mbar_arrive_expect_tx(&bars[s_issue], C::PLANE_BYTES);
+          tma_load_3d(dst, &tmap, x0 - C::PADX, y0 - R, z, &bars[s_issue]);
+        }
+      } else {
+        const bool zok = z >= 0 && z < nz;
+        for (int e = tid; e < C::PLANE; e += C::NT) {
+          const int r = e / SW, c = e - r * SW;
+          const int gx = x0 - C::PADX + c, gy = y0 - R + r;
+          const bool ok = zok && gx >= 0 && gx < nx && gy >= 0 && gy < ny;
+          const T* src = ok ? p.uin + (size_t)z * sxy + (size_t)gy * nx + gx : p.uin;
+          cp_async_zfill<sizeof(T)>(dst + e, src, ok);
+        }
+        cp_async_commit();
+      }
+      s_issue = s_issue + 1 == C::NS ? 0 : s_issue + 1;
+    };
+
+    for (int q = 0; q <= C::P && q < Q; ++q) issue(q);
+    if (!TMA)
+      for (int q = Q; q <= C::P; ++q) cp_async_commit();  // one group per plane index
+
+    const int xb = x0 + tx * VX;  // first node of this thread
+    const int ya = y0 + 2 * ty;   // this thread's rows: ya, ya + 1
+    // Node classes of this thread's x-y positions, fixed over the segment (bit r*VX + e):
+    // keep = not updated on interior planes (frozen layer or outside the grid),
+    // edge = on the outermost x/y layer (written 0 under zero_boundary), inside = in the grid.
+    unsigned keep = 0, edge = 0, inside = 0;
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+      for (int e = 0; e < VX; ++e) {
+        const int x = xb + e, y = ya + r;
+        const unsigned bit = 1u << (r * VX + e);
+        if (!(x >= F && x < nx - F && y >= F && y < ny - F)) keep |= bit;
+        if (x == 0 || x == nx - 1 || y == 0 || y == ny - 1) edge |= bit;
+        if (x < nx && y < ny) inside |= bit;
+      }
+    constexpr unsigned ALL = (1u << (2 * VX)) - 1u;
+    const bool warp_clean = __all_sync(0xffffffffu, keep == 0);   // no fix-ups on interior planes
+    const bool warp_inside = __all_sync(0xffffffffu, inside == ALL);
+    const bool row_ok[2] = {ya < ny, ya + 1 < ny};
+    const bool vec_rows = p.vec_ok && xb + VX <= nx;
+    T* obase = p.out + (size_t)zs * sxy + (size_t)ya * nx + xb;  // output row pointer, plane zs
+
+#pragma unroll 1
+    for (int q = 0; q < Q; ++q) {
+      // ---- wait for plane q
+      bool ok = true;
+      if (TMA) {
+        ok = mbar_wait_warp(&bars[s_wait], (parity >> s_wait) & 1u, p.status, tx);
+        if (!ok) abort_flag = 1;
+      } else {
+        cp_async_wait<C::P>();
+        __syncthreads();
+      }
+      parity ^= 1u << s_wait;
+      const int s_cent = s_wait >= RZ ? s_wait - RZ : s_wait - RZ + C::NS;
+      const T* plq = ring + s_wait * C::SLOT_ELEMS + (2 * ty + R) * SW + C::PADX + tx * VX;
+      s_wait = s_wait + 1 == C::NS ? 0 : s_wait + 1;
+      const bool warp_abort = __any_sync(0xffffffffu, !ok);  // shuffles below need all lanes
+
+      // ---- slide the window; push this thread's two rows of plane q
+#pragma unroll
+      for (int s = 0; s < 2 * RZ; ++s)
+#pragma unroll
+        for (int r = 0; r < 2; ++r)
+#pragma unroll
+          for (int e = 0; e < VX; ++e) w[s][r][e] = w[s + 1][r][e];
+#pragma unroll
+      for (int r = 0; r < 2; ++r) {
+        const V v = *reinterpret_cast<const V*>(plq + r * SW);
+#pragma unroll
+        for (int e = 0; e < VX; ++e) w[2 * RZ][r][e] = reinterpret_cast<const T*>(&v)[e];
+      }
+
+      if (q >= 2 * RZ && !warp_abort) {
+        const int z = p0 + q - RZ;  // output plane (stream entry q - RZ)
+        const T* row0 = ring + s_cent * C::SLOT_ELEMS + (2 * ty + R) * SW + C::PADX + tx * VX;
+        // x-neighbourhood of both rows: xr[r][j] holds x = xb - R + j.
+        T xr[2][VX + 2 * R];
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+#pragma unroll
+          for (int e = 0; e < VX; ++e) xr[r][R + e] = w[RZ][r][e];
+#pragma unroll
+          for (int d = 1; d <= R; ++d) {
+            T lft = __shfl_up_sync(0xffffffffu, w[RZ][r][VX - d], 1);
+            T rgt = __shfl_down_sync(0xffffffffu, w[RZ][r][d - 1], 1);
+            if (tx == 0) lft = row0[r * SW - d];
+            if (tx == C::TX - 1) rgt = row0[r * SW + VX - 1 + d];
+            xr[r][R - d] = lft;
+            xr[r][R + VX - 1 + d] = rgt;
+          }
+        }
+        // y-neighbourhood: yv[j][e] holds row ya - R + j (j = 0 .. 2R+1); rows ya, ya+1 are own.
+        T yv[2 * R + 2][VX];
+#pragma unroll
+        for (int d = 1; d <= R; ++d) {
+          const V a = *reinterpret_cast<const V*>(row0 - d * SW);
+          const V b = *reinterpret_cast<const V*>(row0 + (1 + d) * SW);
+#pragma unroll
+          for (int e = 0; e < VX; ++e) {
+            yv[R - d][e] = reinterpret_cast<const T*>(&a)[e];
+            yv[R + 1 + d][e] = reinterpret_cast<const T*>(&b)[e];
+          }
+        }
+#pragma unroll
+        for (int e = 0; e < VX; ++e) {
+          yv[R][e] = w[RZ][0][e];
+          yv[R + 1][e] = w[RZ][1][e];
+        }
+        const bool zin = NDIM == 2 || (z >= F && z < nz - F);
+        // Every lane evaluates the stencil (halo values outside the grid are finite zero fill);
+        // nodes that are not updated are fixed up afterwards with warp-uniform branches.
+        T res[2][VX];
+#pragma unroll
+        for (int r = 0; r < 2; ++r)
+#pragma unroll
+          for (int e = 0; e < VX; ++e) {
+            const T c = w[RZ][r][e];
+            const T L = lap<T, ORDER, NDIM, FAST>(
+                xr[r][R + e - (R >= 2 ? 2 : 1)], xr[r][R + e - 1], c, xr[r][R + e + 1], xr[r][R + e + (R >= 2 ? 2 : 1)],
+                yv[R + r - (R >= 2 ? 2 : 1)][e], yv[R + r - 1][e], yv[R + r + 1][e], yv[R + r + (R >= 2 ? 2 : 1)][e],
+                w[RZ >= 2 ? RZ - 2 : 0][r][e], w[RZ >= 1 ? RZ - 1 : 0][r][e], w[RZ + (RZ >= 1 ? 1 : 0)][r][e],
+                w[RZ + (RZ >= 2 ? 2 : 0)][r][e], kx, ky, kz);
+            T un = c;
+            if (STAGE != 1) {
+              const size_t off = (size_t)(q - 2 * RZ) * sxy + (size_t)r * nx + e;
+              un = (warp_inside || ((inside >> (r * VX + e)) & 1u)) ? p.un[(obase - p.out) + off] : T(0);
+            }
+            res[r][e] = combine<T, FAST>(stage, un, c, dt, L);
+          }
+        if (!zin) {  // frozen plane: copy, or zero on the outermost planes
+          const bool zero_all = p.zero_boundary && NDIM == 3 && (z == 0 || z == nz - 1);
+#pragma unroll
+          for (int r = 0; r < 2; ++r)
+#pragma unroll
+            for (int e = 0; e < VX; ++e) {
+              const bool zb = zero_all || (p.zero_boundary && ((edge >> (r * VX + e)) & 1u));
+              res[r][e] = zb ? T(0) : w[RZ][r][e];
+            }
+        } else if (!warp_clean) {
+#pragma unroll
+          for (int r = 0; r < 2; ++r)
+#pragma unroll
+            for (int e = 0; e < VX; ++e)
+              if ((keep >> (r * VX + e)) & 1u)
+                res[r][e] = (p.zero_boundary && ((edge >> (r * VX + e)) & 1u)) ? T(0) : w[RZ][r][e];
+        }
+        T* dst0 = obase + (size_t)(q - 2 * RZ) * sxy;
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+          if (!row_ok[r]) continue;
+          T* dst = dst0 + (size_t)r * nx;
+          if (vec_rows) {
+            V v;
+#pragma unroll
+            for (int e = 0; e < VX; ++e) reinterpret_cast<T*>(&v)[e] = res[r][e];
+            *reinterpret_cast<V*>(dst) = v;
+          } else {
+#pragma unroll
+            for (int e = 0; e < VX; ++e)
+              if (xb + e < nx) dst[e] = res[r][e];
+          }
+        }
+      }
+      __syncthreads();  // every read of stream entry q - RZ is done: its slot can be refilled
+      if (abort_flag) {
+        // A wait expired: let the copies already issued land (bounded) before the CTA exits.
+        if (TMA && tid == 0) {
+          int s = s_wait;
+          for (int m = q + 1; m < Q && m <= q + C::P; ++m) {
+            mbar_wait_bounded(&bars[s], (parity >> s) & 1u, p.status);
+            s = s + 1 == C::NS ? 0 : s + 1;
+          }
+        }
+        return;
+      }
+      if (q + C::P + 1 < Q) issue(q + C::P + 1);
+      else if (!TMA) cp_async_commit();
+    }
+  }
+}
+
+}  // namespace adv

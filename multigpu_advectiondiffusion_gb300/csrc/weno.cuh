@@ -10,13 +10,21 @@
 //    correctly rounded intrinsics -> equal to the FP64 oracle bit for bit.
 //  * weno_side_fast<D>: the same weights with the common denominator b0*b1*b2 (WENO5-Z) or
 //    (b0*b1*b2)^2 (WENO5-JS) multiplied through, leaving ONE division per side instead of four;
-//    that division runs in type D (FP32 or FP64). Used for the FP32 state.
+//    D selects that division: float (IEEE), double (FP64) or FastDiv (reciprocal based,
+//    at most 2 ulp). Used for the FP32 state.
 #pragma once
 #include "adv_math.cuh"
 
 namespace adv {
 
 // Lax-Friedrichs split of f(u) = u^2/2 (kernels.cu:224-238): f+- = (f +- a u)/2.
+// lf_split: the reference's operand order, correctly rounded (FP64 path, reference operators).
+// lf_split_fast: u * (u/4 +- a/2), the FP32 path.
+__device__ __forceinline__ void lf_split_fast(float u, float a, float& fp, float& fm) {
+  const float hu = 0.25f * u, ha = 0.5f * a;
+  fp = u * (hu + ha);
+  fm = u * (hu - ha);
+}
 template <class T>
 __device__ __forceinline__ void lf_split(T u, T a, T& fp, T& fm) {
   const T f = mul_rn(mul_rn(T(0.5), u), u);
@@ -26,33 +34,46 @@ __device__ __forceinline__ void lf_split(T u, T a, T& fp, T& fm) {
 }
 
 // ---------------------------------------------------------------- fast FP32 form
+struct FastDiv {};  // division tag: __fdividef (reciprocal approximation, <= 2 ulp)
+template <class D>
+__device__ __forceinline__ float side_div(float num, float den) { return (float)((D)num / (D)den); }
+template <>
+__device__ __forceinline__ float side_div<FastDiv>(float num, float den) { return __fdividef(num, den); }
+
+// Left-biased side of one face from a..e = f at i-2..i+2. With the second differences
+// t0 = a-2b+c, t1 = b-2c+d, t2 = c-2d+e and first differences s0 = a-4b+3c, s1 = b-d,
+// s2 = 3c-4d+e, the reference's quantities are
+//   beta_k = 13/12 t_k^2 + 1/4 s_k^2,   q_k/6 = c + t_k/12 + s0/4 | - s1/4 | - s2/4
+// (q_0 = 2a-7b+11c, q_1 = -b+5c+2d, q_2 = 2c+5d-e). The kernel uses 4 beta_k and 4 eps (the
+// factor cancels in the normalised weights), linear weights times 10 (1, 6, 3), and the
+// weighted mean of q_k/6, so each side costs one division and no separate scaling.
 template <bool Z, class D>
 __device__ __forceinline__ float weno_side_fast(float a, float b, float c, float d, float e) {
-  const float t0 = a - 2.f * b + c, t1 = b - 2.f * c + d, t2 = c - 2.f * d + e;
-  const float s0 = a - 4.f * b + 3.f * c, s1 = b - d, s2 = 3.f * c - 4.f * d + e;
-  const float k13 = 13.f / 12.f;
-  const float B0 = k13 * t0 * t0 + 0.25f * s0 * s0;
-  const float B1 = k13 * t1 * t1 + 0.25f * s1 * s1;
-  const float B2 = k13 * t2 * t2 + 0.25f * s2 * s2;
-  const float q0 = 2.f * a - 7.f * b + 11.f * c;
-  const float q1 = -b + 5.f * c + 2.f * d;
-  const float q2 = 2.f * c + 5.f * d - e;
-  const float b0 = B0 + 1e-6f, b1 = B1 + 1e-6f, b2 = B2 + 1e-6f;
+  const float t0 = fmaf(-2.f, b, a) + c, t1 = fmaf(-2.f, c, b) + d, t2 = fmaf(-2.f, d, c) + e;
+  const float s0 = fmaf(3.f, c, fmaf(-4.f, b, a)), s1 = b - d, s2 = fmaf(3.f, c, fmaf(-4.f, d, e));
+  const float k = 13.f / 3.f;
+  const float b0 = fmaf(k * t0, t0, fmaf(s0, s0, 4e-6f));  // 4 (beta_k + eps)
+  const float b1 = fmaf(k * t1, t1, fmaf(s1, s1, 4e-6f));
+  const float b2 = fmaf(k * t2, t2, fmaf(s2, s2, 4e-6f));
+  const float r12 = 1.f / 12.f;
+  const float q0 = fmaf(0.25f, s0, fmaf(r12, t0, c));
+  const float q1 = fmaf(-0.25f, s1, fmaf(r12, t1, c));
+  const float q2 = fmaf(-0.25f, s2, fmaf(r12, t2, c));
   float w0, w1, w2;
-  if (Z) {  // alpha_k = d_k (1 + tau/b_k), times b0 b1 b2
-    const float tau = fabsf(B0 - B2);
-    w0 = 0.1f * (b0 + tau) * (b1 * b2);
-    w1 = 0.6f * (b1 + tau) * (b0 * b2);
-    w2 = 0.3f * (b2 + tau) * (b0 * b1);
-  } else {  // alpha_k = d_k / b_k^2, times (b0 b1 b2)^2
+  if (Z) {  // alpha_k = d_k (1 + tau/b_k), times 10 b0 b1 b2
+    const float tau = fabsf(b0 - b2);
+    w0 = (b0 + tau) * (b1 * b2);
+    w1 = (6.f * (b1 + tau)) * (b0 * b2);
+    w2 = (3.f * (b2 + tau)) * (b0 * b1);
+  } else {  // alpha_k = d_k / b_k^2, times 10 (b0 b1 b2)^2
     const float p12 = b1 * b2, p02 = b0 * b2, p01 = b0 * b1;
-    w0 = 0.1f * p12 * p12;
-    w1 = 0.6f * p02 * p02;
-    w2 = 0.3f * p01 * p01;
+    w0 = p12 * p12;
+    w1 = (6.f * p02) * p02;
+    w2 = (3.f * p01) * p01;
   }
-  const float num = w0 * q0 + w1 * q1 + w2 * q2;
-  const float den = 6.f * (w0 + w1 + w2);
-  return (float)((D)num / (D)den);
+  const float num = fmaf(w2, q2, fmaf(w1, q1, w0 * q0));
+  const float den = w0 + w1 + w2;
+  return side_div<D>(num, den);
 }
 
 // f+ at i-2..i+2 (p0..p4) and f- at i-1..i+3 (m0..m4).

@@ -1,0 +1,61 @@
+"""Direct launches of one hot kernel for profilers (ncu): no CUDA graph, no host loop logic.
+
+    python -m multigpu_advectiondiffusion_gb300.profile_kernels heat3d   [--n 256] [--launches 6]
+    python -m multigpu_advectiondiffusion_gb300.profile_kernels burgers3d [--n 256] [--launches 4]
+
+heat3d: the 3D O2 forward-Euler stage on an n^3 FP32 grid (ping-pong between two buffers).
+burgers3d: the periodic WENO5-Z global-Lax-Friedrichs SSP-RK3 stage 1 on an n^3 FP32 grid.
+Inputs are the seeded initial conditions of the benchmark workloads, generated on the host.
+"""
+from __future__ import annotations
+
+import argparse
+import sys
+from pathlib import Path
+
+import numpy as np
+
+
+def main(argv=None) -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("kernel", choices=["heat3d", "burgers3d"])
+    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--launches", type=int, default=6)
+    ap.add_argument("--dtype", default="f32", choices=["f32", "f64"])
+    ap.add_argument("--div", default="fast", choices=["fast", "f32", "f64"])
+    a = ap.parse_args(argv)
+    import torch
+
+    from . import _native as N
+    from .solvers import BurgersConfig, HeatConfig, burgers_stage, heat_stage
+
+    dev = torch.device("cuda:0")
+    lib = N.load()
+    npdt = np.float32 if a.dtype == "f32" else np.float64
+    n = a.n
+    if a.kernel == "heat3d":
+        cfg = HeatConfig.dirichlet_o2(3, n)
+        u0 = np.empty(n ** 3)
+        N.check(lib.adv_ic_heat3d_blobs(n, n, n, 2, 8, u0.ctypes.data_as(N.C.POINTER(N.C.c_double))), "ic")
+        u = torch.from_numpy(u0.astype(npdt)).to(dev)
+        v = torch.empty_like(u)
+        for _ in range(a.launches):
+            heat_stage(cfg, 1, u, u, v)
+            u, v = v, u
+    else:
+        cfg = BurgersConfig.periodic(n, weno="z", div=a.div)
+        u0 = np.empty(n ** 3)
+        N.check(lib.adv_ic_burgers_fourier(n, n, n, 2.0, 3, 16, 0.1, u0.ctypes.data_as(N.C.POINTER(N.C.c_double))),
+                "ic")
+        u = torch.from_numpy(u0.astype(npdt)).to(dev)
+        v = torch.empty_like(u)
+        alpha = float(np.abs(u0).max())
+        for _ in range(a.launches):
+            burgers_stage(cfg, 1, u, u, v, 1e-3, alpha)
+    torch.cuda.synchronize()
+    print(f"{a.kernel} n={n} {a.dtype}: {a.launches} launches ok")
+
+
+if __name__ == "__main__":
+    sys.path.insert(0, str(Path(__file__).resolve().parent.parent))
+    main()

@@ -134,7 +134,7 @@ class BurgersConfig:
         h = L / n
         return cls(n, n, n, h, h, h, N.ADV_WENO5_Z if weno == "z" else N.ADV_WENO5_JS,
                    N.ADV_LF_GLOBAL if lf == "global" else N.ADV_LF_LOCAL, N.ADV_BC_PERIODIC,
-                   N.ADV_DIV_F64 if div == "f64" else N.ADV_DIV_F32, False, 0.0)
+                   {"f32": N.ADV_DIV_F32, "f64": N.ADV_DIV_F64, "fast": N.ADV_DIV_FAST}[div], False, 0.0)
 
     def desc(self, dtype: int) -> N.BurgersDesc:
         k = [self.C / (12 * h * h) if self.C else 0.0 for h in (self.dx, self.dy, self.dz)]

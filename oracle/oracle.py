@@ -43,6 +43,8 @@ def lib() -> C.CDLL:
             "orc_heat_stage_f32": (None, _HEAT + [_I, C.c_void_p, C.c_void_p, C.c_void_p]),
             "orc_heat_run_f64": (None, _HEAT + [_I, _I64, C.c_void_p]),
             "orc_heat_run_f32": (None, _HEAT + [_I, _I64, C.c_void_p]),
+            "orc_heat_stage_f32_fma": (None, _HEAT + [_I, C.c_void_p, C.c_void_p, C.c_void_p]),
+            "orc_heat_run_f32_fma": (None, _HEAT + [_I, _I64, C.c_void_p]),
             "orc_heat_ref_constants": (None, [_I, _D, _I, _I, _I, _I, _I, _I, _I] + [_PD] * 8),
             "orc_ic_heat_ref": (None, [_I, _I, _I, _I, _D, _D, _D, C.c_void_p]),
             "orc_heat_accuracy": (_I, [_I, _I, _D, _D, _PD, _PD, _PD]),
@@ -81,18 +83,26 @@ def _heat_args(ndim, nx, ny, nz, order, frozen, zero_boundary, periodic, kx, ky,
     return [ndim, nx, ny, nz if ndim == 3 else 1, order, frozen, int(zero_boundary), int(periodic), kx, ky, kz, dt]
 
 
-def heat_stage(cfg, stage: int, uin: np.ndarray, un: np.ndarray, periodic: bool = False) -> np.ndarray:
-    """One stage with the scheme of a solvers.HeatConfig-like object (ndim, nx.., order, ...)."""
+def heat_stage(cfg, stage: int, uin: np.ndarray, un: np.ndarray, periodic: bool = False,
+               fp32_order: str = "gpu") -> np.ndarray:
+    """One stage with the scheme of a solvers.HeatConfig-like object (ndim, nx.., order, ...).
+    FP32 inputs use the GPU path's fused-multiply-add order unless fp32_order == "reference"."""
     out = np.empty_like(uin)
-    f = lib().orc_heat_stage_f64 if uin.dtype == np.float64 else lib().orc_heat_stage_f32
+    if uin.dtype == np.float64:
+        f = lib().orc_heat_stage_f64
+    else:
+        f = lib().orc_heat_stage_f32 if fp32_order == "reference" else lib().orc_heat_stage_f32_fma
     f(*_heat_args(cfg.ndim, cfg.nx, cfg.ny, cfg.nz, cfg.order, cfg.frozen, cfg.zero_boundary, periodic,
                   cfg.kx, cfg.ky, cfg.kz, cfg.dt), stage, _p(uin), _p(un), _p(out))
     return out
 
 
-def heat_run(cfg, u: np.ndarray, nsteps: int, time: int) -> np.ndarray:
+def heat_run(cfg, u: np.ndarray, nsteps: int, time: int, fp32_order: str = "gpu") -> np.ndarray:
     u = np.ascontiguousarray(u).copy()
-    f = lib().orc_heat_run_f64 if u.dtype == np.float64 else lib().orc_heat_run_f32
+    if u.dtype == np.float64:
+        f = lib().orc_heat_run_f64
+    else:
+        f = lib().orc_heat_run_f32 if fp32_order == "reference" else lib().orc_heat_run_f32_fma
     f(*_heat_args(cfg.ndim, cfg.nx, cfg.ny, cfg.nz, cfg.order, cfg.frozen, cfg.zero_boundary, False,
                   cfg.kx, cfg.ky, cfg.kz, cfg.dt), time, nsteps, _p(u))
     return u

@@ -65,7 +65,7 @@ def test_burgers_stage_fp64_bitwise(cuda, oracle, kind, size, weno, stage):
 
 
 @pytest.mark.parametrize("kind,size,weno", _cases()[:6])
-@pytest.mark.parametrize("div", [N.ADV_DIV_F32, N.ADV_DIV_F64])
+@pytest.mark.parametrize("div", [N.ADV_DIV_F32, N.ADV_DIV_F64, N.ADV_DIV_FAST])
 def test_burgers_stage_fp32(cuda, oracle, kind, size, weno, div):
     """FP32 stage vs the FP32 oracle: max |diff| <= 4e-7 * max|u| (a few ulps of the state)."""
     cfg = _cfg(kind, size, weno)
@@ -117,7 +117,7 @@ def test_burgers_run_reference_scheme_fp64_bitwise(cuda, oracle):
     np.testing.assert_array_equal(u.cpu().numpy(), want)
 
 
-@pytest.mark.parametrize("div", [N.ADV_DIV_F32, N.ADV_DIV_F64])
+@pytest.mark.parametrize("div", [N.ADV_DIV_F32, N.ADV_DIV_F64, N.ADV_DIV_FAST])
 def test_burgers_run_fp32_vs_fp64_oracle(cuda, oracle, div):
     """FP32 state to t = 0.5 (past shock formation) within 1e-5 relative L2 of the FP64 oracle."""
     cfg = BurgersConfig.periodic(48, weno="z")
