@@ -95,6 +95,24 @@ adv_status adv_heat_workspace_bytes(const adv_heat_desc* d, int time_scheme, siz
 adv_status adv_heat_run(const adv_heat_desc* d, int time_scheme, int64_t nsteps, void* u,
                         void* workspace, void* stream);
 
+/* Bytes of the fixed device scratch array behind adv_heat_run_noalloc (16 MiB). */
+#define ADV_NOALLOC_SCRATCH_BYTES ((size_t)16 << 20)
+
+/* adv_heat_run without any allocation, for callers that cannot allocate device memory: code
+ * that records its work into its own CUDA graph (cudaMalloc is not allowed while a stream is
+ * being captured) and hosts whose device memory is owned entirely by another allocator.
+ * No counterpart in the reference (its drivers cudaMalloc u, uo and Lu themselves).
+ * The intermediate state lives in one file-scope __device__ array of ADV_NOALLOC_SCRATCH_BYTES
+ * that every GPU loading this library holds until the process exits; the stages are launched
+ * directly on `stream` (no graph, no stream, no cudaMalloc/cudaFree). A run needing more scratch
+ * than adv_heat_workspace_bytes allows within that size (one state array for Euler, two for
+ * SSP-RK3) is rejected with ADV_ERR_INVALID_ARG. The first call on a device looks up the array's
+ * device address (and may load the module): make that first call before any stream capture.
+ * All calls share the one array and it keeps the last call's contents (nothing in it needs to
+ * start at zero): calls that overlap on the GPU, on any streams or threads, race. */
+adv_status adv_heat_run_noalloc(const adv_heat_desc* d, int time_scheme, int64_t nsteps, void* u,
+                                void* stream);
+
 /* --------------------------------------------------------------------------- Burgers
  * u_t + (u^2/2)_x + (u^2/2)_y + (u^2/2)_z = nu * Lap(u). One fused launch per SSP-RK3 stage:
  * Lax-Friedrichs split f+- = (u^2/2 +- a u)/2 with a = |u| per node (local, the reference's
