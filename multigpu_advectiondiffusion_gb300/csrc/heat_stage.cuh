@@ -124,29 +124,251 @@ __device__ __forceinline__ T combine(int stage, T un, T uin, T dt, T L) {
   return fma_rn(dt, L, un);
 }
 
+// Shared-memory pipeline of one CTA, carried across the segments it processes.
+struct HeatPipe {
+  int s_issue, s_wait;  // ring slots of the next plane to issue / to wait for
+  unsigned parity;      // per-slot phase parity of the next wait
+};
+
+// Shared-memory objects of the heat pipeline (one set per CTA, whichever kernel runs it).
+template <class T, int ORDER, int NDIM>
+__device__ __forceinline__ uint64_t* heat_bars() {
+  __shared__ uint64_t bars[HeatTile<T, ORDER, NDIM>::NS];
+  return bars;
+}
+__device__ __forceinline__ int* heat_abort_flag() {
+  __shared__ int flag;
+  return &flag;
+}
+
+// One segment: output planes [zs, ze) of the tile at (x0, y0), streamed through the ring.
 // STAGE: 1 = stage 1 / forward Euler with u_n == u_in (u_n not read); 2, 3 = RK stages;
-// 0 = stage taken at run time with a separate u_n.
+// 0 = stage taken at run time with a separate u_n. Returns the pipeline state for the next
+// segment (by value, so it stays in registers), with s_issue = -1 if a wait timed out (the CTA
+// must then return).
 template <class T, int ORDER, int NDIM, bool TMA, int STAGE>
-__global__ void __launch_bounds__(256, ORDER == 2 ? 4 : (sizeof(T) == 4 ? 3 : 2))
-heat_stage_kernel(const __grid_constant__ CUtensorMap tmap, const HeatParams<T> p) {
+__device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const HeatParams<T>& p, int x0, int y0, int zs,
+                                             int ze, HeatPipe pipe) {
   using C = HeatTile<T, ORDER, NDIM>;
   using V = typename Vec16<T>::type;
   constexpr bool FAST = sizeof(T) == 4;
   constexpr int R = C::R, RZ = C::RZ, VX = C::VX, SW = C::SW;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   T* ring = reinterpret_cast<T*>(smem_raw);
-  __shared__ uint64_t bars[C::NS];
-  __shared__ int abort_flag;
-
+  uint64_t* bars = heat_bars<T, ORDER, NDIM>();
+  int* abort_flag = heat_abort_flag();
+  int s_issue = pipe.s_issue, s_wait = pipe.s_wait;
+  unsigned parity = pipe.parity;
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * C::TX + tx;
   const int nx = p.nx, ny = p.ny, nz = p.nz;
   const size_t sxy = (size_t)nx * ny;
   const int stage = STAGE == 0 ? p.stage : STAGE;
+  const T kx = p.kx, ky = p.ky, kz = p.kz, dt = p.dt;
+  const int F = p.frozen;
+  T w[2 * RZ + 1][2][VX];  // register window along z (w[RZ] = centre plane), re-primed per segment
+  const int Q = (ze - zs) + 2 * RZ;  // planes streamed for this segment
+  const int p0 = zs - RZ;            // z of stream entry 0
+
+  auto issue = [&](int q) {
+    T* dst = ring + s_issue * C::SLOT_ELEMS;
+    const int z = p0 + q;
+    if (TMA) {
+      if (tid == 0) {
+        mbar_arrive_expect_tx(&bars[s_issue], C::PLANE_BYTES);
+        tma_load_3d(dst, tmap, x0 - C::PADX, y0 - R, z, &bars[s_issue]);
+      }
+    } else {
+      const bool zok = z >= 0 && z < nz;
+      for (int e = tid; e < C::PLANE; e += C::NT) {
+        const int r = e / SW, c = e - r * SW;
+        const int gx = x0 - C::PADX + c, gy = y0 - R + r;
+        const bool ok = zok && gx >= 0 && gx < nx && gy >= 0 && gy < ny;
+        const T* src = ok ? p.uin + (size_t)z * sxy + (size_t)gy * nx + gx : p.uin;
+        cp_async_zfill<sizeof(T)>(dst + e, src, ok);
+      }
+      cp_async_commit();
+    }
+    s_issue = s_issue + 1 == C::NS ? 0 : s_issue + 1;
+  };
+
+  for (int q = 0; q <= C::P && q < Q; ++q) issue(q);
+  if (!TMA)
+    for (int q = Q; q <= C::P; ++q) cp_async_commit();  // one group per plane index
+
+  const int xb = x0 + tx * VX;  // first node of this thread
+  const int ya = y0 + 2 * ty;   // this thread's rows: ya, ya + 1
+  // Node classes of this thread's x-y positions, fixed over the segment (bit r*VX + e):
+  // keep = not updated on interior planes (frozen layer or outside the grid),
+  // edge = on the outermost x/y layer (written 0 under zero_boundary), inside = in the grid.
+  unsigned keep = 0, edge = 0, inside = 0;
+#pragma unroll
+  for (int r = 0; r < 2; ++r)
+#pragma unroll
+    for (int e = 0; e < VX; ++e) {
+      const int x = xb + e, y = ya + r;
+      const unsigned bit = 1u << (r * VX + e);
+      if (!(x >= F && x < nx - F && y >= F && y < ny - F)) keep |= bit;
+      if (x == 0 || x == nx - 1 || y == 0 || y == ny - 1) edge |= bit;
+      if (x < nx && y < ny) inside |= bit;
+    }
+  constexpr unsigned ALL = (1u << (2 * VX)) - 1u;
+  const bool warp_clean = __all_sync(0xffffffffu, keep == 0);   // no fix-ups on interior planes
+  const bool warp_inside = __all_sync(0xffffffffu, inside == ALL);
+  const bool row_ok[2] = {ya < ny, ya + 1 < ny};
+  const bool vec_rows = p.vec_ok && xb + VX <= nx;
+  T* obase = p.out + (size_t)zs * sxy + (size_t)ya * nx + xb;  // output row pointer, plane zs
+
+#pragma unroll 1
+  for (int q = 0; q < Q; ++q) {
+    // ---- wait for plane q
+    bool ok = true;
+    if (TMA) {
+      ok = mbar_wait_warp(&bars[s_wait], (parity >> s_wait) & 1u, p.status, tx);
+      if (!ok) *abort_flag = 1;
+    } else {
+      cp_async_wait<C::P>();
+      __syncthreads();
+    }
+    parity ^= 1u << s_wait;
+    const int s_cent = s_wait >= RZ ? s_wait - RZ : s_wait - RZ + C::NS;
+    const T* plq = ring + s_wait * C::SLOT_ELEMS + (2 * ty + R) * SW + C::PADX + tx * VX;
+    s_wait = s_wait + 1 == C::NS ? 0 : s_wait + 1;
+    const bool warp_abort = __any_sync(0xffffffffu, !ok);  // shuffles below need all lanes
+
+    // ---- slide the window; push this thread's two rows of plane q
+#pragma unroll
+    for (int s = 0; s < 2 * RZ; ++s)
+#pragma unroll
+      for (int r = 0; r < 2; ++r)
+#pragma unroll
+        for (int e = 0; e < VX; ++e) w[s][r][e] = w[s + 1][r][e];
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      const V v = *reinterpret_cast<const V*>(plq + r * SW);
+#pragma unroll
+      for (int e = 0; e < VX; ++e) w[2 * RZ][r][e] = reinterpret_cast<const T*>(&v)[e];
+    }
+
+    if (q >= 2 * RZ && !warp_abort) {
+      const int z = p0 + q - RZ;  // output plane (stream entry q - RZ)
+      const T* row0 = ring + s_cent * C::SLOT_ELEMS + (2 * ty + R) * SW + C::PADX + tx * VX;
+      // x-neighbourhood of both rows: xr[r][j] holds x = xb - R + j.
+      T xr[2][VX + 2 * R];
+#pragma unroll
+      for (int r = 0; r < 2; ++r) {
+#pragma unroll
+        for (int e = 0; e < VX; ++e) xr[r][R + e] = w[RZ][r][e];
+#pragma unroll
+        for (int d = 1; d <= R; ++d) {
+          T lft = __shfl_up_sync(0xffffffffu, w[RZ][r][VX - d], 1);
+          T rgt = __shfl_down_sync(0xffffffffu, w[RZ][r][d - 1], 1);
+          if (tx == 0) lft = row0[r * SW - d];
+          if (tx == C::TX - 1) rgt = row0[r * SW + VX - 1 + d];
+          xr[r][R - d] = lft;
+          xr[r][R + VX - 1 + d] = rgt;
+        }
+      }
+      // y-neighbourhood: yv[j][e] holds row ya - R + j (j = 0 .. 2R+1); rows ya, ya+1 are own.
+      T yv[2 * R + 2][VX];
+#pragma unroll
+      for (int d = 1; d <= R; ++d) {
+        const V a = *reinterpret_cast<const V*>(row0 - d * SW);
+        const V b = *reinterpret_cast<const V*>(row0 + (1 + d) * SW);
+#pragma unroll
+        for (int e = 0; e < VX; ++e) {
+          yv[R - d][e] = reinterpret_cast<const T*>(&a)[e];
+          yv[R + 1 + d][e] = reinterpret_cast<const T*>(&b)[e];
+        }
+      }
+#pragma unroll
+      for (int e = 0; e < VX; ++e) {
+        yv[R][e] = w[RZ][0][e];
+        yv[R + 1][e] = w[RZ][1][e];
+      }
+      const bool zin = NDIM == 2 || (z >= F && z < nz - F);
+      // Every lane evaluates the stencil (halo values outside the grid are finite zero fill);
+      // nodes that are not updated are fixed up afterwards with warp-uniform branches.
+      T res[2][VX];
+#pragma unroll
+      for (int r = 0; r < 2; ++r)
+#pragma unroll
+        for (int e = 0; e < VX; ++e) {
+          const T c = w[RZ][r][e];
+          const T L = lap<T, ORDER, NDIM, FAST>(
+              xr[r][R + e - (R >= 2 ? 2 : 1)], xr[r][R + e - 1], c, xr[r][R + e + 1], xr[r][R + e + (R >= 2 ? 2 : 1)],
+              yv[R + r - (R >= 2 ? 2 : 1)][e], yv[R + r - 1][e], yv[R + r + 1][e], yv[R + r + (R >= 2 ? 2 : 1)][e],
+              w[RZ >= 2 ? RZ - 2 : 0][r][e], w[RZ >= 1 ? RZ - 1 : 0][r][e], w[RZ + (RZ >= 1 ? 1 : 0)][r][e],
+              w[RZ + (RZ >= 2 ? 2 : 0)][r][e], kx, ky, kz);
+          T un = c;
+          if (STAGE != 1) {
+            const size_t off = (size_t)(q - 2 * RZ) * sxy + (size_t)r * nx + e;
+            un = (warp_inside || ((inside >> (r * VX + e)) & 1u)) ? p.un[(obase - p.out) + off] : T(0);
+          }
+          res[r][e] = combine<T, FAST>(stage, un, c, dt, L);
+        }
+      if (!zin) {  // frozen plane: copy, or zero on the outermost planes
+        const bool zero_all = p.zero_boundary && NDIM == 3 && (z == 0 || z == nz - 1);
+#pragma unroll
+        for (int r = 0; r < 2; ++r)
+#pragma unroll
+          for (int e = 0; e < VX; ++e) {
+            const bool zb = zero_all || (p.zero_boundary && ((edge >> (r * VX + e)) & 1u));
+            res[r][e] = zb ? T(0) : w[RZ][r][e];
+          }
+      } else if (!warp_clean) {
+#pragma unroll
+        for (int r = 0; r < 2; ++r)
+#pragma unroll
+          for (int e = 0; e < VX; ++e)
+            if ((keep >> (r * VX + e)) & 1u)
+              res[r][e] = (p.zero_boundary && ((edge >> (r * VX + e)) & 1u)) ? T(0) : w[RZ][r][e];
+      }
+      T* dst0 = obase + (size_t)(q - 2 * RZ) * sxy;
+#pragma unroll
+      for (int r = 0; r < 2; ++r) {
+        if (!row_ok[r]) continue;
+        T* dst = dst0 + (size_t)r * nx;
+        if (vec_rows) {
+          V v;
+#pragma unroll
+          for (int e = 0; e < VX; ++e) reinterpret_cast<T*>(&v)[e] = res[r][e];
+          *reinterpret_cast<V*>(dst) = v;
+        } else {
+#pragma unroll
+          for (int e = 0; e < VX; ++e)
+            if (xb + e < nx) dst[e] = res[r][e];
+        }
+      }
+    }
+    __syncthreads();  // every read of stream entry q - RZ is done: its slot can be refilled
+    if (*abort_flag) {
+      // A wait expired: let the copies already issued land (bounded) before the CTA exits.
+      if (TMA && tid == 0) {
+        int s = s_wait;
+        for (int m = q + 1; m < Q && m <= q + C::P; ++m) {
+          mbar_wait_bounded(&bars[s], (parity >> s) & 1u, p.status);
+          s = s + 1 == C::NS ? 0 : s + 1;
+        }
+      }
+      return HeatPipe{-1, -1, 0u};
+    }
+    if (q + C::P + 1 < Q) issue(q + C::P + 1);
+    else if (!TMA) cp_async_commit();
+  }
+  return HeatPipe{s_issue, s_wait, parity};
+}
+
+template <class T, int ORDER, int NDIM, bool TMA, int STAGE>
+__global__ void __launch_bounds__(256, ORDER == 2 ? 4 : (sizeof(T) == 4 ? 3 : 2))
+heat_stage_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ HeatParams<T> p) {
+  using C = HeatTile<T, ORDER, NDIM>;
+  uint64_t* bars = heat_bars<T, ORDER, NDIM>();
+  int& abort_flag = *heat_abort_flag();
+  const int tid = threadIdx.y * C::TX + threadIdx.x;
   // Balanced split: the (tile, z-plane) pairs, tile-major, are cut into gridDim.x equal
   // contiguous ranges; a range that crosses a tile boundary becomes several segments.
-  const int64_t total = (int64_t)p.tiles_x * p.tiles_y * nz;
+  const int64_t total = (int64_t)p.tiles_x * p.tiles_y * p.nz;
   const int64_t seg_a = total * blockIdx.x / gridDim.x, seg_b = total * (blockIdx.x + 1) / gridDim.x;
-
   if (tid == 0) {
     if (TMA) {
       for (int s = 0; s < C::NS; ++s) mbar_init(&bars[s], 1);
@@ -156,208 +378,71 @@ heat_stage_kernel(const __grid_constant__ CUtensorMap tmap, const HeatParams<T> 
     abort_flag = 0;
   }
   __syncthreads();
-
-  const T kx = p.kx, ky = p.ky, kz = p.kz, dt = p.dt;
-  const int F = p.frozen;
-  T w[2 * RZ + 1][2][VX];  // register window along z (w[RZ] = centre plane), two rows
-  int s_issue = 0, s_wait = 0;  // ring slots of the next plane to issue / to wait for
-  unsigned parity = 0;          // per-slot phase parity of the next wait
-
+  HeatPipe pipe{0, 0, 0u};
   for (int64_t pos = seg_a; pos < seg_b;) {
-    const int64_t tile = pos / nz;
-    const int zs = (int)(pos - tile * nz);
-    const int ze = (int)min((int64_t)nz, zs + (seg_b - pos));
+    const int64_t tile = pos / p.nz;
+    const int zs = (int)(pos - tile * p.nz);
+    const int ze = (int)min((int64_t)p.nz, zs + (seg_b - pos));
     pos += ze - zs;
     const int x0 = (int)(tile % p.tiles_x) * C::BX, y0 = (int)(tile / p.tiles_x) * C::BY;
-    const int Q = (ze - zs) + 2 * RZ;  // planes streamed for this segment
-    const int p0 = zs - RZ;            // z of stream entry 0
+    pipe = heat_segment<T, ORDER, NDIM, TMA, STAGE>(&tmap, p, x0, y0, zs, ze, pipe);
+    if (pipe.s_issue < 0) return;
+  }
+}
 
-    auto issue = [&](int q) {
-      T* dst = ring + s_issue * C::SLOT_ELEMS;
-      const int z = p0 + q;
-      if (TMA) {
-        if (tid == 0) {
-          mbar_arrive_expect_tx(&bars[s_issue], C::PLANE_BYTES);
-          tma_load_3d(dst, &tmap, x0 - C::PADX, y0 - R, z, &bars[s_issue]);
-        }
-      } else {
-        const bool zok = z >= 0 && z < nz;
-        for (int e = tid; e < C::PLANE; e += C::NT) {
-          const int r = e / SW, c = e - r * SW;
-          const int gx = x0 - C::PADX + c, gy = y0 - R + r;
-          const bool ok = zok && gx >= 0 && gx < nx && gy >= 0 && gy < ny;
-          const T* src = ok ? p.uin + (size_t)z * sxy + (size_t)gy * nx + gx : p.uin;
-          cp_async_zfill<sizeof(T)>(dst + e, src, ok);
-        }
-        cp_async_commit();
-      }
-      s_issue = s_issue + 1 == C::NS ? 0 : s_issue + 1;
-    };
+// Batched forward-Euler stage over many 3D instances: instance i, ping-pong parity `par`
+// (input buffer par, output 1 - par). The units (instance, tile, z-plane) of all instances,
+// instance-major then tile-major, are cut into gridDim.x equal contiguous ranges.
+template <class T>
+struct alignas(64) HeatBatchInst {
+  CUtensorMap tmap[2];    // tensor maps of buffer 0 / buffer 1
+  HeatParams<T> p[2];     // parameters with input buffer 0 / 1
+  int64_t unit_begin;     // first unit of this instance
+  int64_t pad[7];
+};
 
-    for (int q = 0; q <= C::P && q < Q; ++q) issue(q);
-    if (!TMA)
-      for (int q = Q; q <= C::P; ++q) cp_async_commit();  // one group per plane index
-
-    const int xb = x0 + tx * VX;  // first node of this thread
-    const int ya = y0 + 2 * ty;   // this thread's rows: ya, ya + 1
-    // Node classes of this thread's x-y positions, fixed over the segment (bit r*VX + e):
-    // keep = not updated on interior planes (frozen layer or outside the grid),
-    // edge = on the outermost x/y layer (written 0 under zero_boundary), inside = in the grid.
-    unsigned keep = 0, edge = 0, inside = 0;
-#pragma unroll
-    for (int r = 0; r < 2; ++r)
-#pragma unroll
-      for (int e = 0; e < VX; ++e) {
-        const int x = xb + e, y = ya + r;
-        const unsigned bit = 1u << (r * VX + e);
-        if (!(x >= F && x < nx - F && y >= F && y < ny - F)) keep |= bit;
-        if (x == 0 || x == nx - 1 || y == 0 || y == ny - 1) edge |= bit;
-        if (x < nx && y < ny) inside |= bit;
-      }
-    constexpr unsigned ALL = (1u << (2 * VX)) - 1u;
-    const bool warp_clean = __all_sync(0xffffffffu, keep == 0);   // no fix-ups on interior planes
-    const bool warp_inside = __all_sync(0xffffffffu, inside == ALL);
-    const bool row_ok[2] = {ya < ny, ya + 1 < ny};
-    const bool vec_rows = p.vec_ok && xb + VX <= nx;
-    T* obase = p.out + (size_t)zs * sxy + (size_t)ya * nx + xb;  // output row pointer, plane zs
-
-#pragma unroll 1
-    for (int q = 0; q < Q; ++q) {
-      // ---- wait for plane q
-      bool ok = true;
-      if (TMA) {
-        ok = mbar_wait_warp(&bars[s_wait], (parity >> s_wait) & 1u, p.status, tx);
-        if (!ok) abort_flag = 1;
-      } else {
-        cp_async_wait<C::P>();
-        __syncthreads();
-      }
-      parity ^= 1u << s_wait;
-      const int s_cent = s_wait >= RZ ? s_wait - RZ : s_wait - RZ + C::NS;
-      const T* plq = ring + s_wait * C::SLOT_ELEMS + (2 * ty + R) * SW + C::PADX + tx * VX;
-      s_wait = s_wait + 1 == C::NS ? 0 : s_wait + 1;
-      const bool warp_abort = __any_sync(0xffffffffu, !ok);  // shuffles below need all lanes
-
-      // ---- slide the window; push this thread's two rows of plane q
-#pragma unroll
-      for (int s = 0; s < 2 * RZ; ++s)
-#pragma unroll
-        for (int r = 0; r < 2; ++r)
-#pragma unroll
-          for (int e = 0; e < VX; ++e) w[s][r][e] = w[s + 1][r][e];
-#pragma unroll
-      for (int r = 0; r < 2; ++r) {
-        const V v = *reinterpret_cast<const V*>(plq + r * SW);
-#pragma unroll
-        for (int e = 0; e < VX; ++e) w[2 * RZ][r][e] = reinterpret_cast<const T*>(&v)[e];
-      }
-
-      if (q >= 2 * RZ && !warp_abort) {
-        const int z = p0 + q - RZ;  // output plane (stream entry q - RZ)
-        const T* row0 = ring + s_cent * C::SLOT_ELEMS + (2 * ty + R) * SW + C::PADX + tx * VX;
-        // x-neighbourhood of both rows: xr[r][j] holds x = xb - R + j.
-        T xr[2][VX + 2 * R];
-#pragma unroll
-        for (int r = 0; r < 2; ++r) {
-#pragma unroll
-          for (int e = 0; e < VX; ++e) xr[r][R + e] = w[RZ][r][e];
-#pragma unroll
-          for (int d = 1; d <= R; ++d) {
-            T lft = __shfl_up_sync(0xffffffffu, w[RZ][r][VX - d], 1);
-            T rgt = __shfl_down_sync(0xffffffffu, w[RZ][r][d - 1], 1);
-            if (tx == 0) lft = row0[r * SW - d];
-            if (tx == C::TX - 1) rgt = row0[r * SW + VX - 1 + d];
-            xr[r][R - d] = lft;
-            xr[r][R + VX - 1 + d] = rgt;
-          }
-        }
-        // y-neighbourhood: yv[j][e] holds row ya - R + j (j = 0 .. 2R+1); rows ya, ya+1 are own.
-        T yv[2 * R + 2][VX];
-#pragma unroll
-        for (int d = 1; d <= R; ++d) {
-          const V a = *reinterpret_cast<const V*>(row0 - d * SW);
-          const V b = *reinterpret_cast<const V*>(row0 + (1 + d) * SW);
-#pragma unroll
-          for (int e = 0; e < VX; ++e) {
-            yv[R - d][e] = reinterpret_cast<const T*>(&a)[e];
-            yv[R + 1 + d][e] = reinterpret_cast<const T*>(&b)[e];
-          }
-        }
-#pragma unroll
-        for (int e = 0; e < VX; ++e) {
-          yv[R][e] = w[RZ][0][e];
-          yv[R + 1][e] = w[RZ][1][e];
-        }
-        const bool zin = NDIM == 2 || (z >= F && z < nz - F);
-        // Every lane evaluates the stencil (halo values outside the grid are finite zero fill);
-        // nodes that are not updated are fixed up afterwards with warp-uniform branches.
-        T res[2][VX];
-#pragma unroll
-        for (int r = 0; r < 2; ++r)
-#pragma unroll
-          for (int e = 0; e < VX; ++e) {
-            const T c = w[RZ][r][e];
-            const T L = lap<T, ORDER, NDIM, FAST>(
-                xr[r][R + e - (R >= 2 ? 2 : 1)], xr[r][R + e - 1], c, xr[r][R + e + 1], xr[r][R + e + (R >= 2 ? 2 : 1)],
-                yv[R + r - (R >= 2 ? 2 : 1)][e], yv[R + r - 1][e], yv[R + r + 1][e], yv[R + r + (R >= 2 ? 2 : 1)][e],
-                w[RZ >= 2 ? RZ - 2 : 0][r][e], w[RZ >= 1 ? RZ - 1 : 0][r][e], w[RZ + (RZ >= 1 ? 1 : 0)][r][e],
-                w[RZ + (RZ >= 2 ? 2 : 0)][r][e], kx, ky, kz);
-            T un = c;
-            if (STAGE != 1) {
-              const size_t off = (size_t)(q - 2 * RZ) * sxy + (size_t)r * nx + e;
-              un = (warp_inside || ((inside >> (r * VX + e)) & 1u)) ? p.un[(obase - p.out) + off] : T(0);
-            }
-            res[r][e] = combine<T, FAST>(stage, un, c, dt, L);
-          }
-        if (!zin) {  // frozen plane: copy, or zero on the outermost planes
-          const bool zero_all = p.zero_boundary && NDIM == 3 && (z == 0 || z == nz - 1);
-#pragma unroll
-          for (int r = 0; r < 2; ++r)
-#pragma unroll
-            for (int e = 0; e < VX; ++e) {
-              const bool zb = zero_all || (p.zero_boundary && ((edge >> (r * VX + e)) & 1u));
-              res[r][e] = zb ? T(0) : w[RZ][r][e];
-            }
-        } else if (!warp_clean) {
-#pragma unroll
-          for (int r = 0; r < 2; ++r)
-#pragma unroll
-            for (int e = 0; e < VX; ++e)
-              if ((keep >> (r * VX + e)) & 1u)
-                res[r][e] = (p.zero_boundary && ((edge >> (r * VX + e)) & 1u)) ? T(0) : w[RZ][r][e];
-        }
-        T* dst0 = obase + (size_t)(q - 2 * RZ) * sxy;
-#pragma unroll
-        for (int r = 0; r < 2; ++r) {
-          if (!row_ok[r]) continue;
-          T* dst = dst0 + (size_t)r * nx;
-          if (vec_rows) {
-            V v;
-#pragma unroll
-            for (int e = 0; e < VX; ++e) reinterpret_cast<T*>(&v)[e] = res[r][e];
-            *reinterpret_cast<V*>(dst) = v;
-          } else {
-#pragma unroll
-            for (int e = 0; e < VX; ++e)
-              if (xb + e < nx) dst[e] = res[r][e];
-          }
-        }
-      }
-      __syncthreads();  // every read of stream entry q - RZ is done: its slot can be refilled
-      if (abort_flag) {
-        // A wait expired: let the copies already issued land (bounded) before the CTA exits.
-        if (TMA && tid == 0) {
-          int s = s_wait;
-          for (int m = q + 1; m < Q && m <= q + C::P; ++m) {
-            mbar_wait_bounded(&bars[s], (parity >> s) & 1u, p.status);
-            s = s + 1 == C::NS ? 0 : s + 1;
-          }
-        }
-        return;
-      }
-      if (q + C::P + 1 < Q) issue(q + C::P + 1);
-      else if (!TMA) cp_async_commit();
+template <class T, bool TMA>
+__global__ void __launch_bounds__(256, 4)
+heat_batch_kernel(const HeatBatchInst<T>* __restrict__ inst, int n_inst, int64_t total_units, int par) {
+  using C = HeatTile<T, 2, 3>;
+  uint64_t* bars = heat_bars<T, 2, 3>();
+  int& abort_flag = *heat_abort_flag();
+  const int tid = threadIdx.y * C::TX + threadIdx.x;
+  const int64_t seg_a = total_units * blockIdx.x / gridDim.x, seg_b = total_units * (blockIdx.x + 1) / gridDim.x;
+  if (tid == 0) {
+    if (TMA) {
+      for (int s = 0; s < C::NS; ++s) mbar_init(&bars[s], 1);
+      mbar_fence_init();
     }
+    abort_flag = 0;
+  }
+  __syncthreads();
+  HeatPipe pipe{0, 0, 0u};
+  // instance of the first unit (binary search on unit_begin)
+  int i = 0;
+  {
+    int lo = 0, hi = n_inst - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) / 2;
+      if (inst[mid].unit_begin <= seg_a) lo = mid; else hi = mid - 1;
+    }
+    i = lo;
+  }
+  for (int64_t pos = seg_a; pos < seg_b;) {
+    while (i + 1 < n_inst && inst[i + 1].unit_begin <= pos) ++i;
+    const HeatParams<T>& p = inst[i].p[par];
+    const int64_t local = pos - inst[i].unit_begin;
+    const int64_t inst_end = i + 1 < n_inst ? inst[i + 1].unit_begin : total_units;
+    const int64_t tile = local / p.nz;
+    const int zs = (int)(local - tile * p.nz);
+    const int64_t stop = min(seg_b, inst_end);
+    const int ze = (int)min((int64_t)p.nz, zs + (stop - pos));
+    pos += ze - zs;
+    const int x0 = (int)(tile % p.tiles_x) * C::BX, y0 = (int)(tile / p.tiles_x) * C::BY;
+    const CUtensorMap* tm = &inst[i].tmap[par];
+    if (TMA && tid == 0) tma_prefetch_desc(tm);
+    pipe = heat_segment<T, 2, 3, TMA, 1>(tm, p, x0, y0, zs, ze, pipe);
+    if (pipe.s_issue < 0) return;
   }
 }
 
