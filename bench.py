@@ -4,7 +4,9 @@ Default workload (the configuration the metric is quoted on): 3D heat equation o
 grid, FP32, 7-point Laplacian, forward Euler with r = k dt/h^2 = 1/8, Dirichlet u = 0, initial
 condition the sum of 8 seeded Gaussian blobs; one benchmark step = one full 2000-time-step solve.
 Other workloads: --workload burgers3d (256^3 periodic WENO5-Z, global Lax-Friedrichs, SSP-RK3,
-CFL 0.4; one benchmark step = 20 time steps).
+CFL 0.4; one benchmark step = 20 time steps); --workload ensemble (64 heat + 32 Burgers 3D
+instances of uneven size advanced by one CUDA graph, 500 steps each; one benchmark step = one
+ensemble run; also times the plain per-instance loop over the same instances).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload ...]
 
@@ -107,12 +109,28 @@ class ClockSampler:
 
 
 # ----------------------------------------------------------------------------- workloads
+def ic_heat3d_blobs(nx, ny, nz, seed, nblobs=8):
+    """Seeded initial condition from the library's host generator (adv_ic_heat3d_blobs)."""
+    from multigpu_advectiondiffusion_gb300 import _native as N
+    u = np.empty(nx * ny * nz)
+    N.check(N.load().adv_ic_heat3d_blobs(nx, ny, nz, seed, nblobs, u.ctypes.data_as(C.POINTER(C.c_double))), "ic")
+    return u
+
+
+def ic_burgers_fourier(nx, ny, nz, L, seed, nmodes=16, amax=0.1):
+    """Seeded initial condition from the library's host generator (adv_ic_burgers_fourier)."""
+    from multigpu_advectiondiffusion_gb300 import _native as N
+    u = np.empty(nx * ny * nz)
+    N.check(N.load().adv_ic_burgers_fourier(nx, ny, nz, L, seed, nmodes, amax,
+                                            u.ctypes.data_as(C.POINTER(C.c_double))), "ic")
+    return u
+
+
 def heat_setup(dtype):
-    from oracle import oracle
     from multigpu_advectiondiffusion_gb300.solvers import HeatConfig
     n = 256
     cfg = HeatConfig.dirichlet_o2(3, n)
-    u0 = oracle.ic_heat3d_blobs(n, n, n, 2).astype(dtype)
+    u0 = ic_heat3d_blobs(n, n, n, 2).astype(dtype)
     return cfg, u0, 2000
 
 
@@ -127,6 +145,169 @@ def cpu_heat_rate(cfg, u0, budget_s: float):
     oracle.heat_run(cfg, u0, steps, 0)
     dt = time.perf_counter() - t0
     return cfg.numel * steps / dt / 1e9, steps, dt
+
+
+ENSEMBLE_SEED = 2024
+ENSEMBLE_STEPS = 500
+
+
+def ensemble_members():
+    """The batched-ensemble workload: 64 heat instances, n^3 with n uniform in {64,96,128,160,192},
+    diffusivity log-uniform in [0.1, 10], O2 forward Euler at r = 1/8 (dt per instance), Dirichlet
+    u = 0, 8 seeded Gaussian blobs each; 32 periodic WENO5-Z global-LF Burgers instances, n^3 with n
+    uniform in {96,112,128,144,160}, seeded 16-mode Fourier initial conditions, CFL 0.4. FP32."""
+    from multigpu_advectiondiffusion_gb300.solvers import BurgersConfig, HeatConfig
+    rng = np.random.default_rng(ENSEMBLE_SEED)
+    heat = []
+    for _ in range(64):
+        n = int(rng.choice([64, 96, 128, 160, 192]))
+        k = float(10 ** rng.uniform(-1, 1))
+        heat.append(HeatConfig.dirichlet_o2(3, n, k=k, r=0.125))
+    burgers = [BurgersConfig.periodic(int(rng.choice([96, 112, 128, 144, 160])), weno="z", div="fast")
+               for _ in range(32)]
+    return heat, burgers
+
+
+def ensemble_initial_states(heat, burgers):
+    hs = [ic_heat3d_blobs(c.nx, c.ny, c.nz, 100 + i).astype(np.float32) for i, c in enumerate(heat)]
+    bs = [ic_burgers_fourier(c.nx, c.ny, c.nz, 2.0, 200 + i).astype(np.float32) for i, c in enumerate(burgers)]
+    return hs, bs
+
+
+def bench_ensemble(args, world, rank, dev, stream, flush, lib):
+    import torch
+    import torch.distributed as dist
+    from multigpu_advectiondiffusion_gb300 import _native as N
+    from multigpu_advectiondiffusion_gb300.solvers import (Ensemble, burgers_run, burgers_workspace, heat_run,
+                                                           heat_workspace)
+    heat, burgers = ensemble_members()
+    h0, b0 = ensemble_initial_states(heat, burgers)
+    hu = [torch.from_numpy(a).to(dev) for a in h0]
+    bu = [torch.from_numpy(a).to(dev) for a in b0]
+    S = ENSEMBLE_STEPS
+    ens = Ensemble(heat=list(zip(heat, hu)), burgers=[(c, u, 1e9, 0.4, N.ADV_DT_MAXU, S) for c, u in zip(burgers, bu)])
+    sh = stream.cuda_stream
+    heat_cells = sum(c.numel for c in heat)
+    burg_cells = sum(c.numel for c in burgers)
+    work = heat_cells * S + burg_cells * 3 * S  # cell updates per RK stage in one ensemble run
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    def timed(fn, K):
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier()
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(K):
+            with torch.cuda.stream(stream):
+                flush.fill_(1.0)
+            fn()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        return ev0.elapsed_time(ev1)
+
+    def reset():
+        for u, a in zip(hu + bu, h0 + b0):
+            u.copy_(torch.from_numpy(a).to(dev), non_blocking=False)
+
+    def one_step():
+        ens.run(S, stream=sh)
+
+    for _ in range(args.warmup):
+        reset()
+        one_step()
+    uuid = None
+    try:
+        uuid = "GPU-" + str(torch.cuda.get_device_properties(dev).uuid)
+    except Exception:
+        pass
+    # Each timed step starts from the same initial states (reset outside the timed region would
+    # need K separate regions; the states stay bounded over repeated runs, so the runs continue).
+    reset()
+    with ClockSampler(uuid) as clk:
+        one_step()
+        launches0 = lib.adv_kernel_launch_count()
+        ms = timed(one_step, args.steps)
+        launched = lib.adv_kernel_launch_count() - launches0
+    ms_max = ms
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_max = t.item()
+    value = world * work * args.steps / (ms_max * 1e-3) / 1e9
+
+    # Burgers loop alone (heat_steps = 0): the batched WENO stage dominates; its average launch
+    # time is this loop's time over its 3 S stage launches (the per-step dt kernel included).
+    ms_b = timed(lambda: ens.run(0, stream=sh), 1)
+    fl = timed(lambda: None, 1)
+    launch_ms = (ms_b - fl) / (3 * S)
+    bytes_per_launch = (8 + 12 + 12) / 3 * burg_cells
+    achieved = bytes_per_launch / (launch_ms * 1e-3) / 1e9
+    peak, peak_kind = _peaks()
+
+    # plain per-instance loop over the same instances (each instance its own heat_run /
+    # burgers_run: one-wave grids per instance, one graph per instance)
+    hws = [heat_workspace(c, u) for c, u in zip(heat, hu)]
+    bws = [burgers_workspace(c, u) for c, u in zip(burgers, bu)]
+
+    def loop_step():
+        for c, u, w in zip(heat, hu, hws):
+            heat_run(c, u, S, w, stream=sh)
+        for c, u, w in zip(burgers, bu, bws):
+            burgers_run(c, u, 1e9, 0.4, N.ADV_DT_MAXU, max_steps=S, workspace=w, stream=sh)
+    loop_step()
+    ms_loop = timed(loop_step, 1)
+    loop_value = work / (ms_loop * 1e-3) / 1e9
+
+    # end to end: every instance's state from pinned host memory, results back
+    host_in = [torch.from_numpy(a).pin_memory() for a in h0 + b0]
+    host_out = [torch.empty_like(a) .pin_memory() for a in host_in]
+    dev_all = hu + bu
+
+    def e2e_step():
+        with torch.cuda.stream(stream):
+            for d, h in zip(dev_all, host_in):
+                d.copy_(h, non_blocking=True)
+        one_step()
+        with torch.cuda.stream(stream):
+            for h, d in zip(host_out, dev_all):
+                h.copy_(d, non_blocking=True)
+    e2e_step()
+    ems = timed(e2e_step, args.steps)
+    if world > 1:
+        t = torch.tensor([ems], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ems = t.item()
+    nbytes = sum(a.numel() * a.element_size() for a in host_in)
+    shape = ens.shape()
+    ens.close()
+    if rank == 0:
+        line = {
+            "metric": "Gcell-updates/s/RK-stage", "value": value, "unit": "Gcell-updates/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded sizes, diffusivities and Philox4x32-10 initial conditions)",
+            "config": {"workload": f"ensemble 64 heat (n in 64..192, o2 euler r=1/8) + 32 burgers (n in 96..160, "
+                                   f"weno5-z global-lf periodic cfl 0.4, fast div) x {S} steps, one graph",
+                       "parallelism": f"replicas{world}", "heat_cells": heat_cells, "burgers_cells": burg_cells,
+                       "l2": "1.5 GB heat + 0.9 GB Burgers state > 126 MiB L2; 252 MiB L2 flush between steps",
+                       **shape},
+            "roofline": {"bound": "hbm", "kernel": "burgers_batch_kernel<float,Z,FastDiv>", "achieved": achieved,
+                         "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                         "traffic": _traffic("ensemble"), "algorithmic_bytes_per_launch": bytes_per_launch,
+                         "avg_launch_us": launch_ms * 1e3},
+            "cpu_baseline": None,
+            "e2e": {"value": world * work * args.steps / (ems * 1e-3) / 1e9, "unit": "Gcell-updates/s",
+                    "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
+            "gpu_launches": int(launched),
+            "clocks": clk.summary(),
+            "per_instance_loop_value": loop_value,
+            "speedup_vs_per_instance_loop": value / loop_value,
+        }
+        print(json.dumps(line), flush=True)
 
 
 def run_reference_arm(args, world, rank):
@@ -181,7 +362,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="heat3d", choices=["heat3d", "burgers3d"])
+    ap.add_argument("--workload", default="heat3d", choices=["heat3d", "burgers3d", "ensemble"])
     ap.add_argument("--cpu-budget", type=float, default=10.0, help="seconds of CPU-baseline work")
     ap.add_argument("--div", default="fast", choices=["fast", "f32", "f64"],
                     help="Burgers WENO weight division (FP32 state)")
@@ -216,6 +397,11 @@ def main():
     sh = stream.cuda_stream
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
 
+    if args.workload == "ensemble":
+        bench_ensemble(args, world, rank, dev, stream, flush, lib)
+        if world > 1:
+            dist.destroy_process_group()
+        return
     if args.workload == "heat3d":
         cfg, u0_np, inner = heat_setup(np.float32)
         u0 = torch.from_numpy(u0_np).to(dev)
@@ -230,10 +416,9 @@ def main():
         workload_name = "heat3d 256^3 f32 o2 euler r=1/8 dirichlet 8 blobs x 2000 steps"
         kernel = "heat_stage_kernel<float,2,3,TMA>"
     else:
-        from oracle import oracle
         n = 256
         cfg = BurgersConfig.periodic(n, weno="z", div=args.div)
-        u0 = torch.from_numpy(oracle.ic_burgers_fourier(n, n, n, 2.0, 3).astype(np.float32)).to(dev)
+        u0 = torch.from_numpy(ic_burgers_fourier(n, n, n, 2.0, 3).astype(np.float32)).to(dev)
         u = u0.clone()
         ws = burgers_workspace(cfg, u)
         inner = 20

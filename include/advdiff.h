@@ -151,6 +151,58 @@ adv_status adv_burgers_run(const adv_burgers_desc* d, void* u, void* workspace, 
                            double cfl, int dt_rule, double C, int64_t max_steps, double* t_out,
                            int64_t* steps_out, void* stream);
 
+/* ------------------------------------------------------------------ batched ensembles
+ * Many independent 3D problems of uneven size and coefficients advanced together. No counterpart
+ * in the reference (its drivers run one problem per process). Each stage of all heat members is
+ * ONE launch over every member's (tile, z-plane) units, each SSP-RK3 stage of all Burgers
+ * members likewise, and a whole run is one CUDA graph holding the heat and the Burgers time
+ * loops as two concurrent device-driven while-loops (dt, the Lax-Friedrichs constants and each
+ * Burgers member's stop test are computed on the device, per member).
+ * Heat members share dtype, order and the time scheme (given at create); ndim must be 3; sizes,
+ * coefficients, dt, frozen layers and boundary handling are per member. Burgers members share
+ * dtype, weno, div and whether the viscous term is present; sizes, spacing, lf, bc, bug_b2,
+ * tEnd, CFL and the dt rule are per member. Results equal the per-member adv_heat_run /
+ * adv_burgers_run bit for bit. Each member's state stays in its caller-owned buffer u; `work` is
+ * caller-owned scratch of adv_heat_workspace_bytes / adv_burgers_workspace_bytes bytes.
+ * Buffers must not overlap between members. The plan allocates its device tables, loop states
+ * and graph at create (runs allocate nothing) and frees them at destroy. */
+typedef struct adv_heat_member {
+  adv_heat_desc desc;
+  void* u;
+  void* work;
+} adv_heat_member;
+
+typedef struct adv_burgers_member {
+  adv_burgers_desc desc;
+  void* u;
+  void* work;
+  double tEnd, cfl;
+  int32_t dt_rule; /* adv_dt_rule */
+  int32_t pad0;
+  double C;          /* viscous coefficient for ADV_DT_FIXED's diffusive bound (0 drops it) */
+  int64_t max_steps; /* per-member step limit */
+} adv_burgers_member;
+
+typedef struct adv_ensemble adv_ensemble;
+
+/* Either count may be 0. heat_time_scheme: adv_time. The device current at create is the
+ * plan's device. */
+adv_status adv_ensemble_create(const adv_heat_member* heat, int n_heat, int heat_time_scheme,
+                               const adv_burgers_member* burgers, int n_burgers, adv_ensemble** out);
+/* heat_steps steps of every heat member and every Burgers member run to its tEnd (at most its
+ * max_steps), from the current contents of the members' u. ADV_ENSEMBLE_DIRECT launches the
+ * same kernels from the host instead of the graph (for comparison; Burgers then reads a stop
+ * flag back every 8 steps). Synchronises the stream. */
+#define ADV_ENSEMBLE_DIRECT 1
+adv_status adv_ensemble_run(adv_ensemble* e, int64_t heat_steps, int flags, void* stream);
+/* Time reached and steps taken by Burgers member i in the last run. */
+adv_status adv_ensemble_burgers_result(const adv_ensemble* e, int i, double* t, int64_t* steps);
+/* Units (tile-planes) per heat / Burgers stage launch and the CTAs of each launch (any pointer
+ * may be NULL). */
+adv_status adv_ensemble_shape(const adv_ensemble* e, int64_t* heat_units, int* heat_ctas,
+                              int64_t* burgers_units, int* burgers_ctas);
+adv_status adv_ensemble_destroy(adv_ensemble* e);
+
 /* ------------------------------------------------------------------ reductions
  * max|u| over n values into *out (host double). Synchronises the stream. */
 adv_status adv_max_abs(int dtype, const void* u, int64_t n, double* out, void* stream);

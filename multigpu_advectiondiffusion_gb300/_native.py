@@ -20,6 +20,7 @@ ADV_LF_LOCAL, ADV_LF_GLOBAL = 0, 1
 ADV_BC_FROZEN, ADV_BC_PERIODIC = 0, 1
 ADV_DIV_F32, ADV_DIV_F64, ADV_DIV_FAST = 0, 1, 2
 ADV_DT_FIXED, ADV_DT_MAXU = 0, 1
+ADV_ENSEMBLE_DIRECT = 1
 
 
 class HeatDesc(C.Structure):
@@ -38,6 +39,18 @@ class BurgersDesc(C.Structure):
                 ("kx", C.c_double), ("ky", C.c_double), ("kz", C.c_double)]
 
 
+class HeatMember(C.Structure):
+    """adv_heat_member (include/advdiff.h)."""
+    _fields_ = [("desc", HeatDesc), ("u", C.c_void_p), ("work", C.c_void_p)]
+
+
+class BurgersMember(C.Structure):
+    """adv_burgers_member (include/advdiff.h)."""
+    _fields_ = [("desc", BurgersDesc), ("u", C.c_void_p), ("work", C.c_void_p), ("tEnd", C.c_double),
+                ("cfl", C.c_double), ("dt_rule", C.c_int32), ("pad0", C.c_int32), ("C", C.c_double),
+                ("max_steps", C.c_int64)]
+
+
 # (name, restype, argtypes) for every symbol declared in include/advdiff.h and advdiff_ref_ops.h
 _VP, _I, _I64, _D = C.c_void_p, C.c_int, C.c_int64, C.c_double
 _PD = C.POINTER(C.c_double)
@@ -50,6 +63,13 @@ SIGNATURES = [
     ("adv_burgers_workspace_bytes", _I, [C.POINTER(BurgersDesc), C.POINTER(C.c_size_t)]),
     ("adv_burgers_run", _I, [C.POINTER(BurgersDesc), _VP, _VP, _D, _D, _I, _D, _I64, _PD,
                              C.POINTER(C.c_int64), _VP]),
+    ("adv_ensemble_create", _I, [C.POINTER(HeatMember), _I, _I, C.POINTER(BurgersMember), _I,
+                                 C.POINTER(_VP)]),
+    ("adv_ensemble_run", _I, [_VP, _I64, _I, _VP]),
+    ("adv_ensemble_burgers_result", _I, [_VP, _I, _PD, C.POINTER(C.c_int64)]),
+    ("adv_ensemble_shape", _I, [_VP, C.POINTER(C.c_int64), C.POINTER(C.c_int), C.POINTER(C.c_int64),
+                                C.POINTER(C.c_int)]),
+    ("adv_ensemble_destroy", _I, [_VP]),
     ("adv_max_abs", _I, [_I, _VP, _I64, _PD, _VP]),
     ("adv_ic_heat_ref", _I, [_I, _I, _I, _I, _D, _D, _D, _PD]),
     ("adv_ic_heat2d_gauss_noise", _I, [_I, _I, C.c_uint32, _D, _PD]),

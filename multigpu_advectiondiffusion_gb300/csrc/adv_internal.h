@@ -95,6 +95,13 @@ struct BurgersLoopState {
 };
 adv_status burgers_loop_begin_step(BurgersLoopState* st, int dtype, unsigned long long cond_handle,
                                    int use_cond, cudaStream_t s);
+adv_status burgers_loop_begin_step_batch(BurgersLoopState* st, int n, int dtype, unsigned long long cond_handle,
+                                         int use_cond, int* any_more, cudaStream_t s);
+// The initial loop state of one run (t = 0, the fixed dt of ADV_DT_FIXED, slot-0 key cleared).
+BurgersLoopState burgers_loop_state(const adv_burgers_desc& d, double tEnd, double cfl, int dt_rule, double C,
+                                    int64_t max_steps);
 adv_status max_abs_launch(int dtype, const void* u, int64_t n, void* accum_bits, cudaStream_t s);
+// One iteration of a device-counted loop (see api_device.cu).
+adv_status loop_tick(int64_t* remaining, int* active, unsigned long long cond_handle, int use_cond, cudaStream_t s);
 
 }  // namespace adv

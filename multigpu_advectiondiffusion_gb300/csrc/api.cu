@@ -393,21 +393,7 @@ adv_status adv_burgers_run(const adv_burgers_desc* d, void* u, void* workspace, 
   char* w2 = w1 + one;
   BurgersLoopState* dst = reinterpret_cast<BurgersLoopState*>(w1 + burgers_state_offset(d));
 
-  BurgersLoopState h{};
-  h.t = 0.0;
-  h.tEnd = tEnd;
-  h.cfl = cfl;
-  h.dx = d->dx;
-  {
-    const double dt1 = cfl * d->dx / 1.0;
-    const double dt2 = C > 0 ? 1. / (2 * C * (1 / d->dx / d->dx + 1 / d->dy / d->dy + 1 / d->dz / d->dz)) * 0.9
-                             : std::numeric_limits<double>::infinity();
-    h.dt_fixed = dt1 < dt2 ? dt1 : dt2;
-  }
-  h.step = 0;
-  h.max_steps = max_steps;
-  h.dt_rule = dt_rule;
-  h.active = 1;
+  BurgersLoopState h = burgers_loop_state(*d, tEnd, cfl, dt_rule, C, max_steps);
   ADV_CUDA_TRY(cudaMemcpyAsync(dst, &h, sizeof(h), cudaMemcpyHostToDevice, s));
   ADV_CUDA_TRY(cudaStreamSynchronize(s));
   void* key0 = d->dtype == ADV_F32 ? (void*)&dst->maxbits[0] : (void*)&dst->maxbits64[0];

@@ -100,34 +100,60 @@ struct Face<double, Z, D> {
   __device__ __forceinline__ static void split(double u, double a, double& fp, double& fm) { lf_split<double>(u, a, fp, fm); }
 };
 
-// FP32: at most 80 registers so three CTAs (24 warps) fit per SM; FP64: two CTAs.
+struct BurgersPipe {
+  int s_issue, s_wait;  // ring slots of the next plane to issue / to wait for
+  unsigned parity;      // per-slot phase parity of the next wait
+};
+
+// Shared-memory objects of the Burgers pipeline (one set per CTA, whichever kernel runs it).
+__device__ __forceinline__ uint64_t* burgers_bars() {
+  __shared__ uint64_t bars[BurgersTile::NS];
+  return bars;
+}
+__device__ __forceinline__ int* burgers_abort_flag() {
+  __shared__ int flag;
+  return &flag;
+}
+
+template <class T>
+__device__ __forceinline__ void burgers_cta_init(const CUtensorMap* tmap, bool tma) {
+  if (threadIdx.x == 0) {
+    if (tma) {
+      uint64_t* bars = burgers_bars();
+      for (int s = 0; s < BurgersTile::NS; ++s) mbar_init(&bars[s], 1);
+      mbar_fence_init();
+      if (tmap) tma_prefetch_desc(tmap);
+    }
+    *burgers_abort_flag() = 0;
+  }
+  __syncthreads();
+}
+
+// One segment: output planes [zs, ze) of the column tile at (x0, y0), streamed through the
+// ring. Flushes this segment's max|u_out| into p.maxabs_key. Returns the pipeline state for the
+// next segment (by value, so it stays in registers), with s_issue = -1 if a wait timed out (the
+// CTA must then return).
 template <class T, bool Z, class D, bool VISC>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2)
-burgers_stage_kernel(const __grid_constant__ CUtensorMap tmap, const BurgersParams<T> p) {
+__device__ __forceinline__ BurgersPipe burgers_segment(const CUtensorMap* tmap, const BurgersParams<T>& p, int x0,
+                                                       int y0, int zs, int ze, BurgersPipe pipe) {
   using TL = BurgersTile;
   using SM = BurgersSmem<T>;
   using K = typename KeyOf<T>::type;
   constexpr bool EXACT = sizeof(T) == 8;  // FP64: reference operand order, correctly rounded
 
-  if (p.active && *p.active == 0) return;
-
   extern __shared__ __align__(128) unsigned char smem_raw[];
   T* ring = reinterpret_cast<T*>(smem_raw);
   T* fpS = reinterpret_cast<T*>(smem_raw + SM::RING);
   T* fmS = fpS + TL::PLANE;
-  T* fxS = fmS + TL::PLANE;   // [BY][BX+1]
+  T* fxS = fmS + TL::PLANE;
   // fxS[f] for f < NXF: x-faces [BY][BX+1]; fxS[NXF + g]: y-faces [BY+1][BX]
-  __shared__ uint64_t bars[TL::NS];
-  __shared__ int abort_flag;
+  uint64_t* bars = burgers_bars();
+  int* abort_flag = burgers_abort_flag();
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nx = p.nx, ny = p.ny, nz = p.nz;
   const size_t sxy = (size_t)nx * ny;
   const bool per = p.periodic != 0;
-  // Balanced split: the (tile, z-plane) pairs, tile-major, are cut into gridDim.x equal
-  // contiguous ranges (one wave of CTAs); a range crossing a tile boundary becomes segments.
-  const int64_t total = (int64_t)p.tiles_x * p.tiles_y * nz;
-  const int64_t seg_a = total * blockIdx.x / gridDim.x, seg_b = total * (blockIdx.x + 1) / gridDim.x;
 
   // Lax-Friedrichs constant and dt for this stage.
   T alpha;
@@ -137,20 +163,10 @@ burgers_stage_kernel(const __grid_constant__ CUtensorMap tmap, const BurgersPara
   const T dt = (T)(p.dt_dev ? *p.dt_dev : p.dt_host);
   const bool glob = p.lf_global != 0;
 
-  if (tid == 0) {
-    if (p.tma) {
-      for (int s = 0; s < TL::NS; ++s) mbar_init(&bars[s], 1);
-      mbar_fence_init();
-      tma_prefetch_desc(&tmap);
-    }
-    abort_flag = 0;
-  }
-  __syncthreads();
-
-  // This thread's share of the 1072 x/y faces of a plane, fixed for the whole kernel: face f
-  // (f = tid + 256 r) is x-face f when f < NXF (row f / 33, face f % 33) or y-face g = f - NXF
-  // (face row g / 32, column g % 32). base: shared-memory index of the face's first stencil
-  // value; the other values follow at stride 1 (x) or SW (y).
+  // This thread's share of the 1072 x/y faces of a plane: face f (f = tid + 256 r) is x-face f
+  // when f < NXF (row f / 33, face f % 33) or y-face g = f - NXF (face row g / 32, column
+  // g % 32). base: shared-memory index of the face's first stencil value; the other values
+  // follow at stride 1 (x) or SW (y).
   int fbase[5];
   bool fisx[5], fact[5];
 #pragma unroll
@@ -173,51 +189,44 @@ burgers_stage_kernel(const __grid_constant__ CUtensorMap tmap, const BurgersPara
   const T rdx = T(1.0 / p.dx), rdy = T(1.0 / p.dy), rdz = T(1.0 / p.dz);
   const int F = per ? 0 : 3;
 
-  int s_issue = 0, s_wait = 0;  // ring slots of the next plane to issue / to wait for
-  unsigned parity = 0;          // per-slot phase parity of the next wait
+  int s_issue = pipe.s_issue, s_wait = pipe.s_wait;
+  unsigned parity = pipe.parity;
   // z windows per column: f+ at k-2..k+2, f- at k-1..k+3, the f+ of the newest plane held back
-  // one step, u at k-3..k+3 (viscous variant only); reset for every segment.
+  // one step, u at k-3..k+3 (viscous variant only).
   T fpw[2][5], fmw[2][5], fpn[2], uw[2][VISC ? 7 : 1];
 
-  for (int64_t pos = seg_a; pos < seg_b;) {
-  const int64_t tile = pos / nz;
-  const int zs = (int)(pos - tile * nz);
-  const int ze = (int)min((int64_t)nz, zs + (seg_b - pos));
-  pos += ze - zs;
-  const int x0 = (int)(tile % p.tiles_x) * TL::BX, y0 = (int)(tile / p.tiles_x) * TL::BY;
   const int Q = (ze - zs) + 2 * TL::R;
   const int p0 = zs - TL::R;
   const bool edge = per && (x0 - TL::PADX < 0 || x0 + TL::BX + TL::PADX > nx || y0 - TL::R < 0 || y0 + TL::BY + TL::R > ny);
-    auto plane_z = [&](int q) { return per ? wrapi(p0 + q, nz) : p0 + q; };
-    auto issue = [&](int q) {
-      T* dst = ring + s_issue * SM::SLOT_ELEMS;
-      const int z = plane_z(q);
-      if (p.tma) {
-        if (tid == 0) {
-          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-          uint64_t* bar = &bars[s_issue];
-          mbar_arrive_expect_tx(bar, TL::PLANE * (unsigned)sizeof(T));
-          tma_load_3d(dst, &tmap, x0 - TL::PADX, y0 - TL::R, z, bar);
-        }
-      } else {
-        const bool zok = z >= 0 && z < nz;
-        for (int e = tid; e < TL::PLANE; e += TL::NT) {
-          const int r = e / TL::SW, c = e - r * TL::SW;
-          int gx = x0 - TL::PADX + c, gy = y0 - TL::R + r;
-          if (per) { gx = wrapi(gx, nx); gy = wrapi(gy, ny); }
-          const bool ok = zok && gx >= 0 && gx < nx && gy >= 0 && gy < ny;
-          const T* src = ok ? p.uin + (size_t)z * sxy + (size_t)gy * nx + gx : p.uin;
-          cp_async_zfill<sizeof(T)>(dst + e, src, ok);
-        }
-        cp_async_commit();
+  auto plane_z = [&](int q) { return per ? wrapi(p0 + q, nz) : p0 + q; };
+  auto issue = [&](int q) {
+    T* dst = ring + s_issue * SM::SLOT_ELEMS;
+    const int z = plane_z(q);
+    if (p.tma) {
+      if (tid == 0) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        uint64_t* bar = &bars[s_issue];
+        mbar_arrive_expect_tx(bar, TL::PLANE * (unsigned)sizeof(T));
+        tma_load_3d(dst, tmap, x0 - TL::PADX, y0 - TL::R, z, bar);
       }
-      s_issue = s_issue + 1 == TL::NS ? 0 : s_issue + 1;
-    };
+    } else {
+      const bool zok = z >= 0 && z < nz;
+      for (int e = tid; e < TL::PLANE; e += TL::NT) {
+        const int r = e / TL::SW, c = e - r * TL::SW;
+        int gx = x0 - TL::PADX + c, gy = y0 - TL::R + r;
+        if (per) { gx = wrapi(gx, nx); gy = wrapi(gy, ny); }
+        const bool ok = zok && gx >= 0 && gx < nx && gy >= 0 && gy < ny;
+        const T* src = ok ? p.uin + (size_t)z * sxy + (size_t)gy * nx + gx : p.uin;
+        cp_async_zfill<sizeof(T)>(dst + e, src, ok);
+      }
+      cp_async_commit();
+    }
+    s_issue = s_issue + 1 == TL::NS ? 0 : s_issue + 1;
+  };
 
-    for (int q = 0; q <= TL::P && q < Q; ++q) issue(q);
-    if (!p.tma)
-      for (int q = Q; q <= TL::P; ++q) cp_async_commit();
-
+  for (int q = 0; q <= TL::P && q < Q; ++q) issue(q);
+  if (!p.tma)
+    for (int q = Q; q <= TL::P; ++q) cp_async_commit();
 
   T fz_prev[2] = {T(0), T(0)};
 #pragma unroll
@@ -232,7 +241,7 @@ burgers_stage_kernel(const __grid_constant__ CUtensorMap tmap, const BurgersPara
     T* plq = ring + s_wait * SM::SLOT_ELEMS;
     const int s_cent = s_wait >= 3 ? s_wait - 3 : s_wait - 3 + TL::NS;  // slot of stream entry q - 3
     if (p.tma) {
-      if (!mbar_wait_warp(&bars[s_wait], (parity >> s_wait) & 1u, p.status, lane)) abort_flag = 1;
+      if (!mbar_wait_warp(&bars[s_wait], (parity >> s_wait) & 1u, p.status, lane)) *abort_flag = 1;
       if (edge) {
         // Periodic edge tile: the TMA box zero-filled what lies outside the domain; fill it with
         // the wrapped neighbours. Written here, read only after the next barrier.
@@ -248,7 +257,7 @@ burgers_stage_kernel(const __grid_constant__ CUtensorMap tmap, const BurgersPara
       cp_async_wait<TL::P>();
     }
     __syncthreads();  // plane q visible to all threads; abort_flag now uniform
-    const bool aborted = abort_flag != 0;
+    const bool aborted = *abort_flag != 0;
     parity ^= 1u << s_wait;
     s_wait = s_wait + 1 == TL::NS ? 0 : s_wait + 1;
     // ---- z windows: push plane q for this thread's two columns
@@ -365,15 +374,87 @@ burgers_stage_kernel(const __grid_constant__ CUtensorMap tmap, const BurgersPara
           sl = sl + 1 == TL::NS ? 0 : sl + 1;
         }
       }
-      return;
+      return BurgersPipe{-1, -1, 0u};
     }
     if (q + TL::P + 1 < Q) issue(q + TL::P + 1);
     else if (!p.tma) cp_async_commit();
   }
-  }  // segments
   if (p.maxabs_key) {
     kmax = warp_max(kmax);
     if (lane == 0 && kmax) atomicMax(static_cast<K*>(p.maxabs_key), kmax);
+  }
+  return BurgersPipe{s_issue, s_wait, parity};
+}
+
+// FP32: at most 80 registers so three CTAs (24 warps) fit per SM; FP64: two CTAs.
+template <class T, bool Z, class D, bool VISC>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2)
+burgers_stage_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ BurgersParams<T> p) {
+  using TL = BurgersTile;
+  if (p.active && *p.active == 0) return;
+  // Balanced split: the (tile, z-plane) pairs, tile-major, are cut into gridDim.x equal
+  // contiguous ranges (one wave of CTAs); a range crossing a tile boundary becomes segments.
+  const int nz = p.nz;
+  const int64_t total = (int64_t)p.tiles_x * p.tiles_y * nz;
+  const int64_t seg_a = total * blockIdx.x / gridDim.x, seg_b = total * (blockIdx.x + 1) / gridDim.x;
+  burgers_cta_init<T>(&tmap, p.tma != 0);
+  BurgersPipe pipe{0, 0, 0u};
+  for (int64_t pos = seg_a; pos < seg_b;) {
+    const int64_t tile = pos / nz;
+    const int zs = (int)(pos - tile * nz);
+    const int ze = (int)min((int64_t)nz, zs + (seg_b - pos));
+    pos += ze - zs;
+    const int x0 = (int)(tile % p.tiles_x) * TL::BX, y0 = (int)(tile / p.tiles_x) * TL::BY;
+    pipe = burgers_segment<T, Z, D, VISC>(&tmap, p, x0, y0, zs, ze, pipe);
+    if (pipe.s_issue < 0) return;
+  }
+}
+
+// One instance of a batched Burgers stage: the tensor map of its stage input and the stage's
+// parameters (per-instance buffers, dt / Lax-Friedrichs sources, max|u| key, active flag).
+template <class T>
+struct alignas(64) BurgersBatchInst {
+  CUtensorMap tmap;
+  BurgersParams<T> p;
+  int64_t unit_begin;  // first unit of this instance
+  int64_t pad[7];
+};
+
+// Batched stage over many instances: the units (instance, tile, z-plane) of all instances,
+// instance-major then tile-major, are cut into gridDim.x equal contiguous ranges. Instances
+// whose active flag is 0 are skipped (the choice is per segment, so uniform over the CTA).
+template <class T, bool Z, class D, bool VISC>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2)
+burgers_batch_kernel(const BurgersBatchInst<T>* __restrict__ inst, int n_inst, int64_t total_units, int tma) {
+  using TL = BurgersTile;
+  const int64_t seg_a = total_units * blockIdx.x / gridDim.x, seg_b = total_units * (blockIdx.x + 1) / gridDim.x;
+  burgers_cta_init<T>(nullptr, tma != 0);
+  BurgersPipe pipe{0, 0, 0u};
+  int i = 0;
+  {
+    int lo = 0, hi = n_inst - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) / 2;
+      if (inst[mid].unit_begin <= seg_a) lo = mid; else hi = mid - 1;
+    }
+    i = lo;
+  }
+  for (int64_t pos = seg_a; pos < seg_b;) {
+    while (i + 1 < n_inst && inst[i + 1].unit_begin <= pos) ++i;
+    const BurgersParams<T>& p = inst[i].p;
+    const int64_t local = pos - inst[i].unit_begin;
+    const int64_t inst_end = i + 1 < n_inst ? inst[i + 1].unit_begin : total_units;
+    const int64_t tile = local / p.nz;
+    const int zs = (int)(local - tile * p.nz);
+    const int64_t stop = min(seg_b, inst_end);
+    const int ze = (int)min((int64_t)p.nz, zs + (stop - pos));
+    pos += ze - zs;
+    if (p.active && *p.active == 0) continue;
+    const int x0 = (int)(tile % p.tiles_x) * TL::BX, y0 = (int)(tile / p.tiles_x) * TL::BY;
+    const CUtensorMap* tm = &inst[i].tmap;
+    if (tma && threadIdx.x == 0) tma_prefetch_desc(tm);
+    pipe = burgers_segment<T, Z, D, VISC>(tm, p, x0, y0, zs, ze, pipe);
+    if (pipe.s_issue < 0) return;
   }
 }
 

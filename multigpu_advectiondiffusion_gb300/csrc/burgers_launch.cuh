@@ -9,9 +9,9 @@ namespace adv {
 template <class T>
 void* burgers_kernel_for(const adv_burgers_desc& d);
 
+// Stage parameters of one launch (or of one instance of a batched launch).
 template <class T>
-adv_status burgers_launch_t(const adv_burgers_desc& d, const BurgersLaunch& L, const BurgersStageArgs& a,
-                            cudaStream_t s) {
+BurgersParams<T> burgers_params(const adv_burgers_desc& d, const BurgersLaunch& L, const BurgersStageArgs& a) {
   BurgersParams<T> p;
   p.uin = static_cast<const T*>(a.u_in);
   p.un = static_cast<const T*>(a.u_n);
@@ -35,6 +35,13 @@ adv_status burgers_launch_t(const adv_burgers_desc& d, const BurgersLaunch& L, c
   p.maxabs_key = a.maxabs_key;
   p.active = a.active;
   p.status = device_status_ptr();
+  return p;
+}
+
+template <class T>
+adv_status burgers_launch_t(const adv_burgers_desc& d, const BurgersLaunch& L, const BurgersStageArgs& a,
+                            cudaStream_t s) {
+  BurgersParams<T> p = burgers_params<T>(d, L, a);
   void* k = burgers_kernel_for<T>(d);
   if (!k) return set_error(ADV_ERR_UNSUPPORTED, "burgers: no kernel for this configuration");
   void* args[] = {const_cast<CUtensorMap*>(&L.tmap_in), &p};

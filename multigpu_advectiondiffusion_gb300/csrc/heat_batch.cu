@@ -1,0 +1,36 @@
+// heat_batch.cu -- instantiations of the batched 3D heat stage (heat_batch_kernel in
+// heat_stage.cuh) used by the ensembles.
+#include "adv_internal.h"
+#include "heat_stage.cuh"
+
+namespace adv {
+
+// Kernel for (state type, order, TMA or cp.async loads, stage specialisation 1..3).
+void* heat_batch_kernel_for(int dtype, int order, bool tma, int stage_kind) {
+#define HB(T, O, M, S) reinterpret_cast<void*>(&heat_batch_kernel<T, O, M, S>)
+#define HS(T, O, M)                  \
+  switch (stage_kind) {              \
+    case 1: return HB(T, O, M, 1);   \
+    case 2: return HB(T, O, M, 2);   \
+    case 3: return HB(T, O, M, 3);   \
+    default: return nullptr;         \
+  }
+#define HM(T, O) if (tma) { HS(T, O, true) } else { HS(T, O, false) }
+  if (dtype == ADV_F32) {
+    if (order == 2) { HM(float, 2) }
+    if (order == 4) { HM(float, 4) }
+  } else if (dtype == ADV_F64) {
+    if (order == 2) { HM(double, 2) }
+    if (order == 4) { HM(double, 4) }
+  }
+#undef HM
+#undef HS
+#undef HB
+  return nullptr;
+}
+
+size_t heat_batch_inst_bytes(int dtype) {
+  return dtype == ADV_F32 ? sizeof(HeatBatchInst<float>) : sizeof(HeatBatchInst<double>);
+}
+
+}  // namespace adv

@@ -23,11 +23,3 @@ void* heat_kernel_f32(int order, int ndim, bool tma, int stage_kind) {
 }
 
 }  // namespace adv
-
-namespace adv {
-// Batched forward-Euler stage over many 3D instances (see heat_batch_kernel).
-void* heat_batch_kernel_f32(bool tma) {
-  return tma ? reinterpret_cast<void*>(&heat_batch_kernel<float, true>)
-             : reinterpret_cast<void*>(&heat_batch_kernel<float, false>);
-}
-}  // namespace adv

@@ -3,8 +3,7 @@
 #include <algorithm>
 #include <cstring>
 
-#include "adv_internal.h"
-#include "heat_stage.cuh"
+#include "heat_launch.cuh"
 
 namespace adv {
 
@@ -102,17 +101,7 @@ adv_status heat_prepare(const adv_heat_desc& d, const void* u_in, HeatLaunch* L)
 template <class T>
 static adv_status heat_launch_t(const adv_heat_desc& d, const HeatLaunch& L, int stage, const void* u_in,
                                 const void* u_n, void* u_out, cudaStream_t s) {
-  HeatParams<T> p;
-  p.uin = static_cast<const T*>(u_in);
-  p.un = static_cast<const T*>(u_n);
-  p.out = static_cast<T*>(u_out);
-  p.nx = d.nx; p.ny = d.ny; p.nz = d.ndim == 3 ? d.nz : 1;
-  p.frozen = d.frozen; p.zero_boundary = d.zero_boundary; p.stage = stage;
-  p.tiles_x = L.tiles_x;
-  p.tiles_y = L.tiles_y;
-  p.vec_ok = (((uintptr_t)u_out % 16) == 0 && ((int64_t)d.nx * sizeof(T)) % 16 == 0) ? 1 : 0;
-  p.kx = (T)d.kx; p.ky = (T)d.ky; p.kz = (T)d.kz; p.dt = (T)d.dt;
-  p.status = device_status_ptr();
+  HeatParams<T> p = heat_params<T>(d, L, stage, u_in, u_n, u_out);
   const int stage_kind = (stage == 1 && u_n != u_in) ? 0 : stage;
   void* k = pick_kernel(d.dtype, d.order, d.ndim, L.tma, stage_kind);
   void* args[] = {const_cast<CUtensorMap*>(&L.tmap_in), &p};

@@ -390,22 +390,28 @@ heat_stage_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constan
   }
 }
 
-// Batched forward-Euler stage over many 3D instances: instance i, ping-pong parity `par`
-// (input buffer par, output 1 - par). The units (instance, tile, z-plane) of all instances,
-// instance-major then tile-major, are cut into gridDim.x equal contiguous ranges.
+// One instance of a batched 3D heat run: per slot (the stages of one time step), the tensor map
+// of the stage input and the stage's parameters. Forward Euler uses slots 0 (u -> w1) and
+// 1 (w1 -> u); SSP-RK3 uses slots 0, 1, 2 for its three stages.
 template <class T>
 struct alignas(64) HeatBatchInst {
-  CUtensorMap tmap[2];    // tensor maps of buffer 0 / buffer 1
-  HeatParams<T> p[2];     // parameters with input buffer 0 / 1
-  int64_t unit_begin;     // first unit of this instance
+  CUtensorMap tmap[3];
+  HeatParams<T> p[3];
+  int64_t unit_begin;  // first unit of this instance
   int64_t pad[7];
 };
 
-template <class T, bool TMA>
-__global__ void __launch_bounds__(256, 4)
-heat_batch_kernel(const HeatBatchInst<T>* __restrict__ inst, int n_inst, int64_t total_units, int par) {
-  using C = HeatTile<T, 2, 3>;
-  uint64_t* bars = heat_bars<T, 2, 3>();
+// Batched stage over many 3D instances (slot `slot` of each): the units (instance, tile,
+// z-plane) of all instances, instance-major then tile-major, are cut into gridDim.x equal
+// contiguous ranges. Returns at once when *active == 0 (predicated steps of a device-driven
+// loop).
+template <class T, int ORDER, bool TMA, int STAGE>
+__global__ void __launch_bounds__(256, ORDER == 2 ? 4 : (sizeof(T) == 4 ? 3 : 2))
+heat_batch_kernel(const HeatBatchInst<T>* __restrict__ inst, int n_inst, int64_t total_units, int slot,
+                  const int* active) {
+  using C = HeatTile<T, ORDER, 3>;
+  if (active && *active == 0) return;
+  uint64_t* bars = heat_bars<T, ORDER, 3>();
   int& abort_flag = *heat_abort_flag();
   const int tid = threadIdx.y * C::TX + threadIdx.x;
   const int64_t seg_a = total_units * blockIdx.x / gridDim.x, seg_b = total_units * (blockIdx.x + 1) / gridDim.x;
@@ -430,7 +436,7 @@ heat_batch_kernel(const HeatBatchInst<T>* __restrict__ inst, int n_inst, int64_t
   }
   for (int64_t pos = seg_a; pos < seg_b;) {
     while (i + 1 < n_inst && inst[i + 1].unit_begin <= pos) ++i;
-    const HeatParams<T>& p = inst[i].p[par];
+    const HeatParams<T>& p = inst[i].p[slot];
     const int64_t local = pos - inst[i].unit_begin;
     const int64_t inst_end = i + 1 < n_inst ? inst[i + 1].unit_begin : total_units;
     const int64_t tile = local / p.nz;
@@ -439,9 +445,9 @@ heat_batch_kernel(const HeatBatchInst<T>* __restrict__ inst, int n_inst, int64_t
     const int ze = (int)min((int64_t)p.nz, zs + (stop - pos));
     pos += ze - zs;
     const int x0 = (int)(tile % p.tiles_x) * C::BX, y0 = (int)(tile / p.tiles_x) * C::BY;
-    const CUtensorMap* tm = &inst[i].tmap[par];
+    const CUtensorMap* tm = &inst[i].tmap[slot];
     if (TMA && tid == 0) tma_prefetch_desc(tm);
-    pipe = heat_segment<T, 2, 3, TMA, 1>(tm, p, x0, y0, zs, ze, pipe);
+    pipe = heat_segment<T, ORDER, 3, TMA, STAGE>(tm, p, x0, y0, zs, ze, pipe);
     if (pipe.s_issue < 0) return;
   }
 }

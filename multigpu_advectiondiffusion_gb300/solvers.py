@@ -8,6 +8,7 @@ kernels through the C ABI on torch CUDA tensors (torch supplies device memory an
 from __future__ import annotations
 
 import ctypes as C
+import dataclasses
 import math
 from dataclasses import dataclass
 
@@ -129,12 +130,15 @@ class BurgersConfig:
                    N.ADV_BC_FROZEN, N.ADV_DIV_F32, bug_b2, C)
 
     @classmethod
-    def periodic(cls, n: int, L: float = 2.0, weno: str = "z", lf: str = "global", div: str = "f32") -> "BurgersConfig":
-        """Inviscid periodic [0,L)^3 on n^3 cell centres, dx = L/n."""
+    def periodic(cls, n: int, L: float = 2.0, weno: str = "z", lf: str = "global",
+                 div: str | int = "f32") -> "BurgersConfig":
+        """Inviscid periodic [0,L)^3 on n^3 cell centres, dx = L/n. div: "f32", "f64", "fast" or an
+        adv_div code."""
         h = L / n
+        if isinstance(div, str):
+            div = {"f32": N.ADV_DIV_F32, "f64": N.ADV_DIV_F64, "fast": N.ADV_DIV_FAST}[div]
         return cls(n, n, n, h, h, h, N.ADV_WENO5_Z if weno == "z" else N.ADV_WENO5_JS,
-                   N.ADV_LF_GLOBAL if lf == "global" else N.ADV_LF_LOCAL, N.ADV_BC_PERIODIC,
-                   {"f32": N.ADV_DIV_F32, "f64": N.ADV_DIV_F64, "fast": N.ADV_DIV_FAST}[div], False, 0.0)
+                   N.ADV_LF_GLOBAL if lf == "global" else N.ADV_LF_LOCAL, N.ADV_BC_PERIODIC, int(div), False, 0.0)
 
     def desc(self, dtype: int) -> N.BurgersDesc:
         k = [self.C / (12 * h * h) if self.C else 0.0 for h in (self.dx, self.dy, self.dz)]
@@ -182,6 +186,74 @@ def max_abs(u, stream=None) -> float:
     N.check(N.load().adv_max_abs(_dtype_code(u), _ptr(u), u.numel(), C.byref(out), N.stream_handle(stream)),
             "adv_max_abs")
     return out.value
+
+
+class Ensemble:
+    """Batched ensemble of 3D heat and Burgers problems (adv_ensemble_* in include/advdiff.h).
+
+    heat: list of (HeatConfig, u) with u a CUDA tensor (all members: same dtype and order, 3D);
+    burgers: list of (BurgersConfig, u, tEnd, cfl[, dt_rule[, max_steps]]). Each member's state
+    stays in its own tensor; work buffers are allocated here. run() advances every member in
+    place; burgers_result(i) gives (t, steps) of member i after the last run."""
+
+    def __init__(self, heat=(), burgers=(), heat_time: int = N.ADV_EULER):
+        import torch
+        self._lib = N.load()
+        self._keep = []
+        hm = (N.HeatMember * max(len(heat), 1))()
+        for i, (cfg, u) in enumerate(heat):
+            ws = heat_workspace(dataclasses.replace(cfg, time=heat_time), u)
+            self._keep += [u, ws]
+            hm[i] = N.HeatMember(cfg.desc(_dtype_code(u)), _ptr(u), _ptr(ws))
+        bm = (N.BurgersMember * max(len(burgers), 1))()
+        for i, b in enumerate(burgers):
+            cfg, u, tEnd, cfl = b[:4]
+            dt_rule = b[4] if len(b) > 4 else N.ADV_DT_MAXU
+            max_steps = b[5] if len(b) > 5 else 1 << 40
+            ws = burgers_workspace(cfg, u)
+            self._keep += [u, ws]
+            bm[i] = N.BurgersMember(cfg.desc(_dtype_code(u)), _ptr(u), _ptr(ws), float(tEnd), float(cfl), int(dt_rule),
+                                    0, float(cfg.C), int(max_steps))
+        self.n_heat, self.n_burgers = len(heat), len(burgers)
+        h = C.c_void_p(None)
+        with torch.cuda.device(self._keep[0].device):
+            N.check(self._lib.adv_ensemble_create(hm, self.n_heat, int(heat_time), bm, self.n_burgers, C.byref(h)),
+                    "adv_ensemble_create")
+        self._h = h
+        self.device = self._keep[0].device
+
+    def run(self, heat_steps: int, direct: bool = False, stream=None) -> None:
+        import torch
+        with torch.cuda.device(self.device):
+            N.check(self._lib.adv_ensemble_run(self._h, int(heat_steps), N.ADV_ENSEMBLE_DIRECT if direct else 0,
+                                               N.stream_handle(stream)), "adv_ensemble_run")
+
+    def burgers_result(self, i: int) -> tuple[float, int]:
+        t = C.c_double(0.0)
+        steps = C.c_int64(0)
+        N.check(self._lib.adv_ensemble_burgers_result(self._h, int(i), C.byref(t), C.byref(steps)),
+                "adv_ensemble_burgers_result")
+        return t.value, steps.value
+
+    def shape(self) -> dict:
+        hu, bu = C.c_int64(0), C.c_int64(0)
+        hc, bc = C.c_int(0), C.c_int(0)
+        N.check(self._lib.adv_ensemble_shape(self._h, C.byref(hu), C.byref(hc), C.byref(bu), C.byref(bc)),
+                "adv_ensemble_shape")
+        return {"heat_units": hu.value, "heat_ctas": hc.value, "burgers_units": bu.value, "burgers_ctas": bc.value}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            import torch
+            with torch.cuda.device(self.device):
+                self._lib.adv_ensemble_destroy(self._h)
+            self._h = C.c_void_p(None)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def reference_heat_final_time(dt: float, iters: int, t0: float = 0.1) -> float:

@@ -70,6 +70,19 @@ def test_invalid_descriptors_rejected_without_gpu(native):
     assert native.adv_burgers_workspace_bytes(C.byref(bd), C.byref(nb)) == N.ADV_ERR_INVALID_ARG
 
 
+def test_ensemble_argument_checks_without_gpu(native):
+    out = C.c_void_p(None)
+    assert native.adv_ensemble_create(None, 0, N.ADV_EULER, None, 0, C.byref(out)) == N.ADV_ERR_INVALID_ARG
+    assert b"no members" in native.adv_last_error_string()
+    hm = (N.HeatMember * 1)()
+    assert native.adv_ensemble_create(hm, 1, 7, None, 0, C.byref(out)) == N.ADV_ERR_INVALID_ARG
+    assert b"time scheme" in native.adv_last_error_string()
+    assert native.adv_ensemble_create(None, 2, N.ADV_EULER, None, 0, C.byref(out)) == N.ADV_ERR_INVALID_ARG
+    assert out.value is None
+    assert native.adv_ensemble_run(None, 1, 0, None) == N.ADV_ERR_INVALID_ARG
+    assert native.adv_ensemble_destroy(None) == N.ADV_OK
+
+
 def _dp(a):
     return a.ctypes.data_as(C.POINTER(C.c_double))
 
