@@ -310,6 +310,69 @@ def bench_ensemble(args, world, rank, dev, stream, flush, lib):
         print(json.dumps(line), flush=True)
 
 
+def reference_sg_gpu(workload: str, warmup: int) -> dict | None:
+    """The reference's own single-GPU CUDA build on this GPU: its kernels compiled from its sources
+    with its flags (-O3, FMA contraction on) into cubins, launched with its launch geometry (run.sh
+    block sizes) in its host loop (oracle/ref_gpu.py). FP64, its only precision. None when the
+    cubins or the GPU are absent."""
+    try:
+        import torch
+        from oracle import ref_gpu
+        if not torch.cuda.is_available() or not ref_gpu.available("heat3d"):
+            return None
+    except Exception:
+        return None
+    from multigpu_advectiondiffusion_gb300.solvers import HeatConfig
+    dev = torch.device("cuda:0")
+    out = {"precision": "f64", "source": "reference kernels.cu compiled -O3 for sm_103a, reference launch geometry"}
+
+    def timed(fn):
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record()
+        fn()
+        ev1.record()
+        torch.cuda.synchronize()
+        return ev0.elapsed_time(ev1) * 1e-3
+
+    n = 256
+    if workload in ("heat3d", "ensemble"):
+        mod = ref_gpu.RefModule("heat3d")
+        base = HeatConfig.reference_3d(1.0, 10, 10, 10, n, n, n)
+        u = torch.from_numpy(ic_heat3d_blobs(n, n, n, 2)).to(dev)
+        for _ in range(max(1, warmup)):
+            ref_gpu.heat3d_run(mod, u, n, n, n, base.kx, base.ky, base.kz, base.dt, 2, block=(32, 4, 4),
+                               scheme="o2-euler")
+        steps = 200
+        t = timed(lambda: ref_gpu.heat3d_run(mod, u, n, n, n, base.kx, base.ky, base.kz, base.dt, steps,
+                                             block=(32, 4, 4), scheme="o2-euler"))
+        out["heat3d_256_o2_euler"] = {"value": n ** 3 * steps / t / 1e9, "unit": "Gcell-updates/s",
+                                      "sample": f"{steps} forward-Euler steps (Compute_Laplace3d_O2 + Compute_RK, "
+                                                "uo copy per step)"}
+        steps = 20
+        t = timed(lambda: ref_gpu.heat3d_run(mod, u, n, n, n, base.kx, base.ky, base.kz, base.dt, steps,
+                                             block=(32, 4, 4)))
+        out["heat3d_256_o4_rk3"] = {"value": n ** 3 * 3 * steps / t / 1e9, "unit": "Gcell-updates/s",
+                                    "sample": f"{steps} SSP-RK3 steps of the baseline code"}
+        mod.close()
+    if workload in ("burgers3d", "ensemble"):
+        mod = ref_gpu.RefModule("burgers3d")
+        nb = 256
+        u0 = np.empty(nb ** 3)
+        from multigpu_advectiondiffusion_gb300 import _native as N
+        dx = 2.0 / (nb - 1)
+        N.check(N.load().adv_ic_burgers_ref(nb, nb, nb, dx, dx, dx, u0.ctypes.data_as(C.POINTER(C.c_double))), "ic")
+        u = torch.from_numpy(u0).to(dev)
+        ref_gpu.burgers3d_run(mod, u, nb, 2.0, 1.0, 0.3, block=8, max_steps=1)
+        steps = 3
+        t = timed(lambda: ref_gpu.burgers3d_run(mod, u, nb, 2.0, 1.0, 0.3, block=8, max_steps=steps))
+        out["burgers3d_256"] = {"value": nb ** 3 * 3 * steps / t / 1e9, "unit": "Gcell-updates/s",
+                                "sample": f"{steps} SSP-RK3 steps (Compute_dF/dG/dH + Compute_Laplace_Async + "
+                                          "Compute_RK per stage), local LF WENO5-Z, viscous, frozen layers"}
+        mod.close()
+    return out
+
+
 def run_reference_arm(args, world, rank):
     from oracle import oracle
     if rank != 0:
@@ -322,20 +385,18 @@ def run_reference_arm(args, world, rank):
         for _ in range(args.warmup):
             cpu_heat_rate(cfg, u0, 0.2)
         rates, samples = [], []
-        t_all = 0.0
         for _ in range(args.steps):
             r, s, dt = cpu_heat_rate(cfg, u0, per_step_budget)
             rates.append(r)
             samples.append(s)
-            t_all += dt
         value = float(np.median(rates))
         sample = f"256^3 FP32 O2 Euler, {int(np.median(samples))} of the 2000 time steps per step"
         config = {"workload": "heat3d 256^3 f32 o2 euler r=1/8 dirichlet 8 blobs x 2000 steps"}
-    else:
+    elif args.workload == "burgers3d":
         from multigpu_advectiondiffusion_gb300.solvers import BurgersConfig
         n = 256
         cfg = BurgersConfig.periodic(n, weno="z")
-        u0 = oracle.ic_burgers_fourier(n, n, n, 2.0, 3).astype(np.float32)
+        u0 = ic_burgers_fourier(n, n, n, 2.0, 3).astype(np.float32)
         rates = []
         for i in range(args.warmup + args.steps):
             t0 = time.perf_counter()
@@ -346,13 +407,34 @@ def run_reference_arm(args, world, rank):
         value = float(np.median(rates))
         sample = "256^3 FP32 WENO5-Z periodic, 1 SSP-RK3 time step per step"
         config = {"workload": "burgers3d 256^3 f32 weno5-z global-lf periodic cfl 0.4"}
+    else:
+        # the ensemble: per step, two heat instances for 4 steps and one Burgers instance for one
+        # RK3 step, in proportion to the ensemble's heat / Burgers cell updates
+        heat, burgers = ensemble_members()
+        h0, b0 = ensemble_initial_states(heat[:2], burgers[:1])
+        rates = []
+        for i in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            cells = 0
+            for c, a in zip(heat[:2], h0):
+                oracle.heat_run(c, a, 4, 0)
+                cells += c.numel * 4
+            _, _, it = oracle.burgers_run(burgers[0], b0[0], 1e9, 0.4, 1, max_steps=1, div64=False)
+            cells += burgers[0].numel * 3 * it
+            dt = time.perf_counter() - t0
+            if i >= args.warmup:
+                rates.append(cells / dt / 1e9)
+        value = float(np.median(rates))
+        sample = "2 heat instances x 4 Euler steps + 1 Burgers instance x 1 SSP-RK3 step of the ensemble"
+        config = {"workload": f"ensemble 64 heat + 32 burgers x {ENSEMBLE_STEPS} steps"}
     line = {"impl": "reference", "metric": "Gcell-updates/s/RK-stage", "value": value, "unit": "Gcell-updates/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded)", "config": config,
             "cpu_baseline": {"value": value, "unit": "Gcell-updates/s", "cores": threads, "kind": "port",
                              "sample": sample},
-            "e2e": {"value": value, "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": value, "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "sg_gpu": reference_sg_gpu(args.workload, args.warmup)}
     print(json.dumps(line), flush=True)
 
 

@@ -1,0 +1,71 @@
+"""Recipe: the reference's own single-GPU CUDA kernels, compiled from its sources where they lie.
+
+TEST INFRASTRUCTURE (part of the oracle): the outputs are device-only cubins for sm_103a under
+oracle/_ref/ (git-ignored; they are GPU code, not host binaries, so they run on any host of the
+GB300). oracle/ref_gpu.py loads them through the CUDA driver API and drives them with the
+reference's own launch geometry and host loop. Nothing in the library loads them.
+
+Sources (the reference checkout, read-only):
+  SingleGPU/Diffusion3d_baselineCode/kernels.cu  -> heat3d       (Compute_Laplace3d[_O2], Compute_RK)
+  SingleGPU/Diffusion2d/kernels.cu               -> heat2d       (Compute_Laplace2d, Compute_RK)
+  SingleGPU/Burgers3d_WENO5/kernels.cu           -> burgers3d    (Compute_dF/dG/dH, Compute_Laplace_Async,
+                                                                  Compute_RK)
+Each is built twice: `<name>.cubin` with nvcc's default flags (FMA contraction on: the reference's
+own build, used for timing) and `<name>_nofma.cubin` with -fmad=false (every operation rounded as
+written: comparable bit for bit with the FP64 oracle and the library's FP64 path). REAL is double
+in all three (USE_FLOAT false in the reference headers).
+
+    python oracle/ref_build.py [--src /root/reference]
+"""
+from __future__ import annotations
+
+import argparse
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+OUT = HERE / "_ref"
+UNITS = {
+    "heat3d": "SingleGPU/Diffusion3d_baselineCode/kernels.cu",
+    "heat2d": "SingleGPU/Diffusion2d/kernels.cu",
+    "burgers3d": "SingleGPU/Burgers3d_WENO5/kernels.cu",
+}
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def build(src_root: Path) -> list[Path]:
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    OUT.mkdir(parents=True, exist_ok=True)
+    made = []
+    jobs = []
+    for name, rel in UNITS.items():
+        src = src_root / rel
+        if not src.exists():
+            raise FileNotFoundError(src)
+        for tag, extra in (("", []), ("_nofma", ["-fmad=false"])):
+            out = OUT / f"{name}{tag}.cubin"
+            if out.exists() and out.stat().st_mtime >= src.stat().st_mtime:
+                made.append(out)
+                continue
+            cmd = [nvcc, "-cubin", *ARCH, "-O3", *extra, "-o", str(out), str(src)]
+            jobs.append((out, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)))
+    for out, p in jobs:
+        log, _ = p.communicate()
+        if p.returncode != 0:
+            raise RuntimeError(f"reference kernel build failed for {out.name}:\n{log}")
+        made.append(out)
+    return made
+
+
+def main(argv=None) -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--src", default="/root/reference")
+    a = ap.parse_args(argv)
+    for p in build(Path(a.src)):
+        print(p.relative_to(HERE.parent))
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])
