@@ -151,6 +151,59 @@ adv_status adv_burgers_run(const adv_burgers_desc* d, void* u, void* workspace, 
                            double cfl, int dt_rule, double C, int64_t max_steps, double* t_out,
                            int64_t* steps_out, void* stream);
 
+/* ------------------------------------------- heat with a diffusivity field k(x), and its adjoint
+ * u_t = div(k grad u) on a 3D node grid: conservative 7-point form with arithmetic face averages
+ * k_{i+1/2} = (k_i + k_{i+1})/2, forward Euler, c_a = dt / h_a^2:
+ *   u'_i = u_i + sum_a c_a [k_{i+1/2}(u_{i+1} - u_i) - k_{i-1/2}(u_i - u_{i-1})]   (interior)
+ * The outermost layer is frozen (held, or set to 0 with zero_boundary). No counterpart in the
+ * reference (its diffusivity is one constant, SingleGPU/Diffusion3d_baselineCode/main.cpp:58-61).
+ * The adjoint step is the exact transpose of one step: given lam' = dJ/du^{n+1} and u^n it
+ * writes lam = dJ/du^n and adds this step's dJ/dk into grad_k. */
+typedef struct adv_heatk_desc {
+  int32_t nx, ny, nz;
+  int32_t dtype;          /* adv_dtype */
+  int32_t zero_boundary;  /* 0 or 1 */
+  int32_t pad0;
+  double cx, cy, cz;      /* dt / h_a^2 */
+} adv_heatk_desc;
+
+adv_status adv_heatk_step(const adv_heatk_desc* d, const void* k, const void* u_in, void* u_out,
+                          void* stream);
+adv_status adv_heatk_adjoint_step(const adv_heatk_desc* d, const void* k, const void* u_n,
+                                  const void* lam_next, void* lam_out, void* grad_k, void* stream);
+/* sqrt(N) checkpointing: the forward run stores u every `interval` steps (ceil(nsteps/interval)
+ * arrays in ckpt); the backward run recomputes each interval from its checkpoint into `work`
+ * (interval arrays) and sweeps the adjoint through it. Sizes in bytes. */
+adv_status adv_heatk_checkpoint_bytes(const adv_heatk_desc* d, int64_t nsteps, int64_t interval,
+                                      size_t* ckpt_bytes, size_t* work_bytes);
+/* nsteps steps in place on u; ckpt may be NULL (no checkpoints kept). */
+adv_status adv_heatk_forward(const adv_heatk_desc* d, const void* k, void* u, int64_t nsteps,
+                             int64_t interval, void* ckpt, void* work, void* stream);
+/* lam: in dJ/du at step nsteps, out dJ/du at step 0. grad_k += dJ/dk. */
+adv_status adv_heatk_backward(const adv_heatk_desc* d, const void* k, int64_t nsteps,
+                              int64_t interval, const void* ckpt, void* lam, void* grad_k,
+                              void* work, void* stream);
+
+/* --------------------------------------------------------------- Burgers discrete adjoint
+ * Exact transpose of the fixed-dt SSP-RK3 step of the periodic, local Lax-Friedrichs, inviscid
+ * scheme (WENO5-JS or WENO5-Z; FP32 or FP64 state; other schemes return ADV_ERR_UNSUPPORTED).
+ * No counterpart in the reference. adv_burgers_adjoint_step turns lam = dJ/du^{n+1} into
+ * dJ/du^n given the step's stage inputs u^n, u1, u2; `work` holds 3 arrays. The forward run
+ * stores u every `interval` steps; the backward run recomputes each interval (its stage inputs)
+ * from the checkpoint and sweeps the adjoint back through it. */
+adv_status adv_burgers_adjoint_step(const adv_burgers_desc* d, const void* u_n, const void* u1,
+                                    const void* u2, double dt, void* lam, void* work, void* stream);
+/* ckpt: ceil(nsteps/interval) arrays; work: 3*interval + 2 arrays (enough for both runs). */
+adv_status adv_burgers_checkpoint_bytes(const adv_burgers_desc* d, int64_t nsteps, int64_t interval,
+                                        size_t* ckpt_bytes, size_t* work_bytes);
+/* nsteps fixed-dt steps in place on u; ckpt may be NULL. */
+adv_status adv_burgers_forward(const adv_burgers_desc* d, void* u, double dt, int64_t nsteps,
+                               int64_t interval, void* ckpt, void* work, void* stream);
+/* lam: in dJ/du at step nsteps, out dJ/du at step 0. */
+adv_status adv_burgers_backward(const adv_burgers_desc* d, double dt, int64_t nsteps,
+                                int64_t interval, const void* ckpt, void* lam, void* work,
+                                void* stream);
+
 /* ------------------------------------------------------------------ batched ensembles
  * Many independent 3D problems of uneven size and coefficients advanced together. No counterpart
  * in the reference (its drivers run one problem per process). Each stage of all heat members is

@@ -39,6 +39,13 @@ class BurgersDesc(C.Structure):
                 ("kx", C.c_double), ("ky", C.c_double), ("kz", C.c_double)]
 
 
+class HeatKDesc(C.Structure):
+    """adv_heatk_desc (include/advdiff.h)."""
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("dtype", C.c_int32),
+                ("zero_boundary", C.c_int32), ("pad0", C.c_int32),
+                ("cx", C.c_double), ("cy", C.c_double), ("cz", C.c_double)]
+
+
 class HeatMember(C.Structure):
     """adv_heat_member (include/advdiff.h)."""
     _fields_ = [("desc", HeatDesc), ("u", C.c_void_p), ("work", C.c_void_p)]
@@ -63,6 +70,17 @@ SIGNATURES = [
     ("adv_burgers_workspace_bytes", _I, [C.POINTER(BurgersDesc), C.POINTER(C.c_size_t)]),
     ("adv_burgers_run", _I, [C.POINTER(BurgersDesc), _VP, _VP, _D, _D, _I, _D, _I64, _PD,
                              C.POINTER(C.c_int64), _VP]),
+    ("adv_heatk_step", _I, [C.POINTER(HeatKDesc), _VP, _VP, _VP, _VP]),
+    ("adv_heatk_adjoint_step", _I, [C.POINTER(HeatKDesc), _VP, _VP, _VP, _VP, _VP, _VP]),
+    ("adv_heatk_checkpoint_bytes", _I, [C.POINTER(HeatKDesc), _I64, _I64, C.POINTER(C.c_size_t),
+                                        C.POINTER(C.c_size_t)]),
+    ("adv_heatk_forward", _I, [C.POINTER(HeatKDesc), _VP, _VP, _I64, _I64, _VP, _VP, _VP]),
+    ("adv_heatk_backward", _I, [C.POINTER(HeatKDesc), _VP, _I64, _I64, _VP, _VP, _VP, _VP, _VP]),
+    ("adv_burgers_adjoint_step", _I, [C.POINTER(BurgersDesc), _VP, _VP, _VP, _D, _VP, _VP, _VP]),
+    ("adv_burgers_checkpoint_bytes", _I, [C.POINTER(BurgersDesc), _I64, _I64, C.POINTER(C.c_size_t),
+                                          C.POINTER(C.c_size_t)]),
+    ("adv_burgers_forward", _I, [C.POINTER(BurgersDesc), _VP, _D, _I64, _I64, _VP, _VP, _VP]),
+    ("adv_burgers_backward", _I, [C.POINTER(BurgersDesc), _D, _I64, _I64, _VP, _VP, _VP, _VP]),
     ("adv_ensemble_create", _I, [C.POINTER(HeatMember), _I, _I, C.POINTER(BurgersMember), _I,
                                  C.POINTER(_VP)]),
     ("adv_ensemble_run", _I, [_VP, _I64, _I, _VP]),

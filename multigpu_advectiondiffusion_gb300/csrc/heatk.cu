@@ -1,0 +1,259 @@
+// heatk.cu -- 3D heat with a spatially varying diffusivity k(x), its discrete adjoint, and the
+// checkpointed forward/backward runs (adv_heatk_* in advdiff.h). No reference counterpart: the
+// reference's diffusivity is one constant C (SingleGPU/Diffusion3d_baselineCode/main.cpp:58-61).
+//
+// Scheme (conservative 7-point form, arithmetic face averages), for an interior node i and each
+// axis a with neighbours p (+1) and m (-1):
+//   k_p = (k_i + k_p)/2, k_m = (k_i + k_m)/2,  F_a = k_p (u_p - u_i) - k_m (u_i - u_m)
+//   u'_i = u_i + c_x F_x + c_y F_y + c_z F_z,   c_a = dt / h_a^2
+// The outermost layer is frozen (held, or set to 0 with zero_boundary).
+//
+// Adjoint of one step (J depends on u' through lam' = dJ/du'): with the masked adjoint
+// mu_j = [j interior] lam'_j and P_i = [i interior or not zero_boundary],
+//   lam_i  = P_i lam'_i + sum_a c_a sum_{j in nb_a(i)} k_ij (mu_j - mu_i)
+//   dJ/dk_i += 1/2 sum_a c_a sum_{j in nb_a(i)} (u_j - u_i)(mu_i - mu_j)
+// (each face coefficient k_ij = (k_i + k_j)/2 feeds half its derivative to each end). Neighbours
+// outside the domain contribute nothing.
+//
+// Kernels: one thread per (x, y) column over a chunk of z planes, z neighbours from a register
+// window, x/y neighbours from global loads that hit L1 (adjacent threads share them). Every
+// operation is an explicit correctly rounded add/mul/fma, mirrored by the oracle.
+#include <algorithm>
+#include <cstring>
+
+#include "adv_internal.h"
+#include "adv_math.cuh"
+
+namespace adv {
+
+namespace {
+
+constexpr int KX = 32, KY = 8, KZC = 16;  // block and z chunk
+
+__device__ __forceinline__ float fma_k(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fma_k(double a, double b, double c) { return __fma_rn(a, b, c); }
+
+template <class T>
+struct HeatKArgs {
+  const T* k;
+  const T* u;    // forward: u^n; adjoint: u^n (the step's input)
+  const T* lam;  // adjoint: lam^{n+1}
+  T* out;        // forward: u^{n+1}; adjoint: lam^n
+  T* grad;       // adjoint: dJ/dk accumulator
+  int nx, ny, nz, zero_boundary;
+  T cx, cy, cz;
+};
+
+template <class T>
+__global__ void __launch_bounds__(KX * KY) heatk_step_kernel(const __grid_constant__ HeatKArgs<T> a) {
+  const int x = blockIdx.x * KX + threadIdx.x, y = blockIdx.y * KY + threadIdx.y;
+  if (x >= a.nx || y >= a.ny) return;
+  const int z0 = blockIdx.z * KZC, z1 = min(a.nz, z0 + KZC);
+  const size_t sx = 1, sy = (size_t)a.nx, sz = (size_t)a.nx * a.ny;
+  const bool col_in = x > 0 && x < a.nx - 1 && y > 0 && y < a.ny - 1;
+  const T h = T(0.5);
+  size_t o = (size_t)x + sy * y + sz * z0;
+  T uc = a.u[o], kc = a.k[o];
+  T um = z0 > 0 ? a.u[o - sz] : uc, km = z0 > 0 ? a.k[o - sz] : kc;
+  for (int z = z0; z < z1; ++z, o += sz) {
+    const T up = z + 1 < a.nz ? a.u[o + sz] : uc, kp = z + 1 < a.nz ? a.k[o + sz] : kc;
+    T res;
+    if (col_in && z > 0 && z < a.nz - 1) {
+      auto flux = [&](T u_p, T u_m, T k_p, T k_m) {
+        const T fp = mul_rn(h, add_rn(kc, k_p)), fm = mul_rn(h, add_rn(kc, k_m));
+        return fma_k(fp, sub_rn(u_p, uc), -mul_rn(fm, sub_rn(uc, u_m)));
+      };
+      const T Fx = flux(a.u[o + sx], a.u[o - sx], a.k[o + sx], a.k[o - sx]);
+      const T Fy = flux(a.u[o + sy], a.u[o - sy], a.k[o + sy], a.k[o - sy]);
+      const T Fz = flux(up, um, kp, km);
+      res = add_rn(uc, fma_k(a.cz, Fz, fma_k(a.cy, Fy, mul_rn(a.cx, Fx))));
+    } else {
+      res = a.zero_boundary ? T(0) : uc;
+    }
+    a.out[o] = res;
+    um = uc; uc = up; km = kc; kc = kp;
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(KX * KY) heatk_adjoint_kernel(const __grid_constant__ HeatKArgs<T> a) {
+  const int x = blockIdx.x * KX + threadIdx.x, y = blockIdx.y * KY + threadIdx.y;
+  if (x >= a.nx || y >= a.ny) return;
+  const int z0 = blockIdx.z * KZC, z1 = min(a.nz, z0 + KZC);
+  const int nx = a.nx, ny = a.ny, nz = a.nz;
+  const size_t sy = (size_t)nx, sz = (size_t)nx * ny;
+  const T h = T(0.5);
+  auto interior = [&](int xx, int yy, int zz) {
+    return xx > 0 && xx < nx - 1 && yy > 0 && yy < ny - 1 && zz > 0 && zz < nz - 1;
+  };
+  for (int z = z0; z < z1; ++z) {
+    const size_t o = (size_t)x + sy * y + sz * z;
+    const bool in_c = interior(x, y, z);
+    const T lc = a.lam[o];
+    const T muc = in_c ? lc : T(0);
+    const T uc = a.u[o], kc = a.k[o];
+    // one axis: neighbours at +s (if `hp`) and -s (if `hm`), with their interior flags
+    auto axis = [&](size_t s, bool hp, bool hm, bool inp, bool inm, T& S, T& G) {
+      const size_t op = hp ? o + s : o, om = hm ? o - s : o;
+      const T mup = hp && inp ? a.lam[op] : T(0), mum = hm && inm ? a.lam[om] : T(0);
+      const T kfp = mul_rn(h, add_rn(kc, a.k[op])), kfm = mul_rn(h, add_rn(kc, a.k[om]));
+      const T dmp = hp ? sub_rn(mup, muc) : T(0), dmm = hm ? sub_rn(mum, muc) : T(0);
+      const T dup = sub_rn(a.u[op], uc), dum = sub_rn(a.u[om], uc);
+      S = fma_k(kfm, dmm, mul_rn(kfp, dmp));
+      G = fma_k(dum, -dmm, mul_rn(dup, -dmp));
+    };
+    T Sx, Gx, Sy, Gy, Sz, Gz;
+    axis(1, x + 1 < nx, x > 0, interior(x + 1, y, z), interior(x - 1, y, z), Sx, Gx);
+    axis(sy, y + 1 < ny, y > 0, interior(x, y + 1, z), interior(x, y - 1, z), Sy, Gy);
+    axis(sz, z + 1 < nz, z > 0, interior(x, y, z + 1), interior(x, y, z - 1), Sz, Gz);
+    const T keep = (in_c || !a.zero_boundary) ? lc : T(0);
+    a.out[o] = add_rn(keep, fma_k(a.cz, Sz, fma_k(a.cy, Sy, mul_rn(a.cx, Sx))));
+    a.grad[o] = fma_k(h, fma_k(a.cz, Gz, fma_k(a.cy, Gy, mul_rn(a.cx, Gx))), a.grad[o]);
+  }
+}
+
+adv_status heatk_validate(const adv_heatk_desc* d) {
+  if (!d) return set_error(ADV_ERR_INVALID_ARG, "heatk: null descriptor");
+  if (d->dtype != ADV_F32 && d->dtype != ADV_F64) return set_error(ADV_ERR_INVALID_ARG, "heatk: bad dtype");
+  if (d->nx < 1 || d->ny < 1 || d->nz < 1) return set_error(ADV_ERR_INVALID_ARG, "heatk: empty grid");
+  if ((int64_t)d->nx * d->ny * d->nz > ((int64_t)1 << 40) || d->nx > (1 << 30) || d->ny > (1 << 30) ||
+      d->nz > (1 << 30))
+    return set_error(ADV_ERR_INVALID_ARG, "heatk: grid too large");
+  return ADV_OK;
+}
+
+template <class T>
+HeatKArgs<T> make_args(const adv_heatk_desc& d, const void* k, const void* u, const void* lam, void* out, void* grad) {
+  HeatKArgs<T> a;
+  a.k = static_cast<const T*>(k);
+  a.u = static_cast<const T*>(u);
+  a.lam = static_cast<const T*>(lam);
+  a.out = static_cast<T*>(out);
+  a.grad = static_cast<T*>(grad);
+  a.nx = d.nx; a.ny = d.ny; a.nz = d.nz;
+  a.zero_boundary = d.zero_boundary;
+  a.cx = (T)d.cx; a.cy = (T)d.cy; a.cz = (T)d.cz;
+  return a;
+}
+
+dim3 heatk_grid(const adv_heatk_desc& d) {
+  return dim3((unsigned)((d.nx + KX - 1) / KX), (unsigned)((d.ny + KY - 1) / KY), (unsigned)((d.nz + KZC - 1) / KZC));
+}
+
+adv_status heatk_step_launch(const adv_heatk_desc& d, const void* k, const void* u_in, void* u_out, cudaStream_t s) {
+  if (d.dtype == ADV_F32)
+    heatk_step_kernel<float><<<heatk_grid(d), dim3(KX, KY), 0, s>>>(make_args<float>(d, k, u_in, nullptr, u_out, nullptr));
+  else
+    heatk_step_kernel<double><<<heatk_grid(d), dim3(KX, KY), 0, s>>>(make_args<double>(d, k, u_in, nullptr, u_out, nullptr));
+  ADV_CUDA_TRY(cudaGetLastError());
+  count_launches(1);
+  return ADV_OK;
+}
+
+adv_status heatk_adjoint_launch(const adv_heatk_desc& d, const void* k, const void* u_n, const void* lam_next,
+                                void* lam_out, void* grad_k, cudaStream_t s) {
+  if (d.dtype == ADV_F32)
+    heatk_adjoint_kernel<float><<<heatk_grid(d), dim3(KX, KY), 0, s>>>(
+        make_args<float>(d, k, u_n, lam_next, lam_out, grad_k));
+  else
+    heatk_adjoint_kernel<double><<<heatk_grid(d), dim3(KX, KY), 0, s>>>(
+        make_args<double>(d, k, u_n, lam_next, lam_out, grad_k));
+  ADV_CUDA_TRY(cudaGetLastError());
+  count_launches(1);
+  return ADV_OK;
+}
+
+size_t array_bytes(const adv_heatk_desc& d) {
+  const size_t n = (size_t)d.nx * d.ny * d.nz * (d.dtype == ADV_F32 ? 4 : 8);
+  return (n + 255) / 256 * 256;
+}
+
+}  // namespace
+}  // namespace adv
+
+using namespace adv;
+
+extern "C" {
+
+adv_status adv_heatk_step(const adv_heatk_desc* d, const void* k, const void* u_in, void* u_out, void* stream) {
+  adv_status st = heatk_validate(d);
+  if (st != ADV_OK) return st;
+  if (!k || !u_in || !u_out) return set_error(ADV_ERR_INVALID_ARG, "heatk: null buffer");
+  if (u_in == u_out) return set_error(ADV_ERR_INVALID_ARG, "heatk: u_in and u_out must not alias");
+  return heatk_step_launch(*d, k, u_in, u_out, static_cast<cudaStream_t>(stream));
+}
+
+adv_status adv_heatk_adjoint_step(const adv_heatk_desc* d, const void* k, const void* u_n, const void* lam_next,
+                                  void* lam_out, void* grad_k, void* stream) {
+  adv_status st = heatk_validate(d);
+  if (st != ADV_OK) return st;
+  if (!k || !u_n || !lam_next || !lam_out || !grad_k) return set_error(ADV_ERR_INVALID_ARG, "heatk: null buffer");
+  if (lam_next == lam_out) return set_error(ADV_ERR_INVALID_ARG, "heatk: lam_next and lam_out must not alias");
+  return heatk_adjoint_launch(*d, k, u_n, lam_next, lam_out, grad_k, static_cast<cudaStream_t>(stream));
+}
+
+adv_status adv_heatk_checkpoint_bytes(const adv_heatk_desc* d, int64_t nsteps, int64_t interval, size_t* ckpt_bytes,
+                                      size_t* work_bytes) {
+  adv_status st = heatk_validate(d);
+  if (st != ADV_OK) return st;
+  if (nsteps < 0 || interval < 1) return set_error(ADV_ERR_INVALID_ARG, "heatk: bad nsteps/interval");
+  const size_t one = array_bytes(*d);
+  const int64_t m = (nsteps + interval - 1) / interval;
+  if (ckpt_bytes) *ckpt_bytes = (size_t)std::max<int64_t>(m, 1) * one;
+  // forward: one ping-pong array; backward: the segment's states (interval - 1 beyond the
+  // checkpoint) and one adjoint ping-pong array
+  if (work_bytes) *work_bytes = (size_t)std::max<int64_t>(interval, 1) * one;
+  return ADV_OK;
+}
+
+adv_status adv_heatk_forward(const adv_heatk_desc* d, const void* k, void* u, int64_t nsteps, int64_t interval,
+                             void* ckpt, void* work, void* stream) {
+  adv_status st = heatk_validate(d);
+  if (st != ADV_OK) return st;
+  if (!k || !u || !work) return set_error(ADV_ERR_INVALID_ARG, "heatk: null buffer");
+  if (nsteps < 0 || interval < 1) return set_error(ADV_ERR_INVALID_ARG, "heatk: bad nsteps/interval");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const size_t one = array_bytes(*d);
+  const size_t nb = (size_t)d->nx * d->ny * d->nz * (d->dtype == ADV_F32 ? 4 : 8);
+  char* a = static_cast<char*>(u);
+  char* b = static_cast<char*>(work);
+  for (int64_t n = 0; n < nsteps; ++n) {
+    if (ckpt && n % interval == 0)
+      ADV_CUDA_TRY(cudaMemcpyAsync(static_cast<char*>(ckpt) + (n / interval) * one, a, nb, cudaMemcpyDeviceToDevice, s));
+    if ((st = heatk_step_launch(*d, k, a, b, s)) != ADV_OK) return st;
+    std::swap(a, b);
+  }
+  if (a != static_cast<char*>(u)) ADV_CUDA_TRY(cudaMemcpyAsync(u, a, nb, cudaMemcpyDeviceToDevice, s));
+  return ADV_OK;
+}
+
+adv_status adv_heatk_backward(const adv_heatk_desc* d, const void* k, int64_t nsteps, int64_t interval,
+                              const void* ckpt, void* lam, void* grad_k, void* work, void* stream) {
+  adv_status st = heatk_validate(d);
+  if (st != ADV_OK) return st;
+  if (!k || !ckpt || !lam || !grad_k || !work) return set_error(ADV_ERR_INVALID_ARG, "heatk: null buffer");
+  if (nsteps < 0 || interval < 1) return set_error(ADV_ERR_INVALID_ARG, "heatk: bad nsteps/interval");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const size_t one = array_bytes(*d);
+  const size_t nb = (size_t)d->nx * d->ny * d->nz * (d->dtype == ADV_F32 ? 4 : 8);
+  char* states = static_cast<char*>(work);              // u^{n0+1} .. u^{n0+interval-1}
+  char* lam_b = states + (size_t)(interval - 1) * one;  // adjoint ping-pong
+  char* la = static_cast<char*>(lam);
+  char* lb = lam_b;
+  const int64_t m = (nsteps + interval - 1) / interval;
+  for (int64_t seg = m - 1; seg >= 0; --seg) {
+    const int64_t n0 = seg * interval, n1 = std::min(nsteps, n0 + interval);
+    const char* base = static_cast<const char*>(ckpt) + seg * one;
+    auto state = [&](int64_t n) -> const char* { return n == n0 ? base : states + (n - n0 - 1) * one; };
+    for (int64_t n = n0; n + 1 < n1; ++n)
+      if ((st = heatk_step_launch(*d, k, state(n), states + (n - n0) * one, s)) != ADV_OK) return st;
+    for (int64_t n = n1 - 1; n >= n0; --n) {
+      if ((st = heatk_adjoint_launch(*d, k, state(n), la, lb, grad_k, s)) != ADV_OK) return st;
+      std::swap(la, lb);
+    }
+  }
+  if (la != static_cast<char*>(lam)) ADV_CUDA_TRY(cudaMemcpyAsync(lam, la, nb, cudaMemcpyDeviceToDevice, s));
+  return ADV_OK;
+}
+
+}  // extern "C"

@@ -188,6 +188,160 @@ def max_abs(u, stream=None) -> float:
     return out.value
 
 
+@dataclass
+class HeatKConfig:
+    """3D heat with a diffusivity field (adv_heatk_desc): c_a = dt / h_a^2."""
+    nx: int
+    ny: int
+    nz: int
+    cx: float
+    cy: float
+    cz: float
+    zero_boundary: bool = True
+
+    @classmethod
+    def cube(cls, n: int, dt_kmax_over_h2: float, k_max: float, L: float = 1.0) -> "HeatKConfig":
+        """n^3 nodes on [0,L]^3, dt chosen so dt k_max / h^2 = dt_kmax_over_h2 (<= 1/6 is stable)."""
+        c = dt_kmax_over_h2 / k_max
+        return cls(n, n, n, c, c, c, True)
+
+    def desc(self, dtype: int) -> N.HeatKDesc:
+        return N.HeatKDesc(self.nx, self.ny, self.nz, dtype, int(self.zero_boundary), 0, self.cx, self.cy, self.cz)
+
+    @property
+    def numel(self) -> int:
+        return self.nx * self.ny * self.nz
+
+
+def heatk_step(cfg: HeatKConfig, k, u_in, u_out, stream=None) -> None:
+    d = cfg.desc(_dtype_code(u_in))
+    N.check(N.load().adv_heatk_step(C.byref(d), _ptr(k), _ptr(u_in), _ptr(u_out), N.stream_handle(stream)),
+            "adv_heatk_step")
+
+
+def heatk_adjoint_step(cfg: HeatKConfig, k, u_n, lam_next, lam_out, grad_k, stream=None) -> None:
+    d = cfg.desc(_dtype_code(u_n))
+    N.check(N.load().adv_heatk_adjoint_step(C.byref(d), _ptr(k), _ptr(u_n), _ptr(lam_next), _ptr(lam_out),
+                                            _ptr(grad_k), N.stream_handle(stream)), "adv_heatk_adjoint_step")
+
+
+def _heatk_buffers(cfg, like, nsteps, interval):
+    import torch
+    d = cfg.desc(_dtype_code(like))
+    cb, wb = C.c_size_t(0), C.c_size_t(0)
+    N.check(N.load().adv_heatk_checkpoint_bytes(C.byref(d), int(nsteps), int(interval), C.byref(cb), C.byref(wb)),
+            "adv_heatk_checkpoint_bytes")
+    return (torch.empty(cb.value, dtype=torch.uint8, device=like.device),
+            torch.empty(wb.value, dtype=torch.uint8, device=like.device))
+
+
+def default_interval(nsteps: int) -> int:
+    """sqrt(N) checkpoint spacing: about sqrt(N) checkpoints plus sqrt(N) recomputed states."""
+    return max(1, math.ceil(math.sqrt(max(nsteps, 1))))
+
+
+def _autograd():
+    import torch
+
+    class HeatKRun(torch.autograd.Function):
+        """u(T) = heat-with-k(x) forward run from (k, u0); backward by the hand-written adjoint
+        (adv_heatk_backward) over sqrt(N) checkpoints. For gradient checks."""
+
+        @staticmethod
+        def forward(ctx, k, u0, cfg, nsteps, interval):
+            u = u0.detach().clone()
+            ckpt, work = _heatk_buffers(cfg, u, nsteps, interval)
+            d = cfg.desc(_dtype_code(u))
+            N.check(N.load().adv_heatk_forward(C.byref(d), _ptr(k), _ptr(u), int(nsteps), int(interval), _ptr(ckpt),
+                                               _ptr(work), N.stream_handle(torch.cuda.current_stream())),
+                    "adv_heatk_forward")
+            ctx.save_for_backward(k)
+            ctx.cfg, ctx.nsteps, ctx.interval, ctx.ckpt, ctx.work = cfg, nsteps, interval, ckpt, work
+            return u
+
+        @staticmethod
+        def backward(ctx, grad_u):
+            (k,) = ctx.saved_tensors
+            lam = grad_u.detach().clone().contiguous()
+            gk = torch.zeros_like(k)
+            d = ctx.cfg.desc(_dtype_code(lam))
+            N.check(N.load().adv_heatk_backward(C.byref(d), _ptr(k), int(ctx.nsteps), int(ctx.interval),
+                                                _ptr(ctx.ckpt), _ptr(lam), _ptr(gk), _ptr(ctx.work),
+                                                N.stream_handle(torch.cuda.current_stream())), "adv_heatk_backward")
+            return gk, lam, None, None, None
+
+    return HeatKRun
+
+
+def _burgers_autograd():
+    import torch
+
+    class BurgersRun(torch.autograd.Function):
+        """u(T) of nsteps fixed-dt SSP-RK3 steps (periodic, local LF) from u0; backward by the
+        hand-written adjoint (adv_burgers_backward) over sqrt(N) checkpoints. For gradient checks."""
+
+        @staticmethod
+        def forward(ctx, u0, cfg, dt, nsteps, interval):
+            u = u0.detach().clone()
+            d = cfg.desc(_dtype_code(u))
+            cb, wb = C.c_size_t(0), C.c_size_t(0)
+            N.check(N.load().adv_burgers_checkpoint_bytes(C.byref(d), int(nsteps), int(interval), C.byref(cb),
+                                                          C.byref(wb)), "adv_burgers_checkpoint_bytes")
+            ckpt = torch.empty(cb.value, dtype=torch.uint8, device=u.device)
+            work = torch.empty(wb.value, dtype=torch.uint8, device=u.device)
+            N.check(N.load().adv_burgers_forward(C.byref(d), _ptr(u), float(dt), int(nsteps), int(interval),
+                                                 _ptr(ckpt), _ptr(work),
+                                                 N.stream_handle(torch.cuda.current_stream())), "adv_burgers_forward")
+            ctx.cfg, ctx.dt, ctx.nsteps, ctx.interval, ctx.ckpt, ctx.work = cfg, dt, nsteps, interval, ckpt, work
+            return u
+
+        @staticmethod
+        def backward(ctx, grad_u):
+            lam = grad_u.detach().clone().contiguous()
+            d = ctx.cfg.desc(_dtype_code(lam))
+            N.check(N.load().adv_burgers_backward(C.byref(d), float(ctx.dt), int(ctx.nsteps), int(ctx.interval),
+                                                  _ptr(ctx.ckpt), _ptr(lam), _ptr(ctx.work),
+                                                  N.stream_handle(torch.cuda.current_stream())),
+                    "adv_burgers_backward")
+            return lam, None, None, None, None
+
+    return BurgersRun
+
+
+_BurgersRun = None
+
+
+def burgers_run_fixed(cfg: BurgersConfig, u0, dt: float, nsteps: int, interval: int | None = None):
+    """Differentiable (w.r.t. u0) run of nsteps fixed-dt steps; returns u(T)."""
+    global _BurgersRun
+    if _BurgersRun is None:
+        _BurgersRun = _burgers_autograd()
+    return _BurgersRun.apply(u0, cfg, float(dt), int(nsteps), int(interval or default_interval(nsteps)))
+
+
+def burgers_adjoint_step(cfg: BurgersConfig, u_n, u1, u2, dt: float, lam, work=None, stream=None):
+    """lam (dJ/du^{n+1}) becomes dJ/du^n in place; work: 3 arrays of scratch (allocated if None)."""
+    import torch
+    d = cfg.desc(_dtype_code(u_n))
+    if work is None:
+        one = (u_n.numel() * u_n.element_size() + 255) // 256 * 256
+        work = torch.empty(3 * one, dtype=torch.uint8, device=u_n.device)
+    N.check(N.load().adv_burgers_adjoint_step(C.byref(d), _ptr(u_n), _ptr(u1), _ptr(u2), float(dt), _ptr(lam),
+                                              _ptr(work), N.stream_handle(stream)), "adv_burgers_adjoint_step")
+    return lam
+
+
+_HeatKRun = None
+
+
+def heatk_run(cfg: HeatKConfig, k, u0, nsteps: int, interval: int | None = None):
+    """Differentiable (w.r.t. k and u0) forward run of nsteps steps; returns u(T)."""
+    global _HeatKRun
+    if _HeatKRun is None:
+        _HeatKRun = _autograd()
+    return _HeatKRun.apply(k, u0, cfg, int(nsteps), int(interval or default_interval(nsteps)))
+
+
 class Ensemble:
     """Batched ensemble of 3D heat and Burgers problems (adv_ensemble_* in include/advdiff.h).
 

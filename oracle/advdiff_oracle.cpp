@@ -401,6 +401,185 @@ int64_t burgers_run(const BurgersCfg& c, T* u, double tEnd, double CFL, int dt_r
 
 }  // namespace
 
+// ------------------------------------------------------ heat with a diffusivity field k(x)
+// Conservative 7-point form with arithmetic face averages and forward Euler, c_a = dt/h_a^2, the
+// outermost layer frozen (or zeroed), and the exact transpose of one step (the library's
+// adv_heatk_step / adv_heatk_adjoint_step; no reference counterpart). Every operation is rounded
+// as written, fused multiply-adds where the kernels use them, so the GPU agrees bit for bit.
+template <class T>
+void heatk_step(int64_t nx, int64_t ny, int64_t nz, int zero_boundary, T cx, T cy, T cz, const T* k, const T* u,
+                T* out) {
+  const int64_t sy = nx, sz = nx * ny;
+  const T h = T(0.5);
+#pragma omp parallel for collapse(2) schedule(static)
+  for (int64_t z = 0; z < nz; ++z)
+    for (int64_t y = 0; y < ny; ++y)
+      for (int64_t x = 0; x < nx; ++x) {
+        const int64_t o = x + sy * y + sz * z;
+        const bool in = x > 0 && x < nx - 1 && y > 0 && y < ny - 1 && z > 0 && z < nz - 1;
+        const T uc = u[o], kc = k[o];
+        if (!in) {
+          out[o] = zero_boundary ? T(0) : uc;
+          continue;
+        }
+        auto flux = [&](int64_t s) {
+          const T fp = h * (kc + k[o + s]), fm = h * (kc + k[o - s]);
+          return std::fma(fp, u[o + s] - uc, -(fm * (uc - u[o - s])));
+        };
+        const T Fx = flux(1), Fy = flux(sy), Fz = flux(sz);
+        out[o] = uc + std::fma(cz, Fz, std::fma(cy, Fy, cx * Fx));
+      }
+}
+
+template <class T>
+void heatk_adjoint(int64_t nx, int64_t ny, int64_t nz, int zero_boundary, T cx, T cy, T cz, const T* k, const T* u,
+                   const T* lam, T* out, T* grad) {
+  const int64_t sy = nx, sz = nx * ny;
+  const T h = T(0.5);
+  auto interior = [&](int64_t x, int64_t y, int64_t z) {
+    return x > 0 && x < nx - 1 && y > 0 && y < ny - 1 && z > 0 && z < nz - 1;
+  };
+#pragma omp parallel for collapse(2) schedule(static)
+  for (int64_t z = 0; z < nz; ++z)
+    for (int64_t y = 0; y < ny; ++y)
+      for (int64_t x = 0; x < nx; ++x) {
+        const int64_t o = x + sy * y + sz * z;
+        const bool in_c = interior(x, y, z);
+        const T lc = lam[o], muc = in_c ? lc : T(0), uc = u[o], kc = k[o];
+        auto axis = [&](int64_t s, bool hp, bool hm, bool inp, bool inm, T& S, T& G) {
+          const int64_t op = hp ? o + s : o, om = hm ? o - s : o;
+          const T mup = hp && inp ? lam[op] : T(0), mum = hm && inm ? lam[om] : T(0);
+          const T kfp = h * (kc + k[op]), kfm = h * (kc + k[om]);
+          const T dmp = hp ? mup - muc : T(0), dmm = hm ? mum - muc : T(0);
+          const T dup = u[op] - uc, dum = u[om] - uc;
+          S = std::fma(kfm, dmm, kfp * dmp);
+          G = std::fma(dum, -dmm, dup * -dmp);
+        };
+        T Sx, Gx, Sy, Gy, Sz, Gz;
+        axis(1, x + 1 < nx, x > 0, interior(x + 1, y, z), interior(x - 1, y, z), Sx, Gx);
+        axis(sy, y + 1 < ny, y > 0, interior(x, y + 1, z), interior(x, y - 1, z), Sy, Gy);
+        axis(sz, z + 1 < nz, z > 0, interior(x, y, z + 1), interior(x, y, z - 1), Sz, Gz);
+        const T keep = (in_c || !zero_boundary) ? lc : T(0);
+        out[o] = keep + std::fma(cz, Sz, std::fma(cy, Sy, cx * Sx));
+        grad[o] = std::fma(h, std::fma(cz, Gz, std::fma(cy, Gy, cx * Gx)), grad[o]);
+      }
+}
+
+// ------------------------------------------------------------ Burgers discrete adjoint
+// Exact transpose of the periodic, local Lax-Friedrichs WENO5 / WENO5-Z SSP-RK3 step (the
+// library's adv_burgers_adjoint_step; no reference counterpart). Written independently of the
+// kernel, in scatter form: every face pushes its derivative into the ten cells of its stencil.
+//
+// One side of a face from a..e (the left-biased five values); the WENO weights in their
+// common-denominator form w_k (alpha_k times a positive factor shared by the three):
+//   B_k = 13/3 t_k^2 + s_k^2 + 4e-6   (= 4 (beta_k + eps))
+//   Z:  w_0 = (B0+tau) B1 B2, w_1 = 6 (B1+tau) B0 B2, w_2 = 3 (B2+tau) B0 B1, tau = |B0-B2|
+//   JS: w_0 = (B1 B2)^2,      w_1 = 6 (B0 B2)^2,       w_2 = 3 (B0 B1)^2
+//   side = sum w_k q_k / sum w_k,  q_k = c + t_k/12 + sigma_k s_k/4
+// (t, s the second / first differences of the reference's beta_k and candidate polynomials,
+// SingleGPU/Burgers3d_WENO5/kernels.cu:92-192). side_rev returns d side / d(a..e) times ybar.
+template <class T>
+void side_rev(bool Z, T a, T b, T c, T d, T e, T ybar, T g[5]) {
+  const T t0 = a - 2 * b + c, t1 = b - 2 * c + d, t2 = c - 2 * d + e;
+  const T s0 = a - 4 * b + 3 * c, s1 = b - d, s2 = 3 * c - 4 * d + e;
+  const T K = T(13) / T(3), E = T(4e-6);
+  const T B0 = K * t0 * t0 + s0 * s0 + E, B1 = K * t1 * t1 + s1 * s1 + E, B2 = K * t2 * t2 + s2 * s2 + E;
+  const T q0 = c + t0 / 12 + s0 / 4, q1 = c + t1 / 12 - s1 / 4, q2 = c + t2 / 12 - s2 / 4;
+  T w0, w1, w2, tau = 0;
+  if (Z) {
+    tau = std::fabs(B0 - B2);
+    w0 = (B0 + tau) * B1 * B2;
+    w1 = 6 * (B1 + tau) * B0 * B2;
+    w2 = 3 * (B2 + tau) * B0 * B1;
+  } else {
+    w0 = (B1 * B2) * (B1 * B2);
+    w1 = 6 * (B0 * B2) * (B0 * B2);
+    w2 = 3 * (B0 * B1) * (B0 * B1);
+  }
+  const T D = w0 + w1 + w2;
+  const T side = (w0 * q0 + w1 * q1 + w2 * q2) / D;
+  const T Nb = ybar / D;
+  const T wb0 = Nb * (q0 - side), wb1 = Nb * (q1 - side), wb2 = Nb * (q2 - side);
+  const T qb0 = Nb * w0, qb1 = Nb * w1, qb2 = Nb * w2;
+  T Bb0 = 0, Bb1 = 0, Bb2 = 0;
+  if (Z) {
+    T taub = wb0 * B1 * B2 + 6 * wb1 * B0 * B2 + 3 * wb2 * B0 * B1;
+    Bb0 += wb0 * B1 * B2 + 6 * wb1 * (B1 + tau) * B2 + 3 * wb2 * (B2 + tau) * B1;
+    Bb1 += wb0 * (B0 + tau) * B2 + 6 * wb1 * B0 * B2 + 3 * wb2 * (B2 + tau) * B0;
+    Bb2 += wb0 * (B0 + tau) * B1 + 6 * wb1 * (B1 + tau) * B0 + 3 * wb2 * B0 * B1;
+    const T sg = B0 > B2 ? T(1) : (B0 < B2 ? T(-1) : T(0));
+    Bb0 += sg * taub;
+    Bb2 -= sg * taub;
+  } else {
+    const T p12 = B1 * B2, p02 = B0 * B2, p01 = B0 * B1;
+    Bb0 += 12 * wb1 * p02 * B2 + 6 * wb2 * p01 * B1;
+    Bb1 += 2 * wb0 * p12 * B2 + 6 * wb2 * p01 * B0;
+    Bb2 += 2 * wb0 * p12 * B1 + 12 * wb1 * p02 * B0;
+  }
+  const T tb0 = 2 * K * t0 * Bb0 + qb0 / 12, tb1 = 2 * K * t1 * Bb1 + qb1 / 12, tb2 = 2 * K * t2 * Bb2 + qb2 / 12;
+  const T sb0 = 2 * s0 * Bb0 + qb0 / 4, sb1 = 2 * s1 * Bb1 - qb1 / 4, sb2 = 2 * s2 * Bb2 - qb2 / 4;
+  const T cb = qb0 + qb1 + qb2;
+  g[0] = tb0 + sb0;
+  g[1] = -2 * tb0 + tb1 - 4 * sb0 + sb1;
+  g[2] = tb0 - 2 * tb1 + tb2 + 3 * sb0 + 3 * sb2 + cb;
+  g[3] = tb1 - 2 * tb2 - sb1 - 4 * sb2;
+  g[4] = tb2 + sb2;
+}
+
+// lam_out = lam + dt * J(v)^T lam for one stage input v (periodic, local LF).
+template <class T>
+void burgers_stage_adjoint(const BurgersCfg& c, const T* v, const T* lam, T dt, T* out) {
+  const int64_t nx = c.nx, ny = c.ny, nz = c.nz;
+  const size_t n = (size_t)nx * ny * nz;
+  std::vector<T> GP(n, T(0)), GM(n, T(0));
+  const int64_t dims[3] = {nx, ny, nz};
+  const T rd[3] = {T(1) / (T)c.dx, T(1) / (T)c.dy, T(1) / (T)c.dz};
+  auto fp = [](T u) { return u * (u / 4 + std::fabs(u) / 2); };
+  auto fm = [](T u) { return u * (u / 4 - std::fabs(u) / 2); };
+  for (int ax = 0; ax < 3; ++ax) {
+    for (int64_t k = 0; k < nz; ++k)
+      for (int64_t j = 0; j < ny; ++j)
+        for (int64_t i = 0; i < nx; ++i) {
+          int64_t p[3] = {i, j, k};
+          auto idx = [&](int64_t off) {
+            int64_t q[3] = {p[0], p[1], p[2]};
+            q[ax] = ((q[ax] + off) % dims[ax] + dims[ax]) % dims[ax];
+            return (size_t)(q[0] + nx * (q[1] + ny * q[2]));
+          };
+          // face at p + 1/2 along ax
+          const T psi = rd[ax] * (lam[idx(1)] - lam[idx(0)]);
+          T P[5], M[5];
+          side_rev<T>(c.weno_z != 0, fp(v[idx(-2)]), fp(v[idx(-1)]), fp(v[idx(0)]), fp(v[idx(1)]), fp(v[idx(2)]), psi,
+                      P);
+          side_rev<T>(c.weno_z != 0, fm(v[idx(3)]), fm(v[idx(2)]), fm(v[idx(1)]), fm(v[idx(0)]), fm(v[idx(-1)]),
+                      psi, M);
+          for (int q = 0; q < 5; ++q) {
+            GP[idx(q - 2)] += P[q];
+            GM[idx(3 - q)] += M[q];
+          }
+        }
+  }
+  for (size_t o = 0; o < n; ++o) {
+    const T u = v[o];
+    const T jt = (u / 2 + std::fabs(u)) * GP[o] + (u / 2 - std::fabs(u)) * GM[o];
+    out[o] = lam[o] + dt * jt;
+  }
+}
+
+// Adjoint of one SSP-RK3 step from its stage inputs u_n, u1, u2: lam (dJ/du^{n+1}) becomes
+// dJ/du^n. Stage s output: a_s u^n + b_s (v + dt L(v)), (a, b) = (0, 1), (3/4, 1/4), (1/3, 2/3).
+template <class T>
+void burgers_step_adjoint(const BurgersCfg& c, const T* un, const T* u1, const T* u2, T dt, T* lam) {
+  const size_t n = (size_t)c.nx * c.ny * c.nz;
+  std::vector<T> t(n), l2(n), l1(n), acc(n);
+  burgers_stage_adjoint<T>(c, u2, lam, dt, t.data());
+  for (size_t o = 0; o < n; ++o) { l2[o] = T(2) / T(3) * t[o]; acc[o] = lam[o] / T(3); }
+  burgers_stage_adjoint<T>(c, u1, l2.data(), dt, t.data());
+  for (size_t o = 0; o < n; ++o) { l1[o] = T(0.25) * t[o]; acc[o] += T(0.75) * l2[o]; }
+  burgers_stage_adjoint<T>(c, un, l1.data(), dt, t.data());
+  for (size_t o = 0; o < n; ++o) lam[o] = acc[o] + t[o];
+}
+
 extern "C" {
 
 // ----------------------------------------------------------------------------- RNG
@@ -745,5 +924,35 @@ int64_t orc_burgers_ref_steps(double tEnd, double CFL, double L, double W, doubl
 
 double orc_max_abs_f64(const double* u, int64_t n) { return max_abs<double>(u, (size_t)n); }
 float orc_max_abs_f32(const float* u, int64_t n) { return max_abs<float>(u, (size_t)n); }
+
+
+// heat with k(x): one step and the adjoint of one step
+void orc_heatk_step_f64(int nx, int ny, int nz, int zb, double cx, double cy, double cz, const double* k,
+                        const double* u, double* out) {
+  heatk_step<double>(nx, ny, nz, zb, cx, cy, cz, k, u, out);
+}
+void orc_heatk_step_f32(int nx, int ny, int nz, int zb, double cx, double cy, double cz, const float* k,
+                        const float* u, float* out) {
+  heatk_step<float>(nx, ny, nz, zb, (float)cx, (float)cy, (float)cz, k, u, out);
+}
+void orc_heatk_adjoint_f64(int nx, int ny, int nz, int zb, double cx, double cy, double cz, const double* k,
+                           const double* u, const double* lam, double* out, double* grad) {
+  heatk_adjoint<double>(nx, ny, nz, zb, cx, cy, cz, k, u, lam, out, grad);
+}
+void orc_heatk_adjoint_f32(int nx, int ny, int nz, int zb, double cx, double cy, double cz, const float* k,
+                           const float* u, const float* lam, float* out, float* grad) {
+  heatk_adjoint<float>(nx, ny, nz, zb, (float)cx, (float)cy, (float)cz, k, u, lam, out, grad);
+}
+
+
+// Burgers adjoint of one SSP-RK3 step (periodic, local LF): lam in/out.
+void orc_burgers_step_adjoint_f64(BURG_ARGS, const double* un, const double* u1, const double* u2, double dt,
+                                  double* lam) {
+  BURG_CFG burgers_step_adjoint<double>(c, un, u1, u2, dt, lam);
+}
+void orc_burgers_step_adjoint_f32(BURG_ARGS, const float* un, const float* u1, const float* u2, double dt,
+                                  float* lam) {
+  BURG_CFG burgers_step_adjoint<float>(c, un, u1, u2, (float)dt, lam);
+}
 
 }  // extern "C"

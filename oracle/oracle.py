@@ -62,6 +62,12 @@ def lib() -> C.CDLL:
             "orc_burgers_run_f32": (_I64, _BURG + [_I, C.c_void_p, _D, _D, _I, _D, _I64, _PD]),
             "orc_burgers_ref_steps": (_I64, [_D, _D, _D, _D, _D, _I, _I, _I, _D, _PD]),
             "orc_max_abs_f64": (_D, [C.c_void_p, _I64]),
+            "orc_burgers_step_adjoint_f64": (None, _BURG + [C.c_void_p] * 3 + [_D, C.c_void_p]),
+            "orc_burgers_step_adjoint_f32": (None, _BURG + [C.c_void_p] * 3 + [_D, C.c_void_p]),
+            "orc_heatk_step_f64": (None, [_I, _I, _I, _I, _D, _D, _D] + [C.c_void_p] * 3),
+            "orc_heatk_step_f32": (None, [_I, _I, _I, _I, _D, _D, _D] + [C.c_void_p] * 3),
+            "orc_heatk_adjoint_f64": (None, [_I, _I, _I, _I, _D, _D, _D] + [C.c_void_p] * 5),
+            "orc_heatk_adjoint_f32": (None, [_I, _I, _I, _I, _D, _D, _D] + [C.c_void_p] * 5),
             "orc_philox_u01x2": (None, [_U32, _U32, C.c_uint64, _PD, _PD]),
             "orc_num_threads": (_I, []),
             "orc_set_num_threads": (None, [_I]),
@@ -211,3 +217,70 @@ def set_threads(n: int) -> None:
 
 def num_threads() -> int:
     return lib().orc_num_threads()
+
+
+# ------------------------------------------------------------- heat with a diffusivity field k(x)
+def heatk_step(shape, zero_boundary: bool, c, k: np.ndarray, u: np.ndarray) -> np.ndarray:
+    """One forward-Euler step of u_t = div(k grad u) (conservative, face averages); c = dt/h^2 per axis."""
+    nx, ny, nz = shape
+    out = np.empty_like(u)
+    f = lib().orc_heatk_step_f64 if u.dtype == np.float64 else lib().orc_heatk_step_f32
+    f(nx, ny, nz, int(zero_boundary), *c, _p(k), _p(u), _p(out))
+    return out
+
+
+def heatk_adjoint(shape, zero_boundary: bool, c, k, u, lam, grad):
+    """Adjoint of one step: returns dJ/du^n from lam = dJ/du^{n+1}; adds the step's dJ/dk to grad."""
+    nx, ny, nz = shape
+    out = np.empty_like(lam)
+    f = lib().orc_heatk_adjoint_f64 if u.dtype == np.float64 else lib().orc_heatk_adjoint_f32
+    f(nx, ny, nz, int(zero_boundary), *c, _p(k), _p(u), _p(lam), _p(out), _p(grad))
+    return out
+
+
+def heatk_loss_and_gradient(shape, zero_boundary, c, k, u0, target, nsteps):
+    """J = 1/2 |u(T) - target|^2 and (dJ/dk, dJ/du0) by storing every state (small cases only)."""
+    states = [u0]
+    for _ in range(nsteps):
+        states.append(heatk_step(shape, zero_boundary, c, k, states[-1]))
+    r = states[-1] - target
+    J = 0.5 * float(np.dot(r.astype(np.float64), r.astype(np.float64)))
+    lam = r.copy()
+    grad = np.zeros_like(k)
+    for n in range(nsteps - 1, -1, -1):
+        lam = heatk_adjoint(shape, zero_boundary, c, k, states[n], lam, grad)
+    return J, grad, lam
+
+
+# ------------------------------------------------------------------- Burgers discrete adjoint
+def burgers_step_adjoint(cfg, un, u1, u2, dt, lam):
+    """dJ/du^n from lam = dJ/du^{n+1} and the step's stage inputs (periodic, local LF)."""
+    lam = np.ascontiguousarray(lam).copy()
+    f = lib().orc_burgers_step_adjoint_f64 if un.dtype == np.float64 else lib().orc_burgers_step_adjoint_f32
+    f(*_burg_args(cfg), _p(un), _p(u1), _p(u2), dt, _p(lam))
+    return lam
+
+
+def burgers_forward_states(cfg, u0, dt, nsteps, div64=True):
+    """Every stage input of nsteps fixed-dt SSP-RK3 steps: [(u^n, u1, u2)] and u^N."""
+    states = []
+    u = u0
+    for _ in range(nsteps):
+        u1 = burgers_stage(cfg, 1, u, u, dt, div64)
+        u2 = burgers_stage(cfg, 2, u1, u, dt, div64)
+        un1 = burgers_stage(cfg, 3, u2, u, dt, div64)
+        states.append((u, u1, u2))
+        u = un1
+    return states, u
+
+
+def burgers_loss_and_gradient(cfg, u0, target, dt, nsteps):
+    """J = 1/2 |u(T) - target|^2 and dJ/du0 by storing every stage (small cases only)."""
+    states, uT = burgers_forward_states(cfg, u0, dt, nsteps)
+    r = uT - target
+    J = 0.5 * float(np.dot(r.astype(np.float64), r.astype(np.float64)))
+    lam = r.copy()
+    for un, u1, u2 in reversed(states):
+        lam = burgers_step_adjoint(cfg, un, u1, u2, dt, lam)
+    return J, lam
+
