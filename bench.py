@@ -310,6 +310,142 @@ def bench_ensemble(args, world, rank, dev, stream, flush, lib):
         print(json.dumps(line), flush=True)
 
 
+ADJ_N, ADJ_STEPS, ADJ_INTERVAL, ADJ_T = 128, 400, 20, 0.15
+HEATK_N, HEATK_STEPS = 192, 200
+
+
+def adjoint_setup():
+    """Config of the discrete-adjoint workload: Burgers WENO5-Z, local LF, periodic [0,2)^3 at 128^3
+    FP32, 400 SSP-RK3 steps of a fixed dt = 0.15 / 400 from the seeded Fourier state (seed 5), i.e.
+    to t = 0.15, before the first shocks (past them the discrete adjoint of a captured shock is
+    dominated by rounding-level sensitivities and no finite difference can check it);
+    u_target = the forward result of seed 6; checkpoints every 20 steps. Heat: 192^3 FP32, k(x) =
+    exp(g) with g a box-smoothed N(0, 0.25) field (seed 23), dt k_max / h^2 = 1/8, 200 steps, 8
+    seeded blobs, target = the forward result of another diffusivity draw (seed 24)."""
+    from multigpu_advectiondiffusion_gb300 import _native as N
+    from multigpu_advectiondiffusion_gb300.solvers import BurgersConfig, HeatKConfig
+    n = ADJ_N
+    bc = BurgersConfig(n, n, n, 2.0 / n, 2.0 / n, 2.0 / n, N.ADV_WENO5_Z, N.ADV_LF_LOCAL, N.ADV_BC_PERIODIC,
+                       N.ADV_DIV_FAST)
+    u0 = ic_burgers_fourier(n, n, n, 2.0, 5)
+    ut = ic_burgers_fourier(n, n, n, 2.0, 6)
+    dt = ADJ_T / ADJ_STEPS
+    m = HEATK_N
+
+    def kfield(seed):
+        g = np.random.default_rng(seed).normal(0.0, 0.5, (m, m, m))
+        for ax in range(3):
+            g = (np.roll(g, 1, ax) + g + np.roll(g, -1, ax)) / 3.0
+        return np.exp(g / g.std() * 0.5).ravel()
+
+    k = kfield(23)
+    k2 = kfield(24)
+    hc = HeatKConfig.cube(m, 0.125, float(max(k.max(), k2.max())))
+    h0 = ic_heat3d_blobs(m, m, m, 2)
+    return bc, u0, ut, dt, hc, k, k2, h0
+
+
+def bench_adjoint(args, world, rank, dev, lib):
+    import torch
+    from multigpu_advectiondiffusion_gb300.solvers import burgers_run_fixed, heatk_run
+    bc, u0n, utn, dt, hc, kn, k2n, h0n = adjoint_setup()
+    u0 = torch.from_numpy(u0n.astype(np.float32)).to(dev)
+    with torch.no_grad():
+        target = burgers_run_fixed(bc, torch.from_numpy(utn.astype(np.float32)).to(dev), dt, ADJ_STEPS, ADJ_INTERVAL)
+
+    def ev(fn):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record()
+        r = fn()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b), r
+
+    def grad_burgers(u, tgt):
+        uu = u.clone().requires_grad_(True)
+        tf, uT = ev(lambda: burgers_run_fixed(bc, uu, dt, ADJ_STEPS, ADJ_INTERVAL))
+        loss = 0.5 * ((uT - tgt) ** 2).sum()
+        tb, _ = ev(loss.backward)
+        return tf, tb, uu.grad, float(loss.detach())
+
+    for _ in range(args.warmup):
+        grad_burgers(u0, target)
+    uuid = None
+    try:
+        uuid = "GPU-" + str(torch.cuda.get_device_properties(dev).uuid)
+    except Exception:
+        pass
+    tfs, tbs = [], []
+    with ClockSampler(uuid) as clk:
+        launches0 = lib.adv_kernel_launch_count()
+        for _ in range(args.steps):
+            tf, tb, g32, J32 = grad_burgers(u0, target)
+            tfs.append(tf)
+            tbs.append(tb)
+        launched = lib.adv_kernel_launch_count() - launches0
+    tf, tb = float(np.median(tfs)), float(np.median(tbs))
+    cells = ADJ_N ** 3 * 3 * ADJ_STEPS
+    # FP64 adjoint and central differences of the FP64 forward along 16 seeded directions
+    u64 = u0.double()
+    t64 = target.double()
+    _, _, g64, _ = grad_burgers(u64, t64)
+    rel64 = (torch.linalg.vector_norm(g32.double() - g64) / torch.linalg.vector_norm(g64)).item()
+
+    def J64(u):
+        with torch.no_grad():
+            return 0.5 * float(((burgers_run_fixed(bc, u, dt, ADJ_STEPS, ADJ_INTERVAL) - t64) ** 2).sum())
+
+    fd_err = []
+    for i in range(16):
+        d = torch.from_numpy(np.random.default_rng(7 + i).standard_normal(u0.numel())).to(dev)
+        eps = 1e-8
+        fd = (J64(u64 + eps * d) - J64(u64 - eps * d)) / (2 * eps)
+        ad = float((g32.double() * d).sum())
+        fd_err.append(abs(fd - ad) / abs(fd))
+    # heat with k(x): gradient w.r.t. k and u0
+    k = torch.from_numpy(kn.astype(np.float32)).to(dev)
+    h0 = torch.from_numpy(h0n.astype(np.float32)).to(dev)
+    with torch.no_grad():
+        htarget = heatk_run(hc, torch.from_numpy(k2n.astype(np.float32)).to(dev), h0, HEATK_STEPS)
+
+    def grad_heat():
+        kk = k.clone().requires_grad_(True)
+        hh = h0.clone().requires_grad_(True)
+        tfh, uT = ev(lambda: heatk_run(hc, kk, hh, HEATK_STEPS))
+        loss = 0.5 * ((uT - htarget) ** 2).sum()
+        tbh, _ = ev(loss.backward)
+        return tfh, tbh
+    for _ in range(2):
+        grad_heat()
+    hts = [grad_heat() for _ in range(3)]
+    tfh, tbh = float(np.median([h[0] for h in hts])), float(np.median([h[1] for h in hts]))
+    if rank == 0:
+        line = {
+            "metric": "Gcell-updates/s/RK-stage", "value": world * cells / ((tf + tb) * 1e-3) / 1e9,
+            "unit": "Gcell-updates/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": tf + tb, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded Fourier states and log-normal diffusivity)",
+            "config": {"workload": f"adjoint burgers3d {ADJ_N}^3 f32 weno5-z local-lf periodic, {ADJ_STEPS} steps to "
+                                   f"t={ADJ_T} (cfl {dt * float(u0.abs().max()) / bc.dx:.3f}), checkpoints every "
+                                   f"{ADJ_INTERVAL}; heat k(x) {HEATK_N}^3 f32 {HEATK_STEPS} steps",
+                       "parallelism": f"replicas{world}",
+                       "value_is": "forward cell-stage updates per second of forward + backward (one gradient)"},
+            "roofline": None,
+            "cpu_baseline": None,
+            "e2e": None,
+            "gpu_launches": int(launched),
+            "clocks": clk.summary(),
+            "burgers": {"forward_ms": tf, "backward_ms": tb, "backward_over_forward": tb / tf,
+                        "forward_value": cells / (tf * 1e-3) / 1e9, "grad_fp32_vs_fp64_rel_l2": rel64,
+                        "fd_rel_err_max_16_dirs": max(fd_err), "fd_rel_err_median": float(np.median(fd_err)),
+                        "fd": "central differences of the FP64 forward run, step 1e-8, 16 seeded directions"},
+            "heat_k": {"forward_ms": tfh, "backward_ms": tbh, "backward_over_forward": tbh / tfh,
+                       "forward_value": HEATK_N ** 3 * HEATK_STEPS / (tfh * 1e-3) / 1e9},
+        }
+        print(json.dumps(line), flush=True)
+
+
 def reference_sg_gpu(workload: str, warmup: int) -> dict | None:
     """The reference's own single-GPU CUDA build on this GPU: its kernels compiled from its sources
     with its flags (-O3, FMA contraction on) into cubins, launched with its launch geometry (run.sh
@@ -407,6 +543,26 @@ def run_reference_arm(args, world, rank):
         value = float(np.median(rates))
         sample = "256^3 FP32 WENO5-Z periodic, 1 SSP-RK3 time step per step"
         config = {"workload": "burgers3d 256^3 f32 weno5-z global-lf periodic cfl 0.4"}
+    elif args.workload == "adjoint":
+        # the oracle's adjoint (stored states, OpenMP) on a 48^3 sample of the Burgers problem
+        from multigpu_advectiondiffusion_gb300 import _native as N
+        from multigpu_advectiondiffusion_gb300.solvers import BurgersConfig
+        n = 48
+        cfg = BurgersConfig(n, n, n, 2.0 / n, 2.0 / n, 2.0 / n, N.ADV_WENO5_Z, N.ADV_LF_LOCAL, N.ADV_BC_PERIODIC,
+                            N.ADV_DIV_F32)
+        u0 = ic_burgers_fourier(n, n, n, 2.0, 5)
+        ut = ic_burgers_fourier(n, n, n, 2.0, 6)
+        dt = 0.4 * cfg.dx / float(np.abs(u0).max())
+        rates = []
+        for i in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            oracle.burgers_loss_and_gradient(cfg, u0, ut, dt, 2)
+            dt_ = time.perf_counter() - t0
+            if i >= args.warmup:
+                rates.append(n ** 3 * 3 * 2 / dt_ / 1e9)
+        value = float(np.median(rates))
+        sample = "48^3 FP64 WENO5-Z local LF periodic, 2 steps forward + adjoint per step (oracle)"
+        config = {"workload": f"adjoint burgers3d {ADJ_N}^3 f32, {ADJ_STEPS} steps"}
     else:
         # the ensemble: per step, two heat instances for 4 steps and one Burgers instance for one
         # RK3 step, in proportion to the ensemble's heat / Burgers cell updates
@@ -444,7 +600,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="heat3d", choices=["heat3d", "burgers3d", "ensemble"])
+    ap.add_argument("--workload", default="heat3d", choices=["heat3d", "burgers3d", "ensemble", "adjoint"])
     ap.add_argument("--cpu-budget", type=float, default=10.0, help="seconds of CPU-baseline work")
     ap.add_argument("--div", default="fast", choices=["fast", "f32", "f64"],
                     help="Burgers WENO weight division (FP32 state)")
@@ -479,8 +635,11 @@ def main():
     sh = stream.cuda_stream
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
 
-    if args.workload == "ensemble":
-        bench_ensemble(args, world, rank, dev, stream, flush, lib)
+    if args.workload in ("ensemble", "adjoint"):
+        if args.workload == "ensemble":
+            bench_ensemble(args, world, rank, dev, stream, flush, lib)
+        else:
+            bench_adjoint(args, world, rank, dev, lib)
         if world > 1:
             dist.destroy_process_group()
         return

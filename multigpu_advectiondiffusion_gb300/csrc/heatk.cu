@@ -83,32 +83,44 @@ __global__ void __launch_bounds__(KX * KY) heatk_adjoint_kernel(const __grid_con
   const int nx = a.nx, ny = a.ny, nz = a.nz;
   const size_t sy = (size_t)nx, sz = (size_t)nx * ny;
   const T h = T(0.5);
-  auto interior = [&](int xx, int yy, int zz) {
-    return xx > 0 && xx < nx - 1 && yy > 0 && yy < ny - 1 && zz > 0 && zz < nz - 1;
+  // interior tests of this column and of its x / y neighbours' columns
+  auto in1 = [](int i, int n) { return i > 0 && i < n - 1; };
+  const bool xin = in1(x, nx), yin = in1(y, ny);
+  const bool hxp = x + 1 < nx, hxm = x > 0, hyp = y + 1 < ny, hym = y > 0;
+  const bool cxp = in1(x + 1, nx) && yin, cxm = in1(x - 1, nx) && yin;
+  const bool cyp = xin && in1(y + 1, ny), cym = xin && in1(y - 1, ny);
+  const bool ccol = xin && yin;
+  // one axis from the neighbours' values (an absent neighbour passes the centre's values)
+  auto axis = [&](bool hp, bool hm, bool inp, bool inm, T lp, T lm, T up, T um, T kp, T km, T muc, T uc, T kc, T& S,
+                  T& G) {
+    const T mup = hp && inp ? lp : T(0), mum = hm && inm ? lm : T(0);
+    const T kfp = mul_rn(h, add_rn(kc, kp)), kfm = mul_rn(h, add_rn(kc, km));
+    const T dmp = hp ? sub_rn(mup, muc) : T(0), dmm = hm ? sub_rn(mum, muc) : T(0);
+    const T dup = sub_rn(up, uc), dum = sub_rn(um, uc);
+    S = fma_k(kfm, dmm, mul_rn(kfp, dmp));
+    G = fma_k(dum, -dmm, mul_rn(dup, -dmp));
   };
-  for (int z = z0; z < z1; ++z) {
-    const size_t o = (size_t)x + sy * y + sz * z;
-    const bool in_c = interior(x, y, z);
-    const T lc = a.lam[o];
+  size_t o = (size_t)x + sy * y + sz * z0;
+  // z windows of lam, u, k at z-1, z, z+1
+  T lc = a.lam[o], uc = a.u[o], kc = a.k[o];
+  T lm = z0 > 0 ? a.lam[o - sz] : lc, um = z0 > 0 ? a.u[o - sz] : uc, km = z0 > 0 ? a.k[o - sz] : kc;
+  for (int z = z0; z < z1; ++z, o += sz) {
+    const bool hzp = z + 1 < nz, hzm = z > 0;
+    const T lp = hzp ? a.lam[o + sz] : lc, up = hzp ? a.u[o + sz] : uc, kp = hzp ? a.k[o + sz] : kc;
+    const bool zin = in1(z, nz);
+    const bool in_c = ccol && zin;
     const T muc = in_c ? lc : T(0);
-    const T uc = a.u[o], kc = a.k[o];
-    // one axis: neighbours at +s (if `hp`) and -s (if `hm`), with their interior flags
-    auto axis = [&](size_t s, bool hp, bool hm, bool inp, bool inm, T& S, T& G) {
-      const size_t op = hp ? o + s : o, om = hm ? o - s : o;
-      const T mup = hp && inp ? a.lam[op] : T(0), mum = hm && inm ? a.lam[om] : T(0);
-      const T kfp = mul_rn(h, add_rn(kc, a.k[op])), kfm = mul_rn(h, add_rn(kc, a.k[om]));
-      const T dmp = hp ? sub_rn(mup, muc) : T(0), dmm = hm ? sub_rn(mum, muc) : T(0);
-      const T dup = sub_rn(a.u[op], uc), dum = sub_rn(a.u[om], uc);
-      S = fma_k(kfm, dmm, mul_rn(kfp, dmp));
-      G = fma_k(dum, -dmm, mul_rn(dup, -dmp));
-    };
+    const size_t ox = hxp ? o + 1 : o, oxm = hxm ? o - 1 : o, oy = hyp ? o + sy : o, oym = hym ? o - sy : o;
     T Sx, Gx, Sy, Gy, Sz, Gz;
-    axis(1, x + 1 < nx, x > 0, interior(x + 1, y, z), interior(x - 1, y, z), Sx, Gx);
-    axis(sy, y + 1 < ny, y > 0, interior(x, y + 1, z), interior(x, y - 1, z), Sy, Gy);
-    axis(sz, z + 1 < nz, z > 0, interior(x, y, z + 1), interior(x, y, z - 1), Sz, Gz);
+    axis(hxp, hxm, cxp && zin, cxm && zin, a.lam[ox], a.lam[oxm], a.u[ox], a.u[oxm], a.k[ox], a.k[oxm], muc, uc, kc,
+         Sx, Gx);
+    axis(hyp, hym, cyp && zin, cym && zin, a.lam[oy], a.lam[oym], a.u[oy], a.u[oym], a.k[oy], a.k[oym], muc, uc, kc,
+         Sy, Gy);
+    axis(hzp, hzm, ccol && in1(z + 1, nz), ccol && in1(z - 1, nz), lp, lm, up, um, kp, km, muc, uc, kc, Sz, Gz);
     const T keep = (in_c || !a.zero_boundary) ? lc : T(0);
     a.out[o] = add_rn(keep, fma_k(a.cz, Sz, fma_k(a.cy, Sy, mul_rn(a.cx, Sx))));
     a.grad[o] = fma_k(h, fma_k(a.cz, Gz, fma_k(a.cy, Gy, mul_rn(a.cx, Gx))), a.grad[o]);
+    lm = lc; lc = lp; um = uc; uc = up; km = kc; kc = kp;
   }
 }
 
