@@ -409,6 +409,10 @@ def bench_adjoint(args, world, rank, dev, lib):
     with torch.no_grad():
         htarget = heatk_run(hc, torch.from_numpy(k2n.astype(np.float32)).to(dev), h0, HEATK_STEPS)
 
+    if not args.no_tune:
+        from multigpu_advectiondiffusion_gb300.solvers import autotune_heatk
+        autotune_heatk(hc, k, h0)
+
     def grad_heat():
         kk = k.clone().requires_grad_(True)
         hh = h0.clone().requires_grad_(True)
@@ -604,6 +608,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=10.0, help="seconds of CPU-baseline work")
     ap.add_argument("--div", default="fast", choices=["fast", "f32", "f64"],
                     help="Burgers WENO weight division (FP32 state)")
+    ap.add_argument("--no-tune", action="store_true", help="skip the launch-shape autotuner")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -618,8 +623,8 @@ def main():
     import torch
     import torch.distributed as dist
     from multigpu_advectiondiffusion_gb300 import _native as N
-    from multigpu_advectiondiffusion_gb300.solvers import (BurgersConfig, burgers_run, burgers_workspace, heat_run,
-                                                           heat_workspace)
+    from multigpu_advectiondiffusion_gb300.solvers import (BurgersConfig, autotune_burgers, autotune_heat, burgers_run,
+                                                           burgers_workspace, heat_run, heat_workspace)
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
@@ -654,6 +659,7 @@ def main():
 
         def one_step(uu):
             heat_run(cfg, uu, inner, ws, stream=sh)
+        tuned = None if args.no_tune else autotune_heat(cfg, u, stream=sh)
         workload_name = "heat3d 256^3 f32 o2 euler r=1/8 dirichlet 8 blobs x 2000 steps"
         kernel = "heat_stage_kernel<float,2,3,TMA>"
     else:
@@ -669,6 +675,7 @@ def main():
 
         def one_step(uu):
             burgers_run(cfg, uu, 1e9, 0.4, N.ADV_DT_MAXU, max_steps=inner, workspace=ws, stream=sh)
+        tuned = None if args.no_tune else autotune_burgers(cfg, u, stream=sh)
         workload_name = f"burgers3d 256^3 f32 weno5-z global-lf periodic cfl 0.4 x 20 steps, div {args.div}"
         kernel = f"burgers_stage_kernel<float,Z,{args.div}>"
 
@@ -769,7 +776,10 @@ def main():
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded Philox4x32-10 initial condition)",
             "config": {"workload": workload_name, "parallelism": f"replicas{world}",
-                       "l2": "per launch 64 MiB read + 64 MiB written > 126 MiB L2; 252 MiB L2 flush between steps"},
+                       "l2": "per launch 64 MiB read + 64 MiB written > 126 MiB L2; 252 MiB L2 flush between steps",
+                       "launch_shape": ({"ctas_per_sm": tuned["param_a"], "min_planes_per_cta": tuned["param_b"],
+                                         "tuned_us": tuned["best_us"], "default_us": tuned["default_us"]}
+                                        if tuned else "default")},
             "roofline": {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind, "traffic": _traffic(args.workload),
                          "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_us": launch_ms * 1e3},

@@ -256,6 +256,31 @@ adv_status adv_ensemble_shape(const adv_ensemble* e, int64_t* heat_units, int* h
                               int64_t* burgers_units, int* burgers_ctas);
 adv_status adv_ensemble_destroy(adv_ensemble* e);
 
+/* ------------------------------------------------------------------------- autotuner
+ * Times the candidate launch shapes of a problem on the caller's data (out of place: the state is
+ * not modified; a temporary buffer is allocated and freed on the stream) and keeps the fastest for
+ * every later call on this device with the same problem shape, for the life of the process. No
+ * counterpart in the reference (its drivers take the block sizes on the command line).
+ *   heat / Burgers stages: param_a = CTAs per SM (up to the kernel's occupancy), param_b =
+ *     minimum z planes per CTA share (the z-halo re-reads vs tail balance trade-off);
+ *   heat with k(x), step and adjoint kernels: param_a = block height, param_b = z planes per CTA.
+ * Synchronises the stream. */
+typedef struct adv_tune_result {
+  int32_t kind;
+  int32_t param_a, param_b;
+  int32_t candidates;
+  double best_us;     /* mean time per launch of the chosen shape */
+  double default_us;  /* the same for the untuned default shape */
+} adv_tune_result;
+
+adv_status adv_autotune_heat(const adv_heat_desc* d, const void* u, void* stream, adv_tune_result* out);
+adv_status adv_autotune_burgers(const adv_burgers_desc* d, const void* u, void* stream,
+                                adv_tune_result* out);
+adv_status adv_autotune_heatk(const adv_heatk_desc* d, const void* k, const void* u, void* stream,
+                              adv_tune_result* out_step, adv_tune_result* out_adjoint);
+/* Forgets every tuned shape (launches return to the defaults). */
+adv_status adv_autotune_clear(void);
+
 /* ------------------------------------------------------------------ reductions
  * max|u| over n values into *out (host double). Synchronises the stream. */
 adv_status adv_max_abs(int dtype, const void* u, int64_t n, double* out, void* stream);

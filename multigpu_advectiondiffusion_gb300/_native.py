@@ -46,6 +46,12 @@ class HeatKDesc(C.Structure):
                 ("cx", C.c_double), ("cy", C.c_double), ("cz", C.c_double)]
 
 
+class TuneResult(C.Structure):
+    """adv_tune_result (include/advdiff.h)."""
+    _fields_ = [("kind", C.c_int32), ("param_a", C.c_int32), ("param_b", C.c_int32), ("candidates", C.c_int32),
+                ("best_us", C.c_double), ("default_us", C.c_double)]
+
+
 class HeatMember(C.Structure):
     """adv_heat_member (include/advdiff.h)."""
     _fields_ = [("desc", HeatDesc), ("u", C.c_void_p), ("work", C.c_void_p)]
@@ -88,6 +94,10 @@ SIGNATURES = [
     ("adv_ensemble_shape", _I, [_VP, C.POINTER(C.c_int64), C.POINTER(C.c_int), C.POINTER(C.c_int64),
                                 C.POINTER(C.c_int)]),
     ("adv_ensemble_destroy", _I, [_VP]),
+    ("adv_autotune_heat", _I, [C.POINTER(HeatDesc), _VP, _VP, C.POINTER(TuneResult)]),
+    ("adv_autotune_burgers", _I, [C.POINTER(BurgersDesc), _VP, _VP, C.POINTER(TuneResult)]),
+    ("adv_autotune_heatk", _I, [C.POINTER(HeatKDesc), _VP, _VP, _VP, C.POINTER(TuneResult), C.POINTER(TuneResult)]),
+    ("adv_autotune_clear", _I, []),
     ("adv_max_abs", _I, [_I, _VP, _I64, _PD, _VP]),
     ("adv_ic_heat_ref", _I, [_I, _I, _I, _I, _D, _D, _D, _PD]),
     ("adv_ic_heat2d_gauss_noise", _I, [_I, _I, C.c_uint32, _D, _PD]),

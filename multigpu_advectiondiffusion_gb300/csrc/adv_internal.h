@@ -43,10 +43,26 @@ EncodeTiledFn encode_tiled_fn();
 adv_status read_and_clear_device_status(cudaStream_t s);
 int* device_status_ptr();
 
+// ------------------------------------------------------------------ launch-shape tuning
+// Parameters picked by the autotuner (autotune.cu) per device and problem; `set` is false when the
+// problem was never tuned (launchers then use their defaults). Kinds and parameters:
+//   TUNE_HEAT, TUNE_BURGERS: a = CTAs per SM (<= occupancy), b = minimum planes per CTA share
+//   TUNE_HEATK_STEP, TUNE_HEATK_ADJ: a = block height (threads in y), b = z planes per CTA
+enum TuneKind { TUNE_HEAT = 1, TUNE_BURGERS = 2, TUNE_HEATK_STEP = 3, TUNE_HEATK_ADJ = 4 };
+struct TuneParams {
+  int a = 0, b = 0;
+  bool set = false;
+};
+TuneParams tune_lookup(int kind, int variant, int nx, int ny, int nz);
+void tune_store(int kind, int variant, int nx, int ny, int nz, TuneParams p);
+void tune_clear();
+void graph_cache_clear();  // cached CUDA graphs hold launch shapes: drop them when tuning changes
+
 // ------------------------------------------------------------------ heat launchers
 struct HeatLaunch {
   // resolved per plan: whether the TMA path applies and the chosen z-chunk
   bool tma = false;
+  int occ = 0;                   // resident CTAs per SM of the stage kernel (before any tuning cap)
   int tiles_x = 0, tiles_y = 0;  // x-y tiles; the grid is one wave of CTAs sharing the tile-planes
   dim3 grid, block;
   size_t smem = 0;
@@ -56,16 +72,19 @@ adv_status heat_prepare(const adv_heat_desc& d, const void* u_in, HeatLaunch* L)
 adv_status heat_launch(const adv_heat_desc& d, const HeatLaunch& L, int stage, const void* u_in,
                        const void* u_n, void* u_out, cudaStream_t s);
 adv_status heat_validate(const adv_heat_desc* d);
+int heat_tune_variant(const adv_heat_desc& d);
 
 // --------------------------------------------------------------- Burgers launchers
 struct BurgersLaunch {
   bool tma = false;
+  int occ = 0;  // resident CTAs per SM of the stage kernel (before any tuning cap)
   int tiles_x = 0, tiles_y = 0;  // 32 x 16 column tiles; the grid is one wave sharing the tile-planes
   dim3 grid, block;
   size_t smem = 0;
   CUtensorMap tmap_in;
 };
 adv_status burgers_validate(const adv_burgers_desc* d);
+int burgers_tune_variant(const adv_burgers_desc& d);
 adv_status burgers_prepare(const adv_burgers_desc& d, const void* u_in, BurgersLaunch* L);
 // Stage launch arguments. The Lax-Friedrichs constant and dt come from the host values unless
 // a device source is given (used by the graph-resident time loop).

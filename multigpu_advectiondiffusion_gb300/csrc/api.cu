@@ -90,6 +90,11 @@ adv_status burgers_validate(const adv_burgers_desc* d) {
   return ADV_OK;
 }
 
+int burgers_tune_variant(const adv_burgers_desc& d) {
+  const int visc = (d.kx != 0.0 || d.ky != 0.0 || d.kz != 0.0) ? 1 : 0;
+  return d.dtype * 1000 + d.weno * 100 + d.div * 10 + visc;
+}
+
 adv_status burgers_prepare(const adv_burgers_desc& d, const void* u_in, BurgersLaunch* L) {
   DeviceInfo di;
   adv_status st = device_info(&di);
@@ -107,9 +112,17 @@ adv_status burgers_prepare(const adv_burgers_desc& d, const void* u_in, BurgersL
   int occ = 0;
   ADV_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, 256, L->smem));
   occ = std::max(occ, 1);
-  // One wave of CTAs, each with an equal share of the (tile, plane) pairs (at least 8 planes).
+  L->occ = occ;
+  // One wave of CTAs, each with an equal share of the (tile, plane) pairs (at least 8 planes, or
+  // what the autotuner picked).
   const int64_t total = (int64_t)tiles_x * tiles_y * d.nz;
-  const int64_t ctas = std::max<int64_t>(1, std::min<int64_t>((int64_t)di.sms * occ, total / 8));
+  int64_t min_share = 8;
+  const TuneParams tp = tune_lookup(TUNE_BURGERS, burgers_tune_variant(d), d.nx, d.ny, d.nz);
+  if (tp.set) {
+    occ = std::max(1, std::min(occ, tp.a));
+    min_share = std::max(1, tp.b);
+  }
+  const int64_t ctas = std::max<int64_t>(1, std::min<int64_t>((int64_t)di.sms * occ, total / min_share));
   L->tiles_x = tiles_x;
   L->tiles_y = tiles_y;
   L->grid = dim3((unsigned)ctas, 1, 1);
@@ -166,6 +179,13 @@ class GraphCache {
     }
     m_[key] = {e, ++tick_};
   }
+  void clear() {
+    std::lock_guard<std::mutex> lk(mu_);
+    if (m_.empty()) return;
+    cudaDeviceSynchronize();  // a cached graph may still be running
+    for (auto& kv : m_) cudaGraphExecDestroy(kv.second.first);
+    m_.clear();
+  }
 
  private:
   std::mutex mu_;
@@ -173,6 +193,7 @@ class GraphCache {
   uint64_t tick_ = 0;
 };
 static GraphCache g_graphs;
+void graph_cache_clear() { g_graphs.clear(); }
 
 template <class... A>
 static std::string graph_key(const char* tag, const A&... parts) {

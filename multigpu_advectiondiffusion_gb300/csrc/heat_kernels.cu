@@ -48,6 +48,8 @@ void tile_for(int dtype, int order, int ndim, int* bx, int* by, int* sw, int* sh
 
 }  // namespace
 
+int heat_tune_variant(const adv_heat_desc& d) { return d.dtype * 100 + d.order * 10 + d.ndim; }
+
 adv_status heat_prepare(const adv_heat_desc& d, const void* u_in, HeatLaunch* L) {
   DeviceInfo di;
   adv_status st = device_info(&di);
@@ -72,10 +74,16 @@ adv_status heat_prepare(const adv_heat_desc& d, const void* u_in, HeatLaunch* L)
   int occ = 0;
   ADV_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k0, 256, smem));
   occ = std::max(occ, 1);
+  L->occ = occ;
   // One wave: every CTA resident at once, each with an equal share of the (tile, plane) pairs,
-  // at least 8 planes each in 3D so the z halo stays small.
+  // at least 8 planes each in 3D so the z halo stays small (or what the autotuner picked).
   const int64_t total = (int64_t)tiles_x * tiles_y * nz;
-  const int64_t min_share = d.ndim == 3 ? 8 : 1;
+  int64_t min_share = d.ndim == 3 ? 8 : 1;
+  const TuneParams tp = tune_lookup(TUNE_HEAT, heat_tune_variant(d), d.nx, d.ny, nz);
+  if (tp.set) {
+    occ = std::max(1, std::min(occ, tp.a));
+    min_share = std::max(1, tp.b);
+  }
   const int64_t ctas = std::max<int64_t>(1, std::min<int64_t>((int64_t)di.sms * occ, total / min_share));
   L->tiles_x = tiles_x;
   L->tiles_y = tiles_y;

@@ -28,7 +28,7 @@ namespace adv {
 
 namespace {
 
-constexpr int KX = 32, KY = 8, KZC = 16;  // block and z chunk
+constexpr int KX = 32;  // block width; the height (4..16 threads) and the z planes per CTA are tunable
 
 __device__ __forceinline__ float fma_k(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 __device__ __forceinline__ double fma_k(double a, double b, double c) { return __fma_rn(a, b, c); }
@@ -41,14 +41,15 @@ struct HeatKArgs {
   T* out;        // forward: u^{n+1}; adjoint: lam^n
   T* grad;       // adjoint: dJ/dk accumulator
   int nx, ny, nz, zero_boundary;
+  int zc;  // z planes per CTA
   T cx, cy, cz;
 };
 
 template <class T>
-__global__ void __launch_bounds__(KX * KY) heatk_step_kernel(const __grid_constant__ HeatKArgs<T> a) {
-  const int x = blockIdx.x * KX + threadIdx.x, y = blockIdx.y * KY + threadIdx.y;
+__global__ void __launch_bounds__(512) heatk_step_kernel(const __grid_constant__ HeatKArgs<T> a) {
+  const int x = blockIdx.x * KX + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
   if (x >= a.nx || y >= a.ny) return;
-  const int z0 = blockIdx.z * KZC, z1 = min(a.nz, z0 + KZC);
+  const int z0 = blockIdx.z * a.zc, z1 = min(a.nz, z0 + a.zc);
   const size_t sx = 1, sy = (size_t)a.nx, sz = (size_t)a.nx * a.ny;
   const bool col_in = x > 0 && x < a.nx - 1 && y > 0 && y < a.ny - 1;
   const T h = T(0.5);
@@ -76,10 +77,10 @@ __global__ void __launch_bounds__(KX * KY) heatk_step_kernel(const __grid_consta
 }
 
 template <class T>
-__global__ void __launch_bounds__(KX * KY) heatk_adjoint_kernel(const __grid_constant__ HeatKArgs<T> a) {
-  const int x = blockIdx.x * KX + threadIdx.x, y = blockIdx.y * KY + threadIdx.y;
+__global__ void __launch_bounds__(512) heatk_adjoint_kernel(const __grid_constant__ HeatKArgs<T> a) {
+  const int x = blockIdx.x * KX + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
   if (x >= a.nx || y >= a.ny) return;
-  const int z0 = blockIdx.z * KZC, z1 = min(a.nz, z0 + KZC);
+  const int z0 = blockIdx.z * a.zc, z1 = min(a.nz, z0 + a.zc);
   const int nx = a.nx, ny = a.ny, nz = a.nz;
   const size_t sy = (size_t)nx, sz = (size_t)nx * ny;
   const T h = T(0.5);
@@ -148,15 +149,26 @@ HeatKArgs<T> make_args(const adv_heatk_desc& d, const void* k, const void* u, co
   return a;
 }
 
-dim3 heatk_grid(const adv_heatk_desc& d) {
-  return dim3((unsigned)((d.nx + KX - 1) / KX), (unsigned)((d.ny + KY - 1) / KY), (unsigned)((d.nz + KZC - 1) / KZC));
+// Block height and z planes per CTA: the autotuner's choice for this problem, else 8 and 16.
+void heatk_shape(const adv_heatk_desc& d, int kind, int* ky, int* zc) {
+  const TuneParams tp = tune_lookup(kind, d.dtype, d.nx, d.ny, d.nz);
+  *ky = tp.set ? tp.a : 8;
+  *zc = tp.set ? tp.b : 16;
 }
 
 adv_status heatk_step_launch(const adv_heatk_desc& d, const void* k, const void* u_in, void* u_out, cudaStream_t s) {
-  if (d.dtype == ADV_F32)
-    heatk_step_kernel<float><<<heatk_grid(d), dim3(KX, KY), 0, s>>>(make_args<float>(d, k, u_in, nullptr, u_out, nullptr));
-  else
-    heatk_step_kernel<double><<<heatk_grid(d), dim3(KX, KY), 0, s>>>(make_args<double>(d, k, u_in, nullptr, u_out, nullptr));
+  int ky, zc;
+  heatk_shape(d, TUNE_HEATK_STEP, &ky, &zc);
+  const dim3 grid((unsigned)((d.nx + KX - 1) / KX), (unsigned)((d.ny + ky - 1) / ky), (unsigned)((d.nz + zc - 1) / zc));
+  if (d.dtype == ADV_F32) {
+    HeatKArgs<float> a = make_args<float>(d, k, u_in, nullptr, u_out, nullptr);
+    a.zc = zc;
+    heatk_step_kernel<float><<<grid, dim3(KX, ky), 0, s>>>(a);
+  } else {
+    HeatKArgs<double> a = make_args<double>(d, k, u_in, nullptr, u_out, nullptr);
+    a.zc = zc;
+    heatk_step_kernel<double><<<grid, dim3(KX, ky), 0, s>>>(a);
+  }
   ADV_CUDA_TRY(cudaGetLastError());
   count_launches(1);
   return ADV_OK;
@@ -164,12 +176,18 @@ adv_status heatk_step_launch(const adv_heatk_desc& d, const void* k, const void*
 
 adv_status heatk_adjoint_launch(const adv_heatk_desc& d, const void* k, const void* u_n, const void* lam_next,
                                 void* lam_out, void* grad_k, cudaStream_t s) {
-  if (d.dtype == ADV_F32)
-    heatk_adjoint_kernel<float><<<heatk_grid(d), dim3(KX, KY), 0, s>>>(
-        make_args<float>(d, k, u_n, lam_next, lam_out, grad_k));
-  else
-    heatk_adjoint_kernel<double><<<heatk_grid(d), dim3(KX, KY), 0, s>>>(
-        make_args<double>(d, k, u_n, lam_next, lam_out, grad_k));
+  int ky, zc;
+  heatk_shape(d, TUNE_HEATK_ADJ, &ky, &zc);
+  const dim3 grid((unsigned)((d.nx + KX - 1) / KX), (unsigned)((d.ny + ky - 1) / ky), (unsigned)((d.nz + zc - 1) / zc));
+  if (d.dtype == ADV_F32) {
+    HeatKArgs<float> a = make_args<float>(d, k, u_n, lam_next, lam_out, grad_k);
+    a.zc = zc;
+    heatk_adjoint_kernel<float><<<grid, dim3(KX, ky), 0, s>>>(a);
+  } else {
+    HeatKArgs<double> a = make_args<double>(d, k, u_n, lam_next, lam_out, grad_k);
+    a.zc = zc;
+    heatk_adjoint_kernel<double><<<grid, dim3(KX, ky), 0, s>>>(a);
+  }
   ADV_CUDA_TRY(cudaGetLastError());
   count_launches(1);
   return ADV_OK;
@@ -181,6 +199,17 @@ size_t array_bytes(const adv_heatk_desc& d) {
 }
 
 }  // namespace
+
+// for the autotuner
+adv_status heatk_validate_desc(const adv_heatk_desc* d) { return heatk_validate(d); }
+adv_status heatk_step_run(const adv_heatk_desc& d, const void* k, const void* u_in, void* u_out, cudaStream_t s) {
+  return heatk_step_launch(d, k, u_in, u_out, s);
+}
+adv_status heatk_adjoint_run(const adv_heatk_desc& d, const void* k, const void* u_n, const void* lam_next,
+                             void* lam_out, void* grad_k, cudaStream_t s) {
+  return heatk_adjoint_launch(d, k, u_n, lam_next, lam_out, grad_k, s);
+}
+
 }  // namespace adv
 
 using namespace adv;

@@ -410,6 +410,41 @@ class Ensemble:
             pass
 
 
+def _tune_dict(r) -> dict:
+    return {"param_a": r.param_a, "param_b": r.param_b, "candidates": r.candidates, "best_us": r.best_us,
+            "default_us": r.default_us}
+
+
+def autotune_heat(cfg: HeatConfig, u, stream=None) -> dict:
+    """Picks the heat stage's launch shape for this problem (adv_autotune_heat)."""
+    r = N.TuneResult()
+    d = cfg.desc(_dtype_code(u))
+    N.check(N.load().adv_autotune_heat(C.byref(d), _ptr(u), N.stream_handle(stream), C.byref(r)), "adv_autotune_heat")
+    return _tune_dict(r)
+
+
+def autotune_burgers(cfg: BurgersConfig, u, stream=None) -> dict:
+    """Picks the Burgers stage's launch shape for this problem (adv_autotune_burgers)."""
+    r = N.TuneResult()
+    d = cfg.desc(_dtype_code(u))
+    N.check(N.load().adv_autotune_burgers(C.byref(d), _ptr(u), N.stream_handle(stream), C.byref(r)),
+            "adv_autotune_burgers")
+    return _tune_dict(r)
+
+
+def autotune_heatk(cfg: HeatKConfig, k, u, stream=None) -> tuple[dict, dict]:
+    """Picks the heat-with-k(x) step and adjoint launch shapes (adv_autotune_heatk)."""
+    r1, r2 = N.TuneResult(), N.TuneResult()
+    d = cfg.desc(_dtype_code(u))
+    N.check(N.load().adv_autotune_heatk(C.byref(d), _ptr(k), _ptr(u), N.stream_handle(stream), C.byref(r1),
+                                        C.byref(r2)), "adv_autotune_heatk")
+    return _tune_dict(r1), _tune_dict(r2)
+
+
+def autotune_clear() -> None:
+    N.check(N.load().adv_autotune_clear(), "adv_autotune_clear")
+
+
 def reference_heat_final_time(dt: float, iters: int, t0: float = 0.1) -> float:
     """tFinal = t0 + dt*iters as the reference prints it (main.cpp:63)."""
     return t0 + dt * iters
