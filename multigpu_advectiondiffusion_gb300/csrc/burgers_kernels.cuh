@@ -90,6 +90,12 @@ struct Face<float, Z, D> {
     return weno_face_fast<Z, D>(p0, p1, p2, p3, p4, m0, m1, m2, m3, m4);
   }
   __device__ __forceinline__ static void split(float u, float a, float& fp, float& fm) { lf_split_fast(u, a, fp, fm); }
+  // two faces / two splits at once with paired FP32 instructions (bit-identical to the above)
+  __device__ __forceinline__ static float2 f2(float2 p0, float2 p1, float2 p2, float2 p3, float2 p4, float2 m0,
+                                              float2 m1, float2 m2, float2 m3, float2 m4) {
+    return weno_face_fast2<Z, D>(p0, p1, p2, p3, p4, m0, m1, m2, m3, m4);
+  }
+  __device__ __forceinline__ static void split2(float2 u, float2 a, float2& fp, float2& fm) { lf_split_fast2(u, a, fp, fm); }
 };
 template <bool Z, class D>
 struct Face<double, Z, D> {
@@ -261,30 +267,48 @@ __device__ __forceinline__ BurgersPipe burgers_segment(const CUtensorMap* tmap, 
     parity ^= 1u << s_wait;
     s_wait = s_wait + 1 == TL::NS ? 0 : s_wait + 1;
     // ---- z windows: push plane q for this thread's two columns
+    {
+      const T uq[2] = {plq[(cy0 + TL::R) * TL::SW + TL::PADX + cx], plq[(cy1 + TL::R) * TL::SW + TL::PADX + cx]};
+      T fpq[2], fmq[2];
+      if constexpr (sizeof(T) == 4) {
+        const float2 u2 = make_float2(uq[0], uq[1]);
+        const float2 a2 = glob ? f2(alpha) : make_float2(absval(uq[0]), absval(uq[1]));
+        float2 fp2, fm2;
+        Face<T, Z, D>::split2(u2, a2, fp2, fm2);
+        fpq[0] = fp2.x; fpq[1] = fp2.y; fmq[0] = fm2.x; fmq[1] = fm2.y;
+      } else {
 #pragma unroll
-    for (int c = 0; c < 2; ++c) {
-      const int cy = c ? cy1 : cy0;
-      const T u = plq[(cy + TL::R) * TL::SW + TL::PADX + cx];
-      T fp, fm;
-      Face<T, Z, D>::split(u, glob ? alpha : absval(u), fp, fm);
+        for (int c = 0; c < 2; ++c) Face<T, Z, D>::split(uq[c], glob ? alpha : absval(uq[c]), fpq[c], fmq[c]);
+      }
 #pragma unroll
-      for (int s = 0; s < 4; ++s) { fpw[c][s] = fpw[c][s + 1]; fmw[c][s] = fmw[c][s + 1]; }
-      fpw[c][4] = fpn[c];
-      fpn[c] = fp;
-      fmw[c][4] = fm;
-      if (VISC) {
+      for (int c = 0; c < 2; ++c) {
 #pragma unroll
-        for (int s = 0; s < 6; ++s) uw[c][s] = uw[c][s + 1];
-        uw[c][VISC ? 6 : 0] = u;
+        for (int s = 0; s < 4; ++s) { fpw[c][s] = fpw[c][s + 1]; fmw[c][s] = fmw[c][s + 1]; }
+        fpw[c][4] = fpn[c];
+        fpn[c] = fpq[c];
+        fmw[c][4] = fmq[c];
+        if (VISC) {
+#pragma unroll
+          for (int s = 0; s < 6; ++s) uw[c][s] = uw[c][s + 1];
+          uw[c][VISC ? 6 : 0] = uq[c];
+        }
       }
     }
     // z-face at (newest plane - 3) + 1/2 once the windows hold planes newest-5 .. newest.
     T fz_new[2] = {T(0), T(0)};
     if (q >= 5) {
+      if constexpr (sizeof(T) == 4) {
+        auto pk = [&](const T (&w)[2][5], int s) { return make_float2(w[0][s], w[1][s]); };
+        const float2 fz = Face<T, Z, D>::f2(pk(fpw, 0), pk(fpw, 1), pk(fpw, 2), pk(fpw, 3), pk(fpw, 4), pk(fmw, 0),
+                                            pk(fmw, 1), pk(fmw, 2), pk(fmw, 3), pk(fmw, 4));
+        fz_new[0] = fz.x;
+        fz_new[1] = fz.y;
+      } else {
 #pragma unroll
-      for (int c = 0; c < 2; ++c)
-        fz_new[c] = Face<T, Z, D>::f(fpw[c][0], fpw[c][1], fpw[c][2], fpw[c][3], fpw[c][4], fmw[c][0], fmw[c][1],
-                                    fmw[c][2], fmw[c][3], fmw[c][4]);
+        for (int c = 0; c < 2; ++c)
+          fz_new[c] = Face<T, Z, D>::f(fpw[c][0], fpw[c][1], fpw[c][2], fpw[c][3], fpw[c][4], fmw[c][0], fmw[c][1],
+                                      fmw[c][2], fmw[c][3], fmw[c][4]);
+      }
     }
     if (q >= 6) {
       const int k = zs + q - 6;  // output plane; its staged copy is stream entry q - 3
@@ -293,23 +317,66 @@ __device__ __forceinline__ BurgersPipe burgers_segment(const CUtensorMap* tmap, 
       const bool any_upd = kin && !aborted;
       if (any_upd) {
         // f+- of the output plane into shared memory
-        for (int e = tid; e < TL::PLANE; e += TL::NT) {
-          const T u = plc[e];
-          T fp, fm;
-          Face<T, Z, D>::split(u, glob ? alpha : absval(u), fp, fm);
-          fpS[e] = fp;
-          fmS[e] = fm;
+        if constexpr (sizeof(T) == 4) {
+          // elements tid + 256 j, j = 0..3 (880 = 3 * 256 + 112), in pairs (0, 1) and (2, 3)
+          static_assert(TL::PLANE > 3 * TL::NT && TL::PLANE <= 4 * TL::NT, "split pairing assumes 3..4 rounds");
+#pragma unroll
+          for (int j = 0; j < 4; j += 2) {
+            const int e0 = tid + TL::NT * j, e1 = e0 + TL::NT;
+            if (e0 >= TL::PLANE) break;
+            const bool two = e1 < TL::PLANE;
+            const float2 u2 = make_float2(plc[e0], two ? plc[e1] : plc[e0]);
+            const float2 a2 = glob ? f2(alpha) : make_float2(absval(u2.x), absval(u2.y));
+            float2 fp2, fm2;
+            Face<T, Z, D>::split2(u2, a2, fp2, fm2);
+            fpS[e0] = fp2.x;
+            fmS[e0] = fm2.x;
+            if (two) {
+              fpS[e1] = fp2.y;
+              fmS[e1] = fm2.y;
+            }
+          }
+        } else {
+          for (int e = tid; e < TL::PLANE; e += TL::NT) {
+            const T u = plc[e];
+            T fp, fm;
+            Face<T, Z, D>::split(u, glob ? alpha : absval(u), fp, fm);
+            fpS[e] = fp;
+            fmS[e] = fm;
+          }
         }
         __syncthreads();
         // x- and y-faces of the plane, this thread's precomputed share
+        if constexpr (sizeof(T) == 4) {
+          // slots 0..3 are live for every thread (1072 faces >= 4 * 256): pairs (0, 1), (2, 3)
+          static_assert(TL::NXF + TL::NYF >= 4 * TL::NT && TL::NXF + TL::NYF <= 5 * TL::NT, "face slots");
 #pragma unroll
-        for (int r = 0; r < 5; ++r) {
-          if (!fact[r]) continue;
-          const int b = fbase[r];
-          const int st = fisx[r] ? 1 : TL::SW;
-          fxS[tid + TL::NT * r] = Face<T, Z, D>::f(fpS[b], fpS[b + st], fpS[b + 2 * st], fpS[b + 3 * st], fpS[b + 4 * st],
-                                                   fmS[b + st], fmS[b + 2 * st], fmS[b + 3 * st], fmS[b + 4 * st],
-                                                   fmS[b + 5 * st]);
+          for (int r = 0; r < 4; r += 2) {
+            const int b0 = fbase[r], b1 = fbase[r + 1];
+            const int s0 = fisx[r] ? 1 : TL::SW, s1 = fisx[r + 1] ? 1 : TL::SW;
+            auto P = [&](int k) { return make_float2(fpS[b0 + k * s0], fpS[b1 + k * s1]); };
+            auto M = [&](int k) { return make_float2(fmS[b0 + k * s0], fmS[b1 + k * s1]); };
+            const float2 f = Face<T, Z, D>::f2(P(0), P(1), P(2), P(3), P(4), M(1), M(2), M(3), M(4), M(5));
+            fxS[tid + TL::NT * r] = f.x;
+            fxS[tid + TL::NT * (r + 1)] = f.y;
+          }
+          if (fact[4]) {
+            const int b = fbase[4];
+            const int st = fisx[4] ? 1 : TL::SW;
+            fxS[tid + TL::NT * 4] = Face<T, Z, D>::f(fpS[b], fpS[b + st], fpS[b + 2 * st], fpS[b + 3 * st],
+                                                     fpS[b + 4 * st], fmS[b + st], fmS[b + 2 * st], fmS[b + 3 * st],
+                                                     fmS[b + 4 * st], fmS[b + 5 * st]);
+          }
+        } else {
+#pragma unroll
+          for (int r = 0; r < 5; ++r) {
+            if (!fact[r]) continue;
+            const int b = fbase[r];
+            const int st = fisx[r] ? 1 : TL::SW;
+            fxS[tid + TL::NT * r] = Face<T, Z, D>::f(fpS[b], fpS[b + st], fpS[b + 2 * st], fpS[b + 3 * st],
+                                                     fpS[b + 4 * st], fmS[b + st], fmS[b + 2 * st], fmS[b + 3 * st],
+                                                     fmS[b + 4 * st], fmS[b + 5 * st]);
+          }
         }
         __syncthreads();
       }
