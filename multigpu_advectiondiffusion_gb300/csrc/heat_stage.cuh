@@ -37,6 +37,7 @@ template <> struct Vec16<double> { using type = double2; };
 
 __device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 __device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float2 fma_rn(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 
 template <class T, int ORDER, int NDIM>
 struct HeatTile {
@@ -79,29 +80,29 @@ struct HeatParams {
 template <class T, int ORDER, int NDIM, bool FAST>
 __device__ __forceinline__ T lap(T xm2, T xm1, T c, T xp1, T xp2, T ym2, T ym1, T yp1, T yp2, T zm2, T zm1, T zp1,
                                  T zp2, T kx, T ky, T kz) {
-  T Sx, Sy, Sz = T(0);
+  T Sx, Sy, Sz = bc<T>(0);
   if (ORDER == 2) {
     if (FAST) {
-      Sx = add_rn(fma_rn(T(-2), c, xp1), xm1);
-      Sy = add_rn(fma_rn(T(-2), c, yp1), ym1);
-      if (NDIM == 3) Sz = add_rn(fma_rn(T(-2), c, zp1), zm1);
+      Sx = add_rn(fma_rn(bc<T>(-2), c, xp1), xm1);
+      Sy = add_rn(fma_rn(bc<T>(-2), c, yp1), ym1);
+      if (NDIM == 3) Sz = add_rn(fma_rn(bc<T>(-2), c, zp1), zm1);
     } else {
-      Sx = add_rn(sub_rn(xp1, mul_rn(T(2), c)), xm1);
-      Sy = add_rn(sub_rn(yp1, mul_rn(T(2), c)), ym1);
-      if (NDIM == 3) Sz = add_rn(sub_rn(zp1, mul_rn(T(2), c)), zm1);
+      Sx = add_rn(sub_rn(xp1, mul_rn(bc<T>(2), c)), xm1);
+      Sy = add_rn(sub_rn(yp1, mul_rn(bc<T>(2), c)), ym1);
+      if (NDIM == 3) Sz = add_rn(sub_rn(zp1, mul_rn(bc<T>(2), c)), zm1);
     }
   } else {
     // near side first: +1 in 3D, -1 in 2D
     const T ax2 = NDIM == 3 ? xp2 : xm2, ax1 = NDIM == 3 ? xp1 : xm1, bx1 = NDIM == 3 ? xm1 : xp1, bx2 = NDIM == 3 ? xm2 : xp2;
     const T ay2 = NDIM == 3 ? yp2 : ym2, ay1 = NDIM == 3 ? yp1 : ym1, by1 = NDIM == 3 ? ym1 : yp1, by2 = NDIM == 3 ? ym2 : yp2;
     if (FAST) {
-      Sx = sub_rn(fma_rn(T(16), bx1, fma_rn(T(-30), c, fma_rn(T(16), ax1, -ax2))), bx2);
-      Sy = sub_rn(fma_rn(T(16), by1, fma_rn(T(-30), c, fma_rn(T(16), ay1, -ay2))), by2);
-      if (NDIM == 3) Sz = sub_rn(fma_rn(T(16), zm1, fma_rn(T(-30), c, fma_rn(T(16), zp1, -zp2))), zm2);
+      Sx = sub_rn(fma_rn(bc<T>(16), bx1, fma_rn(bc<T>(-30), c, fma_rn(bc<T>(16), ax1, -ax2))), bx2);
+      Sy = sub_rn(fma_rn(bc<T>(16), by1, fma_rn(bc<T>(-30), c, fma_rn(bc<T>(16), ay1, -ay2))), by2);
+      if (NDIM == 3) Sz = sub_rn(fma_rn(bc<T>(16), zm1, fma_rn(bc<T>(-30), c, fma_rn(bc<T>(16), zp1, -zp2))), zm2);
     } else {
-      Sx = sub_rn(add_rn(sub_rn(add_rn(-ax2, mul_rn(T(16), ax1)), mul_rn(T(30), c)), mul_rn(T(16), bx1)), bx2);
-      Sy = sub_rn(add_rn(sub_rn(add_rn(-ay2, mul_rn(T(16), ay1)), mul_rn(T(30), c)), mul_rn(T(16), by1)), by2);
-      if (NDIM == 3) Sz = sub_rn(add_rn(sub_rn(add_rn(-zp2, mul_rn(T(16), zp1)), mul_rn(T(30), c)), mul_rn(T(16), zm1)), zm2);
+      Sx = sub_rn(add_rn(sub_rn(add_rn(-ax2, mul_rn(bc<T>(16), ax1)), mul_rn(bc<T>(30), c)), mul_rn(bc<T>(16), bx1)), bx2);
+      Sy = sub_rn(add_rn(sub_rn(add_rn(-ay2, mul_rn(bc<T>(16), ay1)), mul_rn(bc<T>(30), c)), mul_rn(bc<T>(16), by1)), by2);
+      if (NDIM == 3) Sz = sub_rn(add_rn(sub_rn(add_rn(-zp2, mul_rn(bc<T>(16), zp1)), mul_rn(bc<T>(30), c)), mul_rn(bc<T>(16), zm1)), zm2);
     }
   }
   if (FAST) {
@@ -118,9 +119,9 @@ __device__ __forceinline__ T lap(T xm2, T xm1, T c, T xp1, T xp2, T ym2, T ym1, 
 // 1: fma(dt, L, un); 2: fma(0.25, fma(dt, L, uin), 0.75 * un); 3: (fma(2, fma(dt, L, uin), un)) / 3.
 template <class T, bool FAST>
 __device__ __forceinline__ T combine(int stage, T un, T uin, T dt, T L) {
-  if (!FAST) return stage_combine<T>(stage, un, uin, dt, L);
-  if (stage == 2) return fma_rn(T(0.25), fma_rn(dt, L, uin), mul_rn(T(0.75), un));
-  if (stage == 3) return div_rn(fma_rn(T(2), fma_rn(dt, L, uin), un), T(3));
+  if constexpr (!FAST) return stage_combine<T>(stage, un, uin, dt, L);
+  if (stage == 2) return fma_rn(bc<T>(0.25), fma_rn(dt, L, uin), mul_rn(bc<T>(0.75), un));
+  if (stage == 3) return div_rn(fma_rn(bc<T>(2), fma_rn(dt, L, uin), un), bc<T>(3));
   return fma_rn(dt, L, un);
 }
 
@@ -289,6 +290,38 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
       // Every lane evaluates the stencil (halo values outside the grid are finite zero fill);
       // nodes that are not updated are fixed up afterwards with warp-uniform branches.
       T res[2][VX];
+      if constexpr (FAST && ORDER == 2) {
+        // FP32 O2: node pairs (e, e+1) in paired instructions, the same operations lane by lane
+        // (the O4 stencil stays scalar: paired it needs more registers than its occupancy allows)
+        static_assert(VX % 2 == 0, "node pairs");
+        constexpr int O1 = R >= 2 ? 2 : 1;
+        const float2 kx2 = make_float2(kx, kx), ky2 = make_float2(ky, ky), kz2 = make_float2(kz, kz);
+        const float2 dt2 = make_float2(dt, dt);
+#pragma unroll
+        for (int r = 0; r < 2; ++r)
+#pragma unroll
+          for (int e = 0; e < VX; e += 2) {
+            auto X = [&](int j) { return make_float2(xr[r][j], xr[r][j + 1]); };
+            auto Y = [&](int j) { return make_float2(yv[j][e], yv[j][e + 1]); };
+            auto W = [&](int j) { return make_float2(w[j][r][e], w[j][r][e + 1]); };
+            const float2 c = W(RZ);
+            const float2 L = lap<float2, ORDER, NDIM, true>(
+                X(R + e - O1), X(R + e - 1), c, X(R + e + 1), X(R + e + O1), Y(R + r - O1), Y(R + r - 1),
+                Y(R + r + 1), Y(R + r + O1), W(RZ >= 2 ? RZ - 2 : 0), W(RZ >= 1 ? RZ - 1 : 0),
+                W(RZ + (RZ >= 1 ? 1 : 0)), W(RZ + (RZ >= 2 ? 2 : 0)), kx2, ky2, kz2);
+            float2 un = c;
+            if (STAGE != 1) {
+              const size_t off = (size_t)(q - 2 * RZ) * sxy + (size_t)r * nx + e;
+              const T* src = p.un + (obase - p.out) + off;
+              const bool i0 = warp_inside || ((inside >> (r * VX + e)) & 1u);
+              const bool i1 = warp_inside || ((inside >> (r * VX + e + 1)) & 1u);
+              un = make_float2(i0 ? src[0] : T(0), i1 ? src[1] : T(0));
+            }
+            const float2 v = combine<float2, true>(stage, un, c, dt2, L);
+            res[r][e] = v.x;
+            res[r][e + 1] = v.y;
+          }
+      } else {
 #pragma unroll
       for (int r = 0; r < 2; ++r)
 #pragma unroll
@@ -306,6 +339,7 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
           }
           res[r][e] = combine<T, FAST>(stage, un, c, dt, L);
         }
+      }
       if (!zin) {  // frozen plane: copy, or zero on the outermost planes
         const bool zero_all = p.zero_boundary && NDIM == 3 && (z == 0 || z == nz - 1);
 #pragma unroll
