@@ -36,6 +36,24 @@ sys.path.insert(0, str(ROOT))
 L2_BYTES = 126 * 1024 * 1024
 
 
+def max_over_ranks(x: float, device=None) -> float:
+    """The largest of every rank's x (the job's time is its slowest replica's); x itself when the
+    job has one rank or no process group."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(units_per_rank: float, ms_max: float, world: int) -> float:
+    """Whole-job throughput in G units/s: every rank processes units_per_rank in its replica, and
+    the job takes as long as its slowest rank (ms_max)."""
+    return world * units_per_rank / (ms_max * 1e-3) / 1e9
+
+
 def _peaks() -> tuple[float, str]:
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -232,12 +250,8 @@ def bench_ensemble(args, world, rank, dev, stream, flush, lib):
         launches0 = lib.adv_kernel_launch_count()
         ms = timed(one_step, args.steps)
         launched = lib.adv_kernel_launch_count() - launches0
-    ms_max = ms
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_max = t.item()
-    value = world * work * args.steps / (ms_max * 1e-3) / 1e9
+    ms_max = max_over_ranks(ms, dev)
+    value = replica_throughput(work * args.steps, ms_max, world)
 
     # Burgers loop alone (heat_steps = 0): the batched WENO stage dominates; its average launch
     # time is this loop's time over its 3 S stage launches (the per-step dt kernel included).
@@ -276,11 +290,7 @@ def bench_ensemble(args, world, rank, dev, stream, flush, lib):
             for h, d in zip(host_out, dev_all):
                 h.copy_(d, non_blocking=True)
     e2e_step()
-    ems = timed(e2e_step, args.steps)
-    if world > 1:
-        t = torch.tensor([ems], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ems = t.item()
+    ems = max_over_ranks(timed(e2e_step, args.steps), dev)
     nbytes = sum(a.numel() * a.element_size() for a in host_in)
     shape = ens.shape()
     ens.close()
@@ -300,7 +310,7 @@ def bench_ensemble(args, world, rank, dev, stream, flush, lib):
                          "traffic": _traffic("ensemble"), "algorithmic_bytes_per_launch": bytes_per_launch,
                          "avg_launch_us": launch_ms * 1e3},
             "cpu_baseline": None,
-            "e2e": {"value": world * work * args.steps / (ems * 1e-3) / 1e9, "unit": "Gcell-updates/s",
+            "e2e": {"value": replica_throughput(work * args.steps, ems, world), "unit": "Gcell-updates/s",
                     "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
             "gpu_launches": int(launched),
             "clocks": clk.summary(),
@@ -424,11 +434,12 @@ def bench_adjoint(args, world, rank, dev, lib):
         grad_heat()
     hts = [grad_heat() for _ in range(3)]
     tfh, tbh = float(np.median([h[0] for h in hts])), float(np.median([h[1] for h in hts]))
+    t_grad = max_over_ranks(tf + tb, dev)
     if rank == 0:
         line = {
-            "metric": "Gcell-updates/s/RK-stage", "value": world * cells / ((tf + tb) * 1e-3) / 1e9,
+            "metric": "Gcell-updates/s/RK-stage", "value": replica_throughput(cells, t_grad, world),
             "unit": "Gcell-updates/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": tf + tb, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "ms_per_step": t_grad, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded Fourier states and log-normal diffusivity)",
             "config": {"workload": f"adjoint burgers3d {ADJ_N}^3 f32 weno5-z local-lf periodic, {ADJ_STEPS} steps to "
                                    f"t={ADJ_T} (cfl {dt * float(u0.abs().max()) / bc.dx:.3f}), checkpoints every "
@@ -708,12 +719,8 @@ def main():
         launched = lib.adv_kernel_launch_count() - launches0
     # time of the L2 flushes alone, subtracted from the per-launch figure only
     fl = timed(lambda: None, args.steps)
-    ms_max = ms
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_max = t.item()
-    value = world * cells_stages_per_step * args.steps / (ms_max * 1e-3) / 1e9
+    ms_max = max_over_ranks(ms, dev)
+    value = replica_throughput(cells_stages_per_step * args.steps, ms_max, world)
     launch_ms = (ms - fl) / max(1, args.steps * launches_per_step)
     achieved = bytes_per_launch / (launch_ms * 1e-3) / 1e9
     peak, peak_kind = _peaks()
@@ -730,12 +737,8 @@ def main():
             host_out.copy_(u, non_blocking=True)
     for _ in range(2):
         e2e_step()
-    ems = timed(e2e_step, args.steps)
-    if world > 1:
-        t = torch.tensor([ems], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ems = t.item()
-    e2e_value = world * cells_stages_per_step * args.steps / (ems * 1e-3) / 1e9
+    ems = max_over_ranks(timed(e2e_step, args.steps), dev)
+    e2e_value = replica_throughput(cells_stages_per_step * args.steps, ems, world)
     nbytes = u.numel() * u.element_size()
 
     # ---- accuracy of the FP32 result against FP64 (same device kernels, bit-exact with the oracle)
