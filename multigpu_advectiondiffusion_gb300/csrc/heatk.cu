@@ -20,6 +20,7 @@
 // operation is an explicit correctly rounded add/mul/fma, mirrored by the oracle.
 #include <algorithm>
 #include <cstring>
+#include <initializer_list>
 
 #include "adv_internal.h"
 #include "adv_math.cuh"
@@ -125,6 +126,180 @@ __global__ void __launch_bounds__(512) heatk_adjoint_kernel(const __grid_constan
   }
 }
 
+// ------------------------------------------------------------ vector kernels (16-byte rows)
+// The same per-node arithmetic as the kernels above (so the same bits), with each thread owning
+// VX = 16 / sizeof(T) consecutive nodes of a row: one 16-byte load per field and row instead of
+// one per node, the nodes' x neighbours from the thread's own vector plus one scalar per side.
+// Used when nx is a multiple of VX and every array is 16-byte aligned.
+template <class T> struct V16;
+template <> struct V16<float> { using type = float4; static constexpr int N = 4; };
+template <> struct V16<double> { using type = double2; static constexpr int N = 2; };
+constexpr int KXV = 16;  // threads per block row
+
+template <class T>
+__device__ __forceinline__ void ldv(const T* p, T (&v)[V16<T>::N]) {
+  const typename V16<T>::type w = *reinterpret_cast<const typename V16<T>::type*>(p);
+#pragma unroll
+  for (int e = 0; e < V16<T>::N; ++e) v[e] = reinterpret_cast<const T*>(&w)[e];
+}
+template <class T>
+__device__ __forceinline__ void stv(T* p, const T (&v)[V16<T>::N]) {
+  typename V16<T>::type w;
+#pragma unroll
+  for (int e = 0; e < V16<T>::N; ++e) reinterpret_cast<T*>(&w)[e] = v[e];
+  *reinterpret_cast<typename V16<T>::type*>(p) = w;
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) heatk_step_vec_kernel(const __grid_constant__ HeatKArgs<T> a) {
+  constexpr int VX = V16<T>::N;
+  const int xb = (blockIdx.x * KXV + threadIdx.x) * VX, y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (xb >= a.nx || y >= a.ny) return;
+  const int z0 = blockIdx.z * a.zc, z1 = min(a.nz, z0 + a.zc);
+  const int nx = a.nx, ny = a.ny, nz = a.nz;
+  const size_t sy = (size_t)nx, sz = (size_t)nx * ny;
+  const T h = T(0.5);
+  const bool yin = y > 0 && y < ny - 1;
+  const bool hl = xb > 0, hr = xb + VX < nx;
+  size_t o = (size_t)xb + sy * y + sz * z0;
+  T uc[VX], kc[VX], um[VX], km[VX];
+  ldv(a.u + o, uc);
+  ldv(a.k + o, kc);
+  if (z0 > 0) { ldv(a.u + o - sz, um); ldv(a.k + o - sz, km); }
+  else {
+#pragma unroll
+    for (int e = 0; e < VX; ++e) { um[e] = uc[e]; km[e] = kc[e]; }
+  }
+  for (int z = z0; z < z1; ++z, o += sz) {
+    T up[VX], kp[VX];
+    if (z + 1 < nz) { ldv(a.u + o + sz, up); ldv(a.k + o + sz, kp); }
+    else {
+#pragma unroll
+      for (int e = 0; e < VX; ++e) { up[e] = uc[e]; kp[e] = kc[e]; }
+    }
+    T res[VX];
+    const bool zin = z > 0 && z < nz - 1;
+    if (yin && zin) {
+      T uyp[VX], uym[VX], kyp[VX], kym[VX];
+      ldv(a.u + o + sy, uyp); ldv(a.u + o - sy, uym); ldv(a.k + o + sy, kyp); ldv(a.k + o - sy, kym);
+      const T ul = hl ? a.u[o - 1] : T(0), kl = hl ? a.k[o - 1] : T(0);
+      const T ur = hr ? a.u[o + VX] : T(0), kr = hr ? a.k[o + VX] : T(0);
+#pragma unroll
+      for (int e = 0; e < VX; ++e) {
+        const int x = xb + e;
+        if (x > 0 && x < nx - 1) {
+          const T c = uc[e], kce = kc[e];
+          auto flux = [&](T u_p, T u_m, T k_p, T k_m) {
+            const T fp = mul_rn(h, add_rn(kce, k_p)), fm = mul_rn(h, add_rn(kce, k_m));
+            return fma_k(fp, sub_rn(u_p, c), -mul_rn(fm, sub_rn(c, u_m)));
+          };
+          const T uxp = e + 1 < VX ? uc[e + 1 < VX ? e + 1 : 0] : ur, kxp = e + 1 < VX ? kc[e + 1 < VX ? e + 1 : 0] : kr;
+          const T uxm = e > 0 ? uc[e > 0 ? e - 1 : 0] : ul, kxm = e > 0 ? kc[e > 0 ? e - 1 : 0] : kl;
+          const T Fx = flux(uxp, uxm, kxp, kxm);
+          const T Fy = flux(uyp[e], uym[e], kyp[e], kym[e]);
+          const T Fz = flux(up[e], um[e], kp[e], km[e]);
+          res[e] = add_rn(c, fma_k(a.cz, Fz, fma_k(a.cy, Fy, mul_rn(a.cx, Fx))));
+        } else {
+          res[e] = a.zero_boundary ? T(0) : uc[e];
+        }
+      }
+    } else {
+#pragma unroll
+      for (int e = 0; e < VX; ++e) res[e] = a.zero_boundary ? T(0) : uc[e];
+    }
+    stv(a.out + o, res);
+#pragma unroll
+    for (int e = 0; e < VX; ++e) { um[e] = uc[e]; uc[e] = up[e]; km[e] = kc[e]; kc[e] = kp[e]; }
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) heatk_adjoint_vec_kernel(const __grid_constant__ HeatKArgs<T> a) {
+  constexpr int VX = V16<T>::N;
+  const int xb = (blockIdx.x * KXV + threadIdx.x) * VX, y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (xb >= a.nx || y >= a.ny) return;
+  const int z0 = blockIdx.z * a.zc, z1 = min(a.nz, z0 + a.zc);
+  const int nx = a.nx, ny = a.ny, nz = a.nz;
+  const size_t sy = (size_t)nx, sz = (size_t)nx * ny;
+  const T h = T(0.5);
+  auto in1 = [](int i, int n) { return i > 0 && i < n - 1; };
+  const bool yin = in1(y, ny), hyp = y + 1 < ny, hym = y > 0;
+  const bool hl = xb > 0, hr = xb + VX < nx;
+  auto axis = [&](bool hp, bool hm, bool inp, bool inm, T lp, T lm, T up, T um, T kp, T km, T muc, T uc, T kc, T& S,
+                  T& G) {
+    const T mup = hp && inp ? lp : T(0), mum = hm && inm ? lm : T(0);
+    const T kfp = mul_rn(h, add_rn(kc, kp)), kfm = mul_rn(h, add_rn(kc, km));
+    const T dmp = hp ? sub_rn(mup, muc) : T(0), dmm = hm ? sub_rn(mum, muc) : T(0);
+    const T dup = sub_rn(up, uc), dum = sub_rn(um, uc);
+    S = fma_k(kfm, dmm, mul_rn(kfp, dmp));
+    G = fma_k(dum, -dmm, mul_rn(dup, -dmp));
+  };
+  size_t o = (size_t)xb + sy * y + sz * z0;
+  T lc[VX], uc[VX], kc[VX], lm[VX], um[VX], km[VX];
+  ldv(a.lam + o, lc); ldv(a.u + o, uc); ldv(a.k + o, kc);
+  if (z0 > 0) { ldv(a.lam + o - sz, lm); ldv(a.u + o - sz, um); ldv(a.k + o - sz, km); }
+  else {
+#pragma unroll
+    for (int e = 0; e < VX; ++e) { lm[e] = lc[e]; um[e] = uc[e]; km[e] = kc[e]; }
+  }
+  for (int z = z0; z < z1; ++z, o += sz) {
+    const bool hzp = z + 1 < nz, hzm = z > 0;
+    T lp[VX], up[VX], kp[VX];
+    if (hzp) { ldv(a.lam + o + sz, lp); ldv(a.u + o + sz, up); ldv(a.k + o + sz, kp); }
+    else {
+#pragma unroll
+      for (int e = 0; e < VX; ++e) { lp[e] = lc[e]; up[e] = uc[e]; kp[e] = kc[e]; }
+    }
+    // y neighbours (an absent one passes the centre's values, as in the scalar kernel)
+    T lyp[VX], uyp[VX], kyp[VX], lym[VX], uym[VX], kym[VX];
+    if (hyp) { ldv(a.lam + o + sy, lyp); ldv(a.u + o + sy, uyp); ldv(a.k + o + sy, kyp); }
+    else {
+#pragma unroll
+      for (int e = 0; e < VX; ++e) { lyp[e] = lc[e]; uyp[e] = uc[e]; kyp[e] = kc[e]; }
+    }
+    if (hym) { ldv(a.lam + o - sy, lym); ldv(a.u + o - sy, uym); ldv(a.k + o - sy, kym); }
+    else {
+#pragma unroll
+      for (int e = 0; e < VX; ++e) { lym[e] = lc[e]; uym[e] = uc[e]; kym[e] = kc[e]; }
+    }
+    const T ll = hl ? a.lam[o - 1] : T(0), ul = hl ? a.u[o - 1] : T(0), kl = hl ? a.k[o - 1] : T(0);
+    const T lr = hr ? a.lam[o + VX] : T(0), ur = hr ? a.u[o + VX] : T(0), kr = hr ? a.k[o + VX] : T(0);
+    T g[VX], out[VX];
+    ldv(a.grad + o, g);
+    const bool zin = in1(z, nz), zinp = in1(z + 1, nz), zinm = in1(z - 1, nz);
+#pragma unroll
+    for (int e = 0; e < VX; ++e) {
+      const int x = xb + e;
+      const bool xin = in1(x, nx), hxp = x + 1 < nx, hxm = x > 0;
+      const bool ccol = xin && yin;
+      const bool in_c = ccol && zin;
+      const T muc = in_c ? lc[e] : T(0);
+      // x neighbours of node e: inside the vector, or the scalars past its ends
+      const T lxp = hxp ? (e + 1 < VX ? lc[e + 1 < VX ? e + 1 : 0] : lr) : lc[e];
+      const T uxp = hxp ? (e + 1 < VX ? uc[e + 1 < VX ? e + 1 : 0] : ur) : uc[e];
+      const T kxp = hxp ? (e + 1 < VX ? kc[e + 1 < VX ? e + 1 : 0] : kr) : kc[e];
+      const T lxm = hxm ? (e > 0 ? lc[e > 0 ? e - 1 : 0] : ll) : lc[e];
+      const T uxm = hxm ? (e > 0 ? uc[e > 0 ? e - 1 : 0] : ul) : uc[e];
+      const T kxm = hxm ? (e > 0 ? kc[e > 0 ? e - 1 : 0] : kl) : kc[e];
+      T Sx, Gx, Sy, Gy, Sz, Gz;
+      axis(hxp, hxm, in1(x + 1, nx) && yin && zin, in1(x - 1, nx) && yin && zin, lxp, lxm, uxp, uxm, kxp, kxm, muc,
+           uc[e], kc[e], Sx, Gx);
+      axis(hyp, hym, xin && in1(y + 1, ny) && zin, xin && in1(y - 1, ny) && zin, lyp[e], lym[e], uyp[e], uym[e],
+           kyp[e], kym[e], muc, uc[e], kc[e], Sy, Gy);
+      axis(hzp, hzm, ccol && zinp, ccol && zinm, lp[e], lm[e], up[e], um[e], kp[e], km[e], muc, uc[e], kc[e], Sz, Gz);
+      const T keep = (in_c || !a.zero_boundary) ? lc[e] : T(0);
+      out[e] = add_rn(keep, fma_k(a.cz, Sz, fma_k(a.cy, Sy, mul_rn(a.cx, Sx))));
+      g[e] = fma_k(h, fma_k(a.cz, Gz, fma_k(a.cy, Gy, mul_rn(a.cx, Gx))), g[e]);
+    }
+    stv(a.out + o, out);
+    stv(a.grad + o, g);
+#pragma unroll
+    for (int e = 0; e < VX; ++e) {
+      lm[e] = lc[e]; lc[e] = lp[e]; um[e] = uc[e]; uc[e] = up[e]; km[e] = kc[e]; kc[e] = kp[e];
+    }
+  }
+}
+
 adv_status heatk_validate(const adv_heatk_desc* d) {
   if (!d) return set_error(ADV_ERR_INVALID_ARG, "heatk: null descriptor");
   if (d->dtype != ADV_F32 && d->dtype != ADV_F64) return set_error(ADV_ERR_INVALID_ARG, "heatk: bad dtype");
@@ -149,6 +324,15 @@ HeatKArgs<T> make_args(const adv_heatk_desc& d, const void* k, const void* u, co
   return a;
 }
 
+// The vector kernels need whole 16-byte vectors per row and 16-byte aligned arrays.
+bool vec_ok(const adv_heatk_desc& d, std::initializer_list<const void*> ptrs) {
+  const int vx = d.dtype == ADV_F32 ? 4 : 2;
+  if (d.nx % vx != 0) return false;
+  for (const void* p : ptrs)
+    if ((uintptr_t)p % 16 != 0) return false;
+  return true;
+}
+
 // Block height and z planes per CTA: the autotuner's choice for this problem, else 8 and 16.
 void heatk_shape(const adv_heatk_desc& d, int kind, int* ky, int* zc) {
   const TuneParams tp = tune_lookup(kind, d.dtype, d.nx, d.ny, d.nz);
@@ -159,15 +343,20 @@ void heatk_shape(const adv_heatk_desc& d, int kind, int* ky, int* zc) {
 adv_status heatk_step_launch(const adv_heatk_desc& d, const void* k, const void* u_in, void* u_out, cudaStream_t s) {
   int ky, zc;
   heatk_shape(d, TUNE_HEATK_STEP, &ky, &zc);
-  const dim3 grid((unsigned)((d.nx + KX - 1) / KX), (unsigned)((d.ny + ky - 1) / ky), (unsigned)((d.nz + zc - 1) / zc));
+  const int vx = d.dtype == ADV_F32 ? 4 : 2;
+  const bool vec = vec_ok(d, {k, u_in, u_out});
+  const int bx = vec ? KXV : KX, xs = vec ? KXV * vx : KX;
+  const dim3 grid((unsigned)((d.nx + xs - 1) / xs), (unsigned)((d.ny + ky - 1) / ky), (unsigned)((d.nz + zc - 1) / zc));
   if (d.dtype == ADV_F32) {
     HeatKArgs<float> a = make_args<float>(d, k, u_in, nullptr, u_out, nullptr);
     a.zc = zc;
-    heatk_step_kernel<float><<<grid, dim3(KX, ky), 0, s>>>(a);
+    if (vec) heatk_step_vec_kernel<float><<<grid, dim3(bx, ky), 0, s>>>(a);
+    else heatk_step_kernel<float><<<grid, dim3(bx, ky), 0, s>>>(a);
   } else {
     HeatKArgs<double> a = make_args<double>(d, k, u_in, nullptr, u_out, nullptr);
     a.zc = zc;
-    heatk_step_kernel<double><<<grid, dim3(KX, ky), 0, s>>>(a);
+    if (vec) heatk_step_vec_kernel<double><<<grid, dim3(bx, ky), 0, s>>>(a);
+    else heatk_step_kernel<double><<<grid, dim3(bx, ky), 0, s>>>(a);
   }
   ADV_CUDA_TRY(cudaGetLastError());
   count_launches(1);
@@ -178,15 +367,20 @@ adv_status heatk_adjoint_launch(const adv_heatk_desc& d, const void* k, const vo
                                 void* lam_out, void* grad_k, cudaStream_t s) {
   int ky, zc;
   heatk_shape(d, TUNE_HEATK_ADJ, &ky, &zc);
-  const dim3 grid((unsigned)((d.nx + KX - 1) / KX), (unsigned)((d.ny + ky - 1) / ky), (unsigned)((d.nz + zc - 1) / zc));
+  const int vx = d.dtype == ADV_F32 ? 4 : 2;
+  const bool vec = vec_ok(d, {k, u_n, lam_next, lam_out, grad_k});
+  const int bx = vec ? KXV : KX, xs = vec ? KXV * vx : KX;
+  const dim3 grid((unsigned)((d.nx + xs - 1) / xs), (unsigned)((d.ny + ky - 1) / ky), (unsigned)((d.nz + zc - 1) / zc));
   if (d.dtype == ADV_F32) {
     HeatKArgs<float> a = make_args<float>(d, k, u_n, lam_next, lam_out, grad_k);
     a.zc = zc;
-    heatk_adjoint_kernel<float><<<grid, dim3(KX, ky), 0, s>>>(a);
+    if (vec) heatk_adjoint_vec_kernel<float><<<grid, dim3(bx, ky), 0, s>>>(a);
+    else heatk_adjoint_kernel<float><<<grid, dim3(bx, ky), 0, s>>>(a);
   } else {
     HeatKArgs<double> a = make_args<double>(d, k, u_n, lam_next, lam_out, grad_k);
     a.zc = zc;
-    heatk_adjoint_kernel<double><<<grid, dim3(KX, ky), 0, s>>>(a);
+    if (vec) heatk_adjoint_vec_kernel<double><<<grid, dim3(bx, ky), 0, s>>>(a);
+    else heatk_adjoint_kernel<double><<<grid, dim3(bx, ky), 0, s>>>(a);
   }
   ADV_CUDA_TRY(cudaGetLastError());
   count_launches(1);

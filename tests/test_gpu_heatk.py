@@ -31,11 +31,11 @@ def _t(a, cuda):
     return torch.from_numpy(np.ascontiguousarray(a)).to(cuda)
 
 
+@pytest.mark.parametrize("shape", [(37, 29, 33), (40, 29, 33)], ids=["scalar-rows", "vector-rows"])
 @pytest.mark.parametrize("zb", [True, False], ids=["zero", "held"])
 @pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f32", "f64"])
-def test_step_and_adjoint_step_equal_oracle(cuda, native, oracle, dtype, zb):
+def test_step_and_adjoint_step_equal_oracle(cuda, native, oracle, dtype, zb, shape):
     import torch
-    shape = (37, 29, 33)
     cfg, k, u, _ = _case(shape, dtype, 1, zb)
     rng = np.random.default_rng(9)
     lam = rng.standard_normal(u.size).astype(dtype)
