@@ -145,13 +145,112 @@ __device__ __forceinline__ void side_rev(T a, T b, T c, T d, T e, T ybar, T& ga,
   }
 }
 
+// FP32: the two sides of one face (f+ in lane x, f- in lane y) differentiated together with
+// Blackwell's paired FP32 instructions (FFMA2 / FADD2 / FMUL2), the same algebra as side_rev.
+__device__ __forceinline__ float2 c2(float v) { return make_float2(v, v); }
+__device__ __forceinline__ float2 ad2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sb2(float2 a, float2 b) { return __ffma2_rn(b, c2(-1.f), a); }
+__device__ __forceinline__ float2 ml2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fm2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+template <bool Z>
+__device__ __forceinline__ void side_rev2(float2 a, float2 b, float2 c, float2 d, float2 e, float2 ybar, float2 (&g)[5]) {
+  const float2 m2 = c2(-2.f), m4 = c2(-4.f), p3 = c2(3.f), r12 = c2(1.f / 12.f), qt = c2(0.25f);
+  const float2 t0 = ad2(fm2(m2, b, a), c), t1 = ad2(fm2(m2, c, b), d), t2 = ad2(fm2(m2, d, c), e);
+  const float2 s0 = fm2(p3, c, fm2(m4, b, a)), s1 = sb2(b, d), s2 = fm2(p3, c, fm2(m4, d, e));
+  const float2 K = c2(13.f / 3.f), E = c2(4e-6f);
+  const float2 B0 = fm2(ml2(K, t0), t0, fm2(s0, s0, E)), B1 = fm2(ml2(K, t1), t1, fm2(s1, s1, E)),
+               B2 = fm2(ml2(K, t2), t2, fm2(s2, s2, E));
+  const float2 q0 = fm2(qt, s0, fm2(r12, t0, c)), q1 = fm2(c2(-0.25f), s1, fm2(r12, t1, c)),
+               q2 = fm2(c2(-0.25f), s2, fm2(r12, t2, c));
+  float2 w0, w1, w2, Bb0, Bb1, Bb2;
+  if (Z) {
+    const float2 d02 = sb2(B0, B2);
+    const float2 tau = make_float2(fabsf(d02.x), fabsf(d02.y));
+    const float2 sg = make_float2(d02.x > 0.f ? 1.f : (d02.x < 0.f ? -1.f : 0.f),
+                                  d02.y > 0.f ? 1.f : (d02.y < 0.f ? -1.f : 0.f));
+    const float2 P0 = ad2(B0, tau), P1 = ad2(B1, tau), P2 = ad2(B2, tau);
+    const float2 b12 = ml2(B1, B2), b02 = ml2(B0, B2), b01 = ml2(B0, B1);
+    w0 = ml2(P0, b12);
+    w1 = ml2(ml2(c2(6.f), P1), b02);
+    w2 = ml2(ml2(p3, P2), b01);
+    const float2 den = ad2(ad2(w0, w1), w2);
+    const float2 rD = make_float2(__frcp_rn(den.x), __frcp_rn(den.y));
+    const float2 side = ml2(fm2(w2, q2, fm2(w1, q1, ml2(w0, q0))), rD);
+    const float2 Nb = ml2(ybar, rD);
+    const float2 wb0 = ml2(Nb, sb2(q0, side)), wb1 = ml2(ml2(c2(6.f), Nb), sb2(q1, side)),
+                 wb2 = ml2(ml2(p3, Nb), sb2(q2, side));
+    const float2 taub = fm2(wb2, b01, fm2(wb1, b02, ml2(wb0, b12)));
+    Bb0 = fm2(wb2, ml2(P2, B1), fm2(wb1, ml2(P1, B2), ml2(wb0, b12)));
+    Bb1 = fm2(wb2, ml2(P2, B0), fm2(wb1, b02, ml2(wb0, ml2(P0, B2))));
+    Bb2 = fm2(wb2, b01, fm2(wb1, ml2(P1, B0), ml2(wb0, ml2(P0, B1))));
+    Bb0 = fm2(sg, taub, Bb0);
+    Bb2 = fm2(make_float2(-sg.x, -sg.y), taub, Bb2);
+    const float2 qb0 = ml2(Nb, w0), qb1 = ml2(Nb, w1), qb2 = ml2(Nb, w2);
+    const float2 K2 = c2(26.f / 3.f);
+    const float2 tb0 = fm2(ml2(K2, t0), Bb0, ml2(qb0, r12)), tb1 = fm2(ml2(K2, t1), Bb1, ml2(qb1, r12)),
+                 tb2 = fm2(ml2(K2, t2), Bb2, ml2(qb2, r12));
+    const float2 sv0 = fm2(ml2(c2(2.f), s0), Bb0, ml2(qb0, qt)), sv1 = fm2(ml2(c2(2.f), s1), Bb1, ml2(qb1, c2(-0.25f))),
+                 sv2 = fm2(ml2(c2(2.f), s2), Bb2, ml2(qb2, c2(-0.25f)));
+    const float2 cb = ad2(ad2(qb0, qb1), qb2);
+    g[0] = ad2(tb0, sv0);
+    g[1] = ad2(fm2(m2, tb0, tb1), fm2(m4, sv0, sv1));
+    g[2] = ad2(fm2(m2, tb1, ad2(tb0, tb2)), fm2(p3, ad2(sv0, sv2), cb));
+    g[3] = fm2(m4, sv2, sb2(fm2(m2, tb2, tb1), sv1));
+    g[4] = ad2(tb2, sv2);
+  } else {
+    const float2 p12 = ml2(B1, B2), p02 = ml2(B0, B2), p01 = ml2(B0, B1);
+    w0 = ml2(p12, p12);
+    w1 = ml2(ml2(c2(6.f), p02), p02);
+    w2 = ml2(ml2(p3, p01), p01);
+    const float2 den = ad2(ad2(w0, w1), w2);
+    const float2 rD = make_float2(__frcp_rn(den.x), __frcp_rn(den.y));
+    const float2 side = ml2(fm2(w2, q2, fm2(w1, q1, ml2(w0, q0))), rD);
+    const float2 Nb = ml2(ybar, rD);
+    const float2 wb0 = ml2(Nb, sb2(q0, side)), wb1 = ml2(Nb, sb2(q1, side)), wb2 = ml2(Nb, sb2(q2, side));
+    Bb0 = fm2(ml2(c2(12.f), wb1), ml2(p02, B2), ml2(ml2(c2(6.f), wb2), ml2(p01, B1)));
+    Bb1 = fm2(ml2(c2(2.f), wb0), ml2(p12, B2), ml2(ml2(c2(6.f), wb2), ml2(p01, B0)));
+    Bb2 = fm2(ml2(c2(2.f), wb0), ml2(p12, B1), ml2(ml2(c2(12.f), wb1), ml2(p02, B0)));
+    const float2 qb0 = ml2(Nb, w0), qb1 = ml2(Nb, w1), qb2 = ml2(Nb, w2);
+    const float2 K2 = c2(26.f / 3.f);
+    const float2 tb0 = fm2(ml2(K2, t0), Bb0, ml2(qb0, r12)), tb1 = fm2(ml2(K2, t1), Bb1, ml2(qb1, r12)),
+                 tb2 = fm2(ml2(K2, t2), Bb2, ml2(qb2, r12));
+    const float2 sv0 = fm2(ml2(c2(2.f), s0), Bb0, ml2(qb0, qt)), sv1 = fm2(ml2(c2(2.f), s1), Bb1, ml2(qb1, c2(-0.25f))),
+                 sv2 = fm2(ml2(c2(2.f), s2), Bb2, ml2(qb2, c2(-0.25f)));
+    const float2 cb = ad2(ad2(qb0, qb1), qb2);
+    g[0] = ad2(tb0, sv0);
+    g[1] = ad2(fm2(m2, tb0, tb1), fm2(m4, sv0, sv1));
+    g[2] = ad2(fm2(m2, tb1, ad2(tb0, tb2)), fm2(p3, ad2(sv0, sv2), cb));
+    g[3] = fm2(m4, sv2, sb2(fm2(m2, tb2, tb1), sv1));
+    g[4] = ad2(tb2, sv2);
+  }
+}
+
+// Both sides of one face: gp[k] = d side(pv) / d pv[k] * psi and gm[k] = d side(mv) / d mv[k] * psi.
+template <class T, bool Z>
+__device__ __forceinline__ void sides_rev(const T (&pv)[5], const T (&mv)[5], T psi, T (&gp)[5], T (&gm)[5]) {
+  if constexpr (sizeof(T) == 4) {
+    float2 g[5];
+    side_rev2<Z>(make_float2(pv[0], mv[0]), make_float2(pv[1], mv[1]), make_float2(pv[2], mv[2]),
+                 make_float2(pv[3], mv[3]), make_float2(pv[4], mv[4]), c2(psi), g);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) { gp[k] = g[k].x; gm[k] = g[k].y; }
+  } else {
+    side_rev<T, Z>(pv[0], pv[1], pv[2], pv[3], pv[4], psi, gp[0], gp[1], gp[2], gp[3], gp[4]);
+    side_rev<T, Z>(mv[0], mv[1], mv[2], mv[3], mv[4], psi, gm[0], gm[1], gm[2], gm[3], gm[4]);
+  }
+}
+
 // Partials of one face from the six cells v[0..5] = v at i-2 .. i+3 (split inside) and its
 // weight psi: P[k] for f+ at i-2+k, M[k] for f- at i-1+k.
 template <class T, bool Z>
 __device__ __forceinline__ void face_rev(const T* v, T psi, T* P, T* M) {
-  side_rev<T, Z>(fplus(v[0]), fplus(v[1]), fplus(v[2]), fplus(v[3]), fplus(v[4]), psi, P[0], P[1], P[2], P[3], P[4]);
-  side_rev<T, Z>(fminus(v[5]), fminus(v[4]), fminus(v[3]), fminus(v[2]), fminus(v[1]), psi, M[4], M[3], M[2], M[1],
-                 M[0]);
+  const T pv[5] = {fplus(v[0]), fplus(v[1]), fplus(v[2]), fplus(v[3]), fplus(v[4])};
+  const T mv[5] = {fminus(v[5]), fminus(v[4]), fminus(v[3]), fminus(v[2]), fminus(v[1])};
+  T gp[5], gm[5];
+  sides_rev<T, Z>(pv, mv, psi, gp, gm);
+#pragma unroll
+  for (int k = 0; k < 5; ++k) { P[k] = gp[k]; M[4 - k] = gm[k]; }
 }
 
 template <class T, bool Z>
@@ -242,13 +341,15 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) burgers_adjoint_k
           const int r = f / (TL::BX + 5), i = f - r * (TL::BX + 5) - 3;
           const int b = (r + TL::H) * TL::SW + TL::H + i;  // region index of cell i
           const T psi = a.rdx * (lo[b + 1] - lo[b]);
-          T g[5];
-          side_rev<T, Z>(fpS[b - 2], fpS[b - 1], fpS[b], fpS[b + 1], fpS[b + 2], psi, g[0], g[1], g[2], g[3], g[4]);
+          const T pv[5] = {fpS[b - 2], fpS[b - 1], fpS[b], fpS[b + 1], fpS[b + 2]};
+          const T mv[5] = {fmS[b + 3], fmS[b + 2], fmS[b + 1], fmS[b], fmS[b - 1]};
+          T gp[5], gm[5];
+          sides_rev<T, Z>(pv, mv, psi, gp, gm);
 #pragma unroll
-          for (int k = 0; k < 5; ++k) FB[k * TL::NF + f] = g[k];
-          side_rev<T, Z>(fmS[b + 3], fmS[b + 2], fmS[b + 1], fmS[b], fmS[b - 1], psi, g[4], g[3], g[2], g[1], g[0]);
-#pragma unroll
-          for (int k = 0; k < 5; ++k) FB[(5 + k) * TL::NF + f] = g[k];
+          for (int k = 0; k < 5; ++k) {
+            FB[k * TL::NF + f] = gp[k];
+            FB[(5 + k) * TL::NF + f] = gm[4 - k];
+          }
         }
         __syncthreads();
 #pragma unroll
@@ -270,15 +371,15 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) burgers_adjoint_k
           const int b = (j + TL::H) * TL::SW + TL::H + col;
           constexpr int W = TL::SW;
           const T psi = a.rdy * (lo[b + W] - lo[b]);
-          T g[5];
-          side_rev<T, Z>(fpS[b - 2 * W], fpS[b - W], fpS[b], fpS[b + W], fpS[b + 2 * W], psi, g[0], g[1], g[2], g[3],
-                         g[4]);
+          const T pv[5] = {fpS[b - 2 * W], fpS[b - W], fpS[b], fpS[b + W], fpS[b + 2 * W]};
+          const T mv[5] = {fmS[b + 3 * W], fmS[b + 2 * W], fmS[b + W], fmS[b], fmS[b - W]};
+          T gp[5], gm[5];
+          sides_rev<T, Z>(pv, mv, psi, gp, gm);
 #pragma unroll
-          for (int k = 0; k < 5; ++k) FB[k * TL::NF + f] = g[k];
-          side_rev<T, Z>(fmS[b + 3 * W], fmS[b + 2 * W], fmS[b + W], fmS[b], fmS[b - W], psi, g[4], g[3], g[2], g[1],
-                         g[0]);
-#pragma unroll
-          for (int k = 0; k < 5; ++k) FB[(5 + k) * TL::NF + f] = g[k];
+          for (int k = 0; k < 5; ++k) {
+            FB[k * TL::NF + f] = gp[k];
+            FB[(5 + k) * TL::NF + f] = gm[4 - k];
+          }
         }
         __syncthreads();
         const int ko = wrap(zs - 5 + q - 5, nz);
