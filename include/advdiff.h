@@ -150,6 +150,14 @@ adv_status adv_burgers_workspace_bytes(const adv_burgers_desc* d, size_t* bytes)
 adv_status adv_burgers_run(const adv_burgers_desc* d, void* u, void* workspace, double tEnd,
                            double cfl, int dt_rule, double C, int64_t max_steps, double* t_out,
                            int64_t* steps_out, void* stream);
+/* adv_burgers_run continued from a saved state (adv_checkpoint_save): the time sum starts at t0
+ * and the step count at step0, so a run stopped after step0 steps (max_steps) and resumed ends
+ * bit for bit where the uninterrupted run ends. (A run stopped at a tEnd between steps took a
+ * shortened last step there, so it is a different run.) max_steps, t_out and steps_out count
+ * from the start of the whole run. */
+adv_status adv_burgers_resume(const adv_burgers_desc* d, void* u, void* workspace, double t0,
+                              int64_t step0, double tEnd, double cfl, int dt_rule, double C,
+                              int64_t max_steps, double* t_out, int64_t* steps_out, void* stream);
 
 /* ------------------------------------------- heat with a diffusivity field k(x), and its adjoint
  * u_t = div(k grad u) on a 3D node grid: conservative 7-point form with arithmetic face averages
@@ -306,6 +314,37 @@ adv_status adv_ic_burgers_ref(int nx, int ny, int nz, double dx, double dy, doub
  * result.bin as the reference writes it: float32, x fastest, no header
  * (SingleGPU/Diffusion3d_baselineCode/tools.cpp:59-87). */
 adv_status adv_write_result_bin(const char* path, int dtype, const void* host_u, int64_t n);
+/* Reads a result.bin / initial.bin of exactly n float32 values into doubles (the file size must
+ * match). */
+adv_status adv_read_result_bin(const char* path, int64_t n, double* host_u);
+/* The reference's multi-GPU programs write their whole z-decomposed array, RADIUS ghost slabs at
+ * each z end included: nx*ny*(nz + 2*radius) values (MultiGPU/Burgers3d_Baseline/main.c:65,79,
+ * 355; RADIUS 3 for WENO5). Strip keeps the nz interior slabs; pad writes the ghosts as copies of
+ * the periodic neighbours (periodic != 0) or zeros. */
+adv_status adv_strip_ghost_slabs(int nx, int ny, int nz, int radius, const double* ghosted,
+                                 double* interior);
+adv_status adv_pad_ghost_slabs(int nx, int ny, int nz, int radius, int periodic,
+                               const double* interior, double* ghosted);
+
+/* State snapshot for resuming a run (no counterpart in the reference, which keeps no restart
+ * state): a 128-byte header (magic "ADVSTATE", version 1, dtype, nx, ny, nz, step, t, payload
+ * size, CRC-32 of the payload and of the header) then the state in its own precision, x
+ * fastest. Saved through a temporary file and a rename; loading checks both CRCs and rejects a
+ * truncated, altered or inconsistent file. host_u NULL: read the header only. */
+typedef struct adv_checkpoint_header {
+  int32_t version, dtype;
+  int32_t nx, ny, nz, pad0;
+  int64_t step;
+  double t;
+  uint64_t payload_bytes;
+  uint32_t payload_crc32, pad1;
+} adv_checkpoint_header;
+adv_status adv_checkpoint_save(const char* path, int dtype, int nx, int ny, int nz, int64_t step,
+                               double t, const void* host_u);
+adv_status adv_checkpoint_load(const char* path, adv_checkpoint_header* hdr, void* host_u,
+                               size_t capacity_bytes);
+/* CRC-32 (IEEE 802.3 polynomial, as zlib) of n bytes. */
+uint32_t adv_crc32(const void* data, size_t n);
 
 /* ------------------------------------------------------------------------- misc */
 const char* adv_last_error_string(void);

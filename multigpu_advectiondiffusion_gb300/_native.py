@@ -52,6 +52,13 @@ class TuneResult(C.Structure):
                 ("best_us", C.c_double), ("default_us", C.c_double)]
 
 
+class CheckpointHeader(C.Structure):
+    """adv_checkpoint_header (include/advdiff.h)."""
+    _fields_ = [("version", C.c_int32), ("dtype", C.c_int32), ("nx", C.c_int32), ("ny", C.c_int32),
+                ("nz", C.c_int32), ("pad0", C.c_int32), ("step", C.c_int64), ("t", C.c_double),
+                ("payload_bytes", C.c_uint64), ("payload_crc32", C.c_uint32), ("pad1", C.c_uint32)]
+
+
 class HeatMember(C.Structure):
     """adv_heat_member (include/advdiff.h)."""
     _fields_ = [("desc", HeatDesc), ("u", C.c_void_p), ("work", C.c_void_p)]
@@ -98,6 +105,8 @@ SIGNATURES = [
     ("adv_autotune_burgers", _I, [C.POINTER(BurgersDesc), _VP, _VP, C.POINTER(TuneResult)]),
     ("adv_autotune_heatk", _I, [C.POINTER(HeatKDesc), _VP, _VP, _VP, C.POINTER(TuneResult), C.POINTER(TuneResult)]),
     ("adv_autotune_clear", _I, []),
+    ("adv_burgers_resume", _I, [C.POINTER(BurgersDesc), _VP, _VP, _D, _I64, _D, _D, _I, _D, _I64, _PD,
+                                C.POINTER(C.c_int64), _VP]),
     ("adv_max_abs", _I, [_I, _VP, _I64, _PD, _VP]),
     ("adv_ic_heat_ref", _I, [_I, _I, _I, _I, _D, _D, _D, _PD]),
     ("adv_ic_heat2d_gauss_noise", _I, [_I, _I, C.c_uint32, _D, _PD]),
@@ -105,6 +114,12 @@ SIGNATURES = [
     ("adv_ic_burgers_fourier", _I, [_I, _I, _I, _D, C.c_uint32, _I, _D, _PD]),
     ("adv_ic_burgers_ref", _I, [_I, _I, _I, _D, _D, _D, _PD]),
     ("adv_write_result_bin", _I, [C.c_char_p, _I, _VP, _I64]),
+    ("adv_read_result_bin", _I, [C.c_char_p, _I64, _PD]),
+    ("adv_strip_ghost_slabs", _I, [_I, _I, _I, _I, _PD, _PD]),
+    ("adv_pad_ghost_slabs", _I, [_I, _I, _I, _I, _I, _PD, _PD]),
+    ("adv_checkpoint_save", _I, [C.c_char_p, _I, _I, _I, _I, _I64, _D, _VP]),
+    ("adv_checkpoint_load", _I, [C.c_char_p, C.POINTER(CheckpointHeader), _VP, C.c_size_t]),
+    ("adv_crc32", C.c_uint32, [_VP, C.c_size_t]),
     ("adv_last_error_string", C.c_char_p, []),
     ("adv_status_string", C.c_char_p, [_I]),
     ("adv_abi_version", _I, []),

@@ -401,6 +401,12 @@ adv_status adv_burgers_workspace_bytes(const adv_burgers_desc* d, size_t* bytes)
 
 adv_status adv_burgers_run(const adv_burgers_desc* d, void* u, void* workspace, double tEnd, double cfl, int dt_rule,
                            double C, int64_t max_steps, double* t_out, int64_t* steps_out, void* stream) {
+  return adv_burgers_resume(d, u, workspace, 0.0, 0, tEnd, cfl, dt_rule, C, max_steps, t_out, steps_out, stream);
+}
+
+adv_status adv_burgers_resume(const adv_burgers_desc* d, void* u, void* workspace, double t0, int64_t step0,
+                              double tEnd, double cfl, int dt_rule, double C, int64_t max_steps, double* t_out,
+                              int64_t* steps_out, void* stream) {
   adv_status st = burgers_validate(d);
   if (st != ADV_OK) return st;
   if (!u || !workspace) return set_error(ADV_ERR_INVALID_ARG, "burgers: null buffer");
@@ -414,7 +420,10 @@ adv_status adv_burgers_run(const adv_burgers_desc* d, void* u, void* workspace, 
   char* w2 = w1 + one;
   BurgersLoopState* dst = reinterpret_cast<BurgersLoopState*>(w1 + burgers_state_offset(d));
 
+  if (!std::isfinite(t0) || step0 < 0) return set_error(ADV_ERR_INVALID_ARG, "burgers: bad t0/step0");
   BurgersLoopState h = burgers_loop_state(*d, tEnd, cfl, dt_rule, C, max_steps);
+  h.t = t0;  // a resumed run continues the same time sum and step count
+  h.step = step0;
   ADV_CUDA_TRY(cudaMemcpyAsync(dst, &h, sizeof(h), cudaMemcpyHostToDevice, s));
   ADV_CUDA_TRY(cudaStreamSynchronize(s));
   void* key0 = d->dtype == ADV_F32 ? (void*)&dst->maxbits[0] : (void*)&dst->maxbits64[0];
@@ -514,7 +523,7 @@ adv_status adv_burgers_run(const adv_burgers_desc* d, void* u, void* workspace, 
   }
   ADV_CUDA_TRY(cudaMemcpyAsync(&h, dst, sizeof(h), cudaMemcpyDeviceToHost, s));
   ADV_CUDA_TRY(cudaStreamSynchronize(s));
-  count_launches(4 * h.step);
+  count_launches(4 * (h.step - step0));
   if (t_out) *t_out = h.t;
   if (steps_out) *steps_out = h.step;
   return read_and_clear_device_status(s);

@@ -8,6 +8,9 @@
 //   --weno=z|js --lf=local|global --bc=frozen|periodic --viscosity=C --dt=fixed|maxu
 //   --precision=f64|f32 --div=f32|f64 --ic=ref|fourier --seed=N --modes=16 --amax=0.1
 //   --bug-b2=0|1 --max-steps=N --write=0|1 --out=result.bin
+//   --checkpoint=state.bin (save the final state, step and t) --restart=state.bin (continue a
+//   saved run to tEnd; a run stopped with --max-steps and continued takes the same steps, bit
+//   for bit, as the uninterrupted run)
 // With --bc=periodic the grid is cell-centred, dx = L/N.
 #include <cmath>
 #include <vector>
@@ -19,7 +22,8 @@ int main(int argc, char** argv) {
   if (a.pos.size() != 8 && a.pos.size() != 11) {
     std::printf("Usage: %s tEnd CFL L W H NX NY NZ [block_x block_y block_z] [--weno=z|js] [--lf=local|global] "
                 "[--bc=frozen|periodic] [--viscosity=C] [--dt=fixed|maxu] [--precision=f64|f32] [--div=f32|f64] "
-                "[--ic=ref|fourier] [--seed=N] [--bug-b2=0|1] [--max-steps=N] [--write=0|1] [--out=path]\n", argv[0]);
+                "[--ic=ref|fourier] [--seed=N] [--bug-b2=0|1] [--max-steps=N] [--write=0|1] [--out=path] "
+                "[--checkpoint=path] [--restart=path]\n", argv[0]);
     return 1;
   }
   const double tEnd = std::atof(a.pos[0].c_str()), CFL = std::atof(a.pos[1].c_str());
@@ -52,6 +56,9 @@ int main(int argc, char** argv) {
   std::vector<float> hf;
   const void* hsrc = h.data();
   if (dtype == ADV_F32) { hf.assign(h.begin(), h.end()); hsrc = hf.data(); }
+  int64_t step0 = 0;
+  double t0 = 0.0;
+  drv::restart(a, dtype, nx, ny, nz, const_cast<void*>(hsrc), n * (dtype == ADV_F32 ? 4 : 8), &step0, &t0, 0.0);
 
   cudaStream_t s;
   drv::check(cudaStreamCreate(&s), "stream");
@@ -67,20 +74,23 @@ int main(int argc, char** argv) {
   double t = 0;
   int64_t steps = 0;
   tm.start(s);
-  drv::check(adv_burgers_run(&d, du, dw, tEnd, CFL, rule, C, (int64_t)a.num("max-steps", 1e9), &t, &steps, s), "burgers run");
+  drv::check(adv_burgers_resume(&d, du, dw, t0, step0, tEnd, CFL, rule, C, (int64_t)a.num("max-steps", 1e9), &t, &steps, s),
+             "burgers run");
   const double secs = tm.stop(s);
   std::printf("Computation took %1.6f seconds\n\n", secs);
   std::printf("iterations: %lld, final time: %g\n\n", (long long)steps, t);
   tm.start(s);
   drv::check(cudaMemcpyAsync(dtype == ADV_F32 ? (void*)hf.data() : (void*)h.data(), du, n * es, cudaMemcpyDeviceToHost, s), "D2H");
   const double d2h = tm.stop(s);
+  drv::save_checkpoint(a, dtype, nx, ny, nz, steps, t, dtype == ADV_F32 ? (const void*)hf.data() : (const void*)h.data());
   if (a.num("write", 0) != 0)
     drv::check(adv_write_result_bin(a.get("out", "result.bin").c_str(), dtype,
                                     dtype == ADV_F32 ? (const void*)hf.data() : (const void*)h.data(), (int64_t)n), "write");
   char grid[128], it[64];
   std::snprintf(grid, sizeof grid, "3D Grid Size                                 :  %d x %d x %d", nx, ny, nz);
   std::snprintf(it, sizeof it, "%lld x 3 RK steps", (long long)steps);
-  drv::print_summary("Burgers-3D GPU-WENO5", "gb300 fused stage", secs, h2d, d2h, (double)n * steps * 3 / secs * 1e-9,
+  drv::print_summary("Burgers-3D GPU-WENO5", "gb300 fused stage", secs, h2d, d2h,
+                     (double)n * (steps - step0) * 3 / secs * 1e-9,
                      grid, it, -1);
   cudaFree(du);
   cudaFree(dw);

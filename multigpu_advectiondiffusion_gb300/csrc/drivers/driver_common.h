@@ -55,6 +55,35 @@ inline void check(adv_status s, const char* what) {
   }
 }
 
+// --restart=path: replaces the initial state with a saved snapshot (its grid and precision must
+// match the run's) and returns its step and time; without the flag, step 0 and t = t_start.
+inline void restart(const Args& a, int dtype, int nx, int ny, int nz, void* host_u, size_t bytes, int64_t* step,
+                    double* t, double t_start) {
+  *step = 0;
+  *t = t_start;
+  const std::string path = a.get("restart", "");
+  if (path.empty()) return;
+  adv_checkpoint_header hd{};
+  check(adv_checkpoint_load(path.c_str(), &hd, nullptr, 0), "restart");
+  if (hd.dtype != dtype || hd.nx != nx || hd.ny != ny || hd.nz != nz) {
+    std::fprintf(stderr, "restart: %s holds a %d x %d x %d %s state, the run is %d x %d x %d %s\n", path.c_str(),
+                 hd.nx, hd.ny, hd.nz, hd.dtype == ADV_F32 ? "f32" : "f64", nx, ny, nz, dtype == ADV_F32 ? "f32" : "f64");
+    std::exit(3);
+  }
+  check(adv_checkpoint_load(path.c_str(), &hd, host_u, bytes), "restart");
+  *step = hd.step;
+  *t = hd.t;
+  std::printf("restarted from %s at step %lld, t = %.17g\n\n", path.c_str(), (long long)hd.step, hd.t);
+}
+
+// --checkpoint=path: saves the final state with its step and time.
+inline void save_checkpoint(const Args& a, int dtype, int nx, int ny, int nz, int64_t step, double t,
+                            const void* host_u) {
+  const std::string path = a.get("checkpoint", "");
+  if (path.empty()) return;
+  check(adv_checkpoint_save(path.c_str(), dtype, nx, ny, nz, step, t, host_u), "checkpoint");
+}
+
 // Block layout of the reference's PrintSummary (SingleGPU/Diffusion3d_baselineCode/
 // tools.cpp:185-199, SingleGPU/Burgers3d_WENO5/tools.cpp:335-350); the time is device time
 // measured with CUDA events, and the rate line counts cell updates per RK stage.
