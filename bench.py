@@ -20,6 +20,7 @@ the data path) and value = total cell updates of all ranks / max rank time.
 from __future__ import annotations
 
 import argparse
+import dataclasses
 import ctypes as C
 import json
 import os
@@ -761,6 +762,22 @@ def main():
         ev1.record(stream)
         torch.cuda.synchronize()
         extra["f64_value"] = cells_stages_per_step * 3 / (ev0.elapsed_time(ev1) * 1e-3) / 1e9
+    elif args.workload == "burgers3d":
+        # FP64 state, same problem: the reference's operand order (bit-exact with the oracle) and
+        # the common-denominator form (ADV_DIV_FAST), two steps each
+        for key, div in (("f64_value", N.ADV_DIV_F32), ("f64_fast_value", N.ADV_DIV_FAST)):
+            c64 = dataclasses.replace(cfg, div=div)
+            u64 = u0.double()
+            ws64 = burgers_workspace(c64, u64)
+            burgers_run(c64, u64, 1e9, 0.4, N.ADV_DT_MAXU, max_steps=1, workspace=ws64, stream=sh)
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            ev0.record(stream)
+            burgers_run(c64, u64, 1e9, 0.4, N.ADV_DT_MAXU, max_steps=2, workspace=ws64, stream=sh)
+            ev1.record(stream)
+            torch.cuda.synchronize()
+            extra[key] = cfg.numel * 3 * 2 / (ev0.elapsed_time(ev1) * 1e-3) / 1e9
+            del u64, ws64
 
     # ---- CPU baseline (oracle on the host cores, rank 0, N = 1 only)
     cpu = None

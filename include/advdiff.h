@@ -54,7 +54,10 @@ typedef enum adv_lf { ADV_LF_LOCAL = 0, ADV_LF_GLOBAL = 1 } adv_lf;
 typedef enum adv_bc { ADV_BC_FROZEN = 0, ADV_BC_PERIODIC = 1 } adv_bc;
 /* Division of the WENO weights when the state is FP32 (one division per face side):
  * F32 = IEEE FP32 division, F64 = the division in FP64, FAST = FP32 reciprocal-based division
- * (at most 2 ulp). The FP64 state always uses the reference's own FP64 divisions. */
+ * (at most 2 ulp). An FP64 state uses the reference's own operand order and its four FP64
+ * divisions per side (bit-exact) with F32 or F64, and with FAST the common-denominator form:
+ * one FP64 division per side, fused multiply-adds, flux differences times 1/h (a few ulps from
+ * the reference's rounding). */
 typedef enum adv_div { ADV_DIV_F32 = 0, ADV_DIV_F64 = 1, ADV_DIV_FAST = 2 } adv_div;
 /* Burgers time-step rule. FIXED: dt = min(CFL*dx/1, 0.9/(2C sum 1/h^2)) as the reference driver
  * (SingleGPU/Burgers3d_WENO5/main.cpp:130-133); MAXU: dt = CFL*dx/max|u^n| computed on the
@@ -309,6 +312,9 @@ adv_status adv_ic_burgers_fourier(int nx, int ny, int nz, double L, uint32_t see
                                   double amax, double* u);
 /* Reference Burgers IC 3 (tools.cpp:126-137): exp(-|x-1|^2/0.1) at (i dx, j dy, k dz). */
 adv_status adv_ic_burgers_ref(int nx, int ny, int nz, double dx, double dy, double dz, double* u);
+/* The reference's 2D Burgers IC 3 (MultiGPU/Burgers2d_Baseline/Tools.c:108-119): exp(-(x^2+y^2)/0.1)
+ * with x = (0.5 (nx-1) - i) dx, y = (0.5 (ny-1) - j) dy, zero on the outer ring of nodes. */
+adv_status adv_ic_burgers_ref2d(int nx, int ny, double dx, double dy, double* u);
 
 /* ---------------------------------------------------------------------- output (host)
  * result.bin as the reference writes it: float32, x fastest, no header

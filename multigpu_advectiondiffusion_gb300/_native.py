@@ -113,6 +113,7 @@ SIGNATURES = [
     ("adv_ic_heat3d_blobs", _I, [_I, _I, _I, C.c_uint32, _I, _PD]),
     ("adv_ic_burgers_fourier", _I, [_I, _I, _I, _D, C.c_uint32, _I, _D, _PD]),
     ("adv_ic_burgers_ref", _I, [_I, _I, _I, _D, _D, _D, _PD]),
+    ("adv_ic_burgers_ref2d", _I, [_I, _I, _D, _D, _PD]),
     ("adv_write_result_bin", _I, [C.c_char_p, _I, _VP, _I64]),
     ("adv_read_result_bin", _I, [C.c_char_p, _I64, _PD]),
     ("adv_strip_ghost_slabs", _I, [_I, _I, _I, _I, _PD, _PD]),

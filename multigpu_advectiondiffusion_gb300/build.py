@@ -6,7 +6,7 @@ Outputs (all git-ignored) go to ``multigpu_advectiondiffusion_gb300/_lib``:
 * ``libadvdiff_compat_heat2d.so``  -- the reference's 2D heat extern "C" names
 * ``libadvdiff_compat_heat3d.so``  -- the reference's 3D heat extern "C" names
 * ``libadvdiff_compat_burgers3d.so`` -- the reference's Burgers extern "C" names
-* ``heat2d``, ``heat3d``, ``burgers3d`` -- drivers with the reference's command lines
+* ``heat2d``, ``heat3d``, ``burgers3d``, ``burgers2d`` -- drivers with the reference's command lines
 
 Translation units compile in parallel; a unit is rebuilt only when it or a header changed.
 """
@@ -44,7 +44,7 @@ COMPAT = {
     "libadvdiff_compat_burgers3d_pitched.so": ("compat_burgers3d.cpp", ["-DADV_COMPAT_PITCHED"]),
 }
 DRIVERS = {"heat2d": "drivers/heat2d_main.cpp", "heat3d": "drivers/heat3d_main.cpp",
-           "burgers3d": "drivers/burgers3d_main.cpp"}
+           "burgers3d": "drivers/burgers3d_main.cpp", "burgers2d": "drivers/burgers2d_main.cpp"}
 
 
 def nvcc() -> str:

@@ -84,8 +84,10 @@ adv_status burgers_validate(const adv_burgers_desc* d) {
   if (d->nx < 1 || d->ny < 1 || d->nz < 1) return set_error(ADV_ERR_INVALID_ARG, "burgers: empty grid");
   if (d->nx > (1 << 30) || d->ny > (1 << 30) || d->nz > (1 << 30))
     return set_error(ADV_ERR_INVALID_ARG, "burgers: dimension too large");
-  if (d->bc == ADV_BC_PERIODIC && (d->nx < 6 || d->ny < 6 || d->nz < 6))
+  const bool twod = d->nz == 1;  // a 2D problem: one plane, no z fluxes
+  if (d->bc == ADV_BC_PERIODIC && (d->nx < 6 || d->ny < 6 || (!twod && d->nz < 6)))
     return set_error(ADV_ERR_INVALID_ARG, "burgers: periodic grids need at least 6 cells per axis");
+  if (twod && d->kz != 0.0) return set_error(ADV_ERR_INVALID_ARG, "burgers: a 2D grid (nz == 1) takes kz = 0");
   if (!(d->dx > 0) || !(d->dy > 0) || !(d->dz > 0)) return set_error(ADV_ERR_INVALID_ARG, "burgers: spacing must be > 0");
   return ADV_OK;
 }
@@ -699,6 +701,17 @@ adv_status adv_ic_burgers_ref(int nx, int ny, int nz, double dx, double dy, doub
         u[(size_t)i + (size_t)nx * j + (size_t)nx * ny * k] =
             1.0 * std::exp(-((x - 1.0) * (x - 1.0) + (y - 1.0) * (y - 1.0) + (z - 1.0) * (z - 1.0)) / 0.1);
       }
+  return ADV_OK;
+}
+
+adv_status adv_ic_burgers_ref2d(int nx, int ny, double dx, double dy, double* u) {
+  if (nx < 1 || ny < 1 || !u) return set_error(ADV_ERR_INVALID_ARG, "ic_burgers_ref2d: bad arguments");
+  for (int j = 0; j < ny; ++j)
+    for (int i = 0; i < nx; ++i) {
+      const double x = (0.5 * (nx - 1) - i) * dx, y = (0.5 * (ny - 1) - j) * dy;
+      const bool ring = i == 0 || i == nx - 1 || j == 0 || j == ny - 1;
+      u[(size_t)i + (size_t)nx * j] = ring ? 0.0 : 1.0 * std::exp(-((x * x) + (y * y)) / 0.1);
+    }
   return ADV_OK;
 }
 

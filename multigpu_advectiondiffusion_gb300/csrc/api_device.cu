@@ -114,7 +114,8 @@ BurgersLoopState burgers_loop_state(const adv_burgers_desc& d, double tEnd, doub
   h.cfl = cfl;
   h.dx = d.dx;
   const double dt1 = cfl * d.dx / 1.0;
-  const double dt2 = C > 0 ? 1. / (2 * C * (1 / d.dx / d.dx + 1 / d.dy / d.dy + 1 / d.dz / d.dz)) * 0.9
+  const double iz = d.nz == 1 ? 0.0 : 1 / d.dz / d.dz;  // a 2D grid has no z term
+  const double dt2 = C > 0 ? 1. / (2 * C * (1 / d.dx / d.dx + 1 / d.dy / d.dy + iz)) * 0.9
                            : std::numeric_limits<double>::infinity();
   h.dt_fixed = dt1 < dt2 ? dt1 : dt2;
   h.step = 0;

@@ -440,6 +440,7 @@ adv_status adjoint_validate(const adv_burgers_desc* d) {
   if (d->bc != ADV_BC_PERIODIC || d->lf != ADV_LF_LOCAL || d->kx != 0.0 || d->ky != 0.0 || d->kz != 0.0)
     return set_error(ADV_ERR_UNSUPPORTED,
                      "burgers adjoint: periodic, local Lax-Friedrichs, inviscid schemes only");
+  if (d->nz == 1) return set_error(ADV_ERR_UNSUPPORTED, "burgers adjoint: 3D grids only (nz >= 6)");
   return ADV_OK;
 }
 

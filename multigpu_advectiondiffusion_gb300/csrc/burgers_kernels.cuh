@@ -19,6 +19,8 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "adv_device.cuh"
 #include "adv_math.cuh"
 #include "weno.cuh"
@@ -105,6 +107,15 @@ struct Face<double, Z, D> {
   }
   __device__ __forceinline__ static void split(double u, double a, double& fp, double& fm) { lf_split<double>(u, a, fp, fm); }
 };
+// FP64 state with ADV_DIV_FAST: the common-denominator form, one division per side.
+template <bool Z>
+struct Face<double, Z, FastDiv> {
+  __device__ __forceinline__ static double f(double p0, double p1, double p2, double p3, double p4, double m0,
+                                             double m1, double m2, double m3, double m4) {
+    return weno_face_fast64<Z>(p0, p1, p2, p3, p4, m0, m1, m2, m3, m4);
+  }
+  __device__ __forceinline__ static void split(double u, double a, double& fp, double& fm) { lf_split_fast64(u, a, fp, fm); }
+};
 
 struct BurgersPipe {
   int s_issue, s_wait;  // ring slots of the next plane to issue / to wait for
@@ -145,7 +156,8 @@ __device__ __forceinline__ BurgersPipe burgers_segment(const CUtensorMap* tmap, 
   using TL = BurgersTile;
   using SM = BurgersSmem<T>;
   using K = typename KeyOf<T>::type;
-  constexpr bool EXACT = sizeof(T) == 8;  // FP64: reference operand order, correctly rounded
+  // FP64 (unless ADV_DIV_FAST): reference operand order, correctly rounded
+  constexpr bool EXACT = sizeof(T) == 8 && !std::is_same<D, FastDiv>::value;
 
   extern __shared__ __align__(128) unsigned char smem_raw[];
   T* ring = reinterpret_cast<T*>(smem_raw);
@@ -204,7 +216,10 @@ __device__ __forceinline__ BurgersPipe burgers_segment(const CUtensorMap* tmap, 
   const int Q = (ze - zs) + 2 * TL::R;
   const int p0 = zs - TL::R;
   const bool edge = per && (x0 - TL::PADX < 0 || x0 + TL::BX + TL::PADX > nx || y0 - TL::R < 0 || y0 + TL::BY + TL::R > ny);
-  auto plane_z = [&](int q) { return per ? wrapi(p0 + q, nz) : p0 + q; };
+  // 2D (nz == 1): every streamed plane is the one plane, so the z faces of each column are equal
+  // and their difference is exactly zero; no z layer is frozen.
+  const bool twod = nz == 1;
+  auto plane_z = [&](int q) { return per || twod ? wrapi(p0 + q, nz) : p0 + q; };
   auto issue = [&](int q) {
     T* dst = ring + s_issue * SM::SLOT_ELEMS;
     const int z = plane_z(q);
@@ -296,7 +311,7 @@ __device__ __forceinline__ BurgersPipe burgers_segment(const CUtensorMap* tmap, 
     }
     // z-face at (newest plane - 3) + 1/2 once the windows hold planes newest-5 .. newest.
     T fz_new[2] = {T(0), T(0)};
-    if (q >= 5) {
+    if (q >= 5 && !twod) {  // 2D: both z faces would be equal; their difference stays exactly 0
       if constexpr (sizeof(T) == 4) {
         auto pk = [&](const T (&w)[2][5], int s) { return make_float2(w[0][s], w[1][s]); };
         const float2 fz = Face<T, Z, D>::f2(pk(fpw, 0), pk(fpw, 1), pk(fpw, 2), pk(fpw, 3), pk(fpw, 4), pk(fmw, 0),
@@ -313,7 +328,7 @@ __device__ __forceinline__ BurgersPipe burgers_segment(const CUtensorMap* tmap, 
     if (q >= 6) {
       const int k = zs + q - 6;  // output plane; its staged copy is stream entry q - 3
       const T* plc = ring + s_cent * SM::SLOT_ELEMS;
-      const bool kin = per || (k >= F && k < nz - F);
+      const bool kin = per || twod || (k >= F && k < nz - F);
       const bool any_upd = kin && !aborted;
       if (any_upd) {
         // f+- of the output plane into shared memory

@@ -294,7 +294,8 @@ adv_status create_impl(const adv_heat_member* heat, int n_heat, int scheme, cons
     if (!m.u || !m.work) return set_error(ADV_ERR_INVALID_ARG, "ensemble: null Burgers buffer");
     const bool visc = d.kx != 0.0 || d.ky != 0.0 || d.kz != 0.0;
     const bool visc0 = d0.kx != 0.0 || d0.ky != 0.0 || d0.kz != 0.0;
-    if (d.dtype != d0.dtype || d.weno != d0.weno || visc != visc0 || (d.dtype == ADV_F32 && d.div != d0.div))
+    const bool div_differs = d.dtype == ADV_F32 ? d.div != d0.div : (d.div == ADV_DIV_FAST) != (d0.div == ADV_DIV_FAST);
+    if (d.dtype != d0.dtype || d.weno != d0.weno || visc != visc0 || div_differs)
       return set_error(ADV_ERR_INVALID_ARG, "ensemble: Burgers members must share dtype, weno, div and viscosity");
     if (m.dt_rule != ADV_DT_FIXED && m.dt_rule != ADV_DT_MAXU)
       return set_error(ADV_ERR_INVALID_ARG, "ensemble: bad Burgers dt rule");

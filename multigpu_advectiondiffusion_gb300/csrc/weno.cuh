@@ -139,6 +139,52 @@ __device__ __forceinline__ float2 weno_face_fast2(float2 p0, float2 p1, float2 p
   return add2(weno_side_fast2<Z, D>(p0, p1, p2, p3, p4), weno_side_fast2<Z, D>(m4, m3, m2, m1, m0));
 }
 
+// ------------------------------------------------------------------- fast FP64 form
+// weno_side_fast's common-denominator weights and contracted products for an FP64 state: one
+// IEEE division per side instead of the reference form's four, and fused multiply-adds. The
+// same function of the inputs as the reference form, rounded differently (a few ulps of the
+// face value); selected for FP64 states with ADV_DIV_FAST.
+template <bool Z>
+__device__ __forceinline__ double weno_side_fast64(double a, double b, double c, double d, double e) {
+  const double t0 = fma(-2.0, b, a) + c, t1 = fma(-2.0, c, b) + d, t2 = fma(-2.0, d, c) + e;
+  const double s0 = fma(3.0, c, fma(-4.0, b, a)), s1 = b - d, s2 = fma(3.0, c, fma(-4.0, d, e));
+  const double k = 13.0 / 3.0;
+  const double b0 = fma(k * t0, t0, fma(s0, s0, 4e-6));  // 4 (beta_k + eps)
+  const double b1 = fma(k * t1, t1, fma(s1, s1, 4e-6));
+  const double b2 = fma(k * t2, t2, fma(s2, s2, 4e-6));
+  const double r12 = 1.0 / 12.0;
+  const double q0 = fma(0.25, s0, fma(r12, t0, c));
+  const double q1 = fma(-0.25, s1, fma(r12, t1, c));
+  const double q2 = fma(-0.25, s2, fma(r12, t2, c));
+  double w0, w1, w2;
+  if (Z) {
+    const double tau = fabs(b0 - b2);
+    w0 = (b0 + tau) * (b1 * b2);
+    w1 = (6.0 * (b1 + tau)) * (b0 * b2);
+    w2 = (3.0 * (b2 + tau)) * (b0 * b1);
+  } else {
+    const double p12 = b1 * b2, p02 = b0 * b2, p01 = b0 * b1;
+    w0 = p12 * p12;
+    w1 = (6.0 * p02) * p02;
+    w2 = (3.0 * p01) * p01;
+  }
+  const double num = fma(w2, q2, fma(w1, q1, w0 * q0));
+  const double den = w0 + w1 + w2;
+  return num / den;
+}
+
+template <bool Z>
+__device__ __forceinline__ double weno_face_fast64(double p0, double p1, double p2, double p3, double p4, double m0,
+                                                   double m1, double m2, double m3, double m4) {
+  return weno_side_fast64<Z>(p0, p1, p2, p3, p4) + weno_side_fast64<Z>(m4, m3, m2, m1, m0);
+}
+
+__device__ __forceinline__ void lf_split_fast64(double u, double a, double& fp, double& fm) {
+  const double hu = 0.25 * u, ha = 0.5 * a;
+  fp = u * (hu + ha);
+  fm = u * (hu - ha);
+}
+
 // ---------------------------------------------------------- reference literal form
 // Operand order of kernels.cu:142-192 / :92-140 (and of the CPU oracle), correctly rounded.
 template <bool Z, class T>

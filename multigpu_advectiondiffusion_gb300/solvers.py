@@ -140,8 +140,18 @@ class BurgersConfig:
         return cls(n, n, n, h, h, h, N.ADV_WENO5_Z if weno == "z" else N.ADV_WENO5_JS,
                    N.ADV_LF_GLOBAL if lf == "global" else N.ADV_LF_LOCAL, N.ADV_BC_PERIODIC, int(div), False, 0.0)
 
+    @classmethod
+    def reference_2d(cls, L: float, W: float, nx: int, ny: int, C: float = 0.0) -> "BurgersConfig":
+        """The reference's 2D Burgers scheme on one plane (nz = 1): node grid dx = L/(N-1), local
+        LF, WENO5-JS, inviscid (MultiGPU/Burgers2d_Baseline/main.c:58, Kernels.cu:112-222), with
+        three frozen layers in x and y."""
+        return cls(nx, ny, 1, L / (nx - 1), W / (ny - 1), L / (nx - 1), N.ADV_WENO5_JS, N.ADV_LF_LOCAL,
+                   N.ADV_BC_FROZEN, N.ADV_DIV_F32, False, C)
+
     def desc(self, dtype: int) -> N.BurgersDesc:
         k = [self.C / (12 * h * h) if self.C else 0.0 for h in (self.dx, self.dy, self.dz)]
+        if self.nz == 1:  # 2D: no z term
+            k[2] = 0.0
         return N.BurgersDesc(self.nx, self.ny, self.nz, dtype, self.weno, self.lf, self.bc, self.div,
                              int(self.bug_b2), 0, self.dx, self.dy, self.dz, *k)
 

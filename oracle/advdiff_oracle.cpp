@@ -300,16 +300,18 @@ template <class T, class D>
 void burgers_rhs(const BurgersCfg& c, const T* u, T a_glob, T* Lu) {
   const int64_t nx = c.nx, ny = c.ny, nz = c.nz, sz = nx * ny;
   const int F = c.periodic ? 0 : 3;
+  const int Fz = nz == 1 ? 0 : F;  // 2D (one plane): no frozen z layers, z neighbours are the plane
   const T dx = (T)c.dx, dy = (T)c.dy, dz = (T)c.dz;
   const T kx = (T)c.kx, ky = (T)c.ky, kz = (T)c.kz;
   const bool visc = c.kx != 0.0 || c.ky != 0.0 || c.kz != 0.0;
 #pragma omp parallel for collapse(2) schedule(static)
-  for (int64_t k = F; k < nz - F; ++k)
+  for (int64_t k = Fz; k < nz - Fz; ++k)
     for (int64_t j = F; j < ny - F; ++j)
       for (int64_t i = F; i < nx - F; ++i) {
         const int64_t o = i + nx * j + sz * k;
         auto U = [&](int64_t ii, int64_t jj, int64_t kk) -> T {
           if (c.periodic) return u[wrap(ii, nx) + nx * wrap(jj, ny) + sz * wrap(kk, nz)];
+          if (nz == 1) kk = 0;
           return u[ii + nx * jj + sz * kk];
         };
         T fxp = face_flux<T, D>(c, a_glob, [&](int q) { return U(i + q, j, k); });
@@ -348,12 +350,13 @@ template <class T>
 void burgers_combine(const BurgersCfg& c, int stage, const T* uin, const T* un, const T* Lu, T dt, T* out) {
   const int64_t nx = c.nx, ny = c.ny, nz = c.nz;
   const int F = c.periodic ? 0 : 3;
+  const int Fz = nz == 1 ? 0 : F;
 #pragma omp parallel for collapse(2) schedule(static)
   for (int64_t k = 0; k < nz; ++k)
     for (int64_t j = 0; j < ny; ++j)
       for (int64_t i = 0; i < nx; ++i) {
         const int64_t o = i + nx * j + nx * ny * k;
-        bool interior = i >= F && i < nx - F && j >= F && j < ny - F && k >= F && k < nz - F;
+        bool interior = i >= F && i < nx - F && j >= F && j < ny - F && k >= Fz && k < nz - Fz;
         out[o] = interior ? stage_combine<T>(stage, un[o], uin[o], dt, Lu[o]) : uin[o];
       }
 }
@@ -381,7 +384,8 @@ int64_t burgers_run(const BurgersCfg& c, T* u, double tEnd, double CFL, int dt_r
     double dt;
     if (dt_rule == 0) {
       double dt1 = CFL * c.dx / 1.0;
-      double dt2 = (C > 0) ? 1. / (2 * C * (1 / c.dx / c.dx + 1 / c.dy / c.dy + 1 / c.dz / c.dz)) * 0.9
+      const double iz = c.nz == 1 ? 0.0 : 1 / c.dz / c.dz;  // 2D: no z term
+      double dt2 = (C > 0) ? 1. / (2 * C * (1 / c.dx / c.dx + 1 / c.dy / c.dy + iz)) * 0.9
                            : std::numeric_limits<double>::infinity();
       dt = dt1 < dt2 ? dt1 : dt2;
     } else {

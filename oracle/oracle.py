@@ -170,6 +170,8 @@ def ic_burgers_ref(nx, ny, nz, dx, dy, dz) -> np.ndarray:
 
 def _burg_args(cfg):
     k = [cfg.C / (12 * h * h) if cfg.C else 0.0 for h in (cfg.dx, cfg.dy, cfg.dz)]
+    if cfg.nz == 1:  # 2D: no z term
+        k[2] = 0.0
     return [cfg.nx, cfg.ny, cfg.nz, int(cfg.weno == 1), int(cfg.lf == 1), int(cfg.bc == 1), int(cfg.bug_b2),
             cfg.dx, cfg.dy, cfg.dz, *k]
 

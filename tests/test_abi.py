@@ -116,6 +116,6 @@ def test_result_bin_layout(native, tmp_path):
 
 
 def test_drivers_print_usage_without_gpu(native):
-    for drv in ("heat2d", "heat3d", "burgers3d"):
+    for drv in ("heat2d", "heat3d", "burgers3d", "burgers2d"):
         r = subprocess.run([str(N.LIBDIR / drv)], capture_output=True, text=True)
         assert r.returncode == 1 and "Usage" in r.stdout

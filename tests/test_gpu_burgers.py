@@ -81,6 +81,36 @@ def test_burgers_stage_fp32(cuda, oracle, kind, size, weno, div):
     assert np.abs(got - want).max() <= 4e-7 * np.abs(want).max()
 
 
+@pytest.mark.parametrize("kind,size,weno", _cases()[:6] + _cases()[-2:])
+def test_burgers_stage_fp64_fast(cuda, oracle, kind, size, weno):
+    """FP64 state with ADV_DIV_FAST (common-denominator WENO weights, one division per side, FMAs)
+    vs the FP64 oracle's reference operand order: max |diff| <= 1e-14 * max|u|."""
+    cfg = _cfg(kind, size, weno)
+    cfg.div = N.ADV_DIV_FAST
+    uin, un = _field(cfg, 17), _field(cfg, 18)
+    want = oracle.burgers_stage(cfg, 2, uin, un, 2e-3)
+    a, b = _t(uin, cuda), _t(un, cuda)
+    out = a.new_full(a.shape, np.nan)
+    burgers_stage(cfg, 2, a, b, out, 2e-3, float(np.abs(uin).max()))
+    got = out.cpu().numpy()
+    assert np.abs(got - want).max() <= 1e-14 * np.abs(want).max()
+    assert not np.array_equal(got, want)  # really the other form
+
+
+@pytest.mark.parametrize("t_end,tol", [(0.3, 1e-12), (0.6, 1e-10)], ids=["smooth", "shocks"])
+def test_burgers_run_fp64_fast_vs_oracle(cuda, oracle, t_end, tol):
+    """FP64 fast form over a whole run: same step count; rel-L2 vs the FP64 oracle within tol
+    (the shocks of t = 0.6 amplify rounding differences through the nonlinear weights)."""
+    cfg = BurgersConfig.periodic(32, weno="z", div="fast")
+    u0 = oracle.ic_burgers_fourier(32, 32, 32, 2.0, 3)
+    want, t_w, it_w = oracle.burgers_run(cfg, u0, t_end, 0.4, 1)
+    u = _t(u0, cuda)
+    t, it = burgers_run(cfg, u, t_end, 0.4, N.ADV_DT_MAXU)
+    assert it == it_w and t == pytest.approx(t_w, abs=1e-14)
+    got = u.cpu().numpy()
+    assert np.linalg.norm(got - want) / np.linalg.norm(want) <= tol
+
+
 def test_burgers_stage_reports_max_abs(cuda, oracle):
     import torch
     cfg = _cfg("periodic-global", (32, 32, 24), N.ADV_WENO5_Z)

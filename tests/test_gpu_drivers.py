@@ -59,3 +59,23 @@ def test_burgers3d_driver_resumes_exactly(cuda, native, tmp_path, flags, n):
     assert native.adv_checkpoint_load(str(tmp_path / "resumed.state").encode(), N.C.byref(hb), None, 0) == N.ADV_OK
     assert (ha.step, ha.t, ha.payload_crc32) == (hb.step, hb.t, hb.payload_crc32)
     assert ha.t == pytest.approx(0.12)
+
+
+def test_burgers2d_driver_equals_oracle_and_resumes_exactly(cuda, native, oracle, tmp_path):
+    """burgers2d with the reference's 2D argv (tEnd CFL L W NX NY bx by): WENO5-JS, local LF,
+    dt = CFL dx, its centred Gaussian IC; result.bin equals the FP64 oracle's run, and a run
+    stopped after 5 steps and continued ends on the same bits."""
+    from multigpu_advectiondiffusion_gb300.solvers import BurgersConfig
+    nx, ny = 61, 47
+    base = ["burgers2d", 0.1, 0.3, 2, 2, nx, ny, 16, 16]
+    out = _run(base + ["--write=1", "--out=full.bin"], tmp_path)
+    cfg = BurgersConfig.reference_2d(2.0, 2.0, nx, ny)
+    u0 = np.empty(nx * ny)
+    N.check(native.adv_ic_burgers_ref2d(nx, ny, cfg.dx, cfg.dy, u0.ctypes.data_as(N.C.POINTER(N.C.c_double))), "ic")
+    want, _, it_w = oracle.burgers_run(cfg, u0, 0.1, 0.3, 0)
+    assert int(re.search(r"iterations: (\d+)", out).group(1)) == it_w
+    full = np.fromfile(tmp_path / "full.bin", dtype=np.float32)
+    np.testing.assert_array_equal(full, want.astype(np.float32))
+    _run(base + ["--max-steps=5", "--checkpoint=part.state"], tmp_path)
+    _run(base + ["--write=1", "--out=resumed.bin", "--restart=part.state"], tmp_path)
+    np.testing.assert_array_equal(np.fromfile(tmp_path / "resumed.bin", dtype=np.float32), full)

@@ -91,15 +91,17 @@ def test_heat_ensemble_order4_and_repeated_runs(cuda, native):
 def _burgers_members(dtype, div, cuda):
     cfgs = [BurgersConfig.periodic(32, div=div), BurgersConfig.periodic(48, div=div),
             BurgersConfig(40, 36, 28, 2 / 40, 2 / 36, 2 / 28, N.ADV_WENO5_Z, N.ADV_LF_GLOBAL, N.ADV_BC_PERIODIC, div),
-            BurgersConfig(37, 33, 30, 0.05, 0.05, 0.05, N.ADV_WENO5_Z, N.ADV_LF_LOCAL, N.ADV_BC_FROZEN, div)]
-    ends = [0.05, 0.12, 0.08, 0.1]
+            BurgersConfig(37, 33, 30, 0.05, 0.05, 0.05, N.ADV_WENO5_Z, N.ADV_LF_LOCAL, N.ADV_BC_FROZEN, div),
+            BurgersConfig(72, 40, 1, 2 / 72, 2 / 40, 2 / 72, N.ADV_WENO5_Z, N.ADV_LF_GLOBAL, N.ADV_BC_PERIODIC, div)]
+    ends = [0.05, 0.12, 0.08, 0.1, 0.15]
     us = [_burgers_state(c, dtype, 11 + i, cuda) for i, c in enumerate(cfgs)]
     return cfgs, ends, us
 
 
 @pytest.mark.parametrize("direct", [False, True], ids=["graph", "direct"])
 @pytest.mark.parametrize("dtype,div", [(np.float32, N.ADV_DIV_FAST), (np.float32, N.ADV_DIV_F64),
-                                       (np.float64, N.ADV_DIV_F32)], ids=["f32-fast", "f32-div64", "f64"])
+                                       (np.float64, N.ADV_DIV_F32), (np.float64, N.ADV_DIV_FAST)],
+                         ids=["f32-fast", "f32-div64", "f64", "f64-fast"])
 def test_burgers_ensemble_matches_per_member_runs(cuda, native, dtype, div, direct):
     import torch
     cfgs, ends, us = _burgers_members(dtype, div, cuda)
