@@ -99,7 +99,7 @@ adv_status build_heat_table(adv_ensemble* e, std::vector<unsigned char>& bytes) 
     const int ns = heat_slots_of(m, e->heat_scheme, sl);
     HeatLaunch L;
     for (int s = 0; s < ns; ++s) {
-      adv_status st = heat_prepare(m.desc, sl[s].in, &L);
+      adv_status st = heat_prepare(m.desc, sl[s].in, &L, 2);  // the batched kernel's tile
       if (st != ADV_OK) return st;
       tma = tma && L.tma;
       tab[i].tmap[s] = L.tmap_in;

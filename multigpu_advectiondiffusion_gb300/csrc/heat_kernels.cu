@@ -7,8 +7,8 @@
 
 namespace adv {
 
-void* heat_kernel_f32(int order, int ndim, bool tma, int stage_kind);
-void* heat_kernel_f64(int order, int ndim, bool tma, int stage_kind);
+void* heat_kernel_f32(int order, int ndim, bool tma, int stage_kind, int rows, int warps);
+void* heat_kernel_f64(int order, int ndim, bool tma, int stage_kind, int rows, int warps);
 
 adv_status heat_validate(const adv_heat_desc* d) {
   if (!d) return set_error(ADV_ERR_INVALID_ARG, "heat: null descriptor");
@@ -28,19 +28,22 @@ adv_status heat_validate(const adv_heat_desc* d) {
 
 namespace {
 
-void* pick_kernel(int dtype, int order, int ndim, bool tma, int stage_kind) {
-  return dtype == ADV_F32 ? heat_kernel_f32(order, ndim, tma, stage_kind) : heat_kernel_f64(order, ndim, tma, stage_kind);
+void* pick_kernel(int dtype, int order, int ndim, bool tma, int stage_kind, int rows, int warps) {
+  return dtype == ADV_F32 ? heat_kernel_f32(order, ndim, tma, stage_kind, rows, warps)
+                          : heat_kernel_f64(order, ndim, tma, stage_kind, rows, warps);
 }
 
-template <class T, int ORDER, int NDIM>
+template <class T, int ORDER, int NDIM, int ROWS, int WARPS = 8>
 void tile_dims(int* bx, int* by, int* sw, int* sh, int* padx, int* r, size_t* smem) {
-  using C = HeatTile<T, ORDER, NDIM>;
+  using C = HeatTile<T, ORDER, NDIM, ROWS, WARPS>;
   *bx = C::BX; *by = C::BY; *sw = C::SW; *sh = C::SH; *padx = C::PADX; *r = C::R; *smem = C::SMEM;
 }
 
-void tile_for(int dtype, int order, int ndim, int* bx, int* by, int* sw, int* sh, int* padx, int* r,
-              size_t* smem) {
-#define TD(T, O, N) if (order == O && ndim == N) return tile_dims<T, O, N>(bx, by, sw, sh, padx, r, smem);
+void tile_for(int dtype, int order, int ndim, int rows, int warps, int* bx, int* by, int* sw, int* sh, int* padx,
+              int* r, size_t* smem) {
+  if (rows == 4 && warps == 4) return tile_dims<float, 2, 3, 4, 4>(bx, by, sw, sh, padx, r, smem);
+  if (rows == 4) return tile_dims<float, 2, 3, 4, 8>(bx, by, sw, sh, padx, r, smem);
+#define TD(T, O, N) if (order == O && ndim == N) return tile_dims<T, O, N, 2>(bx, by, sw, sh, padx, r, smem);
   if (dtype == ADV_F32) { TD(float, 2, 3) TD(float, 4, 3) TD(float, 2, 2) TD(float, 4, 2) }
   else { TD(double, 2, 3) TD(double, 4, 3) TD(double, 2, 2) TD(double, 4, 2) }
 #undef TD
@@ -50,29 +53,35 @@ void tile_for(int dtype, int order, int ndim, int* bx, int* by, int* sw, int* sh
 
 int heat_tune_variant(const adv_heat_desc& d) { return d.dtype * 100 + d.order * 10 + d.ndim; }
 
-adv_status heat_prepare(const adv_heat_desc& d, const void* u_in, HeatLaunch* L) {
+adv_status heat_prepare(const adv_heat_desc& d, const void* u_in, HeatLaunch* L, int rows) {
   DeviceInfo di;
   adv_status st = device_info(&di);
   if (st != ADV_OK) return st;
-  int bx, by, sw, sh, padx, r;
-  size_t smem;
-  tile_for(d.dtype, d.order, d.ndim, &bx, &by, &sw, &sh, &padx, &r, &smem);
   const int es = d.dtype == ADV_F32 ? 4 : 8;
   const int nz = d.ndim == 3 ? d.nz : 1;
   // TMA needs 16-byte aligned base and strides.
   const bool aligned = ((uintptr_t)u_in % 16 == 0) && (((int64_t)d.nx * es) % 16 == 0) &&
                        (((int64_t)d.nx * d.ny * es) % 16 == 0);
   L->tma = aligned;
-  L->block = dim3(32, 8, 1);
+  // Four rows per thread (tile 128 x 32): the per-plane bookkeeping of a thread is spread over
+  // 16 nodes instead of 8 (FP32 3D O2 with TMA loads).
+  const bool rows4_ok = aligned && d.dtype == ADV_F32 && d.order == 2 && d.ndim == 3;
+  if (rows == 4 && !rows4_ok) return set_error(ADV_ERR_UNSUPPORTED, "heat: 4 rows per thread need FP32 3D O2 with TMA");
+  L->rows = rows == 0 ? (rows4_ok ? 4 : 2) : rows;
+  L->warps = L->rows == 4 ? 4 : 8;
+  int bx, by, sw, sh, padx, r;
+  size_t smem;
+  tile_for(d.dtype, d.order, d.ndim, L->rows, L->warps, &bx, &by, &sw, &sh, &padx, &r, &smem);
+  L->block = dim3(32, (unsigned)L->warps, 1);
   const int tiles_x = (d.nx + bx - 1) / bx, tiles_y = (d.ny + by - 1) / by;
   for (int sk = 0; sk <= 3; ++sk) {
-    void* k = pick_kernel(d.dtype, d.order, d.ndim, L->tma, sk);
+    void* k = pick_kernel(d.dtype, d.order, d.ndim, L->tma, sk, L->rows, L->warps);
     if (!k) return set_error(ADV_ERR_UNSUPPORTED, "heat: no kernel for this configuration");
     ADV_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   }
-  void* k0 = pick_kernel(d.dtype, d.order, d.ndim, L->tma, 1);
+  void* k0 = pick_kernel(d.dtype, d.order, d.ndim, L->tma, 1, L->rows, L->warps);
   int occ = 0;
-  ADV_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k0, 256, smem));
+  ADV_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k0, 32 * L->warps, smem));
   occ = std::max(occ, 1);
   L->occ = occ;
   // One wave: every CTA resident at once, each with an equal share of the (tile, plane) pairs,
@@ -111,7 +120,7 @@ static adv_status heat_launch_t(const adv_heat_desc& d, const HeatLaunch& L, int
                                 const void* u_n, void* u_out, cudaStream_t s) {
   HeatParams<T> p = heat_params<T>(d, L, stage, u_in, u_n, u_out);
   const int stage_kind = (stage == 1 && u_n != u_in) ? 0 : stage;
-  void* k = pick_kernel(d.dtype, d.order, d.ndim, L.tma, stage_kind);
+  void* k = pick_kernel(d.dtype, d.order, d.ndim, L.tma, stage_kind, L.rows, L.warps);
   void* args[] = {const_cast<CUtensorMap*>(&L.tmap_in), &p};
   ADV_CUDA_TRY(cudaLaunchKernel(k, L.grid, L.block, args, L.smem, s));
   count_launches(1);

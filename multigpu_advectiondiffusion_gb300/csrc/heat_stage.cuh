@@ -39,11 +39,12 @@ __device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fm
 __device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
 __device__ __forceinline__ float2 fma_rn(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 
-template <class T, int ORDER, int NDIM>
+template <class T, int ORDER, int NDIM, int ROWS = 2, int WARPS = 8>
 struct HeatTile {
   static constexpr int VX = 16 / (int)sizeof(T);  // nodes per thread along x (one 16-byte vector)
-  static constexpr int TX = 32, TY = 8, NT = TX * TY;
-  static constexpr int RY = 2;  // rows per thread
+  static constexpr int TX = 32, TY = WARPS, NT = TX * TY;
+  static constexpr int RY = ROWS;  // rows per thread
+  static_assert(RY * VX < 32, "node masks are 32-bit");
   static constexpr int BX = TX * VX, BY = TY * RY;
   static constexpr int R = ORDER / 2;
   static constexpr int RZ = NDIM == 3 ? R : 0;
@@ -147,10 +148,11 @@ __device__ __forceinline__ int* heat_abort_flag() {
 // 0 = stage taken at run time with a separate u_n. Returns the pipeline state for the next
 // segment (by value, so it stays in registers), with s_issue = -1 if a wait timed out (the CTA
 // must then return).
-template <class T, int ORDER, int NDIM, bool TMA, int STAGE>
+template <class T, int ORDER, int NDIM, bool TMA, int STAGE, int ROWS = 2, int WARPS = 8>
 __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const HeatParams<T>& p, int x0, int y0, int zs,
                                              int ze, HeatPipe pipe) {
-  using C = HeatTile<T, ORDER, NDIM>;
+  using C = HeatTile<T, ORDER, NDIM, ROWS, WARPS>;
+  constexpr int RY = C::RY;
   using V = typename Vec16<T>::type;
   constexpr bool FAST = sizeof(T) == 4;
   constexpr int R = C::R, RZ = C::RZ, VX = C::VX, SW = C::SW;
@@ -166,7 +168,7 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
   const int stage = STAGE == 0 ? p.stage : STAGE;
   const T kx = p.kx, ky = p.ky, kz = p.kz, dt = p.dt;
   const int F = p.frozen;
-  T w[2 * RZ + 1][2][VX];  // register window along z (w[RZ] = centre plane), re-primed per segment
+  T w[2 * RZ + 1][RY][VX];  // register window along z (w[RZ] = centre plane), re-primed per segment
   const int Q = (ze - zs) + 2 * RZ;  // planes streamed for this segment
   const int p0 = zs - RZ;            // z of stream entry 0
 
@@ -197,13 +199,13 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
     for (int q = Q; q <= C::P; ++q) cp_async_commit();  // one group per plane index
 
   const int xb = x0 + tx * VX;  // first node of this thread
-  const int ya = y0 + 2 * ty;   // this thread's rows: ya, ya + 1
+  const int ya = y0 + RY * ty;  // this thread's rows: ya .. ya + RY - 1
   // Node classes of this thread's x-y positions, fixed over the segment (bit r*VX + e):
   // keep = not updated on interior planes (frozen layer or outside the grid),
   // edge = on the outermost x/y layer (written 0 under zero_boundary), inside = in the grid.
   unsigned keep = 0, edge = 0, inside = 0;
 #pragma unroll
-  for (int r = 0; r < 2; ++r)
+  for (int r = 0; r < RY; ++r)
 #pragma unroll
     for (int e = 0; e < VX; ++e) {
       const int x = xb + e, y = ya + r;
@@ -212,10 +214,12 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
       if (x == 0 || x == nx - 1 || y == 0 || y == ny - 1) edge |= bit;
       if (x < nx && y < ny) inside |= bit;
     }
-  constexpr unsigned ALL = (1u << (2 * VX)) - 1u;
+  constexpr unsigned ALL = (1u << (RY * VX)) - 1u;
   const bool warp_clean = __all_sync(0xffffffffu, keep == 0);   // no fix-ups on interior planes
   const bool warp_inside = __all_sync(0xffffffffu, inside == ALL);
-  const bool row_ok[2] = {ya < ny, ya + 1 < ny};
+  bool row_ok[RY];
+#pragma unroll
+  for (int r = 0; r < RY; ++r) row_ok[r] = ya + r < ny;
   const bool vec_rows = p.vec_ok && xb + VX <= nx;
   T* obase = p.out + (size_t)zs * sxy + (size_t)ya * nx + xb;  // output row pointer, plane zs
 
@@ -232,19 +236,19 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
     }
     parity ^= 1u << s_wait;
     const int s_cent = s_wait >= RZ ? s_wait - RZ : s_wait - RZ + C::NS;
-    const T* plq = ring + s_wait * C::SLOT_ELEMS + (2 * ty + R) * SW + C::PADX + tx * VX;
+    const T* plq = ring + s_wait * C::SLOT_ELEMS + (RY * ty + R) * SW + C::PADX + tx * VX;
     s_wait = s_wait + 1 == C::NS ? 0 : s_wait + 1;
     const bool warp_abort = __any_sync(0xffffffffu, !ok);  // shuffles below need all lanes
 
-    // ---- slide the window; push this thread's two rows of plane q
+    // ---- slide the window; push this thread's rows of plane q
 #pragma unroll
     for (int s = 0; s < 2 * RZ; ++s)
 #pragma unroll
-      for (int r = 0; r < 2; ++r)
+      for (int r = 0; r < RY; ++r)
 #pragma unroll
         for (int e = 0; e < VX; ++e) w[s][r][e] = w[s + 1][r][e];
 #pragma unroll
-    for (int r = 0; r < 2; ++r) {
+    for (int r = 0; r < RY; ++r) {
       const V v = *reinterpret_cast<const V*>(plq + r * SW);
 #pragma unroll
       for (int e = 0; e < VX; ++e) w[2 * RZ][r][e] = reinterpret_cast<const T*>(&v)[e];
@@ -252,11 +256,11 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
 
     if (q >= 2 * RZ && !warp_abort) {
       const int z = p0 + q - RZ;  // output plane (stream entry q - RZ)
-      const T* row0 = ring + s_cent * C::SLOT_ELEMS + (2 * ty + R) * SW + C::PADX + tx * VX;
-      // x-neighbourhood of both rows: xr[r][j] holds x = xb - R + j.
-      T xr[2][VX + 2 * R];
+      const T* row0 = ring + s_cent * C::SLOT_ELEMS + (RY * ty + R) * SW + C::PADX + tx * VX;
+      // x-neighbourhood of the thread's rows: xr[r][j] holds x = xb - R + j.
+      T xr[RY][VX + 2 * R];
 #pragma unroll
-      for (int r = 0; r < 2; ++r) {
+      for (int r = 0; r < RY; ++r) {
 #pragma unroll
         for (int e = 0; e < VX; ++e) xr[r][R + e] = w[RZ][r][e];
 #pragma unroll
@@ -269,27 +273,27 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
           xr[r][R + VX - 1 + d] = rgt;
         }
       }
-      // y-neighbourhood: yv[j][e] holds row ya - R + j (j = 0 .. 2R+1); rows ya, ya+1 are own.
-      T yv[2 * R + 2][VX];
+      // y-neighbourhood: yv[j][e] holds row ya - R + j (j = 0 .. 2R+RY-1); rows ya .. ya+RY-1
+      // are the thread's own.
+      T yv[2 * R + RY][VX];
 #pragma unroll
       for (int d = 1; d <= R; ++d) {
         const V a = *reinterpret_cast<const V*>(row0 - d * SW);
-        const V b = *reinterpret_cast<const V*>(row0 + (1 + d) * SW);
+        const V b = *reinterpret_cast<const V*>(row0 + (RY - 1 + d) * SW);
 #pragma unroll
         for (int e = 0; e < VX; ++e) {
           yv[R - d][e] = reinterpret_cast<const T*>(&a)[e];
-          yv[R + 1 + d][e] = reinterpret_cast<const T*>(&b)[e];
+          yv[R + RY - 1 + d][e] = reinterpret_cast<const T*>(&b)[e];
         }
       }
 #pragma unroll
-      for (int e = 0; e < VX; ++e) {
-        yv[R][e] = w[RZ][0][e];
-        yv[R + 1][e] = w[RZ][1][e];
-      }
+      for (int r = 0; r < RY; ++r)
+#pragma unroll
+        for (int e = 0; e < VX; ++e) yv[R + r][e] = w[RZ][r][e];
       const bool zin = NDIM == 2 || (z >= F && z < nz - F);
       // Every lane evaluates the stencil (halo values outside the grid are finite zero fill);
       // nodes that are not updated are fixed up afterwards with warp-uniform branches.
-      T res[2][VX];
+      T res[RY][VX];
       if constexpr (FAST && ORDER == 2) {
         // FP32 O2: node pairs (e, e+1) in paired instructions, the same operations lane by lane
         // (the O4 stencil stays scalar: paired it needs more registers than its occupancy allows)
@@ -298,7 +302,7 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
         const float2 kx2 = make_float2(kx, kx), ky2 = make_float2(ky, ky), kz2 = make_float2(kz, kz);
         const float2 dt2 = make_float2(dt, dt);
 #pragma unroll
-        for (int r = 0; r < 2; ++r)
+        for (int r = 0; r < RY; ++r)
 #pragma unroll
           for (int e = 0; e < VX; e += 2) {
             auto X = [&](int j) { return make_float2(xr[r][j], xr[r][j + 1]); };
@@ -323,7 +327,7 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
           }
       } else {
 #pragma unroll
-      for (int r = 0; r < 2; ++r)
+      for (int r = 0; r < RY; ++r)
 #pragma unroll
         for (int e = 0; e < VX; ++e) {
           const T c = w[RZ][r][e];
@@ -343,7 +347,7 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
       if (!zin) {  // frozen plane: copy, or zero on the outermost planes
         const bool zero_all = p.zero_boundary && NDIM == 3 && (z == 0 || z == nz - 1);
 #pragma unroll
-        for (int r = 0; r < 2; ++r)
+        for (int r = 0; r < RY; ++r)
 #pragma unroll
           for (int e = 0; e < VX; ++e) {
             const bool zb = zero_all || (p.zero_boundary && ((edge >> (r * VX + e)) & 1u));
@@ -351,7 +355,7 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
           }
       } else if (!warp_clean) {
 #pragma unroll
-        for (int r = 0; r < 2; ++r)
+        for (int r = 0; r < RY; ++r)
 #pragma unroll
           for (int e = 0; e < VX; ++e)
             if ((keep >> (r * VX + e)) & 1u)
@@ -359,7 +363,7 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
       }
       T* dst0 = obase + (size_t)(q - 2 * RZ) * sxy;
 #pragma unroll
-      for (int r = 0; r < 2; ++r) {
+      for (int r = 0; r < RY; ++r) {
         if (!row_ok[r]) continue;
         T* dst = dst0 + (size_t)r * nx;
         if (vec_rows) {
@@ -392,10 +396,16 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
   return HeatPipe{s_issue, s_wait, parity};
 }
 
-template <class T, int ORDER, int NDIM, bool TMA, int STAGE>
-__global__ void __launch_bounds__(256, ORDER == 2 ? 4 : (sizeof(T) == 4 ? 3 : 2))
+// Resident CTAs per SM the register budget is sized for.
+template <class T, int ORDER, int ROWS, int WARPS>
+constexpr int heat_min_ctas() {
+  return ROWS > 2 ? 16 / WARPS : (ORDER == 2 ? 4 : (sizeof(T) == 4 ? 3 : 2));
+}
+
+template <class T, int ORDER, int NDIM, bool TMA, int STAGE, int ROWS = 2, int WARPS = 8>
+__global__ void __launch_bounds__(32 * WARPS, heat_min_ctas<T, ORDER, ROWS, WARPS>())
 heat_stage_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ HeatParams<T> p) {
-  using C = HeatTile<T, ORDER, NDIM>;
+  using C = HeatTile<T, ORDER, NDIM, ROWS, WARPS>;
   uint64_t* bars = heat_bars<T, ORDER, NDIM>();
   int& abort_flag = *heat_abort_flag();
   const int tid = threadIdx.y * C::TX + threadIdx.x;
@@ -419,7 +429,7 @@ heat_stage_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constan
     const int ze = (int)min((int64_t)p.nz, zs + (seg_b - pos));
     pos += ze - zs;
     const int x0 = (int)(tile % p.tiles_x) * C::BX, y0 = (int)(tile / p.tiles_x) * C::BY;
-    pipe = heat_segment<T, ORDER, NDIM, TMA, STAGE>(&tmap, p, x0, y0, zs, ze, pipe);
+    pipe = heat_segment<T, ORDER, NDIM, TMA, STAGE, ROWS, WARPS>(&tmap, p, x0, y0, zs, ze, pipe);
     if (pipe.s_issue < 0) return;
   }
 }
