@@ -126,6 +126,31 @@ __device__ __forceinline__ T combine(int stage, T un, T uin, T dt, T L) {
   return fma_rn(dt, L, un);
 }
 
+// Bitwise helpers on the representation of a 4- or 8-byte value (masks are 32-bit all-ones or
+// zero; an 8-byte value applies the mask to both halves).
+template <class T>
+__device__ __forceinline__ T bit_and(T v, unsigned m) {
+  if constexpr (sizeof(T) == 4) {
+    return __uint_as_float(__float_as_uint(v) & m);
+  } else {
+    const unsigned long long mm = ((unsigned long long)m << 32) | m;
+    return __longlong_as_double((long long)((unsigned long long)__double_as_longlong(v) & mm));
+  }
+}
+// m ? a : b per bit
+template <class T>
+__device__ __forceinline__ T bit_select(unsigned m, T a, T b) {
+  if constexpr (sizeof(T) == 4) {
+    const unsigned ua = __float_as_uint(a), ub = __float_as_uint(b);
+    return __uint_as_float((ua & m) | (ub & ~m));
+  } else {
+    const unsigned long long mm = ((unsigned long long)m << 32) | m;
+    const unsigned long long ua = (unsigned long long)__double_as_longlong(a);
+    const unsigned long long ub = (unsigned long long)__double_as_longlong(b);
+    return __longlong_as_double((long long)((ua & mm) | (ub & ~mm)));
+  }
+}
+
 // Shared-memory pipeline of one CTA, carried across the segments it processes.
 struct HeatPipe {
   int s_issue, s_wait;  // ring slots of the next plane to issue / to wait for
@@ -201,26 +226,48 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
   const int xb = x0 + tx * VX;  // first node of this thread
   const int ya = y0 + RY * ty;  // this thread's rows: ya .. ya + RY - 1
   // Node classes of this thread's x-y positions, fixed over the segment (bit r*VX + e):
-  // keep = not updated on interior planes (frozen layer or outside the grid),
   // edge = on the outermost x/y layer (written 0 under zero_boundary), inside = in the grid.
-  unsigned keep = 0, edge = 0, inside = 0;
+  // Not updated on interior planes: the rows of a frozen y layer (rowkeep, bit r) and the
+  // elements of a frozen x layer (xkeep, bit e; only the lanes at the x ends of the grid).
+  unsigned edge = 0, inside = 0, rowkeep = 0, xkeep = 0;
 #pragma unroll
-  for (int r = 0; r < RY; ++r)
+  for (int r = 0; r < RY; ++r) {
+    const int y = ya + r;
+    if (!(y >= F && y < ny - F)) rowkeep |= 1u << r;
 #pragma unroll
     for (int e = 0; e < VX; ++e) {
-      const int x = xb + e, y = ya + r;
+      const int x = xb + e;
       const unsigned bit = 1u << (r * VX + e);
-      if (!(x >= F && x < nx - F && y >= F && y < ny - F)) keep |= bit;
       if (x == 0 || x == nx - 1 || y == 0 || y == ny - 1) edge |= bit;
       if (x < nx && y < ny) inside |= bit;
     }
+  }
+  // x fix-up as bit selects on the stencil result: kx_m[e] all ones on a frozen x element,
+  // kx_w[e] all ones where that element keeps its input value (zero there under zero_boundary
+  // on the outermost layer). Rows of a frozen y layer are fixed separately (rare warps).
+  unsigned kx_m[VX], kx_w[VX];
+#pragma unroll
+  for (int e = 0; e < VX; ++e) {
+    const int x = xb + e;
+    const bool k = !(x >= F && x < nx - F);
+    const bool z = p.zero_boundary && (x == 0 || x == nx - 1);
+    if (k) xkeep |= 1u << e;
+    kx_m[e] = k ? 0xffffffffu : 0u;
+    kx_w[e] = (k && !z) ? 0xffffffffu : 0u;
+  }
   constexpr unsigned ALL = (1u << (RY * VX)) - 1u;
-  const bool warp_clean = __all_sync(0xffffffffu, keep == 0);   // no fix-ups on interior planes
+  const bool warp_x_clean = __all_sync(0xffffffffu, xkeep == 0);
+  // the common case (one frozen x layer, rows a multiple of the vector): only the first and last
+  // element of a lane's vector can be frozen
+  const bool warp_x_ends = __all_sync(0xffffffffu, (xkeep & ~(1u | (1u << (VX - 1)))) == 0);
+  const bool warp_rows_clean = __all_sync(0xffffffffu, rowkeep == 0);
   const bool warp_inside = __all_sync(0xffffffffu, inside == ALL);
   bool row_ok[RY];
 #pragma unroll
   for (int r = 0; r < RY; ++r) row_ok[r] = ya + r < ny;
   const bool vec_rows = p.vec_ok && xb + VX <= nx;
+  // every lane stores whole vectors of existing rows: one uniform branch instead of one per row
+  const bool warp_vec_store = __all_sync(0xffffffffu, vec_rows && ya + RY - 1 < ny);
   T* obase = p.out + (size_t)zs * sxy + (size_t)ya * nx + xb;  // output row pointer, plane zs
 
 #pragma unroll 1
@@ -228,7 +275,8 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
     // ---- wait for plane q
     bool ok = true;
     if (TMA) {
-      ok = mbar_wait_warp(&bars[s_wait], (parity >> s_wait) & 1u, p.status, tx);
+      // every lane waits on the barrier itself (converged: same barrier, same phase)
+      ok = mbar_wait_bounded(&bars[s_wait], (parity >> s_wait) & 1u, p.status);
       if (!ok) *abort_flag = 1;
     } else {
       cp_async_wait<C::P>();
@@ -353,15 +401,41 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
             const bool zb = zero_all || (p.zero_boundary && ((edge >> (r * VX + e)) & 1u));
             res[r][e] = zb ? T(0) : w[RZ][r][e];
           }
-      } else if (!warp_clean) {
+      } else {
+        if (!warp_x_clean) {  // frozen x elements: res = kx_m ? (w & kx_w) : res, bitwise
+          if (warp_x_ends) {
 #pragma unroll
-        for (int r = 0; r < RY; ++r)
+            for (int r = 0; r < RY; ++r) {
+              res[r][0] = bit_select<T>(kx_m[0], bit_and<T>(w[RZ][r][0], kx_w[0]), res[r][0]);
+              res[r][VX - 1] = bit_select<T>(kx_m[VX - 1], bit_and<T>(w[RZ][r][VX - 1], kx_w[VX - 1]), res[r][VX - 1]);
+            }
+          } else {
 #pragma unroll
-          for (int e = 0; e < VX; ++e)
-            if ((keep >> (r * VX + e)) & 1u)
-              res[r][e] = (p.zero_boundary && ((edge >> (r * VX + e)) & 1u)) ? T(0) : w[RZ][r][e];
+            for (int r = 0; r < RY; ++r)
+#pragma unroll
+              for (int e = 0; e < VX; ++e)
+                res[r][e] = bit_select<T>(kx_m[e], bit_and<T>(w[RZ][r][e], kx_w[e]), res[r][e]);
+          }
+        }
+        if (!warp_rows_clean) {  // rows of a frozen y layer: copy, or zero on the edges
+#pragma unroll
+          for (int r = 0; r < RY; ++r)
+            if ((rowkeep >> r) & 1u)
+#pragma unroll
+              for (int e = 0; e < VX; ++e)
+                res[r][e] = (p.zero_boundary && ((edge >> (r * VX + e)) & 1u)) ? T(0) : w[RZ][r][e];
+        }
       }
       T* dst0 = obase + (size_t)(q - 2 * RZ) * sxy;
+      if (warp_vec_store) {
+#pragma unroll
+        for (int r = 0; r < RY; ++r) {
+          V v;
+#pragma unroll
+          for (int e = 0; e < VX; ++e) reinterpret_cast<T*>(&v)[e] = res[r][e];
+          *reinterpret_cast<V*>(dst0 + (size_t)r * nx) = v;
+        }
+      } else
 #pragma unroll
       for (int r = 0; r < RY; ++r) {
         if (!row_ok[r]) continue;
