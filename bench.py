@@ -673,7 +673,7 @@ def main():
             heat_run(cfg, uu, inner, ws, stream=sh)
         tuned = None if args.no_tune else autotune_heat(cfg, u, stream=sh)
         workload_name = "heat3d 256^3 f32 o2 euler r=1/8 dirichlet 8 blobs x 2000 steps"
-        kernel = "heat_stage_kernel<float,2,3,TMA>"
+        kernel = "heat_stage_kernel<float,2,3,TMA,stage 1,4 rows,4 warps>"
     else:
         n = 256
         cfg = BurgersConfig.periodic(n, weno="z", div=args.div)
