@@ -166,6 +166,9 @@ def cpu_heat_rate(cfg, u0, budget_s: float):
     return cfg.numel * steps / dt / 1e9, steps, dt
 
 
+# FP32 flops per cell-stage of the fused WENO5-Z stage (ncu instruction mix at 256^3, stage 1)
+BURGERS_FLOPS_PER_CELL_STAGE = 451.4
+
 ENSEMBLE_SEED = 2024
 ENSEMBLE_STEPS = 500
 
@@ -763,6 +766,21 @@ def main():
         torch.cuda.synchronize()
         extra["f64_value"] = cells_stages_per_step * 3 / (ev0.elapsed_time(ev1) * 1e-3) / 1e9
     elif args.workload == "burgers3d":
+        # ALU roofline: the stage is compute-bound. FP32 flops per cell-stage from the ncu
+        # instruction mix of the stage kernel (FFMA2 = 4, FADD2/FMUL2/FFMA = 2, FADD/FMUL = 1;
+        # profiles/burgers_stage_burgers3d_256_f32_ncu.md); peak = nominal FP32 CUDA-core rate.
+        sm_mhz = 2070.0
+        try:
+            sm_mhz = float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text()).get("sm_max_mhz", sm_mhz))
+        except Exception:
+            pass
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        fp32_peak = sms * 128 * 2 * sm_mhz * 1e6 / 1e12
+        flops = BURGERS_FLOPS_PER_CELL_STAGE * cfg.numel / (launch_ms * 1e-3) / 1e12
+        extra["roofline_alu"] = {"bound": "fp32", "kernel": kernel, "achieved": flops, "peak": fp32_peak,
+                                 "unit": "TFLOP/s", "frac": flops / fp32_peak,
+                                 "peak_source": f"nominal: {sms} SMs x 128 FP32 lanes x 2 flop x {sm_mhz:.0f} MHz",
+                                 "flops_per_cell_stage": BURGERS_FLOPS_PER_CELL_STAGE}
         # FP64 state, same problem: the reference's operand order (bit-exact with the oracle) and
         # the common-denominator form (ADV_DIV_FAST), two steps each
         for key, div in (("f64_value", N.ADV_DIV_F32), ("f64_fast_value", N.ADV_DIV_FAST)):
