@@ -64,14 +64,16 @@ struct HeatLaunch {
   bool tma = false;
   int occ = 0;                   // resident CTAs per SM of the stage kernel (before any tuning cap)
   int rows = 2;                  // rows per thread
-  int warps = 8;                 // warps per CTA: tile height warps * rows
+  int warps = 8;                 // warps per CTA
+  int lanes = 32;                // lanes per row (16: two rows per warp); tile lanes*vector x (32*warps/lanes)*rows
   int tiles_x = 0, tiles_y = 0;  // x-y tiles; the grid is one wave of CTAs sharing the tile-planes
   dim3 grid, block;
   size_t smem = 0;
   CUtensorMap tmap_in;  // tensor map of u_in (re-encoded when the pointer changes)
 };
-// rows: rows per thread of the stage kernel (2 or 4), 0 = the library's choice.
-adv_status heat_prepare(const adv_heat_desc& d, const void* u_in, HeatLaunch* L, int rows = 0);
+// rows: rows per thread of the stage kernel (2 or 4), lanes: lanes per row (32 or 16); 0 = the
+// library's choice.
+adv_status heat_prepare(const adv_heat_desc& d, const void* u_in, HeatLaunch* L, int rows = 0, int lanes = 0);
 adv_status heat_launch(const adv_heat_desc& d, const HeatLaunch& L, int stage, const void* u_in,
                        const void* u_n, void* u_out, cudaStream_t s);
 adv_status heat_validate(const adv_heat_desc* d);

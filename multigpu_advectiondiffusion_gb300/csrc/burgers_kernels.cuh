@@ -523,7 +523,7 @@ burgers_batch_kernel(const BurgersBatchInst<T>* __restrict__ inst, int n_inst, i
   }
   for (int64_t pos = seg_a; pos < seg_b;) {
     while (i + 1 < n_inst && inst[i + 1].unit_begin <= pos) ++i;
-    const BurgersParams<T>& p = inst[i].p;
+    const BurgersParams<T> p = inst[i].p;  // a copy: registers, not reloads from the table
     const int64_t local = pos - inst[i].unit_begin;
     const int64_t inst_end = i + 1 < n_inst ? inst[i + 1].unit_begin : total_units;
     const int64_t tile = local / p.nz;

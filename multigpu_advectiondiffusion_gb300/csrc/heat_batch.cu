@@ -5,8 +5,24 @@
 
 namespace adv {
 
-// Kernel for (state type, order, TMA or cp.async loads, stage specialisation 1..3).
-void* heat_batch_kernel_for(int dtype, int order, bool tma, int stage_kind) {
+// Kernel for (state type, order, TMA or cp.async loads, stage specialisation 1..3, rows per
+// thread, lanes per row). Four rows per thread (4 warps; rows of 32 or 16 lanes) exist for FP32
+// O2 with TMA loads.
+void* heat_batch_kernel_for(int dtype, int order, bool tma, int stage_kind, int rows, int lanes) {
+  if (rows == 4) {
+    if (dtype != ADV_F32 || order != 2 || !tma) return nullptr;
+#define B4(L)                                                                                 \
+  switch (stage_kind) {                                                                       \
+    case 1: return reinterpret_cast<void*>(&heat_batch_kernel<float, 2, true, 1, 4, 4, L>);   \
+    case 2: return reinterpret_cast<void*>(&heat_batch_kernel<float, 2, true, 2, 4, 4, L>);   \
+    case 3: return reinterpret_cast<void*>(&heat_batch_kernel<float, 2, true, 3, 4, 4, L>);   \
+    default: return nullptr;                                                                  \
+  }
+    if (lanes == 16) { B4(16) }
+    B4(32)
+#undef B4
+  }
+  if (lanes != 32) return nullptr;
 #define HB(T, O, M, S) reinterpret_cast<void*>(&heat_batch_kernel<T, O, M, S>)
 #define HS(T, O, M)                  \
   switch (stage_kind) {              \

@@ -4,23 +4,23 @@
 namespace adv {
 
 // Kernel for (order, ndim, TMA or cp.async loads, stage specialisation, rows per thread, warps
-// per CTA). Four rows per thread (tiles 128 x 32 with 8 warps, 128 x 16 with 4) exist for the 3D
-// O2 stencil with TMA loads.
-void* heat_kernel_f32(int order, int ndim, bool tma, int stage_kind, int rows, int warps) {
+// per CTA, lanes per row). Four rows per thread with 4 warps exist for the 3D O2 stencil with TMA
+// loads, in rows of 32 lanes (tile 128 x 16) or 16 lanes (tile 64 x 32).
+void* heat_kernel_f32(int order, int ndim, bool tma, int stage_kind, int rows, int warps, int lanes) {
   if (rows == 4) {
-    if (order != 2 || ndim != 3 || !tma) return nullptr;
-#define R4(W)                                                                             \
-  switch (stage_kind) {                                                                   \
-    case 1: return reinterpret_cast<void*>(&heat_stage_kernel<float, 2, 3, true, 1, 4, W>); \
-    case 2: return reinterpret_cast<void*>(&heat_stage_kernel<float, 2, 3, true, 2, 4, W>); \
-    case 3: return reinterpret_cast<void*>(&heat_stage_kernel<float, 2, 3, true, 3, 4, W>); \
-    default: return reinterpret_cast<void*>(&heat_stage_kernel<float, 2, 3, true, 0, 4, W>); \
+    if (order != 2 || ndim != 3 || !tma || warps != 4) return nullptr;
+#define R4(L)                                                                                  \
+  switch (stage_kind) {                                                                        \
+    case 1: return reinterpret_cast<void*>(&heat_stage_kernel<float, 2, 3, true, 1, 4, 4, L>); \
+    case 2: return reinterpret_cast<void*>(&heat_stage_kernel<float, 2, 3, true, 2, 4, 4, L>); \
+    case 3: return reinterpret_cast<void*>(&heat_stage_kernel<float, 2, 3, true, 3, 4, 4, L>); \
+    default: return reinterpret_cast<void*>(&heat_stage_kernel<float, 2, 3, true, 0, 4, 4, L>); \
   }
-    if (warps == 4) { R4(4) }
-    R4(8)
+    if (lanes == 16) { R4(16) }
+    R4(32)
 #undef R4
   }
-  if (warps != 8) return nullptr;
+  if (warps != 8 || lanes != 32) return nullptr;
 #define HK(O, N, M, S) reinterpret_cast<void*>(&heat_stage_kernel<float, O, N, M, S>)
 #define HS(O, N, M)                                            \
   switch (stage_kind) {                                        \

@@ -4,8 +4,8 @@
 namespace adv {
 
 // Kernel for (order, ndim, TMA or cp.async loads, stage specialisation).
-void* heat_kernel_f64(int order, int ndim, bool tma, int stage_kind, int rows, int warps) {
-  if (rows != 2 || warps != 8) return nullptr;
+void* heat_kernel_f64(int order, int ndim, bool tma, int stage_kind, int rows, int warps, int lanes) {
+  if (rows != 2 || warps != 8 || lanes != 32) return nullptr;
 #define HK(O, N, M, S) reinterpret_cast<void*>(&heat_stage_kernel<double, O, N, M, S>)
 #define HS(O, N, M)                                            \
   switch (stage_kind) {                                        \

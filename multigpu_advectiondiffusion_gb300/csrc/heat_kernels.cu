@@ -7,8 +7,8 @@
 
 namespace adv {
 
-void* heat_kernel_f32(int order, int ndim, bool tma, int stage_kind, int rows, int warps);
-void* heat_kernel_f64(int order, int ndim, bool tma, int stage_kind, int rows, int warps);
+void* heat_kernel_f32(int order, int ndim, bool tma, int stage_kind, int rows, int warps, int lanes);
+void* heat_kernel_f64(int order, int ndim, bool tma, int stage_kind, int rows, int warps, int lanes);
 
 adv_status heat_validate(const adv_heat_desc* d) {
   if (!d) return set_error(ADV_ERR_INVALID_ARG, "heat: null descriptor");
@@ -28,21 +28,21 @@ adv_status heat_validate(const adv_heat_desc* d) {
 
 namespace {
 
-void* pick_kernel(int dtype, int order, int ndim, bool tma, int stage_kind, int rows, int warps) {
-  return dtype == ADV_F32 ? heat_kernel_f32(order, ndim, tma, stage_kind, rows, warps)
-                          : heat_kernel_f64(order, ndim, tma, stage_kind, rows, warps);
+void* pick_kernel(int dtype, int order, int ndim, bool tma, int stage_kind, const HeatLaunch& L) {
+  return dtype == ADV_F32 ? heat_kernel_f32(order, ndim, tma, stage_kind, L.rows, L.warps, L.lanes)
+                          : heat_kernel_f64(order, ndim, tma, stage_kind, L.rows, L.warps, L.lanes);
 }
 
-template <class T, int ORDER, int NDIM, int ROWS, int WARPS = 8>
+template <class T, int ORDER, int NDIM, int ROWS, int WARPS = 8, int LANES = 32>
 void tile_dims(int* bx, int* by, int* sw, int* sh, int* padx, int* r, size_t* smem) {
-  using C = HeatTile<T, ORDER, NDIM, ROWS, WARPS>;
+  using C = HeatTile<T, ORDER, NDIM, ROWS, WARPS, LANES>;
   *bx = C::BX; *by = C::BY; *sw = C::SW; *sh = C::SH; *padx = C::PADX; *r = C::R; *smem = C::SMEM;
 }
 
-void tile_for(int dtype, int order, int ndim, int rows, int warps, int* bx, int* by, int* sw, int* sh, int* padx,
+void tile_for(int dtype, int order, int ndim, int rows, int lanes, int* bx, int* by, int* sw, int* sh, int* padx,
               int* r, size_t* smem) {
-  if (rows == 4 && warps == 4) return tile_dims<float, 2, 3, 4, 4>(bx, by, sw, sh, padx, r, smem);
-  if (rows == 4) return tile_dims<float, 2, 3, 4, 8>(bx, by, sw, sh, padx, r, smem);
+  if (rows == 4 && lanes == 16) return tile_dims<float, 2, 3, 4, 4, 16>(bx, by, sw, sh, padx, r, smem);
+  if (rows == 4) return tile_dims<float, 2, 3, 4, 4, 32>(bx, by, sw, sh, padx, r, smem);
 #define TD(T, O, N) if (order == O && ndim == N) return tile_dims<T, O, N, 2>(bx, by, sw, sh, padx, r, smem);
   if (dtype == ADV_F32) { TD(float, 2, 3) TD(float, 4, 3) TD(float, 2, 2) TD(float, 4, 2) }
   else { TD(double, 2, 3) TD(double, 4, 3) TD(double, 2, 2) TD(double, 4, 2) }
@@ -53,7 +53,10 @@ void tile_for(int dtype, int order, int ndim, int rows, int warps, int* bx, int*
 
 int heat_tune_variant(const adv_heat_desc& d) { return d.dtype * 100 + d.order * 10 + d.ndim; }
 
-adv_status heat_prepare(const adv_heat_desc& d, const void* u_in, HeatLaunch* L, int rows) {
+// Fraction of a row's lanes that hold grid nodes when rows of nx nodes are cut into tiles bx wide.
+static double tile_use(int nx, int bx) { return (double)nx / ((double)((nx + bx - 1) / bx) * bx); }
+
+adv_status heat_prepare(const adv_heat_desc& d, const void* u_in, HeatLaunch* L, int rows, int lanes) {
   DeviceInfo di;
   adv_status st = device_info(&di);
   if (st != ADV_OK) return st;
@@ -69,17 +72,19 @@ adv_status heat_prepare(const adv_heat_desc& d, const void* u_in, HeatLaunch* L,
   if (rows == 4 && !rows4_ok) return set_error(ADV_ERR_UNSUPPORTED, "heat: 4 rows per thread need FP32 3D O2 with TMA");
   L->rows = rows == 0 ? (rows4_ok ? 4 : 2) : rows;
   L->warps = L->rows == 4 ? 4 : 8;
+  // rows of 16 lanes (tile 64 wide) where they waste clearly fewer lanes than rows of 32
+  L->lanes = L->rows == 4 ? (lanes != 0 ? lanes : (tile_use(d.nx, 64) > tile_use(d.nx, 128) + 0.02 ? 16 : 32)) : 32;
   int bx, by, sw, sh, padx, r;
   size_t smem;
-  tile_for(d.dtype, d.order, d.ndim, L->rows, L->warps, &bx, &by, &sw, &sh, &padx, &r, &smem);
-  L->block = dim3(32, (unsigned)L->warps, 1);
+  tile_for(d.dtype, d.order, d.ndim, L->rows, L->lanes, &bx, &by, &sw, &sh, &padx, &r, &smem);
+  L->block = dim3((unsigned)L->lanes, (unsigned)(32 * L->warps / L->lanes), 1);
   const int tiles_x = (d.nx + bx - 1) / bx, tiles_y = (d.ny + by - 1) / by;
   for (int sk = 0; sk <= 3; ++sk) {
-    void* k = pick_kernel(d.dtype, d.order, d.ndim, L->tma, sk, L->rows, L->warps);
+    void* k = pick_kernel(d.dtype, d.order, d.ndim, L->tma, sk, *L);
     if (!k) return set_error(ADV_ERR_UNSUPPORTED, "heat: no kernel for this configuration");
     ADV_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   }
-  void* k0 = pick_kernel(d.dtype, d.order, d.ndim, L->tma, 1, L->rows, L->warps);
+  void* k0 = pick_kernel(d.dtype, d.order, d.ndim, L->tma, 1, *L);
   int occ = 0;
   ADV_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k0, 32 * L->warps, smem));
   occ = std::max(occ, 1);
@@ -120,7 +125,7 @@ static adv_status heat_launch_t(const adv_heat_desc& d, const HeatLaunch& L, int
                                 const void* u_n, void* u_out, cudaStream_t s) {
   HeatParams<T> p = heat_params<T>(d, L, stage, u_in, u_n, u_out);
   const int stage_kind = (stage == 1 && u_n != u_in) ? 0 : stage;
-  void* k = pick_kernel(d.dtype, d.order, d.ndim, L.tma, stage_kind, L.rows, L.warps);
+  void* k = pick_kernel(d.dtype, d.order, d.ndim, L.tma, stage_kind, L);
   void* args[] = {const_cast<CUtensorMap*>(&L.tmap_in), &p};
   ADV_CUDA_TRY(cudaLaunchKernel(k, L.grid, L.block, args, L.smem, s));
   count_launches(1);

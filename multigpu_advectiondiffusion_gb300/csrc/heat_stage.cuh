@@ -39,10 +39,13 @@ __device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fm
 __device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
 __device__ __forceinline__ float2 fma_rn(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 
-template <class T, int ORDER, int NDIM, int ROWS = 2, int WARPS = 8>
+// Tile: TX lanes per row (32, or 16 with two rows per warp) x one 16-byte vector each, RY rows per
+// thread, WARPS warps.
+template <class T, int ORDER, int NDIM, int ROWS = 2, int WARPS = 8, int LANES = 32>
 struct HeatTile {
   static constexpr int VX = 16 / (int)sizeof(T);  // nodes per thread along x (one 16-byte vector)
-  static constexpr int TX = 32, TY = WARPS, NT = TX * TY;
+  static constexpr int TX = LANES, NT = 32 * WARPS, TY = NT / TX;
+  static_assert(LANES == 32 || LANES == 16, "rows of 32 or 16 lanes");
   static constexpr int RY = ROWS;  // rows per thread
   static_assert(RY * VX < 32, "node masks are 32-bit");
   static constexpr int BX = TX * VX, BY = TY * RY;
@@ -173,10 +176,10 @@ __device__ __forceinline__ int* heat_abort_flag() {
 // 0 = stage taken at run time with a separate u_n. Returns the pipeline state for the next
 // segment (by value, so it stays in registers), with s_issue = -1 if a wait timed out (the CTA
 // must then return).
-template <class T, int ORDER, int NDIM, bool TMA, int STAGE, int ROWS = 2, int WARPS = 8>
+template <class T, int ORDER, int NDIM, bool TMA, int STAGE, int ROWS = 2, int WARPS = 8, int LANES = 32>
 __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const HeatParams<T>& p, int x0, int y0, int zs,
                                              int ze, HeatPipe pipe) {
-  using C = HeatTile<T, ORDER, NDIM, ROWS, WARPS>;
+  using C = HeatTile<T, ORDER, NDIM, ROWS, WARPS, LANES>;
   constexpr int RY = C::RY;
   using V = typename Vec16<T>::type;
   constexpr bool FAST = sizeof(T) == 4;
@@ -313,8 +316,8 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
         for (int e = 0; e < VX; ++e) xr[r][R + e] = w[RZ][r][e];
 #pragma unroll
         for (int d = 1; d <= R; ++d) {
-          T lft = __shfl_up_sync(0xffffffffu, w[RZ][r][VX - d], 1);
-          T rgt = __shfl_down_sync(0xffffffffu, w[RZ][r][d - 1], 1);
+          T lft = __shfl_up_sync(0xffffffffu, w[RZ][r][VX - d], 1, C::TX);
+          T rgt = __shfl_down_sync(0xffffffffu, w[RZ][r][d - 1], 1, C::TX);
           if (tx == 0) lft = row0[r * SW - d];
           if (tx == C::TX - 1) rgt = row0[r * SW + VX - 1 + d];
           xr[r][R - d] = lft;
@@ -476,10 +479,10 @@ constexpr int heat_min_ctas() {
   return ROWS > 2 ? 16 / WARPS : (ORDER == 2 ? 4 : (sizeof(T) == 4 ? 3 : 2));
 }
 
-template <class T, int ORDER, int NDIM, bool TMA, int STAGE, int ROWS = 2, int WARPS = 8>
+template <class T, int ORDER, int NDIM, bool TMA, int STAGE, int ROWS = 2, int WARPS = 8, int LANES = 32>
 __global__ void __launch_bounds__(32 * WARPS, heat_min_ctas<T, ORDER, ROWS, WARPS>())
 heat_stage_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ HeatParams<T> p) {
-  using C = HeatTile<T, ORDER, NDIM, ROWS, WARPS>;
+  using C = HeatTile<T, ORDER, NDIM, ROWS, WARPS, LANES>;
   uint64_t* bars = heat_bars<T, ORDER, NDIM>();
   int& abort_flag = *heat_abort_flag();
   const int tid = threadIdx.y * C::TX + threadIdx.x;
@@ -503,7 +506,7 @@ heat_stage_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constan
     const int ze = (int)min((int64_t)p.nz, zs + (seg_b - pos));
     pos += ze - zs;
     const int x0 = (int)(tile % p.tiles_x) * C::BX, y0 = (int)(tile / p.tiles_x) * C::BY;
-    pipe = heat_segment<T, ORDER, NDIM, TMA, STAGE, ROWS, WARPS>(&tmap, p, x0, y0, zs, ze, pipe);
+    pipe = heat_segment<T, ORDER, NDIM, TMA, STAGE, ROWS, WARPS, LANES>(&tmap, p, x0, y0, zs, ze, pipe);
     if (pipe.s_issue < 0) return;
   }
 }
@@ -523,11 +526,11 @@ struct alignas(64) HeatBatchInst {
 // z-plane) of all instances, instance-major then tile-major, are cut into gridDim.x equal
 // contiguous ranges. Returns at once when *active == 0 (predicated steps of a device-driven
 // loop).
-template <class T, int ORDER, bool TMA, int STAGE>
-__global__ void __launch_bounds__(256, ORDER == 2 ? 4 : (sizeof(T) == 4 ? 3 : 2))
+template <class T, int ORDER, bool TMA, int STAGE, int ROWS = 2, int WARPS = 8, int LANES = 32>
+__global__ void __launch_bounds__(32 * WARPS, heat_min_ctas<T, ORDER, ROWS, WARPS>())
 heat_batch_kernel(const HeatBatchInst<T>* __restrict__ inst, int n_inst, int64_t total_units, int slot,
                   const int* active) {
-  using C = HeatTile<T, ORDER, 3>;
+  using C = HeatTile<T, ORDER, 3, ROWS, WARPS, LANES>;
   if (active && *active == 0) return;
   uint64_t* bars = heat_bars<T, ORDER, 3>();
   int& abort_flag = *heat_abort_flag();
@@ -554,7 +557,7 @@ heat_batch_kernel(const HeatBatchInst<T>* __restrict__ inst, int n_inst, int64_t
   }
   for (int64_t pos = seg_a; pos < seg_b;) {
     while (i + 1 < n_inst && inst[i + 1].unit_begin <= pos) ++i;
-    const HeatParams<T>& p = inst[i].p[slot];
+    const HeatParams<T> p = inst[i].p[slot];  // a copy: registers, not reloads from the table
     const int64_t local = pos - inst[i].unit_begin;
     const int64_t inst_end = i + 1 < n_inst ? inst[i + 1].unit_begin : total_units;
     const int64_t tile = local / p.nz;
@@ -565,7 +568,7 @@ heat_batch_kernel(const HeatBatchInst<T>* __restrict__ inst, int n_inst, int64_t
     const int x0 = (int)(tile % p.tiles_x) * C::BX, y0 = (int)(tile / p.tiles_x) * C::BY;
     const CUtensorMap* tm = &inst[i].tmap[slot];
     if (TMA && tid == 0) tma_prefetch_desc(tm);
-    pipe = heat_segment<T, ORDER, 3, TMA, STAGE>(tm, p, x0, y0, zs, ze, pipe);
+    pipe = heat_segment<T, ORDER, 3, TMA, STAGE, ROWS, WARPS, LANES>(tm, p, x0, y0, zs, ze, pipe);
     if (pipe.s_issue < 0) return;
   }
 }

@@ -20,7 +20,7 @@ def _t(a, cuda):
     return torch.from_numpy(np.ascontiguousarray(a)).to(cuda)
 
 
-SIZES3 = [(64, 40, 24), (37, 29, 23), (5, 6, 7), (130, 9, 17), (256, 12, 5)]
+SIZES3 = [(64, 40, 24), (37, 29, 23), (5, 6, 7), (130, 9, 17), (256, 12, 5), (160, 50, 17), (192, 33, 40), (132, 70, 9)]
 SIZES2 = [(64, 40), (37, 29), (6, 5), (300, 17)]
 
 
