@@ -181,25 +181,23 @@ __device__ __forceinline__ BurgersPipe burgers_segment(const CUtensorMap* tmap, 
   const T dt = (T)(p.dt_dev ? *p.dt_dev : p.dt_host);
   const bool glob = p.lf_global != 0;
 
-  // This thread's share of the 1072 x/y faces of a plane: face f (f = tid + 256 r) is x-face f
-  // when f < NXF (row f / 33, face f % 33) or y-face g = f - NXF (face row g / 32, column
-  // g % 32). base: shared-memory index of the face's first stencil value; the other values
-  // follow at stride 1 (x) or SW (y).
-  int fbase[5];
-  bool fisx[5], fact[5];
-#pragma unroll
-  for (int r = 0; r < 5; ++r) {
-    const int f = tid + TL::NT * r;
-    fact[r] = f < TL::NXF + TL::NYF;
-    fisx[r] = f < TL::NXF;
-    if (fisx[r]) {
-      const int row = f / (TL::BX + 1), fi = f - row * (TL::BX + 1);
-      fbase[r] = (row + TL::R) * TL::SW + fi + 1;  // column of x0+fi-3
-    } else {
-      const int g = f - TL::NXF, fj = g / TL::BX, c = g - fj * TL::BX;
-      fbase[r] = fj * TL::SW + TL::PADX + c;  // row of y0+fj-3
-    }
-  }
+  // This thread's share of the 1072 x/y faces of a plane: x-faces tid and tid + 256 (of 528:
+  // face row f / 33, face f % 33), y-faces tid and tid + 256 (of 544: face row g / 32, column
+  // g % 32), and one of the 48 left over (x-faces 512..527 in warp 0, y-faces 512..543 in warp
+  // 1). base: shared-memory index of the face's first stencil value; the others follow at stride
+  // 1 (x) or SW (y), known at compile time per slot, so the loads take immediate offsets.
+  static_assert(TL::NXF - 2 * TL::NT == 16 && TL::NYF - 2 * TL::NT == 32, "face slots");
+  auto xbase = [](int f) {
+    const int row = f / (TL::BX + 1), fi = f - row * (TL::BX + 1);
+    return (row + TL::R) * TL::SW + fi + 1;  // column of x0+fi-3
+  };
+  auto ybase = [](int g) {
+    const int fj = g / TL::BX, c = g - fj * TL::BX;
+    return fj * TL::SW + TL::PADX + c;  // row of y0+fj-3
+  };
+  const int fbx0 = xbase(tid), fbx1 = xbase(tid + TL::NT), fby0 = ybase(tid), fby1 = ybase(tid + TL::NT);
+  const bool left_x = tid < 16, left_y = tid >= 32 && tid < 64;
+  const int fbl = left_x ? xbase(2 * TL::NT + tid) : ybase(2 * TL::NT + (left_y ? tid - 32 : 0));
   // Per-thread columns: (lane, warp) and (lane, warp + 8).
   const int cx = lane;
   const int cy0 = warp, cy1 = warp + 8;
@@ -262,7 +260,7 @@ __device__ __forceinline__ BurgersPipe burgers_segment(const CUtensorMap* tmap, 
     T* plq = ring + s_wait * SM::SLOT_ELEMS;
     const int s_cent = s_wait >= 3 ? s_wait - 3 : s_wait - 3 + TL::NS;  // slot of stream entry q - 3
     if (p.tma) {
-      if (!mbar_wait_warp(&bars[s_wait], (parity >> s_wait) & 1u, p.status, lane)) *abort_flag = 1;
+      if (!mbar_wait_bounded(&bars[s_wait], (parity >> s_wait) & 1u, p.status)) *abort_flag = 1;  // every lane waits (converged)
       if (edge) {
         // Periodic edge tile: the TMA box zero-filled what lies outside the domain; fill it with
         // the wrapped neighbours. Written here, read only after the next barrier.
@@ -362,37 +360,35 @@ __device__ __forceinline__ BurgersPipe burgers_segment(const CUtensorMap* tmap, 
         }
         __syncthreads();
         // x- and y-faces of the plane, this thread's precomputed share
+        auto face1 = [&](int b, auto stride) {
+          constexpr int st = decltype(stride)::value;
+          return Face<T, Z, D>::f(fpS[b], fpS[b + st], fpS[b + 2 * st], fpS[b + 3 * st], fpS[b + 4 * st],
+                                  fmS[b + st], fmS[b + 2 * st], fmS[b + 3 * st], fmS[b + 4 * st], fmS[b + 5 * st]);
+        };
+        using X1 = std::integral_constant<int, 1>;
+        using YS = std::integral_constant<int, TL::SW>;
         if constexpr (sizeof(T) == 4) {
-          // slots 0..3 are live for every thread (1072 faces >= 4 * 256): pairs (0, 1), (2, 3)
-          static_assert(TL::NXF + TL::NYF >= 4 * TL::NT && TL::NXF + TL::NYF <= 5 * TL::NT, "face slots");
-#pragma unroll
-          for (int r = 0; r < 4; r += 2) {
-            const int b0 = fbase[r], b1 = fbase[r + 1];
-            const int s0 = fisx[r] ? 1 : TL::SW, s1 = fisx[r + 1] ? 1 : TL::SW;
-            auto P = [&](int k) { return make_float2(fpS[b0 + k * s0], fpS[b1 + k * s1]); };
-            auto M = [&](int k) { return make_float2(fmS[b0 + k * s0], fmS[b1 + k * s1]); };
-            const float2 f = Face<T, Z, D>::f2(P(0), P(1), P(2), P(3), P(4), M(1), M(2), M(3), M(4), M(5));
-            fxS[tid + TL::NT * r] = f.x;
-            fxS[tid + TL::NT * (r + 1)] = f.y;
-          }
-          if (fact[4]) {
-            const int b = fbase[4];
-            const int st = fisx[4] ? 1 : TL::SW;
-            fxS[tid + TL::NT * 4] = Face<T, Z, D>::f(fpS[b], fpS[b + st], fpS[b + 2 * st], fpS[b + 3 * st],
-                                                     fpS[b + 4 * st], fmS[b + st], fmS[b + 2 * st], fmS[b + 3 * st],
-                                                     fmS[b + 4 * st], fmS[b + 5 * st]);
-          }
+          // two faces per paired FP32 instruction: (x tid, x tid + 256), (y tid, y tid + 256)
+          auto face2 = [&](int b0, int b1, auto stride) {
+            constexpr int st = decltype(stride)::value;
+            auto P = [&](int k) { return make_float2(fpS[b0 + k * st], fpS[b1 + k * st]); };
+            auto M = [&](int k) { return make_float2(fmS[b0 + k * st], fmS[b1 + k * st]); };
+            return Face<T, Z, D>::f2(P(0), P(1), P(2), P(3), P(4), M(1), M(2), M(3), M(4), M(5));
+          };
+          const float2 fx = face2(fbx0, fbx1, X1{});
+          fxS[tid] = fx.x;
+          fxS[tid + TL::NT] = fx.y;
+          const float2 fy = face2(fby0, fby1, YS{});
+          fxS[TL::NXF + tid] = fy.x;
+          fxS[TL::NXF + tid + TL::NT] = fy.y;
         } else {
-#pragma unroll
-          for (int r = 0; r < 5; ++r) {
-            if (!fact[r]) continue;
-            const int b = fbase[r];
-            const int st = fisx[r] ? 1 : TL::SW;
-            fxS[tid + TL::NT * r] = Face<T, Z, D>::f(fpS[b], fpS[b + st], fpS[b + 2 * st], fpS[b + 3 * st],
-                                                     fpS[b + 4 * st], fmS[b + st], fmS[b + 2 * st], fmS[b + 3 * st],
-                                                     fmS[b + 4 * st], fmS[b + 5 * st]);
-          }
+          fxS[tid] = face1(fbx0, X1{});
+          fxS[tid + TL::NT] = face1(fbx1, X1{});
+          fxS[TL::NXF + tid] = face1(fby0, YS{});
+          fxS[TL::NXF + tid + TL::NT] = face1(fby1, YS{});
         }
+        if (left_x) fxS[2 * TL::NT + tid] = face1(fbl, X1{});
+        else if (left_y) fxS[TL::NXF + 2 * TL::NT + (tid - 32)] = face1(fbl, YS{});
         __syncthreads();
       }
       // ---- RHS, stage combine, store, max|u_out|
