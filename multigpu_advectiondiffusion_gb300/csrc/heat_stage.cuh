@@ -26,6 +26,8 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "adv_device.cuh"
 #include "adv_math.cuh"
 
@@ -273,8 +275,14 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
   const bool warp_vec_store = __all_sync(0xffffffffu, vec_rows && ya + RY - 1 < ny);
   T* obase = p.out + (size_t)zs * sxy + (size_t)ya * nx + xb;  // output row pointer, plane zs
 
-#pragma unroll 1
-  for (int q = 0; q < Q; ++q) {
+  // The z window is a ring of NW = 2 RZ + 1 plane slots: after ROT pushes, logical plane sl
+  // (0 = oldest) sits in slot (sl + ROT) % NW. With the plane loop unrolled NW times (O2 in 3D)
+  // ROT is a compile-time constant in each copy, so the window never moves between registers;
+  // otherwise the slots are shifted once per plane and ROT stays 0.
+  constexpr int NW = 2 * RZ + 1;
+  auto plane_step = [&](auto rot, int q) -> bool {
+    constexpr int ROT = decltype(rot)::value;
+    auto WS = [&](int sl) -> T (&)[RY][VX] { return w[(sl + ROT) % NW]; };
     // ---- wait for plane q
     bool ok = true;
     if (TMA) {
@@ -291,18 +299,12 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
     s_wait = s_wait + 1 == C::NS ? 0 : s_wait + 1;
     const bool warp_abort = __any_sync(0xffffffffu, !ok);  // shuffles below need all lanes
 
-    // ---- slide the window; push this thread's rows of plane q
-#pragma unroll
-    for (int s = 0; s < 2 * RZ; ++s)
-#pragma unroll
-      for (int r = 0; r < RY; ++r)
-#pragma unroll
-        for (int e = 0; e < VX; ++e) w[s][r][e] = w[s + 1][r][e];
+    // ---- push this thread's rows of plane q into the window's newest slot
 #pragma unroll
     for (int r = 0; r < RY; ++r) {
       const V v = *reinterpret_cast<const V*>(plq + r * SW);
 #pragma unroll
-      for (int e = 0; e < VX; ++e) w[2 * RZ][r][e] = reinterpret_cast<const T*>(&v)[e];
+      for (int e = 0; e < VX; ++e) WS(2 * RZ)[r][e] = reinterpret_cast<const T*>(&v)[e];
     }
 
     if (q >= 2 * RZ && !warp_abort) {
@@ -313,11 +315,11 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
 #pragma unroll
       for (int r = 0; r < RY; ++r) {
 #pragma unroll
-        for (int e = 0; e < VX; ++e) xr[r][R + e] = w[RZ][r][e];
+        for (int e = 0; e < VX; ++e) xr[r][R + e] = WS(RZ)[r][e];
 #pragma unroll
         for (int d = 1; d <= R; ++d) {
-          T lft = __shfl_up_sync(0xffffffffu, w[RZ][r][VX - d], 1, C::TX);
-          T rgt = __shfl_down_sync(0xffffffffu, w[RZ][r][d - 1], 1, C::TX);
+          T lft = __shfl_up_sync(0xffffffffu, WS(RZ)[r][VX - d], 1, C::TX);
+          T rgt = __shfl_down_sync(0xffffffffu, WS(RZ)[r][d - 1], 1, C::TX);
           if (tx == 0) lft = row0[r * SW - d];
           if (tx == C::TX - 1) rgt = row0[r * SW + VX - 1 + d];
           xr[r][R - d] = lft;
@@ -340,7 +342,7 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
 #pragma unroll
       for (int r = 0; r < RY; ++r)
 #pragma unroll
-        for (int e = 0; e < VX; ++e) yv[R + r][e] = w[RZ][r][e];
+        for (int e = 0; e < VX; ++e) yv[R + r][e] = WS(RZ)[r][e];
       const bool zin = NDIM == 2 || (z >= F && z < nz - F);
       // Every lane evaluates the stencil (halo values outside the grid are finite zero fill);
       // nodes that are not updated are fixed up afterwards with warp-uniform branches.
@@ -358,7 +360,7 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
           for (int e = 0; e < VX; e += 2) {
             auto X = [&](int j) { return make_float2(xr[r][j], xr[r][j + 1]); };
             auto Y = [&](int j) { return make_float2(yv[j][e], yv[j][e + 1]); };
-            auto W = [&](int j) { return make_float2(w[j][r][e], w[j][r][e + 1]); };
+            auto W = [&](int j) { return make_float2(WS(j)[r][e], WS(j)[r][e + 1]); };
             const float2 c = W(RZ);
             const float2 L = lap<float2, ORDER, NDIM, true>(
                 X(R + e - O1), X(R + e - 1), c, X(R + e + 1), X(R + e + O1), Y(R + r - O1), Y(R + r - 1),
@@ -381,12 +383,12 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
       for (int r = 0; r < RY; ++r)
 #pragma unroll
         for (int e = 0; e < VX; ++e) {
-          const T c = w[RZ][r][e];
+          const T c = WS(RZ)[r][e];
           const T L = lap<T, ORDER, NDIM, FAST>(
               xr[r][R + e - (R >= 2 ? 2 : 1)], xr[r][R + e - 1], c, xr[r][R + e + 1], xr[r][R + e + (R >= 2 ? 2 : 1)],
               yv[R + r - (R >= 2 ? 2 : 1)][e], yv[R + r - 1][e], yv[R + r + 1][e], yv[R + r + (R >= 2 ? 2 : 1)][e],
-              w[RZ >= 2 ? RZ - 2 : 0][r][e], w[RZ >= 1 ? RZ - 1 : 0][r][e], w[RZ + (RZ >= 1 ? 1 : 0)][r][e],
-              w[RZ + (RZ >= 2 ? 2 : 0)][r][e], kx, ky, kz);
+              WS(RZ >= 2 ? RZ - 2 : 0)[r][e], WS(RZ >= 1 ? RZ - 1 : 0)[r][e], WS(RZ + (RZ >= 1 ? 1 : 0))[r][e],
+              WS(RZ + (RZ >= 2 ? 2 : 0))[r][e], kx, ky, kz);
           T un = c;
           if (STAGE != 1) {
             const size_t off = (size_t)(q - 2 * RZ) * sxy + (size_t)r * nx + e;
@@ -402,22 +404,22 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
 #pragma unroll
           for (int e = 0; e < VX; ++e) {
             const bool zb = zero_all || (p.zero_boundary && ((edge >> (r * VX + e)) & 1u));
-            res[r][e] = zb ? T(0) : w[RZ][r][e];
+            res[r][e] = zb ? T(0) : WS(RZ)[r][e];
           }
       } else {
         if (!warp_x_clean) {  // frozen x elements: res = kx_m ? (w & kx_w) : res, bitwise
           if (warp_x_ends) {
 #pragma unroll
             for (int r = 0; r < RY; ++r) {
-              res[r][0] = bit_select<T>(kx_m[0], bit_and<T>(w[RZ][r][0], kx_w[0]), res[r][0]);
-              res[r][VX - 1] = bit_select<T>(kx_m[VX - 1], bit_and<T>(w[RZ][r][VX - 1], kx_w[VX - 1]), res[r][VX - 1]);
+              res[r][0] = bit_select<T>(kx_m[0], bit_and<T>(WS(RZ)[r][0], kx_w[0]), res[r][0]);
+              res[r][VX - 1] = bit_select<T>(kx_m[VX - 1], bit_and<T>(WS(RZ)[r][VX - 1], kx_w[VX - 1]), res[r][VX - 1]);
             }
           } else {
 #pragma unroll
             for (int r = 0; r < RY; ++r)
 #pragma unroll
               for (int e = 0; e < VX; ++e)
-                res[r][e] = bit_select<T>(kx_m[e], bit_and<T>(w[RZ][r][e], kx_w[e]), res[r][e]);
+                res[r][e] = bit_select<T>(kx_m[e], bit_and<T>(WS(RZ)[r][e], kx_w[e]), res[r][e]);
           }
         }
         if (!warp_rows_clean) {  // rows of a frozen y layer: copy, or zero on the edges
@@ -426,7 +428,7 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
             if ((rowkeep >> r) & 1u)
 #pragma unroll
               for (int e = 0; e < VX; ++e)
-                res[r][e] = (p.zero_boundary && ((edge >> (r * VX + e)) & 1u)) ? T(0) : w[RZ][r][e];
+                res[r][e] = (p.zero_boundary && ((edge >> (r * VX + e)) & 1u)) ? T(0) : WS(RZ)[r][e];
         }
       }
       T* dst0 = obase + (size_t)(q - 2 * RZ) * sxy;
@@ -465,10 +467,30 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
           s = s + 1 == C::NS ? 0 : s + 1;
         }
       }
-      return HeatPipe{-1, -1, 0u};
+      return false;
     }
     if (q + C::P + 1 < Q) issue(q + C::P + 1);
     else if (!TMA) cp_async_commit();
+      return true;
+  };
+  if constexpr (NW == 3) {
+#pragma unroll 1
+    for (int q = 0; q < Q; q += 3) {
+      if (!plane_step(std::integral_constant<int, 0>{}, q)) return HeatPipe{-1, -1, 0u};
+      if (q + 1 < Q && !plane_step(std::integral_constant<int, 1>{}, q + 1)) return HeatPipe{-1, -1, 0u};
+      if (q + 2 < Q && !plane_step(std::integral_constant<int, 2>{}, q + 2)) return HeatPipe{-1, -1, 0u};
+    }
+  } else {
+#pragma unroll 1
+    for (int q = 0; q < Q; ++q) {
+#pragma unroll
+      for (int sl = 0; sl < NW - 1; ++sl)
+#pragma unroll
+        for (int r = 0; r < RY; ++r)
+#pragma unroll
+          for (int e = 0; e < VX; ++e) w[sl][r][e] = w[sl + 1][r][e];
+      if (!plane_step(std::integral_constant<int, 0>{}, q)) return HeatPipe{-1, -1, 0u};
+    }
   }
   return HeatPipe{s_issue, s_wait, parity};
 }
