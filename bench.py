@@ -37,6 +37,32 @@ sys.path.insert(0, str(ROOT))
 L2_BYTES = 126 * 1024 * 1024
 
 
+def settle(step, seconds: float = 2.0, max_steps: int = 1000) -> None:
+    """Untimed steps until `seconds` of wall time have passed after the warm-up (clocks and
+    caches in their steady state before the timed region)."""
+    import torch
+    t_end = time.perf_counter() + seconds
+    for _ in range(max_steps):
+        step()
+        torch.cuda.synchronize()
+        if time.perf_counter() >= t_end:
+            break
+
+
+def prime_device(local: int) -> None:
+    """Creates and releases one CUDA context on this rank's GPU in a short-lived child process
+    before this process creates its own. Measured on freshly started boxes: when the benchmark
+    was the first process to use the GPU, its memory-bound kernels ran 35% slower for the whole
+    process (heat 497 vs 771 Gcell/s; the same code, shapes and clocks, and every later process
+    fast), and one earlier process that only created a context removed the difference."""
+    code = f"import torch; torch.zeros(1, device='cuda:{local}'); torch.cuda.synchronize()"
+    try:
+        subprocess.run([sys.executable, "-c", code], stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL,
+                       timeout=300, check=False)
+    except (OSError, subprocess.SubprocessError):
+        pass
+
+
 def max_over_ranks(x: float, device=None) -> float:
     """The largest of every rank's x (the job's time is its slowest replica's); x itself when the
     job has one rank or no process group."""
@@ -241,6 +267,7 @@ def bench_ensemble(args, world, rank, dev, stream, flush, lib):
     for _ in range(args.warmup):
         reset()
         one_step()
+    settle(one_step)
     uuid = None
     try:
         uuid = "GPU-" + str(torch.cuda.get_device_properties(dev).uuid)
@@ -250,7 +277,7 @@ def bench_ensemble(args, world, rank, dev, stream, flush, lib):
     # need K separate regions; the states stay bounded over repeated runs, so the runs continue).
     reset()
     with ClockSampler(uuid) as clk:
-        one_step()
+        settle(one_step, 1.0)  # the sampler's start-up (NVML) overlaps untimed work
         launches0 = lib.adv_kernel_launch_count()
         ms = timed(one_step, args.steps)
         launched = lib.adv_kernel_launch_count() - launches0
@@ -404,6 +431,7 @@ def bench_adjoint(args, world, rank, dev, lib):
 
     for _ in range(args.warmup):
         grad_burgers(u0, target)
+    settle(lambda: grad_burgers(u0, target))
     uuid = None
     try:
         uuid = "GPU-" + str(torch.cuda.get_device_properties(dev).uuid)
@@ -650,6 +678,9 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
 
+    if args.impl != "reference":
+        prime_device(local)
+
     if args.impl == "reference":
         run_reference_arm(args, world, rank)
         return
@@ -730,13 +761,14 @@ def main():
     # ---- device-resident value
     for _ in range(args.warmup):
         one_step(u)
+    settle(lambda: one_step(u))
     uuid = None
     try:
         uuid = "GPU-" + str(torch.cuda.get_device_properties(dev).uuid)
     except Exception:
         pass
     with ClockSampler(uuid) as clk:
-        one_step(u)  # bring the clocks back up after the sampler's start-up pause
+        settle(lambda: one_step(u), 1.0)  # the sampler's start-up (NVML) overlaps untimed work
         launches0 = lib.adv_kernel_launch_count()
         ms = timed(lambda: one_step(u), args.steps)
         launched = lib.adv_kernel_launch_count() - launches0
