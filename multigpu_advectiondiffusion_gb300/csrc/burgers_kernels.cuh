@@ -471,7 +471,7 @@ burgers_stage_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_cons
   using TL = BurgersTile;
   if (p.active && *p.active == 0) return;
   // Balanced split: the (tile, z-plane) pairs, tile-major, are cut into gridDim.x equal
-  // contiguous ranges (one wave of CTAs); a range crossing a tile boundary becomes segments.
+  // contiguous ranges (several waves of CTAs); a range crossing a tile boundary becomes segments.
   const int nz = p.nz;
   const int64_t total = (int64_t)p.tiles_x * p.tiles_y * nz;
   const int64_t seg_a = total * blockIdx.x / gridDim.x, seg_b = total * (blockIdx.x + 1) / gridDim.x;

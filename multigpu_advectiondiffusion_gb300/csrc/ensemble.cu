@@ -2,8 +2,9 @@
 // Burgers problems of uneven size advanced by one CUDA graph.
 //
 // Each member contributes its (tile, z-plane) units to one flat range per kind; a batched stage
-// launch is one wave of CTAs that cuts that range into equal contiguous shares, so small members
-// neither leave SMs idle nor pay a launch each (heat_batch_kernel, burgers_batch_kernel). The
+// launch cuts that range into equal contiguous shares, one per CTA (two waves of CTAs for heat,
+// eight for Burgers), so small members neither leave SMs idle nor pay a launch each
+// (heat_batch_kernel, burgers_batch_kernel). The
 // device tables hold, per member and per stage slot, the stage parameters and the tensor map of
 // the stage input. A run is one graph with two while-nodes that run concurrently: the heat loop
 // (a device counter) and the Burgers loop (per-member dt, Lax-Friedrichs constant and stop test,
@@ -376,6 +377,10 @@ adv_status create_impl(const adv_heat_member* heat, int n_heat, int scheme, cons
     ADV_CUDA_TRY(cudaFuncSetAttribute(e->burg_k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->burg_smem));
     e->burg_ctas = one_wave_ctas(e->burg_k, 256, e->burg_smem, e->sms, e->burg_units, &st);
     if (st != ADV_OK) return st;
+    // eight waves of equal shares: the batched WENO stage's per-pair cost varies across members
+    // and segments, and later waves balance it (measured on the 32-member Burgers batch: 198 ms
+    // per 30 steps with one wave, 177 with four, 169 with eight, 170 with sixteen)
+    e->burg_ctas = (int)std::max<int64_t>(1, std::min<int64_t>(8 * (int64_t)e->burg_ctas, e->burg_units / 4));
     e->h_states.resize((size_t)n_burgers);
   }
   return ADV_OK;
