@@ -478,7 +478,8 @@ adv_status adjoint_stage_t(const adv_burgers_desc& d, int stage, const void* v, 
   ADV_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, 256, smem));
   occ = std::max(occ, 1);
   const int64_t units = (int64_t)a.tiles_x * a.tiles_y * d.nz;
-  const int64_t ctas = std::max<int64_t>(1, std::min<int64_t>((int64_t)di.sms * occ, units / 8));
+  // four waves of equal shares, as the forward stage: later waves balance the uneven pair costs
+  const int64_t ctas = std::max<int64_t>(1, std::min<int64_t>(4 * (int64_t)di.sms * occ, units / 8));
   void* args[] = {&a};
   ADV_CUDA_TRY(cudaLaunchKernel(k, dim3((unsigned)ctas), dim3(256), args, smem, s));
   count_launches(1);
