@@ -58,7 +58,9 @@ struct BurgersTile {
   static constexpr int SW = BX + 2 * PADX;  // 40
   static constexpr int SH = BY + 2 * R;     // 22
   static constexpr int PLANE = SW * SH;     // 880
-  static constexpr int NS = 6;              // ring: planes k .. k+5 (k+3 consumed, 2 prefetched)
+  // ring: 7 slots; while plane q is consumed the slot of plane q-4 (the previous centre plane)
+  // is refilled with plane q+3, so two planes stay in flight ahead of the one awaited
+  static constexpr int NS = 7;
   static constexpr int P = 2;
   static constexpr int NXF = (BX + 1) * BY;  // x-faces
   static constexpr int NYF = BX * (BY + 1);  // y-faces
@@ -275,10 +277,26 @@ __device__ __forceinline__ BurgersPipe burgers_segment(const CUtensorMap* tmap, 
     } else {
       cp_async_wait<TL::P>();
     }
-    __syncthreads();  // plane q visible to all threads; abort_flag now uniform
+    // plane q visible to all threads; abort_flag uniform; and every read of stream entry q - 4
+    // (the centre plane of the previous iteration) is done, so its slot can be refilled
+    __syncthreads();
     const bool aborted = *abort_flag != 0;
     parity ^= 1u << s_wait;
     s_wait = s_wait + 1 == TL::NS ? 0 : s_wait + 1;
+    if (p.tma) {
+      if (aborted) {
+        // A wait expired: let the copies already issued (planes q+1 .. q+P) land before returning.
+        if (tid == 0) {
+          int sl = s_wait;
+          for (int m = q + 1; m < Q && m <= q + TL::P; ++m) {
+            mbar_wait_bounded(&bars[sl], (parity >> sl) & 1u, p.status);
+            sl = sl + 1 == TL::NS ? 0 : sl + 1;
+          }
+        }
+        return BurgersPipe{-1, -1, 0u};
+      }
+      if (q + TL::P + 1 < Q) issue(q + TL::P + 1);  // into the slot of entry q - 4
+    }
     // ---- z windows: push plane q for this thread's two columns
     {
       const T uq[2] = {plq[(cy0 + TL::R) * TL::SW + TL::PADX + cx], plq[(cy1 + TL::R) * TL::SW + TL::PADX + cx]};
@@ -443,19 +461,13 @@ __device__ __forceinline__ BurgersPipe burgers_segment(const CUtensorMap* tmap, 
       fz_prev[0] = fz_new[0];
       fz_prev[1] = fz_new[1];
     }
-    __syncthreads();  // stream entry q - 3 fully consumed
-    if (aborted) {
-      if (p.tma && tid == 0) {
-        int sl = s_wait;
-        for (int m = q + 1; m < Q && m <= q + TL::P; ++m) {
-          mbar_wait_bounded(&bars[sl], (parity >> sl) & 1u, p.status);
-          sl = sl + 1 == TL::NS ? 0 : sl + 1;
-        }
-      }
-      return BurgersPipe{-1, -1, 0u};
+    if (!p.tma) {
+      // cp.async: one commit group per plane index; the refill of entry q - 3's slot waits here
+      __syncthreads();  // stream entry q - 3 fully consumed
+      if (aborted) return BurgersPipe{-1, -1, 0u};
+      if (q + TL::P + 1 < Q) issue(q + TL::P + 1);
+      else cp_async_commit();
     }
-    if (q + TL::P + 1 < Q) issue(q + TL::P + 1);
-    else if (!p.tma) cp_async_commit();
   }
   if (p.maxabs_key) {
     kmax = warp_max(kmax);
