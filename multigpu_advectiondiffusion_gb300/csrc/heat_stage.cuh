@@ -5,16 +5,18 @@
 // (SingleGPU/Diffusion3d_baselineCode/kernels.cu:37-142, main.cpp:106-122;
 // SingleGPU/Diffusion2d/kernels.cu:36-88).
 //
-// Work layout. A tile is BX x 16 nodes of an x-y plane (BX = 32 lanes x one 16-byte vector);
-// each thread owns one vector in each of two adjacent rows. The grid is one wave of CTAs; the
-// (tile, z-plane) pairs, tile-major, are split into equal contiguous ranges, one per CTA, so every
-// SM gets the same work. A CTA streams its planes through a shared-memory ring: each plane of the
-// tile plus its stencil halo is copied by TMA (cp.async.bulk.tensor.3d, one mbarrier per slot;
-// the x start is rounded down to a 16-byte boundary, so the box is one vector wider per side).
-// z neighbours come from a per-thread register window sliding along z, y neighbours from 16-byte
-// shared-memory rows (the thread's own second row serves the first and vice versa), x neighbours
-// from the thread's own vector plus warp shuffles (lanes 0 and 31 read the halo from shared
-// memory). Each node is read from HBM once per stage and written once, with 16-byte stores.
+// Work layout. A tile is BX x BY nodes of an x-y plane: rows of LANES threads (32, or 16 with two
+// rows per warp) x one 16-byte vector each, every thread owning that vector in ROWS adjacent rows
+// (2 or 4), WARPS warps per CTA. The grid is one wave of CTAs; the (tile, z-plane) pairs,
+// tile-major, are split into equal contiguous ranges, one per CTA, so every SM gets the same
+// work. A CTA streams its planes through a shared-memory ring: each plane of the tile plus its
+// stencil halo is copied by TMA (cp.async.bulk.tensor.3d, one mbarrier per slot; the x start is
+// rounded down to a 16-byte boundary, so the box is one vector wider per side). z neighbours
+// come from a per-thread register window (a ring of slots addressed by constant index in an
+// unrolled plane loop), y neighbours from 16-byte shared-memory rows (the thread's own rows serve
+// each other), x neighbours from the thread's own vector plus warp shuffles (the first and last
+// lane of a row read the halo from shared memory). Each node is read from HBM once per stage and
+// written once, with 16-byte stores.
 // Row pitches TMA cannot describe (not a multiple of 16 bytes, e.g. the reference's 201-node rows)
 // take the same pipeline with cp.async element copies.
 //
