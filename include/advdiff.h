@@ -43,7 +43,7 @@ typedef enum adv_status {
   ADV_ERR_TIMEOUT = 3,     /* a bounded device-side wait gave up (status word) */
   ADV_ERR_NONFINITE = 4,   /* a NaN/Inf was seen in the state (max|u| reduction) */
   ADV_ERR_CFL = 5,         /* dt rule produced a non-positive or non-finite step */
-  ADV_ERR_UNSUPPORTED = 6, /* valid request this build does not implement */
+  ADV_ERR_UNSUPPORTED = 6, /* valid request this library does not implement */
   ADV_ERR_ALLOC = 7        /* host or device allocation failed */
 } adv_status;
 

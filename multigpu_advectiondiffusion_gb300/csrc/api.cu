@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "adv_internal.h"
+#include "nvtx_range.h"
 
 namespace adv {
 
@@ -278,6 +279,7 @@ const char* adv_status_string(adv_status s) {
 // ------------------------------------------------------------------------------ heat
 adv_status adv_heat_stage(const adv_heat_desc* d, int stage, const void* u_in, const void* u_n, void* u_out,
                           void* stream) {
+  ADV_NVTX_RANGE("adv_heat_stage");
   adv_status st = heat_validate(d);
   if (st != ADV_OK) return st;
   if (!u_in || !u_n || !u_out) return set_error(ADV_ERR_INVALID_ARG, "heat: null buffer");
@@ -302,6 +304,7 @@ adv_status adv_heat_workspace_bytes(const adv_heat_desc* d, int time_scheme, siz
 
 adv_status adv_heat_run(const adv_heat_desc* d, int time_scheme, int64_t nsteps, void* u, void* workspace,
                         void* stream) {
+  ADV_NVTX_RANGE("adv_heat_run");
   size_t ws = 0;
   adv_status st = adv_heat_workspace_bytes(d, time_scheme, &ws);
   if (st != ADV_OK) return st;
@@ -373,6 +376,7 @@ adv_status adv_heat_run(const adv_heat_desc* d, int time_scheme, int64_t nsteps,
 // --------------------------------------------------------------------------- Burgers
 adv_status adv_burgers_stage(const adv_burgers_desc* d, int stage, const void* u_in, const void* u_n, void* u_out,
                              double dt, double alpha, void* maxabs_out, void* stream) {
+  ADV_NVTX_RANGE("adv_burgers_stage");
   adv_status st = burgers_validate(d);
   if (st != ADV_OK) return st;
   if (!u_in || !u_n || !u_out) return set_error(ADV_ERR_INVALID_ARG, "burgers: null buffer");
@@ -412,6 +416,7 @@ adv_status adv_burgers_run(const adv_burgers_desc* d, void* u, void* workspace, 
 adv_status adv_burgers_resume(const adv_burgers_desc* d, void* u, void* workspace, double t0, int64_t step0,
                               double tEnd, double cfl, int dt_rule, double C, int64_t max_steps, double* t_out,
                               int64_t* steps_out, void* stream) {
+  ADV_NVTX_RANGE("adv_burgers_resume");
   adv_status st = burgers_validate(d);
   if (st != ADV_OK) return st;
   if (!u || !workspace) return set_error(ADV_ERR_INVALID_ARG, "burgers: null buffer");
@@ -536,6 +541,7 @@ adv_status adv_burgers_resume(const adv_burgers_desc* d, void* u, void* workspac
 
 // ------------------------------------------------------------------------ reduction
 adv_status adv_max_abs(int dtype, const void* u, int64_t n, double* out, void* stream) {
+  ADV_NVTX_RANGE("adv_max_abs");
   if (dtype != ADV_F32 && dtype != ADV_F64) return set_error(ADV_ERR_INVALID_ARG, "max_abs: bad dtype");
   if (!u || !out || n < 0) return set_error(ADV_ERR_INVALID_ARG, "max_abs: bad arguments");
   cudaStream_t s = static_cast<cudaStream_t>(stream);

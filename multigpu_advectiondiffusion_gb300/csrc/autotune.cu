@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "adv_internal.h"
+#include "nvtx_range.h"
 
 namespace adv {
 
@@ -157,6 +158,7 @@ using namespace adv;
 extern "C" {
 
 adv_status adv_autotune_heat(const adv_heat_desc* d, const void* u, void* stream, adv_tune_result* out) {
+  ADV_NVTX_RANGE("adv_autotune_heat");
   adv_status st = heat_validate(d);
   if (st != ADV_OK) return st;
   if (!u) return set_error(ADV_ERR_INVALID_ARG, "autotune: null buffer");
@@ -195,6 +197,7 @@ adv_status adv_autotune_heat(const adv_heat_desc* d, const void* u, void* stream
 }
 
 adv_status adv_autotune_burgers(const adv_burgers_desc* d, const void* u, void* stream, adv_tune_result* out) {
+  ADV_NVTX_RANGE("adv_autotune_burgers");
   adv_status st = burgers_validate(d);
   if (st != ADV_OK) return st;
   if (!u) return set_error(ADV_ERR_INVALID_ARG, "autotune: null buffer");
@@ -225,6 +228,7 @@ adv_status adv_autotune_burgers(const adv_burgers_desc* d, const void* u, void* 
 
 adv_status adv_autotune_heatk(const adv_heatk_desc* d, const void* k, const void* u, void* stream,
                               adv_tune_result* out_step, adv_tune_result* out_adjoint) {
+  ADV_NVTX_RANGE("adv_autotune_heatk");
   adv_status st = heatk_validate_desc(d);
   if (st != ADV_OK) return st;
   if (!k || !u) return set_error(ADV_ERR_INVALID_ARG, "autotune: null buffer");

@@ -26,6 +26,7 @@
 
 #include "adv_device.cuh"
 #include "adv_internal.h"
+#include "nvtx_range.h"
 #include "adv_math.cuh"
 
 namespace adv {
@@ -536,6 +537,7 @@ extern "C" {
 
 adv_status adv_burgers_adjoint_step(const adv_burgers_desc* d, const void* u_n, const void* u1, const void* u2,
                                     double dt, void* lam, void* work, void* stream) {
+  ADV_NVTX_RANGE("adv_burgers_adjoint_step");
   adv_status st = adjoint_validate(d);
   if (st != ADV_OK) return st;
   if (!u_n || !u1 || !u2 || !lam || !work) return set_error(ADV_ERR_INVALID_ARG, "burgers adjoint: null buffer");
@@ -558,6 +560,7 @@ adv_status adv_burgers_checkpoint_bytes(const adv_burgers_desc* d, int64_t nstep
 
 adv_status adv_burgers_forward(const adv_burgers_desc* d, void* u, double dt, int64_t nsteps, int64_t interval,
                                void* ckpt, void* work, void* stream) {
+  ADV_NVTX_RANGE("adv_burgers_forward");
   adv_status st = adjoint_validate(d);
   if (st != ADV_OK) return st;
   if (!u || !work) return set_error(ADV_ERR_INVALID_ARG, "burgers adjoint: null buffer");
@@ -577,6 +580,7 @@ adv_status adv_burgers_forward(const adv_burgers_desc* d, void* u, double dt, in
 
 adv_status adv_burgers_backward(const adv_burgers_desc* d, double dt, int64_t nsteps, int64_t interval,
                                 const void* ckpt, void* lam, void* work, void* stream) {
+  ADV_NVTX_RANGE("adv_burgers_backward");
   adv_status st = adjoint_validate(d);
   if (st != ADV_OK) return st;
   if (!ckpt || !lam || !work) return set_error(ADV_ERR_INVALID_ARG, "burgers adjoint: null buffer");

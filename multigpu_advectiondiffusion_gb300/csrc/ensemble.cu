@@ -17,6 +17,7 @@
 
 #include "burgers_launch.cuh"
 #include "heat_launch.cuh"
+#include "nvtx_range.h"
 
 namespace adv {
 void* heat_batch_kernel_for(int dtype, int order, bool tma, int stage_kind, int rows, int lanes);
@@ -398,6 +399,7 @@ extern "C" {
 
 adv_status adv_ensemble_create(const adv_heat_member* heat, int n_heat, int heat_time_scheme,
                                const adv_burgers_member* burgers, int n_burgers, adv_ensemble** out) {
+  ADV_NVTX_RANGE("adv_ensemble_create");
   if (!out) return set_error(ADV_ERR_INVALID_ARG, "ensemble: null output");
   *out = nullptr;
   adv_ensemble* e = new (std::nothrow) adv_ensemble();
@@ -412,6 +414,7 @@ adv_status adv_ensemble_create(const adv_heat_member* heat, int n_heat, int heat
 }
 
 adv_status adv_ensemble_run(adv_ensemble* e, int64_t heat_steps, int flags, void* stream) {
+  ADV_NVTX_RANGE("adv_ensemble_run");
   if (!e) return set_error(ADV_ERR_INVALID_ARG, "ensemble: null plan");
   if (heat_steps < 0) return set_error(ADV_ERR_INVALID_ARG, "ensemble: negative heat step count");
   if (flags & ~ADV_ENSEMBLE_DIRECT) return set_error(ADV_ERR_INVALID_ARG, "ensemble: unknown flags");

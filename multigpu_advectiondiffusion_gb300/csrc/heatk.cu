@@ -23,6 +23,7 @@
 #include <initializer_list>
 
 #include "adv_internal.h"
+#include "nvtx_range.h"
 #include "adv_math.cuh"
 
 namespace adv {
@@ -434,6 +435,7 @@ using namespace adv;
 extern "C" {
 
 adv_status adv_heatk_step(const adv_heatk_desc* d, const void* k, const void* u_in, void* u_out, void* stream) {
+  ADV_NVTX_RANGE("adv_heatk_step");
   adv_status st = heatk_validate(d);
   if (st != ADV_OK) return st;
   if (!k || !u_in || !u_out) return set_error(ADV_ERR_INVALID_ARG, "heatk: null buffer");
@@ -443,6 +445,7 @@ adv_status adv_heatk_step(const adv_heatk_desc* d, const void* k, const void* u_
 
 adv_status adv_heatk_adjoint_step(const adv_heatk_desc* d, const void* k, const void* u_n, const void* lam_next,
                                   void* lam_out, void* grad_k, void* stream) {
+  ADV_NVTX_RANGE("adv_heatk_adjoint_step");
   adv_status st = heatk_validate(d);
   if (st != ADV_OK) return st;
   if (!k || !u_n || !lam_next || !lam_out || !grad_k) return set_error(ADV_ERR_INVALID_ARG, "heatk: null buffer");
@@ -466,6 +469,7 @@ adv_status adv_heatk_checkpoint_bytes(const adv_heatk_desc* d, int64_t nsteps, i
 
 adv_status adv_heatk_forward(const adv_heatk_desc* d, const void* k, void* u, int64_t nsteps, int64_t interval,
                              void* ckpt, void* work, void* stream) {
+  ADV_NVTX_RANGE("adv_heatk_forward");
   adv_status st = heatk_validate(d);
   if (st != ADV_OK) return st;
   if (!k || !u || !work) return set_error(ADV_ERR_INVALID_ARG, "heatk: null buffer");
@@ -487,6 +491,7 @@ adv_status adv_heatk_forward(const adv_heatk_desc* d, const void* k, void* u, in
 
 adv_status adv_heatk_backward(const adv_heatk_desc* d, const void* k, int64_t nsteps, int64_t interval,
                               const void* ckpt, void* lam, void* grad_k, void* work, void* stream) {
+  ADV_NVTX_RANGE("adv_heatk_backward");
   adv_status st = heatk_validate(d);
   if (st != ADV_OK) return st;
   if (!k || !ckpt || !lam || !grad_k || !work) return set_error(ADV_ERR_INVALID_ARG, "heatk: null buffer");

@@ -6,6 +6,7 @@
 #include <string>
 
 #include "adv_internal.h"
+#include "nvtx_range.h"
 
 namespace adv {
 
@@ -38,6 +39,7 @@ using namespace adv;
 
 extern "C" adv_status adv_heat_run_noalloc(const adv_heat_desc* d, int time_scheme, int64_t nsteps, void* u,
                                            void* stream) {
+  ADV_NVTX_RANGE("adv_heat_run_noalloc");
   size_t need = 0;
   adv_status st = adv_heat_workspace_bytes(d, time_scheme, &need);
   if (st != ADV_OK) return st;

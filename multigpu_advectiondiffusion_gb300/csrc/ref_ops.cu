@@ -8,6 +8,7 @@
 
 #include "../../include/advdiff_ref_ops.h"
 #include "adv_internal.h"
+#include "nvtx_range.h"
 #include "adv_math.cuh"
 #include "weno.cuh"
 
@@ -151,6 +152,7 @@ extern "C" {
 
 adv_status adv_ref_laplace(int dtype, int ndim, int order, int lo, int zero_outside, int64_t pitch, int nx, int ny, int nz,
                            double kx, double ky, double kz, const void* u, void* Lu, void* stream) {
+  ADV_NVTX_RANGE("adv_ref_laplace");
   if (ndim == 2) nz = 1;
   adv_status st = check_grid(dtype, pitch, nx, ny, nz, u, Lu);
   if (st != ADV_OK) return st;
@@ -171,6 +173,7 @@ adv_status adv_ref_laplace(int dtype, int ndim, int order, int lo, int zero_outs
 
 adv_status adv_ref_rk(int dtype, int ndim, int lo, int64_t pitch, int nx, int ny, int nz, int step, double dt, void* u,
                       const void* uo, const void* Lu, void* stream) {
+  ADV_NVTX_RANGE("adv_ref_rk");
   if (ndim == 2) nz = 1;
   adv_status st = check_grid(dtype, pitch, nx, ny, nz, u, uo);
   if (st != ADV_OK) return st;
@@ -190,6 +193,7 @@ adv_status adv_ref_rk(int dtype, int ndim, int lo, int64_t pitch, int nx, int ny
 
 adv_status adv_ref_burgers_sweep(int dtype, int axis, int weno, int64_t pitch, int nx, int ny, int nz, double h,
                                  const void* u, void* Lu, void* stream) {
+  ADV_NVTX_RANGE("adv_ref_burgers_sweep");
   adv_status st = check_grid(dtype, pitch, nx, ny, nz, u, Lu);
   if (st != ADV_OK) return st;
   if (axis < 0 || axis > 2 || (weno != ADV_WENO5_JS && weno != ADV_WENO5_Z) || !(h != 0.0))
@@ -212,6 +216,7 @@ adv_status adv_ref_burgers_sweep(int dtype, int axis, int weno, int64_t pitch, i
 
 adv_status adv_ref_burgers_viscous(int dtype, int64_t pitch, int nx, int ny, int nz, double kx, double ky, double kz,
                                    int bug_b2, const void* u, void* Lu, void* stream) {
+  ADV_NVTX_RANGE("adv_ref_burgers_viscous");
   adv_status st = check_grid(dtype, pitch, nx, ny, nz, u, Lu);
   if (st != ADV_OK) return st;
   Grid3 g{nx, ny, nz, pitch};

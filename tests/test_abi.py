@@ -70,6 +70,25 @@ def test_invalid_descriptors_rejected_without_gpu(native):
     assert native.adv_burgers_workspace_bytes(C.byref(bd), C.byref(nb)) == N.ADV_ERR_INVALID_ARG
 
 
+def test_launching_entry_points_reject_bad_arguments_without_gpu(native):
+    """Each entry point that launches work opens its NVTX range, then validates its arguments
+    before any CUDA call: with no GPU the bad request still comes back as ADV_ERR_INVALID_ARG."""
+    bad = N.HeatDesc(4, 8, 8, 8, N.ADV_F32, 2, 1, 1, 1.0, 1.0, 1.0, 0.1)
+    assert native.adv_heat_run(C.byref(bad), N.ADV_EULER, 4, None, None, None) == N.ADV_ERR_INVALID_ARG
+    assert native.adv_heat_run_noalloc(C.byref(bad), N.ADV_EULER, 4, None, None) == N.ADV_ERR_INVALID_ARG
+    bd = N.BurgersDesc(4, 8, 8, N.ADV_F32, 1, 1, N.ADV_BC_PERIODIC, 0, 0, 0, 1.0, 1.0, 1.0, 0, 0, 0)
+    t, s = C.c_double(0.0), C.c_int64(0)
+    assert native.adv_burgers_run(C.byref(bd), None, None, 1.0, 0.5, N.ADV_DT_FIXED, 0.0, 10, C.byref(t),
+                                  C.byref(s), None) == N.ADV_ERR_INVALID_ARG
+    assert b"at least 6 cells" in native.adv_last_error_string()
+    out = C.c_double(0.0)
+    assert native.adv_max_abs(99, None, 4, C.byref(out), None) == N.ADV_ERR_INVALID_ARG
+    assert native.adv_ref_laplace(99, 3, 2, 1, 0, 8, 8, 8, 8, 1.0, 1.0, 1.0, None, None, None) == N.ADV_ERR_INVALID_ARG
+    # repeated calls: the ranges push and pop in pairs, nothing accumulates
+    for _ in range(1000):
+        assert native.adv_max_abs(99, None, 4, C.byref(out), None) == N.ADV_ERR_INVALID_ARG
+
+
 def test_ensemble_argument_checks_without_gpu(native):
     out = C.c_void_p(None)
     assert native.adv_ensemble_create(None, 0, N.ADV_EULER, None, 0, C.byref(out)) == N.ADV_ERR_INVALID_ARG
