@@ -16,7 +16,10 @@
 //   * recorded "Final Time" 0.325 / 0.329157 (SingleGPU/Diffusion2d/Run.m:11,
 //     SingleGPU/Diffusion3d_baselineCode/Run.m:11) via the reference dt rule;
 //   * recorded iteration counts 86 / 167 / 267 of the Burgers dt loop
-//     (SingleGPU/Burgers3d_WENO5/Run.m:24,36; SingleGPU/Burgers3d_WENO5_Hybrid2/Run.m:12).
+//     (SingleGPU/Burgers3d_WENO5/Run.m:24,36; SingleGPU/Burgers3d_WENO5_Hybrid2/Run.m:12);
+//   * the MATLAB Burgers prototypes (WENO5 / WENO7 residuals and solver loops of
+//     Matlab_Prototipes/InviscidBurgersNd), whose outputs were produced by running those .m
+//     files through an interpreter for their MATLAB subset (tests/test_oracle_prototypes.py).
 //
 // Built with -ffp-contract=off so x86 and Arm hosts give bitwise identical results.
 
@@ -584,6 +587,174 @@ void burgers_step_adjoint(const BurgersCfg& c, const T* un, const T* u1, const T
   for (size_t o = 0; o < n; ++o) lam[o] = acc[o] + t[o];
 }
 
+// ------------------------------------------------------------------------------------------
+// The MATLAB prototypes of the inviscid Burgers solver (Matlab_Prototipes/InviscidBurgersNd),
+// restated: the residual functions WENO{5,7}resAdv_{X,Y,Z}.m / WENO{5,7}resAdv1d.m and the
+// solver loops of LFWENO{5,7}FDM{1,2,3}d.m. Flux f = u^2/2 (the drivers' 'burgers' case).
+//   * Split f+- = (f +- a u)/2 with a = |u| at every node (the X/Y/Z files) or a = max|u| of
+//     the line (the 1d files).
+//   * Along each axis the line is extended by copies of its end values (2 left / 3 right for
+//     WENO5, 3 left / 4 right for WENO7: a clamped index); fluxes are formed at the faces
+//     i+1/2, i = 0..N-1, and the face left of cell 0 is taken as 0, so
+//     res_i = (F_{i+1/2} - F_{i-1/2}) / h with F_{-1/2} = 0 (WENO7resAdv_X.m:56-58, 148).
+//   * WENO5: Jiang-Shu weights, the same candidate stencils as the CUDA code (weno_face).
+//   * WENO7: the seven-point WENO of Balsara & Shu (J. Comput. Phys. 160 (2000) 405-452):
+//     four cubic candidates with linear weights 1/35, 12/35, 18/35, 4/35 and weights
+//     d_k / (eps + beta_k)^2, eps = 1e-6; the smoothness indicators are the prototype's
+//     integer quadratic forms (WENO7resAdv_X.m:75-82).
+//   * Time loops: dt = CFL dx / max|u| trimmed to land on tEnd; WENO5 with SSP-RK3, WENO7 with
+//     the five-stage, fourth-order low-storage Runge-Kutta scheme of Carpenter & Kennedy
+//     (NASA TM-109112, 1994) in its 2N-storage form r = A_s r + dt R(u), u = u - B_s r
+//     (LFWENO7FDM3d.m:65-104).
+// ------------------------------------------------------------------------------------------
+namespace {
+
+// beta_0 of the WENO7 stencil over (f0, f1, f2, f3) and beta_1 over (f1, f2, f3, f4) as upper-
+// triangular quadratic forms, entries (00, 01, 02, 03, 11, 12, 13, 22, 23, 33). beta_2 and beta_3
+// are beta_1 and beta_0 of the mirrored stencil (the prototype's coefficients have that symmetry).
+constexpr double kW7Beta0[10] = {6649, -47214, 56694, -22778, 85641, -210282, 86214, 134241, -114894, 25729};
+constexpr double kW7Beta1[10] = {3169, -19374, 19014, -5978, 33441, -70602, 23094, 41001, -30414, 6649};
+
+template <class T>
+inline T quad_form4(const double q[10], T a, T b, T c, T d) {
+  return a * ((T)q[0] * a + (T)q[1] * b + (T)q[2] * c + (T)q[3] * d) + b * ((T)q[4] * b + (T)q[5] * c + (T)q[6] * d) +
+         c * ((T)q[7] * c + (T)q[8] * d) + (T)q[9] * d * d;
+}
+
+// Reconstruction at the face between f[3] and f[4] of the flux part moving towards +x, from
+// the seven cells f[0..6] around it. The part moving towards -x uses the mirrored stencil.
+template <class T>
+inline T weno7_side(const T f[7]) {
+  const T eps = (T)1e-6;
+  const T b0 = quad_form4<T>(kW7Beta0, f[0], f[1], f[2], f[3]);
+  const T b1 = quad_form4<T>(kW7Beta1, f[1], f[2], f[3], f[4]);
+  const T b2 = quad_form4<T>(kW7Beta1, f[5], f[4], f[3], f[2]);
+  const T b3 = quad_form4<T>(kW7Beta0, f[6], f[5], f[4], f[3]);
+  const T a0 = (T)(1. / 35.) / ((eps + b0) * (eps + b0));
+  const T a1 = (T)(12. / 35.) / ((eps + b1) * (eps + b1));
+  const T a2 = (T)(18. / 35.) / ((eps + b2) * (eps + b2));
+  const T a3 = (T)(4. / 35.) / ((eps + b3) * (eps + b3));
+  const T q0 = (-(T)3 * f[0] + (T)13 * f[1] - (T)23 * f[2] + (T)25 * f[3]) / (T)12;
+  const T q1 = (f[1] - (T)5 * f[2] + (T)13 * f[3] + (T)3 * f[4]) / (T)12;
+  const T q2 = (-f[2] + (T)7 * f[3] + (T)7 * f[4] - f[5]) / (T)12;
+  const T q3 = ((T)3 * f[3] + (T)13 * f[4] - (T)5 * f[5] + f[6]) / (T)12;
+  return (a0 * q0 + a1 * q1 + a2 * q2 + a3 * q3) / (a0 + a1 + a2 + a3);
+}
+
+// Face flux at i+1/2 from the split parts: `fp(j)` / `fm(j)` give the parts at cell i+j.
+template <class T, class G>
+inline T proto_face(int order, G part) {
+  if (order == 7) {
+    T p[7], m[7];
+    for (int j = 0; j < 7; ++j) {
+      p[j] = part(j - 3, 0);   // cells i-3 .. i+3
+      m[j] = part(4 - j, 1);   // cells i+4 .. i-2 (mirrored)
+    }
+    return weno7_side<T>(p) + weno7_side<T>(m);
+  }
+  return weno_face<T, T>(0, part(-2, 0), part(-1, 0), part(0, 0), part(1, 0), part(2, 0), part(-1, 1), part(0, 1),
+                         part(1, 1), part(2, 1), part(3, 1));
+}
+
+// res = d f(u) / d axis on every node, by the prototype residual function of `order` (5 or 7);
+// line_max = 1 takes a = max|u| along each line (the 1d files), else a = |u| per node.
+template <class T>
+void proto_residual(int order, int axis, int line_max, int nx, int ny, int nz, double h, const T* u, T* res) {
+  const int n[3] = {nx, ny, nz};
+  const int N = n[axis];
+  const size_t stride = axis == 0 ? 1 : axis == 1 ? (size_t)nx : (size_t)nx * ny;
+  const int o1 = axis == 0 ? 1 : 0, o2 = axis == 2 ? 1 : 2;  // the two other axes
+  const int lines = n[o1] * n[o2];
+#pragma omp parallel for schedule(static)
+  for (int l = 0; l < lines; ++l) {
+    int c[3] = {0, 0, 0};
+    c[o1] = l % n[o1];
+    c[o2] = l / n[o1];
+    const T* line = u + (size_t)c[0] + (size_t)nx * ((size_t)c[1] + (size_t)ny * c[2]);
+    T* out = res + (line - u);
+    std::vector<T> fp(N), fm(N);
+    T amax = 0;
+    if (line_max)
+      for (int i = 0; i < N; ++i) amax = std::max(amax, (T)std::fabs(line[(size_t)i * stride]));
+    for (int i = 0; i < N; ++i) {
+      const T v = line[(size_t)i * stride];
+      const T f = v * v / (T)2;
+      const T a = line_max ? amax : (T)std::fabs(v);
+      fp[i] = (T)0.5 * (f + a * v);
+      fm[i] = (T)0.5 * (f - a * v);
+    }
+    T left = 0;  // F_{-1/2}
+    for (int i = 0; i < N; ++i) {
+      auto part = [&](int j, int side) -> T {
+        const int k = std::min(std::max(i + j, 0), N - 1);
+        return side == 0 ? fp[k] : fm[k];
+      };
+      const T right = proto_face<T>(order, part);
+      out[(size_t)i * stride] = (right - left) / (T)h;
+      left = right;
+    }
+  }
+}
+
+// Carpenter & Kennedy's five-stage fourth-order 2N-storage Runge-Kutta coefficients (the
+// published rational values, also those of LFWENO7FDM3d.m:66-79).
+constexpr double kLsrkA[5] = {0.0, -567301805773.0 / 1357537059087.0, -2404267990393.0 / 2016746695238.0,
+                              -3550918686646.0 / 2091501179385.0, -1275806237668.0 / 842570457699.0};
+constexpr double kLsrkB[5] = {1432997174477.0 / 9575080441755.0, 5161836677717.0 / 13612068292357.0,
+                              1720146321549.0 / 2090206949498.0, 3134564353537.0 / 4481467310338.0,
+                              2277821191437.0 / 14882151754819.0};
+
+// Sum of the residuals of every axis of an ndim-dimensional grid, accumulated in axis order.
+template <class T>
+void proto_rhs(int order, int ndim, int nx, int ny, int nz, const double h[3], const T* u, T* acc, T* tmp) {
+  const size_t n = (size_t)nx * ny * nz;
+  proto_residual<T>(order, 0, ndim == 1, nx, ny, nz, h[0], u, acc);
+  for (int ax = 1; ax < ndim; ++ax) {
+    proto_residual<T>(order, ax, 0, nx, ny, nz, h[ax], u, tmp);
+    for (size_t o = 0; o < n; ++o) acc[o] += tmp[o];
+  }
+}
+
+// The prototype solver loop; returns the number of time steps, the end time in *t_out.
+template <class T>
+int64_t proto_run(int order, int ndim, int nx, int ny, int nz, const double h[3], double cfl, double tEnd,
+                  int64_t max_steps, T* u, double* t_out) {
+  const size_t n = (size_t)nx * ny * nz;
+  std::vector<T> L(n), tmp(n), uo(n), r(n, (T)0);
+  double t = 0;
+  int64_t it = 0;
+  while (t < tEnd && it < max_steps) {
+    T umax = 0;
+    for (size_t o = 0; o < n; ++o) umax = std::max(umax, (T)std::fabs(u[o]));
+    double dt = cfl * h[0] / (double)umax;
+    if (t + dt > tEnd) dt = tEnd - t;
+    t += dt;
+    ++it;
+    const T tdt = (T)dt;
+    if (order == 7) {
+      for (int s = 0; s < 5; ++s) {
+        proto_rhs<T>(order, ndim, nx, ny, nz, h, u, L.data(), tmp.data());
+        for (size_t o = 0; o < n; ++o) {
+          r[o] = (T)kLsrkA[s] * r[o] + tdt * L[o];
+          u[o] = u[o] - (T)kLsrkB[s] * r[o];
+        }
+      }
+    } else {
+      std::memcpy(uo.data(), u, n * sizeof(T));
+      proto_rhs<T>(order, ndim, nx, ny, nz, h, u, L.data(), tmp.data());
+      for (size_t o = 0; o < n; ++o) u[o] = uo[o] - tdt * L[o];
+      proto_rhs<T>(order, ndim, nx, ny, nz, h, u, L.data(), tmp.data());
+      for (size_t o = 0; o < n; ++o) u[o] = (T)0.75 * uo[o] + (T)0.25 * (u[o] - tdt * L[o]);
+      proto_rhs<T>(order, ndim, nx, ny, nz, h, u, L.data(), tmp.data());
+      for (size_t o = 0; o < n; ++o) u[o] = (uo[o] + (T)2 * (u[o] - tdt * L[o])) / (T)3;
+    }
+  }
+  *t_out = t;
+  return it;
+}
+
+}  // namespace
+
 extern "C" {
 
 // ----------------------------------------------------------------------------- RNG
@@ -957,6 +1128,33 @@ void orc_burgers_step_adjoint_f64(BURG_ARGS, const double* un, const double* u1,
 void orc_burgers_step_adjoint_f32(BURG_ARGS, const float* un, const float* u1, const float* u2, double dt,
                                   float* lam) {
   BURG_CFG burgers_step_adjoint<float>(c, un, u1, u2, (float)dt, lam);
+}
+
+// ------------------------------------------------------------- MATLAB Burgers prototypes
+// order 5 or 7; axis 0/1/2 = x/y/z of an x-fastest nx*ny*nz array; line_max 1 = the 1d files.
+void orc_proto_residual_f64(int order, int axis, int line_max, int nx, int ny, int nz, double h, const double* u,
+                            double* res) {
+  proto_residual<double>(order, axis, line_max, nx, ny, nz, h, u, res);
+}
+// LFWENO{5,7}FDM{ndim}d.m solver loop on u (in place); h = {dx, dy, dz}.
+int64_t orc_proto_run_f64(int order, int ndim, int nx, int ny, int nz, const double* h, double cfl, double tEnd,
+                          int64_t max_steps, double* u, double* t_out) {
+  return proto_run<double>(order, ndim, nx, ny, nz, h, cfl, tEnd, max_steps, u, t_out);
+}
+// The WENO7 reconstruction of one face from seven cell values (parts moving towards +x).
+double orc_weno7_side_f64(const double* f) { return weno7_side<double>(f); }
+// Amplification factor R(z) of one Carpenter-Kennedy LSRK(5,4) step on du/dt = z u (dt = 1).
+void orc_lsrk54_gain(double zr, double zi, double* gr, double* gi) {
+  double ur = 1, ui = 0, rr = 0, ri = 0;
+  for (int s = 0; s < 5; ++s) {
+    const double lr = zr * ur - zi * ui, li = zr * ui + zi * ur;  // R(u) = -z u, du/dt = -R
+    rr = kLsrkA[s] * rr - lr;
+    ri = kLsrkA[s] * ri - li;
+    ur = ur - kLsrkB[s] * rr;
+    ui = ui - kLsrkB[s] * ri;
+  }
+  *gr = ur;
+  *gi = ui;
 }
 
 }  // extern "C"

@@ -69,6 +69,10 @@ def lib() -> C.CDLL:
             "orc_heatk_adjoint_f64": (None, [_I, _I, _I, _I, _D, _D, _D] + [C.c_void_p] * 5),
             "orc_heatk_adjoint_f32": (None, [_I, _I, _I, _I, _D, _D, _D] + [C.c_void_p] * 5),
             "orc_philox_u01x2": (None, [_U32, _U32, C.c_uint64, _PD, _PD]),
+            "orc_proto_residual_f64": (None, [_I, _I, _I, _I, _I, _I, _D, C.c_void_p, C.c_void_p]),
+            "orc_proto_run_f64": (_I64, [_I, _I, _I, _I, _I, _PD, _D, _D, _I64, C.c_void_p, _PD]),
+            "orc_weno7_side_f64": (_D, [_PD]),
+            "orc_lsrk54_gain": (None, [_D, _D, _PD, _PD]),
             "orc_num_threads": (_I, []),
             "orc_set_num_threads": (None, [_I]),
         }
@@ -286,3 +290,39 @@ def burgers_loss_and_gradient(cfg, u0, target, dt, nsteps):
         lam = burgers_step_adjoint(cfg, un, u1, u2, dt, lam)
     return J, lam
 
+
+# ---------------------------------------------------------------- MATLAB Burgers prototypes
+def _xyz(a: np.ndarray):
+    """(nx, ny, nz) of an x-fastest field stored [z][y][x], [y][x] or [x]."""
+    s = a.shape[::-1]
+    return s[0], (s[1] if len(s) > 1 else 1), (s[2] if len(s) > 2 else 1)
+
+
+def proto_residual(order: int, axis: int, u: np.ndarray, h: float, line_max: bool = False) -> np.ndarray:
+    """d f(u)/d axis by WENO{order}resAdv_{X,Y,Z}.m (line_max: WENO{order}resAdv1d.m)."""
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    res = np.empty_like(u)
+    nx, ny, nz = _xyz(u)
+    lib().orc_proto_residual_f64(order, axis, int(line_max), nx, ny, nz, h, _p(u), _p(res))
+    return res
+
+
+def proto_run(order: int, u0: np.ndarray, h, cfl: float, tEnd: float, max_steps: int = 1 << 30):
+    """The LFWENO{order}FDM{ndim}d.m solver loop from u0; returns (u, t, steps)."""
+    u = np.array(u0, dtype=np.float64, copy=True, order="C")
+    nx, ny, nz = _xyz(u)
+    hh = (C.c_double * 3)(*(list(h) + [1.0] * (3 - len(h))))
+    t = C.c_double(0.0)
+    it = lib().orc_proto_run_f64(order, u.ndim, nx, ny, nz, hh, cfl, tEnd, max_steps, _p(u), C.byref(t))
+    return u, t.value, int(it)
+
+
+def weno7_side(f) -> float:
+    a = (C.c_double * 7)(*[float(x) for x in f])
+    return lib().orc_weno7_side_f64(a)
+
+
+def lsrk54_gain(z: complex) -> complex:
+    gr, gi = C.c_double(), C.c_double()
+    lib().orc_lsrk54_gain(z.real, z.imag, C.byref(gr), C.byref(gi))
+    return complex(gr.value, gi.value)

@@ -1,0 +1,564 @@
+"""A small interpreter for the subset of MATLAB used by the reference's Burgers prototypes.
+
+Fixture generation only (see make_weno_golden.py). It runs, on numpy arrays, the prototype
+files Matlab_Prototipes/InviscidBurgersNd/WENO{5,7}resAdv_{X,Y,Z,1d}.m and the solver-loop
+sections of LFWENO{5,7}FDM{2,3}d.m, so that the CPU oracle's restatement of those schemes can
+be checked against the reference's own code without MATLAB.
+
+Supported: numbers, identifiers, `+ - * / ^ .* ./ .^`, unary minus, comparisons, ranges
+`a:b` / `a:s:b`, row literals `[a b, c]`, anonymous functions `@(w) expr`, 1-based indexing
+with `:` (MATLAB's outer-product semantics; a single index is linear, column-major), indexed
+assignment, `function out = name(args)` files, `while` / `if` / `for` ... `end`, and the
+builtins the files call (cat, zeros, size, abs, max, exp, rem, ones; plotting calls are
+no-ops). Elementwise operations are evaluated one at a time in the order the source writes
+them, as MATLAB does, so results match MATLAB's double arithmetic operation by operation.
+Anything outside the subset raises an error instead of guessing.
+"""
+from __future__ import annotations
+
+import re
+from pathlib import Path
+
+import numpy as np
+
+_TOKEN = re.compile(r"""
+  (?P<num>(?:\d+\.\d*|\.\d+|\d+)(?:[eE][+-]?\d+)?)
+| (?P<id>[A-Za-z_]\w*)
+| (?P<op>\.\*|\./|\.\^|==|~=|<=|>=|&&|\|\||[-+*/^()\[\],;:=<>@])
+| (?P<nl>\n)
+| (?P<ws>[ \t\r]+)
+""", re.X)
+
+_NOOP_CALLS = {"surf", "plot", "axis", "view", "drawnow", "shg", "title", "xlabel", "ylabel",
+               "zlabel", "colorbar", "print", "figure", "hold", "grid"}
+
+
+class MatlabError(RuntimeError):
+    pass
+
+
+def _strip(src: str) -> str:
+    """Removes % comments and joins `...` continuation lines (no strings in the subset)."""
+    lines = []
+    for line in src.splitlines():
+        if "'" in line.split("%", 1)[0]:
+            raise MatlabError("strings/transpose are outside the subset: " + line.strip())
+        lines.append(line.split("%", 1)[0])
+    out = "\n".join(lines)
+    return re.sub(r"\.\.\.[^\n]*\n", " ", out)
+
+
+def _tokenize(src: str):
+    """Tokens as (kind, text). Whitespace is kept only directly inside [ ] (element separator)."""
+    toks, stack, pos = [], [], 0
+    while pos < len(src):
+        m = _TOKEN.match(src, pos)
+        if not m:
+            raise MatlabError(f"unexpected character {src[pos]!r}")
+        pos = m.end()
+        kind = m.lastgroup
+        text = m.group()
+        if kind == "ws":
+            if stack and stack[-1] == "[":
+                toks.append(("ws", " "))
+            continue
+        if kind == "op" and text in "([":
+            stack.append(text)
+        elif kind == "op" and text in ")]":
+            if not stack:
+                raise MatlabError("unbalanced " + text)
+            stack.pop()
+        toks.append((kind, text))
+    toks.append(("eof", ""))
+    return toks
+
+
+# ---------------------------------------------------------------------------- parser (AST)
+class _Parser:
+    def __init__(self, toks):
+        self.t = toks
+        self.i = 0
+        self.depth_bracket = 0
+
+    def peek(self, k=0):
+        return self.t[self.i + k]
+
+    def next(self):
+        tok = self.t[self.i]
+        self.i += 1
+        return tok
+
+    def accept(self, text):
+        if self.peek()[1] == text and self.peek()[0] in ("op", "id"):
+            self.i += 1
+            return True
+        return False
+
+    def expect(self, text):
+        if not self.accept(text):
+            raise MatlabError(f"expected {text!r}, found {self.peek()[1]!r}")
+
+    def skip_ws(self):
+        while self.peek()[0] == "ws":
+            self.i += 1
+
+    # statements ------------------------------------------------------------------------
+    def block(self, terminators):
+        body = []
+        while True:
+            tok = self.peek()
+            if tok[0] == "eof":
+                if terminators:
+                    raise MatlabError("missing end")
+                return body
+            if tok[0] == "nl" or tok[1] in (";", ","):
+                self.next()
+                continue
+            if tok[0] == "id" and tok[1] in terminators:
+                return body
+            body.append(self.statement())
+
+    def statement(self):
+        tok = self.peek()
+        if tok == ("id", "while"):
+            self.next()
+            cond = self.expr()
+            body = self.block({"end"})
+            self.expect("end")
+            return ("while", cond, body)
+        if tok == ("id", "if"):
+            self.next()
+            cond = self.expr()
+            body = self.block({"end"})
+            self.expect("end")
+            return ("if", cond, body)
+        if tok == ("id", "for"):
+            self.next()
+            var = self.next()[1]
+            self.expect("=")
+            rng = self.expr()
+            body = self.block({"end"})
+            self.expect("end")
+            return ("for", var, rng, body)
+        # assignment `name = e` / `name(args) = e`, or a bare call
+        if tok[0] == "id":
+            save = self.i
+            name = self.next()[1]
+            args = None
+            if self.peek()[1] == "(":
+                self.next()
+                args = self.args()
+            if self.peek()[1] == "=" and self.peek(1)[1] != "=":
+                self.next()
+                return ("assign", name, args, self.expr())
+            self.i = save
+        return ("expr", self.expr())
+
+    # expressions -----------------------------------------------------------------------
+    def expr(self):
+        return self.comparison()
+
+    def comparison(self):
+        left = self.range_()
+        while self.peek()[1] in ("<", ">", "<=", ">=", "==", "~="):
+            op = self.next()[1]
+            left = ("bin", op, left, self.range_())
+        return left
+
+    def range_(self):
+        first = self.additive()
+        if self.peek()[1] == ":" and self.depth_bracket == 0:
+            self.next()
+            second = self.additive()
+            if self.peek()[1] == ":":
+                self.next()
+                return ("range", first, second, self.additive())
+            return ("range", first, None, second)
+        return first
+
+    def _element_break(self):
+        # inside [ ], `a -b` starts a new element; `a - b` and `a-b` do not
+        return (self.depth_bracket > 0 and self.peek()[0] == "ws" and self.peek(1)[1] in ("+", "-")
+                and self.peek(2)[0] != "ws")
+
+    def additive(self):
+        left = self.mult()
+        while True:
+            if self._element_break():
+                return left
+            save = self.i
+            if self.depth_bracket:
+                self.skip_ws()
+            if self.peek()[1] in ("+", "-"):
+                op = self.next()[1]
+                if self.depth_bracket:
+                    self.skip_ws()
+                left = ("bin", op, left, self.mult())
+            else:
+                self.i = save
+                return left
+
+    def mult(self):
+        left = self.unary()
+        while True:
+            save = self.i
+            if self.depth_bracket:
+                self.skip_ws()
+            if self.peek()[1] in ("*", "/", ".*", "./"):
+                op = self.next()[1]
+                if self.depth_bracket:
+                    self.skip_ws()
+                left = ("bin", op, left, self.unary())
+            else:
+                self.i = save
+                return left
+
+    def unary(self):
+        if self.peek()[1] in ("-", "+"):
+            op = self.next()[1]
+            operand = self.unary()
+            return ("neg", operand) if op == "-" else operand
+        return self.power()
+
+    def power(self):
+        left = self.postfix()
+        while self.peek()[1] in ("^", ".^"):
+            op = self.next()[1]
+            if self.peek()[1] in ("-", "+"):
+                sign = self.next()[1]
+                rhs = self.postfix()
+                rhs = ("neg", rhs) if sign == "-" else rhs
+            else:
+                rhs = self.postfix()
+            left = ("bin", op, left, rhs)
+        return left
+
+    def postfix(self):
+        node = self.primary()
+        while self.peek()[1] == "(":
+            self.next()
+            node = ("call", node, self.args())
+        return node
+
+    def args(self):
+        out = []
+        saved = self.depth_bracket
+        self.depth_bracket = 0
+        if self.accept(")"):
+            self.depth_bracket = saved
+            return out
+        while True:
+            if self.peek()[1] == ":" and self.peek(1)[1] in (",", ")"):
+                self.next()
+                out.append(("colon",))
+            else:
+                out.append(self.expr())
+            if self.accept(")"):
+                break
+            self.expect(",")
+        self.depth_bracket = saved
+        return out
+
+    def primary(self):
+        kind, text = self.next()
+        if kind == "num":
+            return ("num", float(text))
+        if kind == "id":
+            return ("id", text)
+        if text == "(":
+            saved = self.depth_bracket
+            self.depth_bracket = 0
+            e = self.expr()
+            self.depth_bracket = saved
+            self.expect(")")
+            return e
+        if text == "[":
+            self.depth_bracket += 1
+            elems = []
+            self.skip_ws()
+            while not self.accept("]"):
+                elems.append(self.expr())
+                self.skip_ws()
+                self.accept(",")
+                self.skip_ws()
+            self.depth_bracket -= 1
+            return ("row", elems)
+        if text == "@":
+            self.expect("(")
+            params = []
+            while not self.accept(")"):
+                params.append(self.next()[1])
+                self.accept(",")
+            return ("lambda", params, self.expr())
+        raise MatlabError(f"unexpected token {text!r}")
+
+
+# ---------------------------------------------------------------------------- evaluation
+def _is_scalar(v) -> bool:
+    return np.ndim(v) == 0 or np.size(v) == 1
+
+
+def _scalar(v) -> float:
+    return float(np.asarray(v).reshape(-1)[0])
+
+
+def _as_index(v, extent):
+    if isinstance(v, tuple) and v == ("colon",):
+        return np.arange(extent)
+    a = np.asarray(v, dtype=np.float64).reshape(-1)
+    if np.any(a != np.round(a)) or np.any(a < 1):
+        raise MatlabError("non-integer or non-positive index")
+    return a.astype(np.int64) - 1
+
+
+def _squeeze_trailing(a):
+    while a.ndim > 2 and a.shape[-1] == 1:
+        a = a[..., 0]
+    return a
+
+
+def _index(arr, idx):
+    arr = np.asarray(arr, dtype=np.float64)
+    if arr.ndim < 2:
+        arr = arr.reshape(1, -1)
+    if len(idx) == 1:
+        flat = arr.reshape(-1, order="F")
+        if isinstance(idx[0], tuple):
+            return flat.reshape(-1, 1).copy()
+        sel = _as_index(idx[0], flat.size)
+        out = flat[sel]
+        return out.reshape(1, -1) if arr.shape[0] == 1 else out.reshape(-1, 1)
+    if len(idx) < arr.ndim:
+        raise MatlabError("fewer indices than dimensions is outside the subset")
+    view = arr.reshape(arr.shape + (1,) * (len(idx) - arr.ndim))
+    sel = [_as_index(v, view.shape[d]) for d, v in enumerate(idx)]
+    return _squeeze_trailing(view[np.ix_(*sel)].copy())
+
+
+def _matlab_max(a):
+    a = np.asarray(a, dtype=np.float64)
+    if a.ndim < 2 or min(a.shape[:2]) == 1 and a.ndim == 2:
+        return float(np.max(a))
+    raise MatlabError("max over a matrix is outside the subset")
+
+
+def _cat(dim, *arrays):
+    d = int(dim) - 1
+    mats = []
+    for a in arrays:
+        a = np.asarray(a, dtype=np.float64)
+        if a.ndim < 2:
+            a = a.reshape(1, -1)
+        while a.ndim <= d:
+            a = a[..., None]
+        mats.append(a)
+    nd = max(m.ndim for m in mats)
+    mats = [m.reshape(m.shape + (1,) * (nd - m.ndim)) for m in mats]
+    return _squeeze_trailing(np.concatenate(mats, axis=d))
+
+
+def _zeros(*args):
+    if len(args) == 1:
+        shape = tuple(int(x) for x in np.asarray(args[0]).reshape(-1))
+        if len(shape) == 1:
+            shape = (shape[0], shape[0])
+    else:
+        shape = tuple(int(_scalar(x)) for x in args)
+    return np.zeros(shape)
+
+
+def _ones(*args):
+    return _zeros(*args) + 1.0
+
+
+BUILTINS = {
+    "cat": _cat,
+    "zeros": _zeros,
+    "ones": _ones,
+    "size": lambda a: np.array(np.shape(a) if np.ndim(a) >= 2 else (1, np.size(a)),
+                               dtype=np.float64).reshape(1, -1),
+    "abs": lambda a: np.abs(np.asarray(a, dtype=np.float64)),
+    "exp": lambda a: np.exp(np.asarray(a, dtype=np.float64)),
+    "max": _matlab_max,
+    "rem": lambda a, b: float(np.fmod(_scalar(a), _scalar(b))),
+}
+
+
+class Interpreter:
+    """Runs statements of the subset; functions not in the environment are loaded from
+    `<name>.m` in `fdir`."""
+
+    def __init__(self, fdir: Path | None = None):
+        self.fdir = Path(fdir) if fdir else None
+        self._files: dict[str, tuple] = {}
+        self.calls: dict[str, int] = {}
+
+    # -- entry points -------------------------------------------------------------------
+    def run(self, src: str, env: dict) -> dict:
+        body = _Parser(_tokenize(_strip(src))).block(set())
+        self._exec(body, env)
+        return env
+
+    def call_file(self, name: str, args: list):
+        if name not in self._files:
+            if self.fdir is None:
+                raise MatlabError(f"unknown function {name}")
+            src = _strip((self.fdir / f"{name}.m").read_text())
+            m = re.match(r"\s*function\s+(\w+)\s*=\s*(\w+)\s*\(([^)]*)\)", src)
+            if not m or m.group(2) != name:
+                raise MatlabError(f"{name}.m is not a one-output function file")
+            params = [p.strip() for p in m.group(3).split(",") if p.strip()]
+            body = _Parser(_tokenize(src[m.end():])).block(set())
+            self._files[name] = (m.group(1), params, body)
+        out, params, body = self._files[name]
+        if len(args) != len(params):
+            raise MatlabError(f"{name} takes {len(params)} arguments")
+        self.calls[name] = self.calls.get(name, 0) + 1
+        env = dict(zip(params, args))
+        self._exec(body, env)
+        return env[out]
+
+    # -- statements ---------------------------------------------------------------------
+    def _exec(self, body, env):
+        for st in body:
+            kind = st[0]
+            if kind == "assign":
+                _, name, args, e = st
+                val = self._eval(e, env)
+                if args is None:
+                    env[name] = val
+                else:
+                    self._assign_index(env, name, args, val)
+            elif kind == "expr":
+                self._eval(st[1], env)
+            elif kind == "while":
+                guard = 0
+                while self._truth(self._eval(st[1], env)):
+                    self._exec(st[2], env)
+                    guard += 1
+                    if guard > 1_000_000:
+                        raise MatlabError("while loop did not end")
+            elif kind == "if":
+                if self._truth(self._eval(st[1], env)):
+                    self._exec(st[2], env)
+            elif kind == "for":
+                rng = np.asarray(self._eval(st[2], env), dtype=np.float64).reshape(-1)
+                for v in rng:
+                    env[st[1]] = float(v)
+                    self._exec(st[3], env)
+            else:
+                raise MatlabError("statement kind " + kind)
+
+    @staticmethod
+    def _truth(v) -> bool:
+        a = np.asarray(v)
+        return bool(a.size) and bool(np.all(a != 0))
+
+    def _assign_index(self, env, name, args, val):
+        arr = env[name]
+        if not isinstance(arr, np.ndarray):
+            raise MatlabError("indexed assignment to a non-array")
+        idx = [("colon",) if a == ("colon",) else self._eval(a, env) for a in args]
+        if len(idx) < arr.ndim:
+            raise MatlabError("fewer indices than dimensions is outside the subset")
+        view = arr.reshape(arr.shape + (1,) * (len(idx) - arr.ndim))
+        if not np.shares_memory(view, arr):
+            raise MatlabError("indexed assignment needs a contiguous array")
+        sel = [_as_index(v, view.shape[d]) for d, v in enumerate(idx)]
+        target_shape = tuple(len(s) for s in sel)
+        v = np.asarray(val, dtype=np.float64)
+        if v.size != 1:
+            v = v.reshape(v.shape + (1,) * (len(target_shape) - v.ndim))
+            if v.shape != target_shape:
+                raise MatlabError(f"assignment shape {v.shape} into {target_shape}")
+        view[np.ix_(*sel)] = v
+
+    # -- expressions --------------------------------------------------------------------
+    def _eval(self, n, env):
+        kind = n[0]
+        if kind == "num":
+            return n[1]
+        if kind == "id":
+            name = n[1]
+            if name in env:
+                return env[name]
+            if name in _NOOP_CALLS:
+                return None
+            if name in BUILTINS:
+                return BUILTINS[name]()
+            return self.call_file(name, [])
+        if kind == "neg":
+            return -self._eval(n[1], env)
+        if kind == "bin":
+            return self._binary(n[1], self._eval(n[2], env), self._eval(n[3], env))
+        if kind == "range":
+            a = _scalar(self._eval(n[1], env))
+            s = 1.0 if n[2] is None else _scalar(self._eval(n[2], env))
+            b = _scalar(self._eval(n[3], env))
+            if s != 1.0 or a != round(a):
+                raise MatlabError("only integer ranges with unit step are in the subset")
+            return np.arange(a, b + 1.0, 1.0).reshape(1, -1)
+        if kind == "row":
+            vals = [self._eval(e, env) for e in n[1]]
+            if all(_is_scalar(v) for v in vals):
+                return np.array([_scalar(v) for v in vals], dtype=np.float64).reshape(1, -1)
+            return _cat(2, *vals)
+        if kind == "lambda":
+            params, body = n[1], n[2]
+            closure = dict(env)
+
+            def fn(*args):
+                local = dict(closure)
+                local.update(zip(params, args))
+                return self._eval(body, local)
+            return fn
+        if kind == "call":
+            target = n[1]
+            if target[0] == "id":
+                name = target[1]
+                if name in env and isinstance(env[name], (np.ndarray, float)):
+                    idx = [("colon",) if a == ("colon",) else self._eval(a, env) for a in n[2]]
+                    out = _index(env[name], idx)
+                    return out
+                if name not in env and name in _NOOP_CALLS:
+                    return None  # plotting: its arguments are never evaluated
+                args = [self._eval(a, env) for a in n[2]]
+                if name in env and callable(env[name]):
+                    return env[name](*args)
+                if name in BUILTINS:
+                    return BUILTINS[name](*args)
+                return self.call_file(name, args)
+            raise MatlabError("call of an expression")
+        raise MatlabError("node kind " + kind)
+
+    @staticmethod
+    def _binary(op, a, b):
+        fa = np.asarray(a, dtype=np.float64) if not isinstance(a, float) else a
+        fb = np.asarray(b, dtype=np.float64) if not isinstance(b, float) else b
+        if op in ("+", "-", ".*", "./", ".^", "<", ">", "<=", ">=", "==", "~="):
+            if op == "+":
+                return fa + fb
+            if op == "-":
+                return fa - fb
+            if op == ".*":
+                return fa * fb
+            if op == "./":
+                return fa / fb
+            if op == ".^":
+                return np.power(fa, fb)
+            r = {"<": np.less, ">": np.greater, "<=": np.less_equal, ">=": np.greater_equal,
+                 "==": np.equal, "~=": np.not_equal}[op](fa, fb)
+            return np.asarray(r, dtype=np.float64)
+        if op == "*":
+            if _is_scalar(fa) or _is_scalar(fb):
+                return fa * fb
+            raise MatlabError("matrix product is outside the subset")
+        if op == "/":
+            if _is_scalar(fb):
+                return fa / fb
+            raise MatlabError("matrix division is outside the subset")
+        if op == "^":
+            if _is_scalar(fa) and _is_scalar(fb):
+                return np.power(fa, fb)
+            raise MatlabError("matrix power is outside the subset")
+        raise MatlabError("operator " + op)
