@@ -30,6 +30,32 @@ def _dtype_code(t) -> int:
     raise ValueError(f"unsupported dtype {t.dtype}")
 
 
+def _fields(numel: int, *ts) -> int:
+    """Checks the grid-shaped tensors of one call and returns their dtype code. The C ABI takes
+    plain pointers and cannot see sizes, so each must be a contiguous CUDA tensor of one dtype,
+    on one device, with at least `numel` elements; otherwise the kernels would read or write
+    past it (an FP64 state in an FP32 buffer of the same length included)."""
+    first = ts[0]
+    code = _dtype_code(first)
+    for t in ts:
+        _ptr(t)
+        if t.dtype != first.dtype:
+            raise ValueError(f"fields of one call must share a dtype: {first.dtype} and {t.dtype}")
+        if t.device != first.device:
+            raise ValueError(f"fields of one call must share a device: {first.device} and {t.device}")
+        if t.numel() < numel:
+            raise ValueError(f"a field has {t.numel()} elements; the grid has {numel}")
+    return code
+
+
+def _buffer(t, nbytes: int, what: str) -> int:
+    """Pointer of a caller-supplied work buffer after checking it holds `nbytes`."""
+    p = _ptr(t)
+    if t.numel() * t.element_size() < nbytes:
+        raise ValueError(f"{what} has {t.numel() * t.element_size()} bytes; {nbytes} are needed")
+    return p
+
+
 @dataclass
 class HeatConfig:
     """Heat-equation scheme (fields as adv_heat_desc in include/advdiff.h)."""
@@ -83,24 +109,30 @@ class HeatConfig:
 
 def heat_stage(cfg: HeatConfig, stage: int, u_in, u_n, u_out, stream=None) -> None:
     """One fused stage u_out = combine(u_n, u_in + dt L(u_in)) (adv_heat_stage)."""
-    d = cfg.desc(_dtype_code(u_in))
+    d = cfg.desc(_fields(cfg.numel, u_in, u_n, u_out))
     N.check(N.load().adv_heat_stage(C.byref(d), stage, _ptr(u_in), _ptr(u_n), _ptr(u_out), N.stream_handle(stream)),
             "adv_heat_stage")
 
 
-def heat_workspace(cfg: HeatConfig, like):
-    import torch
-    d = cfg.desc(_dtype_code(like))
+def _heat_workspace_bytes(cfg: HeatConfig, dtype: int) -> int:
+    d = cfg.desc(dtype)
     nb = C.c_size_t(0)
     N.check(N.load().adv_heat_workspace_bytes(C.byref(d), cfg.time, C.byref(nb)), "adv_heat_workspace_bytes")
-    return torch.empty(nb.value, dtype=torch.uint8, device=like.device)
+    return nb.value
+
+
+def heat_workspace(cfg: HeatConfig, like):
+    import torch
+    return torch.empty(_heat_workspace_bytes(cfg, _dtype_code(like)), dtype=torch.uint8, device=like.device)
 
 
 def heat_run(cfg: HeatConfig, u, nsteps: int, workspace=None, stream=None):
     """nsteps time steps in place on u (adv_heat_run); returns u."""
+    code = _fields(cfg.numel, u)
     ws = heat_workspace(cfg, u) if workspace is None else workspace
-    d = cfg.desc(_dtype_code(u))
-    N.check(N.load().adv_heat_run(C.byref(d), cfg.time, int(nsteps), _ptr(u), _ptr(ws), N.stream_handle(stream)),
+    wp = _buffer(ws, _heat_workspace_bytes(cfg, code), "the heat workspace")
+    d = cfg.desc(code)
+    N.check(N.load().adv_heat_run(C.byref(d), cfg.time, int(nsteps), _ptr(u), wp, N.stream_handle(stream)),
             "adv_heat_run")
     return u
 
@@ -164,28 +196,39 @@ def burgers_stage(cfg: BurgersConfig, stage: int, u_in, u_n, u_out, dt: float, a
                   maxabs_key=None, stream=None) -> None:
     """One fused SSP-RK3 stage (adv_burgers_stage). maxabs_key: optional device tensor of one
     int32 (FP32 state) / int64 (FP64 state), zeroed by the caller, receiving max|u_out| bits."""
-    d = cfg.desc(_dtype_code(u_in))
-    key = None if maxabs_key is None else maxabs_key.data_ptr()
+    code = _fields(cfg.numel, u_in, u_n, u_out)
+    d = cfg.desc(code)
+    key = None
+    if maxabs_key is not None:
+        key = _buffer(maxabs_key, u_in.element_size(), "maxabs_key")
+        if maxabs_key.element_size() != u_in.element_size():
+            raise ValueError("maxabs_key must be int32 for an FP32 state and int64 for an FP64 state")
     N.check(N.load().adv_burgers_stage(C.byref(d), stage, _ptr(u_in), _ptr(u_n), _ptr(u_out), float(dt), float(alpha),
                                        key, N.stream_handle(stream)), "adv_burgers_stage")
 
 
-def burgers_workspace(cfg: BurgersConfig, like):
-    import torch
-    d = cfg.desc(_dtype_code(like))
+def _burgers_workspace_bytes(cfg: BurgersConfig, dtype: int) -> int:
+    d = cfg.desc(dtype)
     nb = C.c_size_t(0)
     N.check(N.load().adv_burgers_workspace_bytes(C.byref(d), C.byref(nb)), "adv_burgers_workspace_bytes")
-    return torch.empty(nb.value, dtype=torch.uint8, device=like.device)
+    return nb.value
+
+
+def burgers_workspace(cfg: BurgersConfig, like):
+    import torch
+    return torch.empty(_burgers_workspace_bytes(cfg, _dtype_code(like)), dtype=torch.uint8, device=like.device)
 
 
 def burgers_run(cfg: BurgersConfig, u, tEnd: float, cfl: float, dt_rule: int = N.ADV_DT_MAXU,
                 max_steps: int = 1 << 40, workspace=None, stream=None) -> tuple[float, int]:
     """Time loop to tEnd in place on u (adv_burgers_run); returns (t, steps)."""
+    code = _fields(cfg.numel, u)
     ws = burgers_workspace(cfg, u) if workspace is None else workspace
-    d = cfg.desc(_dtype_code(u))
+    wp = _buffer(ws, _burgers_workspace_bytes(cfg, code), "the Burgers workspace")
+    d = cfg.desc(code)
     t = C.c_double(0.0)
     steps = C.c_int64(0)
-    N.check(N.load().adv_burgers_run(C.byref(d), _ptr(u), _ptr(ws), float(tEnd), float(cfl), int(dt_rule),
+    N.check(N.load().adv_burgers_run(C.byref(d), _ptr(u), wp, float(tEnd), float(cfl), int(dt_rule),
                                      float(cfg.C), int(max_steps), C.byref(t), C.byref(steps),
                                      N.stream_handle(stream)), "adv_burgers_run")
     return t.value, steps.value
@@ -224,13 +267,13 @@ class HeatKConfig:
 
 
 def heatk_step(cfg: HeatKConfig, k, u_in, u_out, stream=None) -> None:
-    d = cfg.desc(_dtype_code(u_in))
+    d = cfg.desc(_fields(cfg.numel, u_in, k, u_out))
     N.check(N.load().adv_heatk_step(C.byref(d), _ptr(k), _ptr(u_in), _ptr(u_out), N.stream_handle(stream)),
             "adv_heatk_step")
 
 
 def heatk_adjoint_step(cfg: HeatKConfig, k, u_n, lam_next, lam_out, grad_k, stream=None) -> None:
-    d = cfg.desc(_dtype_code(u_n))
+    d = cfg.desc(_fields(cfg.numel, u_n, k, lam_next, lam_out, grad_k))
     N.check(N.load().adv_heatk_adjoint_step(C.byref(d), _ptr(k), _ptr(u_n), _ptr(lam_next), _ptr(lam_out),
                                             _ptr(grad_k), N.stream_handle(stream)), "adv_heatk_adjoint_step")
 
@@ -260,8 +303,8 @@ def _autograd():
         @staticmethod
         def forward(ctx, k, u0, cfg, nsteps, interval):
             u = u0.detach().clone()
+            d = cfg.desc(_fields(cfg.numel, u, k))
             ckpt, work = _heatk_buffers(cfg, u, nsteps, interval)
-            d = cfg.desc(_dtype_code(u))
             N.check(N.load().adv_heatk_forward(C.byref(d), _ptr(k), _ptr(u), int(nsteps), int(interval), _ptr(ckpt),
                                                _ptr(work), N.stream_handle(torch.cuda.current_stream())),
                     "adv_heatk_forward")
@@ -274,7 +317,7 @@ def _autograd():
             (k,) = ctx.saved_tensors
             lam = grad_u.detach().clone().contiguous()
             gk = torch.zeros_like(k)
-            d = ctx.cfg.desc(_dtype_code(lam))
+            d = ctx.cfg.desc(_fields(ctx.cfg.numel, lam, k, gk))
             N.check(N.load().adv_heatk_backward(C.byref(d), _ptr(k), int(ctx.nsteps), int(ctx.interval),
                                                 _ptr(ctx.ckpt), _ptr(lam), _ptr(gk), _ptr(ctx.work),
                                                 N.stream_handle(torch.cuda.current_stream())), "adv_heatk_backward")
@@ -293,7 +336,7 @@ def _burgers_autograd():
         @staticmethod
         def forward(ctx, u0, cfg, dt, nsteps, interval):
             u = u0.detach().clone()
-            d = cfg.desc(_dtype_code(u))
+            d = cfg.desc(_fields(cfg.numel, u))
             cb, wb = C.c_size_t(0), C.c_size_t(0)
             N.check(N.load().adv_burgers_checkpoint_bytes(C.byref(d), int(nsteps), int(interval), C.byref(cb),
                                                           C.byref(wb)), "adv_burgers_checkpoint_bytes")
@@ -308,7 +351,7 @@ def _burgers_autograd():
         @staticmethod
         def backward(ctx, grad_u):
             lam = grad_u.detach().clone().contiguous()
-            d = ctx.cfg.desc(_dtype_code(lam))
+            d = ctx.cfg.desc(_fields(ctx.cfg.numel, lam))
             N.check(N.load().adv_burgers_backward(C.byref(d), float(ctx.dt), int(ctx.nsteps), int(ctx.interval),
                                                   _ptr(ctx.ckpt), _ptr(lam), _ptr(ctx.work),
                                                   N.stream_handle(torch.cuda.current_stream())),
@@ -332,12 +375,13 @@ def burgers_run_fixed(cfg: BurgersConfig, u0, dt: float, nsteps: int, interval: 
 def burgers_adjoint_step(cfg: BurgersConfig, u_n, u1, u2, dt: float, lam, work=None, stream=None):
     """lam (dJ/du^{n+1}) becomes dJ/du^n in place; work: 3 arrays of scratch (allocated if None)."""
     import torch
-    d = cfg.desc(_dtype_code(u_n))
+    d = cfg.desc(_fields(cfg.numel, u_n, u1, u2, lam))
+    one = (cfg.numel * u_n.element_size() + 255) // 256 * 256
     if work is None:
-        one = (u_n.numel() * u_n.element_size() + 255) // 256 * 256
         work = torch.empty(3 * one, dtype=torch.uint8, device=u_n.device)
+    wp = _buffer(work, 3 * one, "the adjoint work buffer")
     N.check(N.load().adv_burgers_adjoint_step(C.byref(d), _ptr(u_n), _ptr(u1), _ptr(u2), float(dt), _ptr(lam),
-                                              _ptr(work), N.stream_handle(stream)), "adv_burgers_adjoint_step")
+                                              wp, N.stream_handle(stream)), "adv_burgers_adjoint_step")
     return lam
 
 
@@ -366,17 +410,19 @@ class Ensemble:
         self._keep = []
         hm = (N.HeatMember * max(len(heat), 1))()
         for i, (cfg, u) in enumerate(heat):
+            code = _fields(cfg.numel, u)
             ws = heat_workspace(dataclasses.replace(cfg, time=heat_time), u)
             self._keep += [u, ws]
-            hm[i] = N.HeatMember(cfg.desc(_dtype_code(u)), _ptr(u), _ptr(ws))
+            hm[i] = N.HeatMember(cfg.desc(code), _ptr(u), _ptr(ws))
         bm = (N.BurgersMember * max(len(burgers), 1))()
         for i, b in enumerate(burgers):
             cfg, u, tEnd, cfl = b[:4]
             dt_rule = b[4] if len(b) > 4 else N.ADV_DT_MAXU
             max_steps = b[5] if len(b) > 5 else 1 << 40
+            code = _fields(cfg.numel, u)
             ws = burgers_workspace(cfg, u)
             self._keep += [u, ws]
-            bm[i] = N.BurgersMember(cfg.desc(_dtype_code(u)), _ptr(u), _ptr(ws), float(tEnd), float(cfl), int(dt_rule),
+            bm[i] = N.BurgersMember(cfg.desc(code), _ptr(u), _ptr(ws), float(tEnd), float(cfl), int(dt_rule),
                                     0, float(cfg.C), int(max_steps))
         self.n_heat, self.n_burgers = len(heat), len(burgers)
         h = C.c_void_p(None)
@@ -428,7 +474,7 @@ def _tune_dict(r) -> dict:
 def autotune_heat(cfg: HeatConfig, u, stream=None) -> dict:
     """Picks the heat stage's launch shape for this problem (adv_autotune_heat)."""
     r = N.TuneResult()
-    d = cfg.desc(_dtype_code(u))
+    d = cfg.desc(_fields(cfg.numel, u))
     N.check(N.load().adv_autotune_heat(C.byref(d), _ptr(u), N.stream_handle(stream), C.byref(r)), "adv_autotune_heat")
     return _tune_dict(r)
 
@@ -436,7 +482,7 @@ def autotune_heat(cfg: HeatConfig, u, stream=None) -> dict:
 def autotune_burgers(cfg: BurgersConfig, u, stream=None) -> dict:
     """Picks the Burgers stage's launch shape for this problem (adv_autotune_burgers)."""
     r = N.TuneResult()
-    d = cfg.desc(_dtype_code(u))
+    d = cfg.desc(_fields(cfg.numel, u))
     N.check(N.load().adv_autotune_burgers(C.byref(d), _ptr(u), N.stream_handle(stream), C.byref(r)),
             "adv_autotune_burgers")
     return _tune_dict(r)
@@ -445,7 +491,7 @@ def autotune_burgers(cfg: BurgersConfig, u, stream=None) -> dict:
 def autotune_heatk(cfg: HeatKConfig, k, u, stream=None) -> tuple[dict, dict]:
     """Picks the heat-with-k(x) step and adjoint launch shapes (adv_autotune_heatk)."""
     r1, r2 = N.TuneResult(), N.TuneResult()
-    d = cfg.desc(_dtype_code(u))
+    d = cfg.desc(_fields(cfg.numel, u, k))
     N.check(N.load().adv_autotune_heatk(C.byref(d), _ptr(k), _ptr(u), N.stream_handle(stream), C.byref(r1),
                                         C.byref(r2)), "adv_autotune_heatk")
     return _tune_dict(r1), _tune_dict(r2)

@@ -1,0 +1,91 @@
+"""Host-side argument checks of the Python solver surface (no GPU): every grid-shaped tensor
+handed to the C ABI must be a contiguous CUDA tensor of the call's dtype and device with at
+least the grid's element count, and caller-supplied work buffers must be large enough. The
+checks run before any native call, so stand-in tensor objects exercise them on the CPU."""
+from __future__ import annotations
+
+import pytest
+import torch
+
+from multigpu_advectiondiffusion_gb300 import _native as N
+from multigpu_advectiondiffusion_gb300 import solvers as S
+
+
+class FakeCuda:
+    """Just enough of a CUDA tensor for the checks; its pointer is never dereferenced."""
+
+    def __init__(self, n, dtype=torch.float32, device="cuda:0", contiguous=True):
+        self._n, self.dtype, self.device, self._contig = n, dtype, torch.device(device), contiguous
+        self.is_cuda = True
+
+    def numel(self):
+        return self._n
+
+    def element_size(self):
+        return torch.empty(0, dtype=self.dtype).element_size()
+
+    def is_contiguous(self):
+        return self._contig
+
+    def data_ptr(self):
+        return 0x10000
+
+
+HEAT = S.HeatConfig.dirichlet_o2(3, 16)          # 4096 nodes
+BURG = S.BurgersConfig.periodic(12)              # 1728 cells
+
+
+def test_heat_stage_rejects_short_mixed_or_strided_fields():
+    n = HEAT.numel
+    with pytest.raises(ValueError, match="elements"):
+        S.heat_stage(HEAT, 1, FakeCuda(n), FakeCuda(n), FakeCuda(n - 1))
+    with pytest.raises(ValueError, match="dtype"):
+        S.heat_stage(HEAT, 1, FakeCuda(n), FakeCuda(n), FakeCuda(n, torch.float64))
+    with pytest.raises(ValueError, match="device"):
+        S.heat_stage(HEAT, 1, FakeCuda(n), FakeCuda(n, device="cuda:1"), FakeCuda(n))
+    with pytest.raises(ValueError, match="contiguous"):
+        S.heat_stage(HEAT, 1, FakeCuda(n), FakeCuda(n, contiguous=False), FakeCuda(n))
+    with pytest.raises(ValueError, match="CUDA"):
+        S.heat_stage(HEAT, 1, torch.zeros(n), torch.zeros(n), torch.zeros(n))
+    with pytest.raises(ValueError, match="unsupported dtype"):
+        S.heat_stage(HEAT, 1, FakeCuda(n, torch.float16), FakeCuda(n, torch.float16), FakeCuda(n, torch.float16))
+
+
+def test_heat_run_rejects_a_small_workspace():
+    need = S._heat_workspace_bytes(HEAT, N.ADV_F32)
+    assert need >= HEAT.numel * 4
+    with pytest.raises(ValueError, match="bytes"):
+        S.heat_run(HEAT, FakeCuda(HEAT.numel), 10, workspace=FakeCuda(need - 1, torch.uint8))
+    with pytest.raises(ValueError, match="elements"):
+        S.heat_run(HEAT, FakeCuda(HEAT.numel // 2), 10, workspace=FakeCuda(need, torch.uint8))
+
+
+def test_burgers_calls_check_fields_key_and_workspace():
+    n = BURG.numel
+    with pytest.raises(ValueError, match="elements"):
+        S.burgers_stage(BURG, 1, FakeCuda(n), FakeCuda(n - 5), FakeCuda(n), 1e-3)
+    with pytest.raises(ValueError, match="int64"):
+        S.burgers_stage(BURG, 1, FakeCuda(n, torch.float64), FakeCuda(n, torch.float64), FakeCuda(n, torch.float64),
+                        1e-3, maxabs_key=FakeCuda(2, torch.int32))
+    need = S._burgers_workspace_bytes(BURG, N.ADV_F64)
+    with pytest.raises(ValueError, match="bytes"):
+        S.burgers_run(BURG, FakeCuda(n, torch.float64), 0.1, 0.4, workspace=FakeCuda(need // 2, torch.uint8))
+    one = (n * 4 + 255) // 256 * 256
+    with pytest.raises(ValueError, match="bytes"):
+        S.burgers_adjoint_step(BURG, FakeCuda(n), FakeCuda(n), FakeCuda(n), 1e-3, FakeCuda(n),
+                               work=FakeCuda(3 * one - 1, torch.uint8))
+    with pytest.raises(ValueError, match="dtype"):
+        S.burgers_adjoint_step(BURG, FakeCuda(n), FakeCuda(n), FakeCuda(n), 1e-3, FakeCuda(n, torch.float64))
+
+
+def test_heatk_and_ensemble_members_are_checked():
+    cfg = S.HeatKConfig.cube(10, 0.1, 1.0)
+    n = cfg.numel
+    with pytest.raises(ValueError, match="elements"):
+        S.heatk_step(cfg, FakeCuda(n - 1), FakeCuda(n), FakeCuda(n))
+    with pytest.raises(ValueError, match="dtype"):
+        S.heatk_adjoint_step(cfg, FakeCuda(n), FakeCuda(n), FakeCuda(n), FakeCuda(n), FakeCuda(n, torch.float64))
+    with pytest.raises(ValueError, match="elements"):
+        S.Ensemble(heat=[(HEAT, FakeCuda(HEAT.numel - 1))])
+    with pytest.raises(ValueError, match="elements"):
+        S.Ensemble(burgers=[(BURG, FakeCuda(10), 0.1, 0.4)])
