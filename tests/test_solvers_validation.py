@@ -89,3 +89,47 @@ def test_heatk_and_ensemble_members_are_checked():
         S.Ensemble(heat=[(HEAT, FakeCuda(HEAT.numel - 1))])
     with pytest.raises(ValueError, match="elements"):
         S.Ensemble(burgers=[(BURG, FakeCuda(10), 0.1, 0.4)])
+
+
+class FakeLib:
+    """Records native calls and reports success (no GPU work is done)."""
+
+    def __init__(self):
+        self.calls = []
+
+    def __getattr__(self, name):
+        def fn(*args):
+            self.calls.append((name, args))
+            return N.ADV_OK
+        return fn
+
+
+def test_valid_calls_reach_the_native_library(monkeypatch):
+    """Every checked wrapper, given valid stand-in tensors, passes its pointers to the library."""
+    fake = FakeLib()
+    monkeypatch.setattr(N, "load", lambda: fake)
+    n, nb = HEAT.numel, BURG.numel
+    ws = FakeCuda(1 << 30, torch.uint8)
+    S.heat_stage(HEAT, 1, FakeCuda(n), FakeCuda(n), FakeCuda(n))
+    S.heat_run(HEAT, FakeCuda(n), 5, workspace=ws)
+    d64 = torch.float64
+    S.burgers_stage(BURG, 2, FakeCuda(nb, d64), FakeCuda(nb, d64), FakeCuda(nb, d64), 1e-3, 0.5,
+                    maxabs_key=FakeCuda(1, torch.int64))
+    S.burgers_run(BURG, FakeCuda(nb), 0.1, 0.4, workspace=ws)
+    S.burgers_adjoint_step(BURG, FakeCuda(nb), FakeCuda(nb), FakeCuda(nb), 1e-3, FakeCuda(nb), work=ws)
+    kc = S.HeatKConfig.cube(10, 0.1, 1.0)
+    f = [FakeCuda(kc.numel) for _ in range(5)]
+    S.heatk_step(kc, f[0], f[1], f[2])
+    S.heatk_adjoint_step(kc, *f)
+    S.autotune_heat(HEAT, FakeCuda(n))
+    S.autotune_burgers(BURG, FakeCuda(nb))
+    S.autotune_heatk(kc, f[0], f[1])
+    S.max_abs(FakeCuda(n))
+    names = [c[0] for c in fake.calls]
+    for want in ("adv_heat_stage", "adv_heat_workspace_bytes", "adv_heat_run", "adv_burgers_stage",
+                 "adv_burgers_workspace_bytes", "adv_burgers_run", "adv_burgers_adjoint_step", "adv_heatk_step",
+                 "adv_heatk_adjoint_step", "adv_autotune_heat", "adv_autotune_burgers", "adv_autotune_heatk",
+                 "adv_max_abs"):
+        assert want in names, want
+    stage = dict(fake.calls)["adv_burgers_stage"]
+    assert stage[2:5] == (0x10000, 0x10000, 0x10000) and stage[7] == 0x10000  # fields and the key
