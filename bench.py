@@ -24,6 +24,8 @@ import dataclasses
 import ctypes as C
 import json
 import os
+import platform
+import re
 import subprocess
 import sys
 import time
@@ -190,6 +192,43 @@ def cpu_heat_rate(cfg, u0, budget_s: float):
     oracle.heat_run(cfg, u0, steps, 0)
     dt = time.perf_counter() - t0
     return cfg.numel * steps / dt / 1e9, steps, dt
+
+
+def cpu_model() -> str:
+    """The host CPU's name: /proc/cpuinfo's model name (x86) or implementer/part codes (Arm)."""
+    try:
+        txt = Path("/proc/cpuinfo").read_text()
+    except OSError:
+        return platform.machine()
+    m = re.search(r"^model name\s*:\s*(.+)$", txt, re.M)
+    if m:
+        return m.group(1).strip()
+    part = re.search(r"^CPU part\s*:\s*(\S+)$", txt, re.M)
+    impl = re.search(r"^CPU implementer\s*:\s*(\S+)$", txt, re.M)
+    if part:
+        known = {("0x41", "0xd4f"): "Arm Neoverse-V2"}
+        key = (impl.group(1) if impl else "", part.group(1))
+        return known.get(key, f"{platform.machine()} implementer {key[0]} part {key[1]}")
+    return platform.machine()
+
+
+def cpu_baseline_heat(cfg, u0, budget_s: float) -> dict:
+    """The oracle's rate on the heat workload with all host threads, then on one thread (a
+    bounded sample of each: about budget_s and min(budget_s, 3) seconds)."""
+    from oracle import oracle
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    r, s, dtc = cpu_heat_rate(cfg, u0, budget_s)
+    oracle.set_threads(1)
+    try:
+        r1, s1, dt1 = cpu_heat_rate(cfg, u0, min(budget_s, 3.0))
+    finally:
+        oracle.set_threads(threads)
+    n = round(cfg.numel ** (1 / 3)) if cfg.ndim == 3 else cfg.nx
+    return {"value": r, "unit": "Gcell-updates/s", "cores": threads, "kind": "port",
+            "sample": f"{n}^{cfg.ndim} FP32 O2 Euler, {s} time steps in {dtc:.1f} s (oracle, OpenMP)",
+            "one_core_value": r1, "one_core_sample": f"{s1} time steps in {dt1:.1f} s on one thread",
+            "cpu_model": cpu_model()}
 
 
 # FP32 flops per cell-stage of the fused WENO5-Z stage (ncu instruction mix at 256^3, stage 1)
@@ -654,7 +693,7 @@ def run_reference_arm(args, world, rank):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded)", "config": config,
             "cpu_baseline": {"value": value, "unit": "Gcell-updates/s", "cores": threads, "kind": "port",
-                             "sample": sample},
+                             "sample": sample, "cpu_model": cpu_model()},
             "e2e": {"value": value, "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "sg_gpu": reference_sg_gpu(args.workload, args.warmup)}
     print(json.dumps(line), flush=True)
@@ -851,12 +890,7 @@ def main():
     # ---- CPU baseline (oracle on the host cores, rank 0, N = 1 only)
     cpu = None
     if rank == 0 and world == 1 and args.workload == "heat3d":
-        from oracle import oracle
-        threads = os.cpu_count() or 1
-        oracle.set_threads(threads)
-        r, s, dtc = cpu_heat_rate(cfg, u0_np, args.cpu_budget)
-        cpu = {"value": r, "unit": "Gcell-updates/s", "cores": threads, "kind": "port",
-               "sample": f"256^3 FP32 O2 Euler, {s} time steps in {dtc:.1f} s (oracle, OpenMP)"}
+        cpu = cpu_baseline_heat(cfg, u0_np, args.cpu_budget)
 
     if rank == 0:
         line = {
