@@ -138,3 +138,28 @@ def test_drivers_print_usage_without_gpu(native):
     for drv in ("heat2d", "heat3d", "burgers3d", "burgers2d"):
         r = subprocess.run([str(N.LIBDIR / drv)], capture_output=True, text=True)
         assert r.returncode == 1 and "Usage" in r.stdout
+
+
+@pytest.mark.parametrize("header", ["advdiff.h", "advdiff_ref_ops.h", "advdiff_compat_heat2d.h",
+                                    "advdiff_compat_heat3d.h", "advdiff_compat_burgers3d.h"])
+@pytest.mark.parametrize("lang", ["c99", "c++17"])
+def test_headers_compile_as_c_and_cpp(tmp_path, header, lang):
+    """The boundary headers are plain C (what a cgo / FFI / C host includes) and valid C++; the
+    native ones need no CUDA header, the compatibility ones include cuda_runtime.h for dim3."""
+    import shutil
+    cc = shutil.which("gcc" if lang == "c99" else "g++")
+    if cc is None:
+        pytest.skip("no host compiler")
+    src = tmp_path / ("t.c" if lang == "c99" else "t.cpp")
+    src.write_text(f'#include "{header}"\nint main(void) {{ return 0; }}\n')
+    cmd = [cc, f"-std={lang}", "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-I", str(ROOT / "include")]
+    if "compat" in header:
+        nvcc = shutil.which("nvcc")
+        cuda_inc = Path(nvcc).resolve().parent.parent / "include" if nvcc else Path("/usr/local/cuda/include")
+        if not (cuda_inc / "cuda_runtime.h").exists():
+            pytest.skip("no CUDA toolkit headers")
+        cmd += ["-I", str(cuda_inc)]
+    else:
+        cmd += ["-pedantic"]
+    r = subprocess.run(cmd + [str(src)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
