@@ -163,3 +163,40 @@ def test_headers_compile_as_c_and_cpp(tmp_path, header, lang):
         cmd += ["-pedantic"]
     r = subprocess.run(cmd + [str(src)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_c_host_links_and_calls_the_library(native, tmp_path):
+    """A plain C99 program links libadvdiff.so and uses its host-side entry points (no GPU):
+    the seeded initial condition, result.bin written and read back, status strings."""
+    import shutil
+    if shutil.which("gcc") is None:
+        pytest.skip("no host compiler")
+    src = tmp_path / "host.c"
+    src.write_text(r'''
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include "advdiff.h"
+int main(int argc, char** argv) {
+  enum { NX = 9, NY = 8, NZ = 7, N = NX * NY * NZ };
+  double u[N], back[N];
+  if (adv_abi_version() != 1) return 2;
+  if (adv_ic_heat_ref(3, NX, NY, NZ, 0.5, 0.5, 0.5, u) != ADV_OK) return 3;
+  if (adv_write_result_bin(argv[1], ADV_F64, u, N) != ADV_OK) return 4;
+  if (adv_read_result_bin(argv[1], N, back) != ADV_OK) return 5;
+  for (int i = 0; i < N; ++i)
+    if (back[i] != (double)(float)u[i]) return 6;
+  if (adv_read_result_bin(argv[1], N + 1, back) != ADV_ERR_INVALID_ARG) return 7;
+  if (strcmp(adv_status_string(ADV_ERR_CFL), "ADV_ERR_CFL") != 0) return 8;
+  printf("ok %s\n", adv_last_error_string());
+  return argc == 2 ? 0 : 9;
+}
+''')
+    exe = tmp_path / "host"
+    lib = N.lib_path()
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", str(ROOT / "include"), str(src), "-o", str(exe),
+                        "-L", str(lib.parent), "-ladvdiff", f"-Wl,-rpath,{lib.parent}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    run = subprocess.run([str(exe), str(tmp_path / "result.bin")], capture_output=True, text=True, timeout=60)
+    assert run.returncode == 0, (run.returncode, run.stdout, run.stderr)
+    assert run.stdout.startswith("ok")
