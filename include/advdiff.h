@@ -291,6 +291,15 @@ adv_status adv_autotune_heatk(const adv_heatk_desc* d, const void* k, const void
                               adv_tune_result* out_step, adv_tune_result* out_adjoint);
 /* Forgets every tuned shape (launches return to the defaults). */
 adv_status adv_autotune_clear(void);
+/* The tuned shapes of the current device as JSON text, to keep them between processes:
+ * {"advdiff_autotune": 1, "entries": [{"kind": .., "variant": .., "nx": .., "ny": .., "nz": ..,
+ * "a": .., "b": ..}, ...]}. *length receives the size including the terminating NUL; with
+ * buf == NULL only the size is returned. */
+adv_status adv_autotune_export(char* buf, size_t capacity, size_t* length);
+/* Loads a table written by adv_autotune_export for the current device (entries replace tuned
+ * shapes of the same problems). Rejects, without loading anything, text in any other form and
+ * values outside the tuner's own candidates (ADV_ERR_INVALID_ARG). */
+adv_status adv_autotune_import(const char* json);
 
 /* ------------------------------------------------------------------ reductions
  * max|u| over n values into *out (host double). Synchronises the stream. */

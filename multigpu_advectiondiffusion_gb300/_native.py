@@ -105,6 +105,8 @@ SIGNATURES = [
     ("adv_autotune_burgers", _I, [C.POINTER(BurgersDesc), _VP, _VP, C.POINTER(TuneResult)]),
     ("adv_autotune_heatk", _I, [C.POINTER(HeatKDesc), _VP, _VP, _VP, C.POINTER(TuneResult), C.POINTER(TuneResult)]),
     ("adv_autotune_clear", _I, []),
+    ("adv_autotune_export", _I, [C.c_char_p, C.c_size_t, C.POINTER(C.c_size_t)]),
+    ("adv_autotune_import", _I, [C.c_char_p]),
     ("adv_burgers_resume", _I, [C.POINTER(BurgersDesc), _VP, _VP, _D, _I64, _D, _D, _I, _D, _I64, _PD,
                                 C.POINTER(C.c_int64), _VP]),
     ("adv_max_abs", _I, [_I, _VP, _I64, _PD, _VP]),

@@ -10,8 +10,15 @@
 // then on (per device and problem shape, for the life of the process). Cached CUDA graphs are
 // dropped when a choice changes because they hold the old launch shapes.
 #include <algorithm>
+#include <cctype>
+#include <cerrno>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <initializer_list>
 #include <map>
 #include <mutex>
+#include <string>
 #include <tuple>
 #include <vector>
 
@@ -151,6 +158,158 @@ void tune_clear() {
   g_table.clear();
 }
 
+// ------------------------------------------------------------------ table export / import
+// The table of this device as JSON, so a tuned set of shapes can be kept between processes:
+//   {"advdiff_autotune": 1, "entries": [{"kind": 1, "variant": 5, "nx": 256, "ny": 256,
+//    "nz": 256, "a": 4, "b": 8}, ...]}
+// An import accepts only values the tuner itself tries (the launch shapes the kernels are
+// tested with), so a stale or edited file cannot produce an untested launch.
+namespace {
+
+bool tune_allowed(int kind, long long a, long long b) {
+  auto in = [](long long v, std::initializer_list<int> set) {
+    return std::find(set.begin(), set.end(), (int)v) != set.end() && v == (int)v;
+  };
+  switch (kind) {
+    case TUNE_HEAT: return a >= 1 && a <= 32 && in(b, {1, 2, 4, 8, 16, 32});
+    case TUNE_BURGERS: return a >= 1 && a <= 32 && in(b, {4, 8, 16, 32});
+    case TUNE_HEATK_STEP:
+    case TUNE_HEATK_ADJ: return in(a, {4, 8, 16}) && in(b, {4, 8, 16, 32});
+    default: return false;
+  }
+}
+
+// Reader for the export format only: objects with identifier keys, integer values and the one
+// array of entry objects. Anything else fails.
+struct TuneJson {
+  const char* p;
+  void ws() {
+    while (*p == ' ' || *p == '\n' || *p == '\t' || *p == '\r') ++p;
+  }
+  bool lit(char c) {
+    ws();
+    if (*p != c) return false;
+    ++p;
+    return true;
+  }
+  bool key(std::string* out) {
+    if (!lit('"')) return false;
+    const char* b = p;
+    while (*p && (std::isalnum((unsigned char)*p) || *p == '_')) ++p;
+    if (*p != '"' || p == b) return false;
+    out->assign(b, (size_t)(p - b));
+    ++p;
+    return lit(':');
+  }
+  bool integer(long long* v) {
+    ws();
+    if (!(*p == '-' || std::isdigit((unsigned char)*p))) return false;
+    char* end = nullptr;
+    errno = 0;
+    const long long x = std::strtoll(p, &end, 10);
+    if (end == p || errno) return false;
+    p = end;
+    *v = x;
+    return true;
+  }
+};
+
+struct TuneEntry {
+  int kind, variant, nx, ny, nz;
+  TuneParams p;
+};
+
+bool parse_entry(TuneJson& j, TuneEntry* e) {
+  if (!j.lit('{')) return false;
+  const char* names[7] = {"kind", "variant", "nx", "ny", "nz", "a", "b"};
+  long long v[7];
+  bool seen[7] = {false, false, false, false, false, false, false};
+  do {
+    std::string k;
+    long long x;
+    if (!j.key(&k) || !j.integer(&x)) return false;
+    int i = 0;
+    while (i < 7 && k != names[i]) ++i;
+    if (i == 7 || seen[i]) return false;
+    seen[i] = true;
+    v[i] = x;
+  } while (j.lit(','));
+  if (!j.lit('}')) return false;
+  for (bool b : seen)
+    if (!b) return false;
+  for (int i = 1; i < 5; ++i)
+    if (v[i] < 0 || v[i] > (1 << 24)) return false;
+  if (v[2] < 1 || v[3] < 1 || v[4] < 1 || !tune_allowed((int)v[0], v[5], v[6])) return false;
+  *e = TuneEntry{(int)v[0], (int)v[1], (int)v[2], (int)v[3], (int)v[4], TuneParams{(int)v[5], (int)v[6], true}};
+  return true;
+}
+
+bool parse_table(const char* text, std::vector<TuneEntry>* out) {
+  TuneJson j{text};
+  if (!j.lit('{')) return false;
+  bool version = false, entries = false;
+  do {
+    std::string k;
+    if (!j.key(&k)) return false;
+    if (k == "advdiff_autotune" && !version) {
+      long long x;
+      if (!j.integer(&x) || x != 1) return false;
+      version = true;
+    } else if (k == "entries" && !entries) {
+      if (!j.lit('[')) return false;
+      if (!j.lit(']')) {
+        do {
+          TuneEntry e;
+          if (!parse_entry(j, &e)) return false;
+          out->push_back(e);
+        } while (j.lit(','));
+        if (!j.lit(']')) return false;
+      }
+      entries = true;
+    } else {
+      return false;
+    }
+  } while (j.lit(','));
+  if (!j.lit('}') || !version || !entries) return false;
+  j.ws();
+  return *j.p == '\0';
+}
+
+}  // namespace
+
+std::string tune_export_json() {
+  std::lock_guard<std::mutex> lk(g_mu);
+  const int dev = current_device();
+  std::string s = "{\"advdiff_autotune\": 1, \"entries\": [";
+  bool first = true;
+  for (const auto& kv : g_table) {
+    if (std::get<0>(kv.first) != dev || !kv.second.set) continue;
+    char line[256];
+    std::snprintf(line, sizeof line,
+                  "%s\n  {\"kind\": %d, \"variant\": %d, \"nx\": %d, \"ny\": %d, \"nz\": %d, \"a\": %d, \"b\": %d}",
+                  first ? "" : ",", std::get<1>(kv.first), std::get<2>(kv.first), std::get<3>(kv.first),
+                  std::get<4>(kv.first), std::get<5>(kv.first), kv.second.a, kv.second.b);
+    s += line;
+    first = false;
+  }
+  s += first ? "]}\n" : "\n]}\n";
+  return s;
+}
+
+adv_status tune_import_json(const char* text) {
+  std::vector<TuneEntry> es;
+  if (!parse_table(text, &es))
+    return set_error(ADV_ERR_INVALID_ARG, "autotune import: not a table written by adv_autotune_export, "
+                                          "or a value outside the tuner's candidates");
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    const int dev = current_device();
+    for (const TuneEntry& e : es) g_table[Key{dev, e.kind, e.variant, e.nx, e.ny, e.nz}] = e.p;
+  }
+  graph_cache_clear();
+  return ADV_OK;
+}
+
 }  // namespace adv
 
 using namespace adv;
@@ -257,6 +416,21 @@ adv_status adv_autotune_clear(void) {
   tune_clear();
   graph_cache_clear();
   return ADV_OK;
+}
+
+adv_status adv_autotune_export(char* buf, size_t capacity, size_t* length) {
+  if (!length) return set_error(ADV_ERR_INVALID_ARG, "autotune export: null length");
+  const std::string s = tune_export_json();
+  *length = s.size() + 1;
+  if (!buf) return ADV_OK;
+  if (capacity < s.size() + 1) return set_error(ADV_ERR_INVALID_ARG, "autotune export: buffer too small");
+  std::memcpy(buf, s.c_str(), s.size() + 1);
+  return ADV_OK;
+}
+
+adv_status adv_autotune_import(const char* json) {
+  if (!json) return set_error(ADV_ERR_INVALID_ARG, "autotune import: null text");
+  return tune_import_json(json);
 }
 
 }  // extern "C"

@@ -501,6 +501,31 @@ def autotune_clear() -> None:
     N.check(N.load().adv_autotune_clear(), "adv_autotune_clear")
 
 
+def autotune_export() -> str:
+    """The current device's tuned launch shapes as JSON text (adv_autotune_export)."""
+    lib = N.load()
+    n = C.c_size_t(0)
+    N.check(lib.adv_autotune_export(None, 0, C.byref(n)), "adv_autotune_export")
+    buf = C.create_string_buffer(n.value)
+    N.check(lib.adv_autotune_export(buf, n.value, C.byref(n)), "adv_autotune_export")
+    return buf.value.decode()
+
+
+def autotune_import(text: str) -> None:
+    """Loads shapes written by autotune_export for the current device (adv_autotune_import)."""
+    N.check(N.load().adv_autotune_import(text.encode()), "adv_autotune_import")
+
+
+def autotune_save(path) -> None:
+    with open(path, "w") as f:
+        f.write(autotune_export())
+
+
+def autotune_load(path) -> None:
+    with open(path) as f:
+        autotune_import(f.read())
+
+
 def reference_heat_final_time(dt: float, iters: int, t0: float = 0.1) -> float:
     """tFinal = t0 + dt*iters as the reference prints it (main.cpp:63)."""
     return t0 + dt * iters
