@@ -94,7 +94,9 @@ adv_status adv_heat_stage(const adv_heat_desc* d, int stage, const void* u_in, c
 /* Bytes of caller-provided workspace adv_heat_run needs: one state array for Euler, two for
  * SSP-RK3. */
 adv_status adv_heat_workspace_bytes(const adv_heat_desc* d, int time_scheme, size_t* bytes);
-/* nsteps time steps of the chosen scheme; the result is left in u. */
+/* nsteps time steps of the chosen scheme; the result is left in u. Asynchronous on `stream`.
+ * Inside a caller's stream capture the stage launches are recorded into that capture (no graph
+ * of the library's own), so the whole run can be part of the caller's graph. */
 adv_status adv_heat_run(const adv_heat_desc* d, int time_scheme, int64_t nsteps, void* u,
                         void* workspace, void* stream);
 
@@ -149,7 +151,11 @@ adv_status adv_burgers_workspace_bytes(const adv_burgers_desc* d, size_t* bytes)
 /* Full time loop to tEnd (at most max_steps steps). dt and the global-LF constant are computed
  * on the device; the loop runs as one CUDA graph (a while-conditional node when the driver
  * supports it, else fixed-size predicated chunks). C is the viscous coefficient used only by
- * ADV_DT_FIXED's diffusive bound (0 drops it). t_out / steps_out may be NULL. */
+ * ADV_DT_FIXED's diffusive bound (0 drops it). t_out / steps_out may be NULL. Synchronises the
+ * stream to read t and the step count back; called while the stream is being captured it
+ * returns ADV_ERR_UNSUPPORTED and leaves the stream and the capture untouched (record
+ * adv_burgers_stage calls instead). The same holds for adv_burgers_resume, adv_max_abs,
+ * adv_ensemble_run and the autotuner. */
 adv_status adv_burgers_run(const adv_burgers_desc* d, void* u, void* workspace, double tEnd,
                            double cfl, int dt_rule, double C, int64_t max_steps, double* t_out,
                            int64_t* steps_out, void* stream);

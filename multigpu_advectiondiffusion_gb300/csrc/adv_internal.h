@@ -39,6 +39,12 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 EncodeTiledFn encode_tiled_fn();
 
+// True while `s` is being captured into a CUDA graph.
+bool stream_capturing(cudaStream_t s);
+// ADV_ERR_UNSUPPORTED for a call that reads results back to the host (and so synchronises `s`)
+// while `s` is being captured; the stream and the caller's capture are left untouched.
+adv_status reject_capture(cudaStream_t s, const char* what);
+
 // Device status word (per device): 0 = OK, else an adv_status raised by a kernel.
 adv_status read_and_clear_device_status(cudaStream_t s);
 int* device_status_ptr();

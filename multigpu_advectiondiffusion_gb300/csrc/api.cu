@@ -155,10 +155,17 @@ adv_status burgers_launch(const adv_burgers_desc& d, const BurgersLaunch& L, con
   return d.dtype == ADV_F32 ? burgers_launch_f32(d, L, a, s) : burgers_launch_f64(d, L, a, s);
 }
 
-static bool stream_capturing(cudaStream_t s) {
+bool stream_capturing(cudaStream_t s) {
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) return false;
   return cs != cudaStreamCaptureStatusNone;
+}
+
+adv_status reject_capture(cudaStream_t s, const char* what) {
+  if (!stream_capturing(s)) return ADV_OK;
+  return set_error(ADV_ERR_UNSUPPORTED, std::string(what) +
+                                            ": reads its results back to the host, so it cannot be recorded into a "
+                                            "stream capture (capture the stage calls instead)");
 }
 
 // Instantiated CUDA graphs of the run loops, keyed by everything the captured launches depend
@@ -423,6 +430,7 @@ adv_status adv_burgers_resume(const adv_burgers_desc* d, void* u, void* workspac
   if (dt_rule != ADV_DT_FIXED && dt_rule != ADV_DT_MAXU) return set_error(ADV_ERR_INVALID_ARG, "burgers: bad dt rule");
   if (!(cfl > 0) || !std::isfinite(tEnd) || max_steps < 0) return set_error(ADV_ERR_INVALID_ARG, "burgers: bad cfl/tEnd/max_steps");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if ((st = reject_capture(s, "burgers run")) != ADV_OK) return st;
   const size_t es = d->dtype == ADV_F32 ? 4 : 8;
   const size_t n = (size_t)d->nx * d->ny * d->nz;
   const size_t one = (n * es + 255) / 256 * 256;
@@ -462,72 +470,66 @@ adv_status adv_burgers_resume(const adv_burgers_desc* d, void* u, void* workspac
 
   const bool can_loop = max_steps > 0 && tEnd > 0.0;
   if (can_loop) {
-    if (stream_capturing(s)) {
-      // Inside a caller's capture: enqueue predicated steps up to max_steps.
-      for (int64_t i = 0; i < max_steps; ++i)
-        if ((st = body(s, 0, 0)) != ADV_OK) return st;
-    } else {
-      // One graph: a while-conditional node whose body is one step; the condition is set on the
-      // device by the step-start kernel. Cached per (device, descriptor, buffers).
-      const std::string wkey = graph_key("burgers-while", *d, u, workspace);
-      cudaGraphExec_t ge = g_graphs.get(wkey);
-      cudaError_t e = cudaSuccess;
-      if (!ge) {
-        cudaStream_t cs;
-        ADV_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
-        cudaGraph_t g = nullptr;
-        e = cudaGraphCreate(&g, 0);
-        cudaGraphConditionalHandle h_cond = 0;
-        if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h_cond, g, 1, cudaGraphCondAssignDefault);
-        cudaGraphNode_t node;
-        cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
-        cp.conditional.handle = h_cond;
-        cp.conditional.type = cudaGraphCondTypeWhile;
-        cp.conditional.size = 1;
-        if (e == cudaSuccess) e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp);
-        adv_status bst = ADV_OK;
+    // One graph: a while-conditional node whose body is one step; the condition is set on the
+    // device by the step-start kernel. Cached per (device, descriptor, buffers).
+    const std::string wkey = graph_key("burgers-while", *d, u, workspace);
+    cudaGraphExec_t ge = g_graphs.get(wkey);
+    cudaError_t e = cudaSuccess;
+    if (!ge) {
+      cudaStream_t cs;
+      ADV_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+      cudaGraph_t g = nullptr;
+      e = cudaGraphCreate(&g, 0);
+      cudaGraphConditionalHandle h_cond = 0;
+      if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h_cond, g, 1, cudaGraphCondAssignDefault);
+      cudaGraphNode_t node;
+      cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+      cp.conditional.handle = h_cond;
+      cp.conditional.type = cudaGraphCondTypeWhile;
+      cp.conditional.size = 1;
+      if (e == cudaSuccess) e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp);
+      adv_status bst = ADV_OK;
+      if (e == cudaSuccess) {
+        e = cudaStreamBeginCaptureToGraph(cs, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeThreadLocal);
         if (e == cudaSuccess) {
-          e = cudaStreamBeginCaptureToGraph(cs, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
-                                            cudaStreamCaptureModeThreadLocal);
-          if (e == cudaSuccess) {
-            const int64_t before = g_launches.load();
-            bst = body(cs, (unsigned long long)h_cond, 1);
-            g_launches.store(before);
-            cudaGraph_t outg = nullptr;
-            e = cudaStreamEndCapture(cs, &outg);
-          }
-          if (e == cudaSuccess && bst == ADV_OK) e = cudaGraphInstantiate(&ge, g, 0);
+          const int64_t before = g_launches.load();
+          bst = body(cs, (unsigned long long)h_cond, 1);
+          g_launches.store(before);
+          cudaGraph_t outg = nullptr;
+          e = cudaStreamEndCapture(cs, &outg);
         }
-        if (g) cudaGraphDestroy(g);
-        cudaStreamDestroy(cs);
-        if (bst != ADV_OK) return bst;
-        if (e == cudaSuccess && ge) g_graphs.put(wkey, ge);
-        else ge = nullptr;
+        if (e == cudaSuccess && bst == ADV_OK) e = cudaGraphInstantiate(&ge, g, 0);
       }
-      if (ge) {
-        e = cudaGraphLaunch(ge, s);
-        if (e != cudaSuccess) return cuda_error(e, "burgers: graph launch");
-      } else {
-        cudaGetLastError();  // conditional nodes unavailable: clear the non-sticky error
-        // Fallback: fixed chunks of predicated steps, replayed until the device clears `active`.
-        const int64_t Cch = std::min<int64_t>(max_steps, 8);
-        auto chunk = [&](cudaStream_t c2) -> adv_status {
-          for (int64_t i = 0; i < Cch; ++i) {
-            adv_status r = body(c2, 0, 0);
-            if (r != ADV_OK) return r;
-          }
-          return ADV_OK;
-        };
-        const std::string key = graph_key("burgers-chunk", *d, u, workspace, Cch);
-        int64_t done = 0;
-        while (done < max_steps) {
-          if ((st = replay(key, s, 1, chunk, 4 * Cch)) != ADV_OK) return st;
-          done += Cch;
-          int active = 0;
-          ADV_CUDA_TRY(cudaMemcpyAsync(&active, &dst->active, sizeof(int), cudaMemcpyDeviceToHost, s));
-          ADV_CUDA_TRY(cudaStreamSynchronize(s));
-          if (!active) break;
+      if (g) cudaGraphDestroy(g);
+      cudaStreamDestroy(cs);
+      if (bst != ADV_OK) return bst;
+      if (e == cudaSuccess && ge) g_graphs.put(wkey, ge);
+      else ge = nullptr;
+    }
+    if (ge) {
+      e = cudaGraphLaunch(ge, s);
+      if (e != cudaSuccess) return cuda_error(e, "burgers: graph launch");
+    } else {
+      cudaGetLastError();  // conditional nodes unavailable: clear the non-sticky error
+      // Fallback: fixed chunks of predicated steps, replayed until the device clears `active`.
+      const int64_t Cch = std::min<int64_t>(max_steps, 8);
+      auto chunk = [&](cudaStream_t c2) -> adv_status {
+        for (int64_t i = 0; i < Cch; ++i) {
+          adv_status r = body(c2, 0, 0);
+          if (r != ADV_OK) return r;
         }
+        return ADV_OK;
+      };
+      const std::string key = graph_key("burgers-chunk", *d, u, workspace, Cch);
+      int64_t done = 0;
+      while (done < max_steps) {
+        if ((st = replay(key, s, 1, chunk, 4 * Cch)) != ADV_OK) return st;
+        done += Cch;
+        int active = 0;
+        ADV_CUDA_TRY(cudaMemcpyAsync(&active, &dst->active, sizeof(int), cudaMemcpyDeviceToHost, s));
+        ADV_CUDA_TRY(cudaStreamSynchronize(s));
+        if (!active) break;
       }
     }
   }
@@ -545,6 +547,7 @@ adv_status adv_max_abs(int dtype, const void* u, int64_t n, double* out, void* s
   if (dtype != ADV_F32 && dtype != ADV_F64) return set_error(ADV_ERR_INVALID_ARG, "max_abs: bad dtype");
   if (!u || !out || n < 0) return set_error(ADV_ERR_INVALID_ARG, "max_abs: bad arguments");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (adv_status st = reject_capture(s, "max_abs"); st != ADV_OK) return st;
   if (n == 0) { *out = 0.0; return ADV_OK; }
   unsigned long long* acc = nullptr;
   ADV_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&acc), sizeof(unsigned long long), s));

@@ -322,6 +322,7 @@ adv_status adv_autotune_heat(const adv_heat_desc* d, const void* u, void* stream
   if (st != ADV_OK) return st;
   if (!u) return set_error(ADV_ERR_INVALID_ARG, "autotune: null buffer");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if ((st = reject_capture(s, "autotune")) != ADV_OK) return st;
   const int nz = d->ndim == 3 ? d->nz : 1;
   const size_t bytes = (size_t)d->nx * d->ny * nz * (d->dtype == ADV_F32 ? 4 : 8);
   // Time stages the way a run issues them: each launch reads the previous launch's output
@@ -361,6 +362,7 @@ adv_status adv_autotune_burgers(const adv_burgers_desc* d, const void* u, void* 
   if (st != ADV_OK) return st;
   if (!u) return set_error(ADV_ERR_INVALID_ARG, "autotune: null buffer");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if ((st = reject_capture(s, "autotune")) != ADV_OK) return st;
   const size_t cells = (size_t)d->nx * d->ny * d->nz;
   Scratch tmp(s);
   if ((st = tmp.alloc(cells * (d->dtype == ADV_F32 ? 4 : 8))) != ADV_OK) return st;
@@ -392,6 +394,7 @@ adv_status adv_autotune_heatk(const adv_heatk_desc* d, const void* k, const void
   if (st != ADV_OK) return st;
   if (!k || !u) return set_error(ADV_ERR_INVALID_ARG, "autotune: null buffer");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if ((st = reject_capture(s, "autotune")) != ADV_OK) return st;
   const size_t cells = (size_t)d->nx * d->ny * d->nz;
   const size_t bytes = cells * (d->dtype == ADV_F32 ? 4 : 8);
   Scratch tmp(s), grad(s);

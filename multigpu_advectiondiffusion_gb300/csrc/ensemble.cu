@@ -421,6 +421,7 @@ adv_status adv_ensemble_run(adv_ensemble* e, int64_t heat_steps, int flags, void
   adv_status st = check_device(e);
   if (st != ADV_OK) return st;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if ((st = reject_capture(s, "ensemble run")) != ADV_OK) return st;
   const int64_t heat_iters = e->n_heat == 0 ? 0 : (e->heat_scheme == ADV_EULER ? heat_steps / 2 : heat_steps);
 
   // Burgers loop states: t = 0, then max|u^0| of every member into its slot-0 key.
