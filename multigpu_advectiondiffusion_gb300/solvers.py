@@ -48,6 +48,18 @@ def _fields(numel: int, *ts) -> int:
     return code
 
 
+def _stream(stream, like):
+    """Stream handle of a call: the caller's stream if given, else torch's current stream on the
+    device of `like` (so the library's work is ordered with the caller's torch work, also under
+    `with torch.cuda.stream(...)`); None (the default stream) without CUDA."""
+    if stream is not None:
+        return N.stream_handle(stream)
+    import torch
+    if getattr(like, "is_cuda", False) and torch.cuda.is_available():
+        return torch.cuda.current_stream(like.device).cuda_stream or None
+    return None
+
+
 def _buffer(t, nbytes: int, what: str) -> int:
     """Pointer of a caller-supplied work buffer after checking it holds `nbytes`."""
     p = _ptr(t)
@@ -110,7 +122,7 @@ class HeatConfig:
 def heat_stage(cfg: HeatConfig, stage: int, u_in, u_n, u_out, stream=None) -> None:
     """One fused stage u_out = combine(u_n, u_in + dt L(u_in)) (adv_heat_stage)."""
     d = cfg.desc(_fields(cfg.numel, u_in, u_n, u_out))
-    N.check(N.load().adv_heat_stage(C.byref(d), stage, _ptr(u_in), _ptr(u_n), _ptr(u_out), N.stream_handle(stream)),
+    N.check(N.load().adv_heat_stage(C.byref(d), stage, _ptr(u_in), _ptr(u_n), _ptr(u_out), _stream(stream, u_in)),
             "adv_heat_stage")
 
 
@@ -132,7 +144,7 @@ def heat_run(cfg: HeatConfig, u, nsteps: int, workspace=None, stream=None):
     ws = heat_workspace(cfg, u) if workspace is None else workspace
     wp = _buffer(ws, _heat_workspace_bytes(cfg, code), "the heat workspace")
     d = cfg.desc(code)
-    N.check(N.load().adv_heat_run(C.byref(d), cfg.time, int(nsteps), _ptr(u), wp, N.stream_handle(stream)),
+    N.check(N.load().adv_heat_run(C.byref(d), cfg.time, int(nsteps), _ptr(u), wp, _stream(stream, u)),
             "adv_heat_run")
     return u
 
@@ -204,7 +216,7 @@ def burgers_stage(cfg: BurgersConfig, stage: int, u_in, u_n, u_out, dt: float, a
         if maxabs_key.element_size() != u_in.element_size():
             raise ValueError("maxabs_key must be int32 for an FP32 state and int64 for an FP64 state")
     N.check(N.load().adv_burgers_stage(C.byref(d), stage, _ptr(u_in), _ptr(u_n), _ptr(u_out), float(dt), float(alpha),
-                                       key, N.stream_handle(stream)), "adv_burgers_stage")
+                                       key, _stream(stream, u_in)), "adv_burgers_stage")
 
 
 def _burgers_workspace_bytes(cfg: BurgersConfig, dtype: int) -> int:
@@ -230,13 +242,13 @@ def burgers_run(cfg: BurgersConfig, u, tEnd: float, cfl: float, dt_rule: int = N
     steps = C.c_int64(0)
     N.check(N.load().adv_burgers_run(C.byref(d), _ptr(u), wp, float(tEnd), float(cfl), int(dt_rule),
                                      float(cfg.C), int(max_steps), C.byref(t), C.byref(steps),
-                                     N.stream_handle(stream)), "adv_burgers_run")
+                                     _stream(stream, u)), "adv_burgers_run")
     return t.value, steps.value
 
 
 def max_abs(u, stream=None) -> float:
     out = C.c_double(0.0)
-    N.check(N.load().adv_max_abs(_dtype_code(u), _ptr(u), u.numel(), C.byref(out), N.stream_handle(stream)),
+    N.check(N.load().adv_max_abs(_dtype_code(u), _ptr(u), u.numel(), C.byref(out), _stream(stream, u)),
             "adv_max_abs")
     return out.value
 
@@ -268,14 +280,14 @@ class HeatKConfig:
 
 def heatk_step(cfg: HeatKConfig, k, u_in, u_out, stream=None) -> None:
     d = cfg.desc(_fields(cfg.numel, u_in, k, u_out))
-    N.check(N.load().adv_heatk_step(C.byref(d), _ptr(k), _ptr(u_in), _ptr(u_out), N.stream_handle(stream)),
+    N.check(N.load().adv_heatk_step(C.byref(d), _ptr(k), _ptr(u_in), _ptr(u_out), _stream(stream, u_in)),
             "adv_heatk_step")
 
 
 def heatk_adjoint_step(cfg: HeatKConfig, k, u_n, lam_next, lam_out, grad_k, stream=None) -> None:
     d = cfg.desc(_fields(cfg.numel, u_n, k, lam_next, lam_out, grad_k))
     N.check(N.load().adv_heatk_adjoint_step(C.byref(d), _ptr(k), _ptr(u_n), _ptr(lam_next), _ptr(lam_out),
-                                            _ptr(grad_k), N.stream_handle(stream)), "adv_heatk_adjoint_step")
+                                            _ptr(grad_k), _stream(stream, u_n)), "adv_heatk_adjoint_step")
 
 
 def _heatk_buffers(cfg, like, nsteps, interval):
@@ -381,7 +393,7 @@ def burgers_adjoint_step(cfg: BurgersConfig, u_n, u1, u2, dt: float, lam, work=N
         work = torch.empty(3 * one, dtype=torch.uint8, device=u_n.device)
     wp = _buffer(work, 3 * one, "the adjoint work buffer")
     N.check(N.load().adv_burgers_adjoint_step(C.byref(d), _ptr(u_n), _ptr(u1), _ptr(u2), float(dt), _ptr(lam),
-                                              wp, N.stream_handle(stream)), "adv_burgers_adjoint_step")
+                                              wp, _stream(stream, u_n)), "adv_burgers_adjoint_step")
     return lam
 
 
@@ -436,7 +448,7 @@ class Ensemble:
         import torch
         with torch.cuda.device(self.device):
             N.check(self._lib.adv_ensemble_run(self._h, int(heat_steps), N.ADV_ENSEMBLE_DIRECT if direct else 0,
-                                               N.stream_handle(stream)), "adv_ensemble_run")
+                                               _stream(stream, self._keep[0])), "adv_ensemble_run")
 
     def burgers_result(self, i: int) -> tuple[float, int]:
         t = C.c_double(0.0)
@@ -475,7 +487,7 @@ def autotune_heat(cfg: HeatConfig, u, stream=None) -> dict:
     """Picks the heat stage's launch shape for this problem (adv_autotune_heat)."""
     r = N.TuneResult()
     d = cfg.desc(_fields(cfg.numel, u))
-    N.check(N.load().adv_autotune_heat(C.byref(d), _ptr(u), N.stream_handle(stream), C.byref(r)), "adv_autotune_heat")
+    N.check(N.load().adv_autotune_heat(C.byref(d), _ptr(u), _stream(stream, u), C.byref(r)), "adv_autotune_heat")
     return _tune_dict(r)
 
 
@@ -483,7 +495,7 @@ def autotune_burgers(cfg: BurgersConfig, u, stream=None) -> dict:
     """Picks the Burgers stage's launch shape for this problem (adv_autotune_burgers)."""
     r = N.TuneResult()
     d = cfg.desc(_fields(cfg.numel, u))
-    N.check(N.load().adv_autotune_burgers(C.byref(d), _ptr(u), N.stream_handle(stream), C.byref(r)),
+    N.check(N.load().adv_autotune_burgers(C.byref(d), _ptr(u), _stream(stream, u), C.byref(r)),
             "adv_autotune_burgers")
     return _tune_dict(r)
 
@@ -492,7 +504,7 @@ def autotune_heatk(cfg: HeatKConfig, k, u, stream=None) -> tuple[dict, dict]:
     """Picks the heat-with-k(x) step and adjoint launch shapes (adv_autotune_heatk)."""
     r1, r2 = N.TuneResult(), N.TuneResult()
     d = cfg.desc(_fields(cfg.numel, u, k))
-    N.check(N.load().adv_autotune_heatk(C.byref(d), _ptr(k), _ptr(u), N.stream_handle(stream), C.byref(r1),
+    N.check(N.load().adv_autotune_heatk(C.byref(d), _ptr(k), _ptr(u), _stream(stream, u), C.byref(r1),
                                         C.byref(r2)), "adv_autotune_heatk")
     return _tune_dict(r1), _tune_dict(r2)
 
