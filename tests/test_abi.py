@@ -200,3 +200,57 @@ int main(int argc, char** argv) {
     run = subprocess.run([str(exe), str(tmp_path / "result.bin")], capture_output=True, text=True, timeout=60)
     assert run.returncode == 0, (run.returncode, run.stdout, run.stderr)
     assert run.stdout.startswith("ok")
+
+
+def _prototypes(header: Path) -> dict[str, tuple[str, list[str]]]:
+    txt = re.sub(r"/\*.*?\*/", "", header.read_text(), flags=re.S)
+    txt = re.sub(r"^\s*#.*$", "", txt, flags=re.M)
+    out = {}
+    for m in re.finditer(r"([A-Za-z_][\w\s\*]*?)\b(adv_\w+)\s*\(([^()]*)\)\s*;", txt):
+        params = [p.strip() for p in m.group(3).split(",")]
+        if params == ["void"] or params == [""]:
+            params = []
+        out[m.group(2)] = (m.group(1).strip(), params)
+    return out
+
+
+def _ctype_ok(decl: str, ct) -> bool:
+    """Does the ctypes type `ct` pass a C parameter / return value declared as `decl`?"""
+    decl = re.sub(r"\b(const|struct)\b", "", decl)
+    if "*" in decl:
+        base = decl.split("*")[0].split()[0]
+        structs = {"adv_heat_desc": N.HeatDesc, "adv_burgers_desc": N.BurgersDesc, "adv_heatk_desc": N.HeatKDesc,
+                   "adv_heat_member": N.HeatMember, "adv_burgers_member": N.BurgersMember,
+                   "adv_tune_result": N.TuneResult, "adv_checkpoint_header": N.CheckpointHeader}
+        if base == "char":
+            return ct is C.c_char_p
+        if decl.count("*") == 2:
+            return ct is C.POINTER(C.c_void_p)
+        if base in structs:
+            return ct is C.POINTER(structs[base])
+        if base == "adv_ensemble":
+            return ct is C.c_void_p
+        if base == "void":
+            return ct is C.c_void_p
+        scalar = {"double": C.c_double, "int64_t": C.c_int64, "size_t": C.c_size_t, "int": C.c_int,
+                  "int32_t": C.c_int32}[base]
+        return ct is C.POINTER(scalar) or ct is C.c_void_p
+    base = decl.split()[0]
+    scalar = {"double": C.c_double, "int64_t": C.c_int64, "size_t": C.c_size_t, "int": C.c_int, "int32_t": C.c_int32,
+              "uint32_t": C.c_uint32, "adv_status": C.c_int}
+    return ct is scalar[base]
+
+
+def test_ctypes_signatures_match_the_header_prototypes():
+    """Every entry of _native.SIGNATURES passes the same number and kinds of arguments as the C
+    prototype it binds, and every declared entry point is bound."""
+    protos = {**_prototypes(ROOT / "include" / "advdiff.h"), **_prototypes(ROOT / "include" / "advdiff_ref_ops.h")}
+    bound = {name: (res, args) for name, res, args in N.SIGNATURES}
+    assert set(protos) <= set(bound), set(protos) - set(bound)
+    for name, (ret, params) in protos.items():
+        res, args = bound[name]
+        assert len(args) == len(params), (name, params)
+        assert _ctype_ok(ret, res), (name, ret, res)
+        for p, a in zip(params, args):
+            typ = re.sub(r"\s*\b\w+$", "", p) if not p.endswith("*") else p  # drop the parameter name
+            assert _ctype_ok(typ, a), (name, p, a)
