@@ -254,3 +254,31 @@ def test_ctypes_signatures_match_the_header_prototypes():
         for p, a in zip(params, args):
             typ = re.sub(r"\s*\b\w+$", "", p) if not p.endswith("*") else p  # drop the parameter name
             assert _ctype_ok(typ, a), (name, p, a)
+
+
+def test_ctypes_structures_match_the_c_layout(tmp_path):
+    """sizeof and every field offset of the descriptor / member / result structs, as a C compiler
+    lays them out, equal the ctypes Structures the Python host passes."""
+    import shutil
+    if shutil.which("gcc") is None:
+        pytest.skip("no host compiler")
+    structs = {"adv_heat_desc": N.HeatDesc, "adv_burgers_desc": N.BurgersDesc, "adv_heatk_desc": N.HeatKDesc,
+               "adv_heat_member": N.HeatMember, "adv_burgers_member": N.BurgersMember,
+               "adv_tune_result": N.TuneResult, "adv_checkpoint_header": N.CheckpointHeader}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "advdiff.h"', "int main(void) {"]
+    want = []
+    for cname, py in structs.items():
+        lines.append(f'  printf("%zu\\n", sizeof({cname}));')
+        want.append(C.sizeof(py))
+        for fname, _ in py._fields_:
+            lines.append(f'  printf("%zu\\n", offsetof({cname}, {fname}));')
+            want.append(getattr(py, fname).offset)
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", str(ROOT / "include"), str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    assert got == want
