@@ -418,6 +418,8 @@ class Ensemble:
 
     def __init__(self, heat=(), burgers=(), heat_time: int = N.ADV_EULER):
         import torch
+        if not heat and not burgers:
+            raise ValueError("an ensemble needs at least one member")
         self._lib = N.load()
         self._keep = []
         hm = (N.HeatMember * max(len(heat), 1))()

@@ -89,6 +89,8 @@ def test_heatk_and_ensemble_members_are_checked():
         S.Ensemble(heat=[(HEAT, FakeCuda(HEAT.numel - 1))])
     with pytest.raises(ValueError, match="elements"):
         S.Ensemble(burgers=[(BURG, FakeCuda(10), 0.1, 0.4)])
+    with pytest.raises(ValueError, match="at least one member"):
+        S.Ensemble()
 
 
 class FakeLib:
