@@ -871,6 +871,9 @@ def main():
                                  "unit": "TFLOP/s", "frac": flops / fp32_peak,
                                  "peak_source": f"nominal: {sms} SMs x 128 FP32 lanes x 2 flop x {sm_mhz:.0f} MHz",
                                  "flops_per_cell_stage": BURGERS_FLOPS_PER_CELL_STAGE}
+        # FP32 state after three time steps from the initial state, to compare with the FP64 run
+        u32 = u0.clone()
+        burgers_run(cfg, u32, 1e9, 0.4, N.ADV_DT_MAXU, max_steps=3, workspace=burgers_workspace(cfg, u32), stream=sh)
         # FP64 state, same problem: the reference's operand order (bit-exact with the oracle) and
         # the common-denominator form (ADV_DIV_FAST), two steps each
         for key, div in (("f64_value", N.ADV_DIV_F32), ("f64_fast_value", N.ADV_DIV_FAST)):
@@ -885,6 +888,10 @@ def main():
             ev1.record(stream)
             torch.cuda.synchronize()
             extra[key] = cfg.numel * 3 * 2 / (ev0.elapsed_time(ev1) * 1e-3) / 1e9
+            if key == "f64_value":  # u64: three steps in the reference's FP64 arithmetic
+                extra["rel_l2_vs_fp64"] = (torch.linalg.vector_norm(u32.double() - u64) /
+                                           torch.linalg.vector_norm(u64)).item()
+                extra["rel_l2_vs_fp64_after"] = "3 time steps (FP32 with its own max|u| dt)"
             del u64, ws64
 
     # ---- CPU baseline (oracle on the host cores, rank 0, N = 1 only)
