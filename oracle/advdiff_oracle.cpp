@@ -12,7 +12,8 @@
 //
 // Parity pins (checked by tests/test_oracle_golden.py):
 //   * Matlab_Prototipes/DiffusionNd/TestingAccuracy.log:53-72 (O4 + SSP-RK3 heat 1D/2D/3D),
-//     reproduced by orc_heat_accuracy() which follows diffusion{1,2,3}dTest.m literally;
+//     reproduced by orc_heat_accuracy() which follows diffusion{1,2,3}dTest.m literally, and
+//     the same functions run through an interpreter for their MATLAB subset (full precision);
 //   * recorded "Final Time" 0.325 / 0.329157 (SingleGPU/Diffusion2d/Run.m:11,
 //     SingleGPU/Diffusion3d_baselineCode/Run.m:11) via the reference dt rule;
 //   * recorded iteration counts 86 / 167 / 267 of the Burgers dt loop

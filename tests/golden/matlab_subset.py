@@ -1,21 +1,27 @@
 """A small interpreter for the subset of MATLAB used by the reference's Burgers prototypes.
 
-Fixture generation only (see make_weno_golden.py). It runs, on numpy arrays, the prototype
-files Matlab_Prototipes/InviscidBurgersNd/WENO{5,7}resAdv_{X,Y,Z,1d}.m and the solver-loop
-sections of LFWENO{5,7}FDM{2,3}d.m, so that the CPU oracle's restatement of those schemes can
-be checked against the reference's own code without MATLAB.
+Fixture generation only (see make_weno_golden.py and make_heat_golden.py). It runs, on numpy
+arrays, the prototype files Matlab_Prototipes/InviscidBurgersNd/WENO{5,7}resAdv_{X,Y,Z,1d}.m,
+the solver-loop sections of LFWENO{5,7}FDM{2,3}d.m and the heat accuracy functions
+Matlab_Prototipes/DiffusionNd/diffusion{1,2,3}dTest.m with Laplace{1,2,3}d.m, so that the CPU
+oracle's restatement of those schemes can be checked against the reference's own code without
+MATLAB.
 
-Supported: numbers, identifiers, `+ - * / ^ .* ./ .^`, unary minus, comparisons, ranges
-`a:b` / `a:s:b`, row literals `[a b, c]`, anonymous functions `@(w) expr`, 1-based indexing
-with `:` (MATLAB's outer-product semantics; a single index is linear, column-major), indexed
-assignment, `function out = name(args)` files, `while` / `if` / `for` ... `end`, and the
-builtins the files call (cat, zeros, size, abs, max, exp, rem, ones; plotting calls are
-no-ops). Elementwise operations are evaluated one at a time in the order the source writes
-them, as MATLAB does, so results match MATLAB's double arithmetic operation by operation.
-Anything outside the subset raises an error instead of guessing.
+Supported: numbers, strings, identifiers, `+ - * / ^ .* ./ .^`, unary minus, comparisons,
+`&&` / `||`, ranges `a:b` / `a:s:b` (a non-unit step gives a + k*s), row literals `[a b, c]`,
+anonymous functions `@(w) expr`, 1-based indexing with `:` (MATLAB's outer-product semantics;
+a single index is linear, column-major), indexed assignment, `function out = name(args)` and
+`function [a, b] = name(args)` files, `[a, b] = f(...)`, `while` / `if` / `for` / `switch` ...
+`end`, and the builtins the files call (cat, zeros, ones, size, abs, exp, sqrt, sum, max,
+norm(v, inf), rem, meshgrid; plotting and printing calls are no-ops). Elementwise operations are
+evaluated one at a time in the order the source writes them, as MATLAB does, so results match
+MATLAB's double arithmetic operation by operation (ranges with a non-unit step may differ from
+MATLAB's colon in the last bit). Anything outside the subset raises an error instead of
+guessing.
 """
 from __future__ import annotations
 
+import math
 import re
 from pathlib import Path
 
@@ -23,6 +29,7 @@ import numpy as np
 
 _TOKEN = re.compile(r"""
   (?P<num>(?:\d+\.\d*|\.\d+|\d+)(?:[eE][+-]?\d+)?)
+| (?P<str>'(?:[^'\n]|'')*')
 | (?P<id>[A-Za-z_]\w*)
 | (?P<op>\.\*|\./|\.\^|==|~=|<=|>=|&&|\|\||[-+*/^()\[\],;:=<>@])
 | (?P<nl>\n)
@@ -30,7 +37,8 @@ _TOKEN = re.compile(r"""
 """, re.X)
 
 _NOOP_CALLS = {"surf", "plot", "axis", "view", "drawnow", "shg", "title", "xlabel", "ylabel",
-               "zlabel", "colorbar", "print", "figure", "hold", "grid"}
+               "zlabel", "colorbar", "print", "figure", "hold", "grid", "fprintf", "disp", "tic",
+               "toc", "clc", "clear", "close"}
 
 
 class MatlabError(RuntimeError):
@@ -38,14 +46,36 @@ class MatlabError(RuntimeError):
 
 
 def _strip(src: str) -> str:
-    """Removes % comments and joins `...` continuation lines (no strings in the subset)."""
-    lines = []
-    for line in src.splitlines():
-        if "'" in line.split("%", 1)[0]:
-            raise MatlabError("strings/transpose are outside the subset: " + line.strip())
-        lines.append(line.split("%", 1)[0])
-    out = "\n".join(lines)
-    return re.sub(r"\.\.\.[^\n]*\n", " ", out)
+    """Removes % comments and joins `...` continuation lines, leaving strings intact. A quote
+    directly after a value (MATLAB's transpose) is outside the subset."""
+    out, i, n = [], 0, len(src)
+    while i < n:
+        c = src[i]
+        if c == "%":
+            while i < n and src[i] != "\n":
+                i += 1
+            continue
+        if src.startswith("...", i):
+            while i < n and src[i] != "\n":
+                i += 1
+            out.append(" ")
+            i += 1
+            continue
+        if c == "'":
+            before = src[i - 1] if i else ""
+            if before and (before.isalnum() or before in "_)]}.'"):  # a quote right after a value
+                raise MatlabError("transpose is outside the subset")
+            j = i + 1
+            while j < n and not (src[j] == "'" and not src.startswith("''", j)):
+                if src[j] == "\n":
+                    raise MatlabError("unterminated string")
+                j += 2 if src.startswith("''", j) else 1
+            out.append(src[i:j + 1])
+            i = j + 1
+            continue
+        out.append(c)
+        i += 1
+    return "".join(out)
 
 
 def _tokenize(src: str):
@@ -128,10 +158,16 @@ class _Parser:
             return ("while", cond, body)
         if tok == ("id", "if"):
             self.next()
-            cond = self.expr()
-            body = self.block({"end"})
-            self.expect("end")
-            return ("if", cond, body)
+            branches = [(self.expr(), self.block({"elseif", "else", "end"}))]
+            orelse = []
+            while True:
+                if self.accept("elseif"):
+                    branches.append((self.expr(), self.block({"elseif", "else", "end"})))
+                elif self.accept("else"):
+                    orelse = self.block({"end"})
+                else:
+                    self.expect("end")
+                    return ("if", branches, orelse)
         if tok == ("id", "for"):
             self.next()
             var = self.next()[1]
@@ -140,6 +176,38 @@ class _Parser:
             body = self.block({"end"})
             self.expect("end")
             return ("for", var, rng, body)
+        if tok == ("id", "switch"):
+            self.next()
+            subject = self.expr()
+            cases, otherwise = [], []
+            while True:
+                while self.peek()[0] == "nl" or self.peek()[1] in (";", ","):
+                    self.next()
+                if self.accept("case"):
+                    value = self.expr()
+                    cases.append((value, self.block({"case", "otherwise", "end"})))
+                elif self.accept("otherwise"):
+                    otherwise = self.block({"case", "otherwise", "end"})
+                else:
+                    self.expect("end")
+                    return ("switch", subject, cases, otherwise)
+        # multiple assignment `[a, b] = f(...)`
+        if tok == ("op", "["):
+            save = self.i
+            self.next()
+            names = []
+            while True:
+                self.skip_ws()
+                if self.peek()[0] != "id":
+                    break
+                names.append(self.next()[1])
+                self.skip_ws()
+                if not self.accept(","):
+                    break
+            if names and self.accept("]") and self.peek()[1] == "=":
+                self.next()
+                return ("massign", names, self.expr())
+            self.i = save
         # assignment `name = e` / `name(args) = e`, or a bare call
         if tok[0] == "id":
             save = self.i
@@ -156,7 +224,21 @@ class _Parser:
 
     # expressions -----------------------------------------------------------------------
     def expr(self):
-        return self.comparison()
+        return self.oror()
+
+    def oror(self):
+        left = self.andand()
+        while self.peek()[1] == "||":
+            self.next()
+            left = ("or", left, self.andand())
+        return left
+
+    def andand(self):
+        left = self.comparison()
+        while self.peek()[1] == "&&":
+            self.next()
+            left = ("and", left, self.comparison())
+        return left
 
     def comparison(self):
         left = self.range_()
@@ -263,6 +345,8 @@ class _Parser:
         kind, text = self.next()
         if kind == "num":
             return ("num", float(text))
+        if kind == "str":
+            return ("str", text[1:-1].replace("''", "'"))
         if kind == "id":
             return ("id", text)
         if text == "(":
@@ -317,10 +401,33 @@ def _squeeze_trailing(a):
     return a
 
 
+def _scalar_index(shape, idx):
+    """Zero-based multi-index of all-scalar MATLAB indices (a single one is linear,
+    column-major), or None when any index is not a scalar."""
+    if not all(isinstance(v, (float, int)) for v in idx):
+        return None
+    ints = [int(v) for v in idx]
+    if any(v != w or v < 1 for v, w in zip(ints, idx)):
+        raise MatlabError("non-integer or non-positive index")
+    if len(ints) == 1:
+        if ints[0] > int(np.prod(shape)):
+            raise MatlabError("index out of range")
+        return np.unravel_index(ints[0] - 1, shape, order="F")
+    if len(ints) < len(shape) or any(v != 1 for v in ints[len(shape):]):
+        return None
+    out = tuple(v - 1 for v in ints[:len(shape)])
+    if any(v >= n for v, n in zip(out, shape)):
+        raise MatlabError("index out of range")
+    return out
+
+
 def _index(arr, idx):
     arr = np.asarray(arr, dtype=np.float64)
     if arr.ndim < 2:
         arr = arr.reshape(1, -1)
+    at = _scalar_index(arr.shape, idx)
+    if at is not None:
+        return float(arr[at])
     if len(idx) == 1:
         flat = arr.reshape(-1, order="F")
         if isinstance(idx[0], tuple):
@@ -371,6 +478,34 @@ def _ones(*args):
     return _zeros(*args) + 1.0
 
 
+def _matlab_sum(a):
+    a = np.asarray(a, dtype=np.float64)
+    if a.ndim <= 2 and (a.ndim < 2 or min(a.shape) == 1):
+        total = 0.0
+        for v in a.reshape(-1):  # left to right, one rounding per addition
+            total += float(v)
+        return total
+    raise MatlabError("sum over a matrix is outside the subset")
+
+
+def _norm(a, p=2.0):
+    a = np.asarray(a, dtype=np.float64)
+    if (a.ndim < 2 or min(a.shape) == 1) and np.isinf(p):
+        return float(np.max(np.abs(a)))
+    raise MatlabError("only the vector infinity norm is in the subset")
+
+
+def _meshgrid(*axes):
+    vs = [np.asarray(v, dtype=np.float64).reshape(-1) for v in axes]
+    if len(vs) == 2:
+        x, y = np.meshgrid(vs[0], vs[1], indexing="xy")
+        return x, y
+    if len(vs) == 3:
+        x, y, z = np.meshgrid(vs[0], vs[1], vs[2], indexing="xy")  # (ny, nx, nz), as MATLAB
+        return x, y, z
+    raise MatlabError("meshgrid of 2 or 3 vectors only")
+
+
 BUILTINS = {
     "cat": _cat,
     "zeros": _zeros,
@@ -381,7 +516,15 @@ BUILTINS = {
     "exp": lambda a: np.exp(np.asarray(a, dtype=np.float64)),
     "max": _matlab_max,
     "rem": lambda a, b: float(np.fmod(_scalar(a), _scalar(b))),
+    "sqrt": lambda a: np.sqrt(a) if isinstance(a, float) else np.sqrt(np.asarray(a, dtype=np.float64)),
+    "sum": _matlab_sum,
+    "norm": _norm,
+    "meshgrid": _meshgrid,
+    "inf": lambda: np.inf,
+    "Inf": lambda: np.inf,
+    "pi": lambda: np.pi,
 }
+_MULTI_OUTPUT = {"meshgrid"}
 
 
 class Interpreter:
@@ -399,24 +542,31 @@ class Interpreter:
         self._exec(body, env)
         return env
 
-    def call_file(self, name: str, args: list):
+    def call_file(self, name: str, args: list, nargout: int = 1, env_out: dict | None = None):
+        """Runs function file `name`.m; returns its first output, or a list of the first
+        `nargout` outputs. env_out, if given, receives the function's final workspace."""
         if name not in self._files:
             if self.fdir is None:
                 raise MatlabError(f"unknown function {name}")
             src = _strip((self.fdir / f"{name}.m").read_text())
-            m = re.match(r"\s*function\s+(\w+)\s*=\s*(\w+)\s*\(([^)]*)\)", src)
-            if not m or m.group(2) != name:
-                raise MatlabError(f"{name}.m is not a one-output function file")
-            params = [p.strip() for p in m.group(3).split(",") if p.strip()]
+            m = re.match(r"\s*function\s+(?:\[([^\]]*)\]|(\w+))\s*=\s*(\w+)\s*\(([^)]*)\)", src)
+            if not m or m.group(3) != name:
+                raise MatlabError(f"{name}.m is not a function file")
+            outs = [o.strip() for o in (m.group(1) or m.group(2)).split(",") if o.strip()]
+            params = [p.strip() for p in m.group(4).split(",") if p.strip()]
             body = _Parser(_tokenize(src[m.end():])).block(set())
-            self._files[name] = (m.group(1), params, body)
-        out, params, body = self._files[name]
+            self._files[name] = (outs, params, body)
+        outs, params, body = self._files[name]
         if len(args) != len(params):
             raise MatlabError(f"{name} takes {len(params)} arguments")
+        if nargout > len(outs):
+            raise MatlabError(f"{name} has {len(outs)} outputs")
         self.calls[name] = self.calls.get(name, 0) + 1
         env = dict(zip(params, args))
         self._exec(body, env)
-        return env[out]
+        if env_out is not None:
+            env_out.update(env)
+        return env[outs[0]] if nargout == 1 else [env[o] for o in outs[:nargout]]
 
     # -- statements ---------------------------------------------------------------------
     def _exec(self, body, env):
@@ -439,13 +589,35 @@ class Interpreter:
                     if guard > 1_000_000:
                         raise MatlabError("while loop did not end")
             elif kind == "if":
-                if self._truth(self._eval(st[1], env)):
+                for cond, body in st[1]:
+                    if self._truth(self._eval(cond, env)):
+                        self._exec(body, env)
+                        break
+                else:
                     self._exec(st[2], env)
             elif kind == "for":
                 rng = np.asarray(self._eval(st[2], env), dtype=np.float64).reshape(-1)
                 for v in rng:
                     env[st[1]] = float(v)
                     self._exec(st[3], env)
+            elif kind == "switch":
+                subject = self._eval(st[1], env)
+                for value, body in st[2]:
+                    v = self._eval(value, env)
+                    same = (subject == v) if isinstance(subject, str) or isinstance(v, str) else \
+                        bool(np.all(np.asarray(subject) == np.asarray(v)))
+                    if same:
+                        self._exec(body, env)
+                        break
+                else:
+                    self._exec(st[3], env)
+            elif kind == "massign":
+                names, e = st[1], st[2]
+                if e[0] != "call" or e[1][0] != "id":
+                    raise MatlabError("multiple assignment needs a function call")
+                vals = self._eval(e, env, nargout=len(names))
+                for nm, v in zip(names, vals):
+                    env[nm] = v
             else:
                 raise MatlabError("statement kind " + kind)
 
@@ -459,6 +631,20 @@ class Interpreter:
         if not isinstance(arr, np.ndarray):
             raise MatlabError("indexed assignment to a non-array")
         idx = [("colon",) if a == ("colon",) else self._eval(a, env) for a in args]
+        at = _scalar_index(arr.shape, idx)
+        if at is not None:
+            if not _is_scalar(val):
+                raise MatlabError("assignment of an array to one element")
+            arr[at] = _scalar(val)
+            return
+        if len(idx) == 1:  # linear (column-major) positions
+            flat = _as_index(idx[0], arr.size)
+            pos = np.unravel_index(flat, arr.shape, order="F")
+            v = np.asarray(val, dtype=np.float64).reshape(-1)
+            if v.size not in (1, flat.size):
+                raise MatlabError("linear assignment of a wrong number of values")
+            arr[pos] = v
+            return
         if len(idx) < arr.ndim:
             raise MatlabError("fewer indices than dimensions is outside the subset")
         view = arr.reshape(arr.shape + (1,) * (len(idx) - arr.ndim))
@@ -474,10 +660,16 @@ class Interpreter:
         view[np.ix_(*sel)] = v
 
     # -- expressions --------------------------------------------------------------------
-    def _eval(self, n, env):
+    def _eval(self, n, env, nargout: int = 1):
         kind = n[0]
         if kind == "num":
             return n[1]
+        if kind == "str":
+            return n[1]
+        if kind == "and":
+            return 1.0 if self._truth(self._eval(n[1], env)) and self._truth(self._eval(n[2], env)) else 0.0
+        if kind == "or":
+            return 1.0 if self._truth(self._eval(n[1], env)) or self._truth(self._eval(n[2], env)) else 0.0
         if kind == "id":
             name = n[1]
             if name in env:
@@ -495,9 +687,11 @@ class Interpreter:
             a = _scalar(self._eval(n[1], env))
             s = 1.0 if n[2] is None else _scalar(self._eval(n[2], env))
             b = _scalar(self._eval(n[3], env))
-            if s != 1.0 or a != round(a):
-                raise MatlabError("only integer ranges with unit step are in the subset")
-            return np.arange(a, b + 1.0, 1.0).reshape(1, -1)
+            if s == 0.0:
+                raise MatlabError("range with a zero step")
+            q = (b - a) / s
+            k = round(q) if abs(q - round(q)) <= 1e-10 * max(1.0, abs(q)) else math.floor(q)
+            return (a + s * np.arange(max(int(k) + 1, 0), dtype=np.float64)).reshape(1, -1)
         if kind == "row":
             vals = [self._eval(e, env) for e in n[1]]
             if all(_is_scalar(v) for v in vals):
@@ -526,8 +720,13 @@ class Interpreter:
                 if name in env and callable(env[name]):
                     return env[name](*args)
                 if name in BUILTINS:
-                    return BUILTINS[name](*args)
-                return self.call_file(name, args)
+                    out = BUILTINS[name](*args)
+                    if name in _MULTI_OUTPUT:
+                        return list(out[:nargout]) if nargout > 1 else out[0]
+                    if nargout > 1:
+                        raise MatlabError(f"{name} has one output")
+                    return out
+                return self.call_file(name, args, nargout)
             raise MatlabError("call of an expression")
         raise MatlabError("node kind " + kind)
 

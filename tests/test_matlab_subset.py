@@ -58,8 +58,33 @@ def test_outside_the_subset_is_refused():
     with pytest.raises(MatlabError):
         run("a = [1 2; 3 4] * [1 2; 3 4];")
     with pytest.raises(MatlabError):
-        run("x = 0:0.5:2;")
+        run("c = {1, 2};")  # cell arrays
     with pytest.raises(MatlabError):
-        run("s = 'text';")
+        run("a = [1 2]; b = a';")  # transpose
     with pytest.raises(MatlabError):
         run("y = undefined_function(1);")
+
+
+def test_strings_switch_logic_ranges_and_multiple_outputs():
+    e = run("s = 'dont'; switch s\n case 'add'; v = 1;\n case 'dont'; v = 2;\n otherwise\n v = 3;\n end\n"
+            "x = -1:0.5:1; k = 0; if (k > 0 && undefined_function(1)) || k == 0, k = 5; end\n"
+            "[X, Y] = meshgrid(1:3, 10:10:20); u = zeros(size(X)); u(4) = 7; u(2, 3) = 9;\n"
+            "t = sum(x); m = norm([1 -4 2], inf); f = 'L: %1.2e \\n'; fprintf(f, t);")
+    assert e["v"] == 2.0 and e["k"] == 5.0 and e["t"] == 0.0 and e["m"] == 4.0
+    np.testing.assert_array_equal(e["x"], [[-1.0, -0.5, 0.0, 0.5, 1.0]])
+    np.testing.assert_array_equal(e["X"], [[1, 2, 3], [1, 2, 3]])
+    np.testing.assert_array_equal(e["Y"], [[10, 10, 10], [20, 20, 20]])
+    np.testing.assert_array_equal(e["u"], [[0, 0, 0], [0, 7, 9]])  # linear index 4 = (2, 2), column-major
+
+
+def test_function_files_with_several_outputs(tmp_path):
+    (tmp_path / "twoout.m").write_text("function [s, p] = twoout(a, b)\n% sum and product\ns = a + b;\np = a * b;\n")
+    it = Interpreter(tmp_path)
+    env = it.run("[a, b] = twoout(3, 4); c = twoout(1, 2);", {})
+    assert (env["a"], env["b"], env["c"]) == (7.0, 12.0, 3.0)
+    assert it.call_file("twoout", [2.0, 5.0], nargout=2) == [7.0, 10.0]
+
+
+def test_if_elseif_else():
+    e = run("for k = 1:3\n if k == 1, a = 1; elseif k == 2\n b = 2; else\n c = 3; end\n end")
+    assert (e["a"], e["b"], e["c"]) == (1.0, 2.0, 3.0)
