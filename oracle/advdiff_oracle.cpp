@@ -598,11 +598,14 @@ void burgers_step_adjoint(const BurgersCfg& c, const T* un, const T* u1, const T
 //     WENO5, 3 left / 4 right for WENO7: a clamped index); fluxes are formed at the faces
 //     i+1/2, i = 0..N-1, and the face left of cell 0 is taken as 0, so
 //     res_i = (F_{i+1/2} - F_{i-1/2}) / h with F_{-1/2} = 0 (WENO7resAdv_X.m:56-58, 148).
-//   * WENO5: Jiang-Shu weights, the same candidate stencils as the CUDA code (weno_face).
+//   * WENO5: Jiang-Shu weights d_k / (eps + beta_k)^2 (WENO5resAdv_X.m:62-120).
 //   * WENO7: the seven-point WENO of Balsara & Shu (J. Comput. Phys. 160 (2000) 405-452):
 //     four cubic candidates with linear weights 1/35, 12/35, 18/35, 4/35 and weights
 //     d_k / (eps + beta_k)^2, eps = 1e-6; the smoothness indicators are the prototype's
 //     integer quadratic forms (WENO7resAdv_X.m:75-82).
+//   * Both are evaluated in the prototypes' operand order: the FP64 results equal theirs bit
+//     for bit (WENO7's indicators cancel to rounding residues that are not small against eps,
+//     so another summation order would differ by far more than one rounding).
 //   * Time loops: dt = CFL dx / max|u| trimmed to land on tEnd; WENO5 with SSP-RK3, WENO7 with
 //     the five-stage, fourth-order low-storage Runge-Kutta scheme of Carpenter & Kennedy
 //     (NASA TM-109112, 1994) in its 2N-storage form r = A_s r + dt R(u), u = u - B_s r
@@ -610,51 +613,112 @@ void burgers_step_adjoint(const BurgersCfg& c, const T* un, const T* u1, const T
 // ------------------------------------------------------------------------------------------
 namespace {
 
-// beta_0 of the WENO7 stencil over (f0, f1, f2, f3) and beta_1 over (f1, f2, f3, f4) as upper-
-// triangular quadratic forms, entries (00, 01, 02, 03, 11, 12, 13, 22, 23, 33). beta_2 and beta_3
-// are beta_1 and beta_0 of the mirrored stencil (the prototype's coefficients have that symmetry).
-constexpr double kW7Beta0[10] = {6649, -47214, 56694, -22778, 85641, -210282, 86214, 134241, -114894, 25729};
-constexpr double kW7Beta1[10] = {3169, -19374, 19014, -5978, 33441, -70602, 23094, 41001, -30414, 6649};
+// The face fluxes below are evaluated in the prototypes' own operand order (sums left to right
+// as the .m files write them, `a - k*b` as `a + (-k)*b`, which rounds identically), so the FP64
+// results are bit for bit those of the prototypes. Every smoothness indicator of WENO7 has the
+// form  x2*(k0*x2 + k1*x3) + x0*(((k2*xb + k3*xc) + k4*xd) + k5*x3) + k6*x3*x3
+//        + x1*((k7*xs + k8*xt) + k9*x3)  over its four cells x0..x3 (WENO7resAdv_X.m:75-82).
+struct W7Beta {
+  int b, c, d;      // cells of the second term's first three products
+  int s, t;         // cells of the fourth term's first two products
+  double k[10];
+};
+constexpr W7Beta kW7Beta[4] = {
+    {2, 1, 0, 2, 1, {134241, -114894, 56694, -47214, 6649, -22778, 25729, -210282, 85641, 86214}},
+    {1, 0, 2, 1, 2, {41001, -30414, -19374, 3169, 19014, -5978, 6649, 33441, -70602, 23094}},
+    {0, 1, 2, 1, 2, {33441, -19374, 6649, -30414, 23094, -5978, 3169, 41001, -70602, 19014}},
+    {0, 1, 2, 1, 2, {85641, -47214, 25729, -114894, 86214, -22778, 6649, 134241, -210282, 56694}},
+};
+// Candidate reconstructions (c0 x0 + c1 x1 + c2 x2 + c3 x3)/12 of the two split parts: rows for
+// the part moving towards +x (cells i-3+k .. i+k) and towards -x (cells i-2+k .. i+1+k).
+constexpr double kW7PolyPlus[4][4] = {{-3, 13, -23, 25}, {1, -5, 13, 3}, {-1, 7, 7, -1}, {3, 13, -5, 1}};
+constexpr double kW7PolyMinus[4][4] = {{1, -5, 13, 3}, {-1, 7, 7, -1}, {3, 13, -5, 1}, {25, -23, 13, -3}};
+constexpr double kW7LinPlus[4] = {1. / 35., 12. / 35., 18. / 35., 4. / 35.};
+constexpr double kW7LinMinus[4] = {4. / 35., 18. / 35., 12. / 35., 1. / 35.};
 
+// One split part's WENO7 face value from its seven cells f[0..6] (its four stencils are
+// f[k..k+3]); `poly` and `lin` select the +x or -x part.
 template <class T>
-inline T quad_form4(const double q[10], T a, T b, T c, T d) {
-  return a * ((T)q[0] * a + (T)q[1] * b + (T)q[2] * c + (T)q[3] * d) + b * ((T)q[4] * b + (T)q[5] * c + (T)q[6] * d) +
-         c * ((T)q[7] * c + (T)q[8] * d) + (T)q[9] * d * d;
+inline T weno7_part(const T f[7], const double (&poly)[4][4], const double (&lin)[4]) {
+  const T eps = (T)1e-6;
+  T a[4];
+  for (int k = 0; k < 4; ++k) {
+    const T* x = f + k;
+    const W7Beta& B = kW7Beta[k];
+    const double* q = B.k;
+    const T t1 = x[2] * ((T)q[0] * x[2] + (T)q[1] * x[3]);
+    const T t2 = x[0] * ((((T)q[2] * x[B.b] + (T)q[3] * x[B.c]) + (T)q[4] * x[B.d]) + (T)q[5] * x[3]);
+    const T t3 = (T)q[6] * (x[3] * x[3]);
+    const T t4 = x[1] * (((T)q[7] * x[B.s] + (T)q[8] * x[B.t]) + (T)q[9] * x[3]);
+    const T beta = ((t1 + t2) + t3) + t4;
+    a[k] = (T)lin[k] / ((eps + beta) * (eps + beta));
+  }
+  const T sum = ((a[0] + a[1]) + a[2]) + a[3];
+  T h = 0;
+  for (int k = 0; k < 4; ++k) {
+    const T* x = f + k;
+    const T cand = (((T)poly[k][0] * x[0] + (T)poly[k][1] * x[1]) + (T)poly[k][2] * x[2]) + (T)poly[k][3] * x[3];
+    const T term = (a[k] / sum) * cand / (T)12;
+    h = k == 0 ? term : h + term;
+  }
+  return h;
 }
 
-// Reconstruction at the face between f[3] and f[4] of the flux part moving towards +x, from
-// the seven cells f[0..6] around it. The part moving towards -x uses the mirrored stencil.
+// WENO7 reconstruction at the face between f[3] and f[4] of the part moving towards +x, from the
+// seven cells f[0..6] around it (the prototypes' hn).
 template <class T>
 inline T weno7_side(const T f[7]) {
-  const T eps = (T)1e-6;
-  const T b0 = quad_form4<T>(kW7Beta0, f[0], f[1], f[2], f[3]);
-  const T b1 = quad_form4<T>(kW7Beta1, f[1], f[2], f[3], f[4]);
-  const T b2 = quad_form4<T>(kW7Beta1, f[5], f[4], f[3], f[2]);
-  const T b3 = quad_form4<T>(kW7Beta0, f[6], f[5], f[4], f[3]);
-  const T a0 = (T)(1. / 35.) / ((eps + b0) * (eps + b0));
-  const T a1 = (T)(12. / 35.) / ((eps + b1) * (eps + b1));
-  const T a2 = (T)(18. / 35.) / ((eps + b2) * (eps + b2));
-  const T a3 = (T)(4. / 35.) / ((eps + b3) * (eps + b3));
-  const T q0 = (-(T)3 * f[0] + (T)13 * f[1] - (T)23 * f[2] + (T)25 * f[3]) / (T)12;
-  const T q1 = (f[1] - (T)5 * f[2] + (T)13 * f[3] + (T)3 * f[4]) / (T)12;
-  const T q2 = (-f[2] + (T)7 * f[3] + (T)7 * f[4] - f[5]) / (T)12;
-  const T q3 = ((T)3 * f[3] + (T)13 * f[4] - (T)5 * f[5] + f[6]) / (T)12;
-  return (a0 * q0 + a1 * q1 + a2 * q2 + a3 * q3) / (a0 + a1 + a2 + a3);
+  return weno7_part<T>(f, kW7PolyPlus, kW7LinPlus);
 }
 
-// Face flux at i+1/2 from the split parts: `fp(j)` / `fm(j)` give the parts at cell i+j.
+// One split part's WENO5 face value in WENO5resAdv_X.m's order (:62-120): cells x[0..4], linear
+// weights d, candidates (c . x[k..k+2]) / 6 with rows `poly`.
+template <class T>
+inline T weno5_part(const T x[5], const double (&d)[3], const double (&poly)[3][3]) {
+  const T eps = (T)1e-6, c1312 = (T)(13. / 12.), c14 = (T)(1. / 4.);
+  // (a, b) of 13/12 a^2 + 1/4 b^2 per stencil
+  const T a0 = (x[0] - (T)2 * x[1]) + x[2], b0 = (x[0] - (T)4 * x[1]) + (T)3 * x[2];
+  const T a1 = (x[1] - (T)2 * x[2]) + x[3], b1 = x[1] - x[3];
+  const T a2 = (x[2] - (T)2 * x[3]) + x[4], b2 = ((T)3 * x[2] - (T)4 * x[3]) + x[4];
+  const T B[3] = {c1312 * (a0 * a0) + c14 * (b0 * b0), c1312 * (a1 * a1) + c14 * (b1 * b1),
+                  c1312 * (a2 * a2) + c14 * (b2 * b2)};
+  T al[3];
+  for (int k = 0; k < 3; ++k) al[k] = (T)d[k] / ((eps + B[k]) * (eps + B[k]));
+  const T sum = (al[0] + al[1]) + al[2];
+  T h = 0;
+  for (int k = 0; k < 3; ++k) {
+    const T cand = ((T)poly[k][0] * x[k] + (T)poly[k][1] * x[k + 1]) + (T)poly[k][2] * x[k + 2];
+    const T term = (al[k] / sum) * cand / (T)6;
+    h = k == 0 ? term : h + term;
+  }
+  return h;
+}
+constexpr double kW5LinPlus[3] = {1. / 10., 6. / 10., 3. / 10.};
+constexpr double kW5LinMinus[3] = {3. / 10., 6. / 10., 1. / 10.};
+constexpr double kW5PolyPlus[3][3] = {{2, -7, 11}, {-1, 5, 2}, {2, 5, -1}};
+constexpr double kW5PolyMinus[3][3] = {{-1, 5, 2}, {2, 5, -1}, {11, -7, 2}};
+
+// The two split parts' face values (hp, hn) at i+1/2: `part(j, side)` gives cell i+j of the
+// part moving towards +x (side 0) or -x (side 1).
 template <class T, class G>
-inline T proto_face(int order, G part) {
+inline void proto_face(int order, G part, T* hp, T* hn) {
   if (order == 7) {
     T p[7], m[7];
     for (int j = 0; j < 7; ++j) {
-      p[j] = part(j - 3, 0);   // cells i-3 .. i+3
-      m[j] = part(4 - j, 1);   // cells i+4 .. i-2 (mirrored)
+      p[j] = part(j - 3, 0);  // cells i-3 .. i+3
+      m[j] = part(j - 2, 1);  // cells i-2 .. i+4
     }
-    return weno7_side<T>(p) + weno7_side<T>(m);
+    *hn = weno7_part<T>(p, kW7PolyPlus, kW7LinPlus);
+    *hp = weno7_part<T>(m, kW7PolyMinus, kW7LinMinus);
+    return;
   }
-  return weno_face<T, T>(0, part(-2, 0), part(-1, 0), part(0, 0), part(1, 0), part(2, 0), part(-1, 1), part(0, 1),
-                         part(1, 1), part(2, 1), part(3, 1));
+  T p[5], m[5];
+  for (int j = 0; j < 5; ++j) {
+    p[j] = part(j - 2, 0);  // cells i-2 .. i+2
+    m[j] = part(j - 1, 1);  // cells i-1 .. i+3
+  }
+  *hn = weno5_part<T>(p, kW5LinPlus, kW5PolyPlus);
+  *hp = weno5_part<T>(m, kW5LinMinus, kW5PolyMinus);
 }
 
 // res = d f(u) / d axis on every node, by the prototype residual function of `order` (5 or 7);
@@ -684,15 +748,17 @@ void proto_residual(int order, int axis, int line_max, int nx, int ny, int nz, d
       fp[i] = (T)0.5 * (f + a * v);
       fm[i] = (T)0.5 * (f - a * v);
     }
-    T left = 0;  // F_{-1/2}
+    T hp0 = 0, hn0 = 0;  // the face left of cell 0 is zero
     for (int i = 0; i < N; ++i) {
       auto part = [&](int j, int side) -> T {
         const int k = std::min(std::max(i + j, 0), N - 1);
         return side == 0 ? fp[k] : fm[k];
       };
-      const T right = proto_face<T>(order, part);
-      out[(size_t)i * stride] = (right - left) / (T)h;
-      left = right;
+      T hp1, hn1;
+      proto_face<T>(order, part, &hp1, &hn1);
+      out[(size_t)i * stride] = (((hp1 + hn1) - hp0) - hn0) / (T)h;  // res = (hp+hn-hp'-hn')/dx
+      hp0 = hp1;
+      hn0 = hn1;
     }
   }
 }

@@ -7,12 +7,14 @@ The prototype files run unmodified through tests/golden/matlab_subset.py:
   2D fields) and WENO{5,7}resAdv1d.m, on seeded random fields (signs mixed, so both split
   parts matter) and on the drivers' smooth Gaussian;
 * the "Solver Loop" sections of LFWENO{5,7}FDM{2,3}d.m, with the drivers' own flux handles,
-  CFL and tEnd, on grids smaller than the drivers' 100^d (the only change: nx, ny, nz).
+  CFL and tEnd, on grids smaller than the drivers' 100^d (the only change: nx, ny, nz);
+* the 1D drivers LFWENO{5,7}FDM1d.m as they stand, up to their final plot: their own grid,
+  CFL, tEnd and initial condition (CommonIC.m case 9, a displaced square jump).
 
 MATLAB arrays are (y, x, z); the fixtures store fields x-fastest as the oracle does
-([z][y][x] in numpy). The initial fields are computed here (the drivers' formula
-u0 = exp(-(x^2+y^2+z^2)/0.1) on the node grid [-1, 1]^d) and stored with the results, so a test
-feeds the same u0 to the oracle. Re-run: python tests/golden/make_weno_golden.py <reference root>
+([z][y][x] in numpy). The 2D/3D initial fields are computed here (the drivers' formula
+u0 = exp(-(x^2+y^2+z^2)/0.1) on the node grid [-1, 1]^d); every run's u0 is stored with its
+results, so a test feeds the same u0 to the oracle. Re-run: python tests/golden/make_weno_golden.py <reference root>
 """
 from __future__ import annotations
 
@@ -121,15 +123,25 @@ def main(root: Path) -> None:
         out[key + "/u"] = from_matlab(env["u"], ndim)
         out[key + "/t_it_cfl_tend_dx"] = np.array([env["t"], env["it"], env["CFL"], env["tEnd"], dx])
 
+    # ---- the 1D drivers, whole (everything before the final plot)
+    for order in ("5", "7"):
+        text = (pdir / f"LFWENO{order}FDM1d.m").read_text()
+        m = re.search(r"^%% (?:Final Plot|Post-process)", text, re.M)
+        env = interp.run(text[:m.start()], {})
+        key = f"run/o{order}/d1"
+        out[key + "/u0"] = from_matlab(env["u0"], 1)
+        out[key + "/u"] = from_matlab(env["u"], 1)
+        out[key + "/t_it_cfl_tend_dx"] = np.array([env["t"], env["it"], env["CFL"], env["tEnd"], env["dx"]])
+
     files = sorted({f"WENO{o}resAdv_{a}.m" for o in (5, 7) for a in "XYZ"} |
-                   {f"WENO{o}resAdv1d.m" for o in (5, 7)} |
-                   {f"LFWENO{o}FDM{d}d.m" for o in (5, 7) for d in (2, 3)})
+                   {f"WENO{o}resAdv1d.m" for o in (5, 7)} | {"CommonIC.m"} |
+                   {f"LFWENO{o}FDM{d}d.m" for o in (5, 7) for d in (1, 2, 3)})
     digest = "\n".join(f"{f} {hashlib.sha256((pdir / f).read_bytes()).hexdigest()}" for f in files)
     out["meta/source_sha256"] = np.array(digest)
     out["meta/calls"] = np.array(repr(sorted(interp.calls.items())))
     dst = Path(__file__).resolve().parent / "matlab_burgers_prototypes.npz"
     np.savez_compressed(dst, **out)
-    print("wrote", dst, f"({count} residual cases, {len(runs)} solver loops)")
+    print("wrote", dst, f"({count} residual cases, {len(runs) + 2} solver loops)")
     print(sorted(interp.calls.items()))
 
 

@@ -208,6 +208,11 @@ class _Parser:
                 self.next()
                 return ("massign", names, self.expr())
             self.i = save
+        # command syntax of a no-op call (`close all`): skip to the end of the statement
+        if tok[0] == "id" and tok[1] in _NOOP_CALLS and self.peek(1)[0] == "id":
+            while self.peek()[0] not in ("nl", "eof") and self.peek()[1] not in (";", ","):
+                self.next()
+            return ("expr", ("num", 0.0))
         # assignment `name = e` / `name(args) = e`, or a bare call
         if tok[0] == "id":
             save = self.i
@@ -488,6 +493,22 @@ def _matlab_sum(a):
     raise MatlabError("sum over a matrix is outside the subset")
 
 
+def _matlab_min(a):
+    a = np.asarray(a, dtype=np.float64)
+    if a.ndim < 2 or min(a.shape[:2]) == 1 and a.ndim == 2:
+        return float(np.min(a))
+    raise MatlabError("min over a matrix is outside the subset")
+
+
+def _rectangular_pulse(a, b, x):
+    """MATLAB's rectangularPulse(a, b, x) for a < b: 1 inside (a, b), 1/2 at x = a or b, else 0."""
+    a, b = _scalar(a), _scalar(b)
+    if not a < b:
+        raise MatlabError("rectangularPulse with a >= b is outside the subset")
+    x = np.asarray(x, dtype=np.float64)
+    return np.where((x > a) & (x < b), 1.0, np.where((x == a) | (x == b), 0.5, 0.0))
+
+
 def _norm(a, p=2.0):
     a = np.asarray(a, dtype=np.float64)
     if (a.ndim < 2 or min(a.shape) == 1) and np.isinf(p):
@@ -515,6 +536,8 @@ BUILTINS = {
     "abs": lambda a: np.abs(np.asarray(a, dtype=np.float64)),
     "exp": lambda a: np.exp(np.asarray(a, dtype=np.float64)),
     "max": _matlab_max,
+    "min": _matlab_min,
+    "rectangularPulse": _rectangular_pulse,
     "rem": lambda a, b: float(np.fmod(_scalar(a), _scalar(b))),
     "sqrt": lambda a: np.sqrt(a) if isinstance(a, float) else np.sqrt(np.asarray(a, dtype=np.float64)),
     "sum": _matlab_sum,
@@ -535,6 +558,7 @@ class Interpreter:
         self.fdir = Path(fdir) if fdir else None
         self._files: dict[str, tuple] = {}
         self.calls: dict[str, int] = {}
+        self._end: list[float] = []  # the value of `end` inside the index being evaluated
 
     # -- entry points -------------------------------------------------------------------
     def run(self, src: str, env: dict) -> dict:
@@ -674,6 +698,10 @@ class Interpreter:
             name = n[1]
             if name in env:
                 return env[name]
+            if name == "end":
+                if not self._end:
+                    raise MatlabError("`end` outside an index")
+                return self._end[-1]
             if name in _NOOP_CALLS:
                 return None
             if name in BUILTINS:
@@ -711,9 +739,20 @@ class Interpreter:
             if target[0] == "id":
                 name = target[1]
                 if name in env and isinstance(env[name], (np.ndarray, float)):
-                    idx = [("colon",) if a == ("colon",) else self._eval(a, env) for a in n[2]]
-                    out = _index(env[name], idx)
-                    return out
+                    arr = env[name]
+                    shape = np.shape(arr) if np.ndim(arr) >= 2 else (1, int(np.size(arr)))
+                    idx = []
+                    for d, a in enumerate(n[2]):
+                        if a == ("colon",):
+                            idx.append(a)
+                            continue
+                        extent = int(np.prod(shape)) if len(n[2]) == 1 else (shape[d] if d < len(shape) else 1)
+                        self._end.append(float(extent))
+                        try:
+                            idx.append(self._eval(a, env))
+                        finally:
+                            self._end.pop()
+                    return _index(arr, idx)
                 if name not in env and name in _NOOP_CALLS:
                     return None  # plotting: its arguments are never evaluated
                 args = [self._eval(a, env) for a in n[2]]

@@ -88,3 +88,10 @@ def test_function_files_with_several_outputs(tmp_path):
 def test_if_elseif_else():
     e = run("for k = 1:3\n if k == 1, a = 1; elseif k == 2\n b = 2; else\n c = 3; end\n end")
     assert (e["a"], e["b"], e["c"]) == (1.0, 2.0, 3.0)
+
+
+def test_end_in_indices_command_syntax_and_pulses():
+    e = run("clear; close all; clc;\nx = [3 5 7 9]; a = x(end); b = x(end-1); m = min(x);\n"
+            "p = rectangularPulse(4, 8, [3 4 5 8 9]);")
+    assert (e["a"], e["b"], e["m"]) == (9.0, 7.0, 3.0)
+    np.testing.assert_array_equal(e["p"], [[0.0, 0.5, 1.0, 0.5, 0.0]])
