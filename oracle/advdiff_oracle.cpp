@@ -958,9 +958,15 @@ int orc_heat_accuracy(int dim, int nc, double tFinal, double param, double* L1, 
           if (!in) continue;
           size_t o = (size_t)i + (size_t)nx * j + (size_t)nx * ny * k;
           size_t sy = nx, sz = (size_t)nx * ny;
-          double v = Dx / 12 * (-w[o + 2] + 16 * w[o + 1] - 30 * w[o] + 16 * w[o - 1] - w[o - 2]);
-          if (dim >= 2) v = v + Dx / 12 * (-w[o + 2 * sy] + 16 * w[o + sy] - 30 * w[o] + 16 * w[o - sy] - w[o - 2 * sy]);
-          if (dim == 3) v = v + Dx / 12 * (-w[o + 2 * sz] + 16 * w[o + sz] - 30 * w[o] + 16 * w[o - sz] - w[o - 2 * sz]);
+          double v;
+          if (dim < 3) {  // Laplace{1,2}d.m: each axis from its + side (i+2 first)
+            v = Dx / 12 * (-w[o + 2] + 16 * w[o + 1] - 30 * w[o] + 16 * w[o - 1] - w[o - 2]);
+            if (dim == 2) v = v + Dx / 12 * (-w[o + 2 * sy] + 16 * w[o + sy] - 30 * w[o] + 16 * w[o - sy] - w[o - 2 * sy]);
+          } else {  // Laplace3d.m's "OMP" branch (:29-52): each axis from its - side (o-2 first)
+            v = Dx / 12 * (-w[o - 2] + 16 * w[o - 1] - 30 * w[o] + 16 * w[o + 1] - w[o + 2]) +
+                Dx / 12 * (-w[o - 2 * sy] + 16 * w[o - sy] - 30 * w[o] + 16 * w[o + sy] - w[o + 2 * sy]);
+            v = v + Dx / 12 * (-w[o - 2 * sz] + 16 * w[o - sz] - 30 * w[o] + 16 * w[o + sz] - w[o + 2 * sz]);
+          }
           dF[o] = v;
         }
   };

@@ -16,8 +16,8 @@ a single index is linear, column-major), indexed assignment, `function out = nam
 norm(v, inf), rem, meshgrid; plotting and printing calls are no-ops). Elementwise operations are
 evaluated one at a time in the order the source writes them, as MATLAB does, so results match
 MATLAB's double arithmetic operation by operation (ranges with a non-unit step may differ from
-MATLAB's colon in the last bit). Anything outside the subset raises an error instead of
-guessing.
+MATLAB's colon in the last bit, and exp is the C library's, which MATLAB's may differ from in
+the last bit). Anything outside the subset raises an error instead of guessing.
 """
 from __future__ import annotations
 
@@ -483,6 +483,15 @@ def _ones(*args):
     return _zeros(*args) + 1.0
 
 
+def _elementwise(fn, a):
+    """A C-library elementary function applied value by value (numpy's vectorised versions may
+    round differently from the C library the oracle calls)."""
+    if isinstance(a, float):
+        return fn(a)
+    arr = np.asarray(a, dtype=np.float64)
+    return np.array([fn(float(v)) for v in arr.reshape(-1)], dtype=np.float64).reshape(arr.shape)
+
+
 def _matlab_sum(a):
     a = np.asarray(a, dtype=np.float64)
     if a.ndim <= 2 and (a.ndim < 2 or min(a.shape) == 1):
@@ -534,7 +543,7 @@ BUILTINS = {
     "size": lambda a: np.array(np.shape(a) if np.ndim(a) >= 2 else (1, np.size(a)),
                                dtype=np.float64).reshape(1, -1),
     "abs": lambda a: np.abs(np.asarray(a, dtype=np.float64)),
-    "exp": lambda a: np.exp(np.asarray(a, dtype=np.float64)),
+    "exp": lambda a: _elementwise(math.exp, a),
     "max": _matlab_max,
     "min": _matlab_min,
     "rectangularPulse": _rectangular_pulse,
