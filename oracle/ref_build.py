@@ -15,6 +15,10 @@ own build, used for timing) and `<name>_nofma.cubin` with -fmad=false (every ope
 written: comparable bit for bit with the FP64 oracle and the library's FP64 path). REAL is double
 in all three (USE_FLOAT false in the reference headers).
 
+The same programs' host tools (SingleGPU/<program>/tools.cpp: initial conditions, result.bin)
+are compiled with g++ together with oracle/ref_tools_shim.cpp into host libraries
+`libref_tools_<name>.so` (-ffp-contract=off, as the library's host code), for the CPU tests.
+
     python oracle/ref_build.py [--src /root/reference]
 """
 from __future__ import annotations
@@ -33,6 +37,17 @@ UNITS = {
     "burgers3d": "SingleGPU/Burgers3d_WENO5/kernels.cu",
 }
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+TOOLS = {
+    "heat3d": ("SingleGPU/Diffusion3d_baselineCode", "REF_HEAT3D"),
+    "heat2d": ("SingleGPU/Diffusion2d", "REF_HEAT2D"),
+    "burgers3d": ("SingleGPU/Burgers3d_WENO5", "REF_BURGERS3D"),
+}
+
+
+def _cuda_include() -> Path:
+    nvcc = shutil.which("nvcc")
+    inc = Path(nvcc).resolve().parent.parent / "include" if nvcc else Path("/usr/local/cuda/include")
+    return inc
 
 
 def build(src_root: Path) -> list[Path]:
@@ -51,10 +66,23 @@ def build(src_root: Path) -> list[Path]:
                 continue
             cmd = [nvcc, "-cubin", *ARCH, "-O3", *extra, "-o", str(out), str(src)]
             jobs.append((out, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)))
+    shim = HERE / "ref_tools_shim.cpp"
+    cxx = shutil.which("g++") or "g++"
+    for name, (rel, define) in TOOLS.items():
+        src = src_root / rel / "tools.cpp"
+        if not src.exists():
+            raise FileNotFoundError(src)
+        out = OUT / f"libref_tools_{name}.so"
+        if out.exists() and out.stat().st_mtime >= max(src.stat().st_mtime, shim.stat().st_mtime):
+            made.append(out)
+            continue
+        cmd = [cxx, "-O2", "-fPIC", "-shared", "-ffp-contract=off", f"-D{define}", "-I", str(src_root / rel),
+               "-I", str(_cuda_include()), "-w", "-o", str(out), str(shim), str(src), "-lm"]
+        jobs.append((out, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)))
     for out, p in jobs:
         log, _ = p.communicate()
         if p.returncode != 0:
-            raise RuntimeError(f"reference kernel build failed for {out.name}:\n{log}")
+            raise RuntimeError(f"reference build failed for {out.name}:\n{log}")
         made.append(out)
     return made
 
