@@ -19,6 +19,11 @@ The same programs' host tools (SingleGPU/<program>/tools.cpp: initial conditions
 are compiled with g++ together with oracle/ref_tools_shim.cpp into host libraries
 `libref_tools_<name>.so` (-ffp-contract=off, as the library's host code), for the CPU tests.
 
+Drop-in link check: each program's own main.cpp + tools.cpp (dense and pitched variants) are
+linked, unmodified and without their kernels.cu, against the GB300 compatibility library that
+replaces it (`refmain_<name>`, once multigpu_advectiondiffusion_gb300/_lib is built). Running
+them needs a GPU; the CPU tests check that every symbol resolves.
+
     python oracle/ref_build.py [--src /root/reference]
 """
 from __future__ import annotations
@@ -42,6 +47,17 @@ TOOLS = {
     "heat2d": ("SingleGPU/Diffusion2d", "REF_HEAT2D"),
     "burgers3d": ("SingleGPU/Burgers3d_WENO5", "REF_BURGERS3D"),
 }
+
+
+MAINS = {  # reference program -> the compatibility library that replaces its kernels.cu
+    "heat3d": ("SingleGPU/Diffusion3d_baselineCode", "advdiff_compat_heat3d"),
+    "heat3d_pitched": ("SingleGPU/Diffusion3d_PitchedMem", "advdiff_compat_heat3d_pitched"),
+    "heat2d": ("SingleGPU/Diffusion2d", "advdiff_compat_heat2d"),
+    "heat2d_pitched": ("SingleGPU/Diffusion2d_PitchedMem", "advdiff_compat_heat2d_pitched"),
+    "burgers3d": ("SingleGPU/Burgers3d_WENO5", "advdiff_compat_burgers3d"),
+    "burgers3d_pitched": ("SingleGPU/Burgers3d_WENO5_PitchedMem", "advdiff_compat_burgers3d_pitched"),
+}
+LIBDIR = HERE.parent / "multigpu_advectiondiffusion_gb300" / "_lib"
 
 
 def _cuda_include() -> Path:
@@ -78,6 +94,18 @@ def build(src_root: Path) -> list[Path]:
             continue
         cmd = [cxx, "-O2", "-fPIC", "-shared", "-ffp-contract=off", f"-D{define}", "-I", str(src_root / rel),
                "-I", str(_cuda_include()), "-w", "-o", str(out), str(shim), str(src), "-lm"]
+        jobs.append((out, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)))
+    for name, (rel, compat) in MAINS.items():
+        lib = LIBDIR / f"lib{compat}.so"
+        srcs = [src_root / rel / "main.cpp", src_root / rel / "tools.cpp"]
+        if not lib.exists() or not all(x.exists() for x in srcs):
+            continue
+        out = OUT / f"refmain_{name}"
+        if out.exists() and out.stat().st_mtime >= max(x.stat().st_mtime for x in srcs + [lib]):
+            made.append(out)
+            continue
+        cmd = [nvcc, *ARCH, "-O3", "-w", "-o", str(out), *map(str, srcs), "-L", str(LIBDIR), f"-l{compat}",
+               "-ladvdiff", "-Xlinker", f"-rpath,{LIBDIR}"]
         jobs.append((out, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)))
     for out, p in jobs:
         log, _ = p.communicate()

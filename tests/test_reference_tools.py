@@ -1,8 +1,11 @@
-"""Row a11 against the reference's own host code (CPU only): the initial conditions and the
-result.bin writer of SingleGPU/{Diffusion3d_baselineCode,Diffusion2d,Burgers3d_WENO5}/tools.cpp,
-compiled from the reference sources by oracle/ref_build.py into oracle/_ref/libref_tools_*.so,
-equal the library's adv_ic_*_ref and adv_write_result_bin bit for bit. Skipped where the
-reference sources were not available at build time."""
+"""The library against the reference's own host code (CPU only), built from the reference
+sources by oracle/ref_build.py into oracle/_ref/:
+* row a11: the initial conditions and the result.bin writer of
+  SingleGPU/{Diffusion3d_baselineCode,Diffusion2d,Burgers3d_WENO5}/tools.cpp equal the library's
+  adv_ic_*_ref and adv_write_result_bin bit for bit;
+* the drop-in link: each program's own main.cpp + tools.cpp, dense and pitched, links unmodified
+  against the compatibility library that replaces its kernels.cu.
+Skipped where the reference sources were not available at build time."""
 from __future__ import annotations
 
 import ctypes as C
@@ -72,3 +75,31 @@ def test_result_bin_equals_the_reference_writer(native, tmp_path, monkeypatch, n
     ours = tmp_path / "ours.bin"
     assert native.adv_write_result_bin(str(ours).encode(), N.ADV_F64, u.ctypes.data, u.size) == N.ADV_OK
     assert (tmp_path / "result.bin").read_bytes() == ours.read_bytes()
+
+
+@pytest.mark.parametrize("name,lib,wrappers", [
+    ("heat3d", "advdiff_compat_heat3d", {"CopyToConstantMemory", "Call_Lu3d", "Call_RK3d"}),
+    ("heat3d_pitched", "advdiff_compat_heat3d_pitched", {"CopyToConstantMemory", "Call_Lu3d", "Call_RK3d"}),
+    ("heat2d", "advdiff_compat_heat2d", {"CopyToConstantMemory", "Call_Lu2d", "Call_RK2d"}),
+    ("heat2d_pitched", "advdiff_compat_heat2d_pitched", {"CopyToConstantMemory", "Call_Lu2d", "Call_RK2d"}),
+    ("burgers3d", "advdiff_compat_burgers3d",
+     {"CopyToConstantMemory", "Call_Adv_x", "Call_Adv_y", "Call_Adv_z", "Call_Diff_", "Call_sspRK"}),
+    ("burgers3d_pitched", "advdiff_compat_burgers3d_pitched",
+     {"CopyToConstantMemory", "Call_Adv_x", "Call_Adv_y", "Call_Adv_z", "Call_Diff_", "Call_sspRK"}),
+])
+def test_reference_main_links_against_the_compat_library(native, name, lib, wrappers):
+    """The reference program's own main.cpp + tools.cpp, unmodified and without its kernels.cu,
+    linked against the compatibility library (oracle/ref_build.py): every symbol resolves, and
+    the kernel wrappers it calls come from the GB300 library."""
+    import subprocess
+    exe = REF / f"refmain_{name}"
+    if not exe.exists():
+        pytest.skip(f"{exe.name} not built (needs the reference sources at build time)")
+    r = subprocess.run(["ldd", "-r", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0 and "undefined symbol" not in r.stdout + r.stderr and "not found" not in r.stdout
+    undefined = subprocess.run(["nm", "-D", "--undefined-only", str(exe)], capture_output=True, text=True,
+                               check=True).stdout
+    assert wrappers <= {l.split()[-1] for l in undefined.splitlines() if l.strip()}
+    exported = subprocess.run(["nm", "-D", "--defined-only", str(N.LIBDIR / f"lib{lib}.so")], capture_output=True,
+                              text=True, check=True).stdout
+    assert wrappers <= {l.split()[-1] for l in exported.splitlines() if " T " in l}
