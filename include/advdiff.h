@@ -103,20 +103,45 @@ adv_status adv_heat_run(const adv_heat_desc* d, int time_scheme, int64_t nsteps,
 /* Bytes of the fixed device scratch array behind adv_heat_run_noalloc (16 MiB). */
 #define ADV_NOALLOC_SCRATCH_BYTES ((size_t)16 << 20)
 
-/* adv_heat_run without any allocation, for callers that cannot allocate device memory: code
- * that records its work into its own CUDA graph (cudaMalloc is not allowed while a stream is
- * being captured) and hosts whose device memory is owned entirely by another allocator.
+/* adv_heat_run without any allocation, for callers that cannot allocate device memory: hosts
+ * whose device memory is owned entirely by their own allocator (a pool that reserves the GPU's
+ * memory at start-up, so a library's cudaMalloc would fail or bypass its accounting), and loops
+ * that must not call cudaMalloc/cudaFree at all because those calls may synchronise the device.
  * No counterpart in the reference (its drivers cudaMalloc u, uo and Lu themselves).
  * The intermediate state lives in one file-scope __device__ array of ADV_NOALLOC_SCRATCH_BYTES
  * that every GPU loading this library holds until the process exits; the stages are launched
  * directly on `stream` (no graph, no stream, no cudaMalloc/cudaFree). A run needing more scratch
  * than adv_heat_workspace_bytes allows within that size (one state array for Euler, two for
- * SSP-RK3) is rejected with ADV_ERR_INVALID_ARG. The first call on a device looks up the array's
- * device address (and may load the module): make that first call before any stream capture.
- * All calls share the one array and it keeps the last call's contents (nothing in it needs to
- * start at zero): calls that overlap on the GPU, on any streams or threads, race. */
+ * SSP-RK3) is rejected with ADV_ERR_INVALID_ARG. The first call on a device (and the first after
+ * the device's context was reset) looks up the array's device address and may load the module:
+ * make that first call before any stream capture. All calls share the one array and it keeps the
+ * last call's contents (nothing in it needs to start at zero): calls that overlap on the GPU, on
+ * any streams or threads, race. */
 adv_status adv_heat_run_noalloc(const adv_heat_desc* d, int time_scheme, int64_t nsteps, void* u,
                                 void* stream);
+
+/* ------------------------------------------------------------------ device-side errors
+ * A kernel that cannot finish (a bounded wait for a shared-memory copy that gave up after 2 s)
+ * or a time loop that meets a NaN/Inf or a non-positive dt records the first such code in a
+ * per-device status word and returns; nothing traps or spins without limit. Calls that read
+ * results back (adv_burgers_run/resume, adv_max_abs, adv_ensemble_run) return the word
+ * themselves. The asynchronous calls (stages, adv_heat_run, adv_heat_run_noalloc, the heat-k and
+ * Burgers adjoint calls) cannot: after them, adv_device_status synchronises `stream`, returns
+ * the recorded code (ADV_OK if none) and clears it. This replaces the reference's checkCuda,
+ * which prints and exits the process (SingleGPU/Burgers3d_WENO5/main.cpp:13-24). Called while
+ * `stream` is being captured it returns ADV_ERR_UNSUPPORTED and touches nothing. */
+adv_status adv_device_status(void* stream);
+
+/* For tests of the failure path only: one adv_heat_stage launch in which the shared-memory copy
+ * of z plane `plane` is never issued, and the waits for planes give up after wait_limit_ns
+ * (1e5 .. 2e9 ns). Every CTA that streams that plane then waits until its limit runs out,
+ * records ADV_ERR_TIMEOUT in the status word, lets its copies already in flight land, and
+ * returns; the output is left incomplete. Nothing faults or waits without limit. Needs the TMA
+ * load path (16-byte aligned buffer and rows); ADV_ERR_UNSUPPORTED otherwise. No counterpart in
+ * the reference. */
+adv_status adv_test_heat_stage_withheld(const adv_heat_desc* d, int stage, const void* u_in,
+                                        const void* u_n, void* u_out, int plane, uint64_t wait_limit_ns,
+                                        void* stream);
 
 /* --------------------------------------------------------------------------- Burgers
  * u_t + (u^2/2)_x + (u^2/2)_y + (u^2/2)_z = nu * Lap(u). One fused launch per SSP-RK3 stage:

@@ -79,6 +79,8 @@ SIGNATURES = [
     ("adv_heat_workspace_bytes", _I, [C.POINTER(HeatDesc), _I, C.POINTER(C.c_size_t)]),
     ("adv_heat_run", _I, [C.POINTER(HeatDesc), _I, _I64, _VP, _VP, _VP]),
     ("adv_heat_run_noalloc", _I, [C.POINTER(HeatDesc), _I, _I64, _VP, _VP]),
+    ("adv_device_status", _I, [_VP]),
+    ("adv_test_heat_stage_withheld", _I, [C.POINTER(HeatDesc), _I, _VP, _VP, _VP, _I, C.c_uint64, _VP]),
     ("adv_burgers_stage", _I, [C.POINTER(BurgersDesc), _I, _VP, _VP, _VP, _D, _D, _VP, _VP]),
     ("adv_burgers_workspace_bytes", _I, [C.POINTER(BurgersDesc), C.POINTER(C.c_size_t)]),
     ("adv_burgers_run", _I, [C.POINTER(BurgersDesc), _VP, _VP, _D, _D, _I, _D, _I64, _PD,

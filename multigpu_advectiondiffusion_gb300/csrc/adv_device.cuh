@@ -49,12 +49,14 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait: returns false (and raises ADV_ERR_TIMEOUT) if the phase did not complete in time.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity, int* status) {
+// Bounded wait: returns false (and raises ADV_ERR_TIMEOUT) if the phase did not complete within
+// limit_ns of the first failed poll.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity, int* status,
+                                                  unsigned long long limit_ns = kWaitLimitNs) {
   if (mbar_try_wait(bar, parity)) return true;
   const unsigned long long t0 = globaltimer_ns();
   while (!mbar_try_wait(bar, parity)) {
-    if (globaltimer_ns() - t0 > kWaitLimitNs) {
+    if (globaltimer_ns() - t0 > limit_ns) {
       raise_status(status, 3 /* ADV_ERR_TIMEOUT */);
       return false;
     }

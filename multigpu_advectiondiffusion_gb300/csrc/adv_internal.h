@@ -45,7 +45,8 @@ bool stream_capturing(cudaStream_t s);
 // while `s` is being captured; the stream and the caller's capture are left untouched.
 adv_status reject_capture(cudaStream_t s, const char* what);
 
-// Device status word (per device): 0 = OK, else an adv_status raised by a kernel.
+// Device status word (per device): 0 = OK, else an adv_status raised by a kernel. Reading it
+// synchronises `s`; a nonzero word is returned as the status and cleared.
 adv_status read_and_clear_device_status(cudaStream_t s);
 int* device_status_ptr();
 
@@ -76,6 +77,10 @@ struct HeatLaunch {
   dim3 grid, block;
   size_t smem = 0;
   CUtensorMap tmap_in;  // tensor map of u_in (re-encoded when the pointer changes)
+  // failure-path testing only (adv_test_heat_stage_withheld): a z plane whose copy is never
+  // issued, and the wait limit for planes (0: the normal limit)
+  int withheld_plane = -1;
+  unsigned long long wait_limit_ns = 0;
 };
 // rows: rows per thread of the stage kernel (2 or 4), lanes: lanes per row (32 or 16); 0 = the
 // library's choice.

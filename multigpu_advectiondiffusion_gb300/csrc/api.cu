@@ -11,6 +11,7 @@
 #include <string>
 #include <vector>
 
+#include "adv_device.cuh"
 #include "adv_internal.h"
 #include "nvtx_range.h"
 
@@ -297,6 +298,31 @@ adv_status adv_heat_stage(const adv_heat_desc* d, int stage, const void* u_in, c
   return heat_launch(*d, L, stage, u_in, u_n, u_out, static_cast<cudaStream_t>(stream));
 }
 
+adv_status adv_test_heat_stage_withheld(const adv_heat_desc* d, int stage, const void* u_in, const void* u_n,
+                                        void* u_out, int plane, uint64_t wait_limit_ns, void* stream) {
+  ADV_NVTX_RANGE("adv_test_heat_stage_withheld");
+  adv_status st = heat_validate(d);
+  if (st != ADV_OK) return st;
+  if (!u_in || !u_n || !u_out) return set_error(ADV_ERR_INVALID_ARG, "heat: null buffer");
+  if (u_in == u_out) return set_error(ADV_ERR_INVALID_ARG, "heat: u_in and u_out must not alias");
+  const int nz = d->ndim == 3 ? d->nz : 1;
+  if (plane < 0 || plane >= nz) return set_error(ADV_ERR_INVALID_ARG, "heat test: withheld plane outside the grid");
+  if (wait_limit_ns < 100000ull || wait_limit_ns > kWaitLimitNs)
+    return set_error(ADV_ERR_INVALID_ARG, "heat test: wait limit must lie in [1e5, 2e9] ns");
+  HeatLaunch L;
+  if ((st = heat_prepare(*d, u_in, &L)) != ADV_OK) return st;
+  if (!L.tma) return set_error(ADV_ERR_UNSUPPORTED, "heat test: the withheld-copy test needs the TMA load path");
+  L.withheld_plane = plane;
+  L.wait_limit_ns = wait_limit_ns;
+  return heat_launch(*d, L, stage, u_in, u_n, u_out, static_cast<cudaStream_t>(stream));
+}
+
+adv_status adv_device_status(void* stream) {
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (adv_status st = reject_capture(s, "device_status"); st != ADV_OK) return st;
+  return read_and_clear_device_status(s);
+}
+
 adv_status adv_heat_workspace_bytes(const adv_heat_desc* d, int time_scheme, size_t* bytes) {
   adv_status st = heat_validate(d);
   if (st != ADV_OK) return st;
@@ -563,6 +589,7 @@ adv_status adv_max_abs(int dtype, const void* u, int64_t n, double* out, void* s
   }
   cudaFreeAsync(acc, s);
   if (st != ADV_OK) return st;
+  if ((st = read_and_clear_device_status(s)) != ADV_OK) return st;
   if (dtype == ADV_F32) {
     unsigned k32 = (unsigned)key;
     float f;

@@ -20,6 +20,8 @@ HeatParams<T> heat_params(const adv_heat_desc& d, const HeatLaunch& L, int stage
   p.vec_ok = (((uintptr_t)u_out % 16) == 0 && ((int64_t)d.nx * sizeof(T)) % 16 == 0) ? 1 : 0;
   p.kx = (T)d.kx; p.ky = (T)d.ky; p.kz = (T)d.kz; p.dt = (T)d.dt;
   p.status = device_status_ptr();
+  p.withheld_plane = L.withheld_plane;
+  p.wait_limit_ns = L.wait_limit_ns ? L.wait_limit_ns : kWaitLimitNs;
   return p;
 }
 

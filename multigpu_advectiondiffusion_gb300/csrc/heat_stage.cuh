@@ -77,6 +77,11 @@ struct HeatParams {
   int vec_ok;  // output rows 16-byte aligned: vector stores
   T kx, ky, kz, dt;
   int* status;  // device status word
+  // Failure-path testing only (adv_test_heat_stage_withheld): the TMA copy of z plane
+  // `withheld_plane` is never issued (-1: none), and the waits for planes give up after
+  // `wait_limit_ns` (the normal limit otherwise).
+  int withheld_plane;
+  unsigned long long wait_limit_ns;
 };
 
 // Laplacian at one node from its neighbours along each axis (m2, m1, centre, p1, p2).
@@ -208,7 +213,7 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
     T* dst = ring + s_issue * C::SLOT_ELEMS;
     const int z = p0 + q;
     if (TMA) {
-      if (tid == 0) {
+      if (tid == 0 && z != p.withheld_plane) {
         mbar_arrive_expect_tx(&bars[s_issue], C::PLANE_BYTES);
         tma_load_3d(dst, tmap, x0 - C::PADX, y0 - R, z, &bars[s_issue]);
       }
@@ -289,7 +294,7 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
     bool ok = true;
     if (TMA) {
       // every lane waits on the barrier itself (converged: same barrier, same phase)
-      ok = mbar_wait_bounded(&bars[s_wait], (parity >> s_wait) & 1u, p.status);
+      ok = mbar_wait_bounded(&bars[s_wait], (parity >> s_wait) & 1u, p.status, p.wait_limit_ns);
       if (!ok) *abort_flag = 1;
     } else {
       cp_async_wait<C::P>();

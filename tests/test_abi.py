@@ -76,6 +76,15 @@ def test_launching_entry_points_reject_bad_arguments_without_gpu(native):
     bad = N.HeatDesc(4, 8, 8, 8, N.ADV_F32, 2, 1, 1, 1.0, 1.0, 1.0, 0.1)
     assert native.adv_heat_run(C.byref(bad), N.ADV_EULER, 4, None, None, None) == N.ADV_ERR_INVALID_ARG
     assert native.adv_heat_run_noalloc(C.byref(bad), N.ADV_EULER, 4, None, None) == N.ADV_ERR_INVALID_ARG
+    ok = N.HeatDesc(3, 16, 16, 16, N.ADV_F32, 2, 1, 1, 1.0, 1.0, 1.0, 0.1)
+    buf = C.c_void_p(16)
+    # the failure-path test launch checks its plane and wait limit before any CUDA call
+    assert native.adv_test_heat_stage_withheld(C.byref(ok), 1, buf, buf, C.c_void_p(32), 16, 10 ** 6,
+                                               None) == N.ADV_ERR_INVALID_ARG
+    assert b"withheld plane" in native.adv_last_error_string()
+    assert native.adv_test_heat_stage_withheld(C.byref(ok), 1, buf, buf, C.c_void_p(32), 3, 10,
+                                               None) == N.ADV_ERR_INVALID_ARG
+    assert b"wait limit" in native.adv_last_error_string()
     bd = N.BurgersDesc(4, 8, 8, N.ADV_F32, 1, 1, N.ADV_BC_PERIODIC, 0, 0, 0, 1.0, 1.0, 1.0, 0, 0, 0)
     t, s = C.c_double(0.0), C.c_int64(0)
     assert native.adv_burgers_run(C.byref(bd), None, None, 1.0, 0.5, N.ADV_DT_FIXED, 0.0, 10, C.byref(t),
@@ -237,7 +246,7 @@ def _ctype_ok(decl: str, ct) -> bool:
         return ct is C.POINTER(scalar) or ct is C.c_void_p
     base = decl.split()[0]
     scalar = {"double": C.c_double, "int64_t": C.c_int64, "size_t": C.c_size_t, "int": C.c_int, "int32_t": C.c_int32,
-              "uint32_t": C.c_uint32, "adv_status": C.c_int}
+              "uint32_t": C.c_uint32, "uint64_t": C.c_uint64, "adv_status": C.c_int}
     return ct is scalar[base]
 
 
