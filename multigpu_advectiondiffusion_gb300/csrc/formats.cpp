@@ -188,6 +188,8 @@ adv_status adv_checkpoint_load(const char* path, adv_checkpoint_header* hdr, voi
     return set_error(ADV_ERR_INVALID_ARG, "checkpoint_load: buffer smaller than the snapshot");
   if (std::fread(host_u, 1, (size_t)H.payload_bytes, fl.f) != (size_t)H.payload_bytes)
     return set_error(ADV_ERR_INVALID_ARG, "checkpoint_load: truncated payload");
+  if (std::fgetc(fl.f) != EOF)  // a snapshot ends with its payload: appended or joined files are not one
+    return set_error(ADV_ERR_INVALID_ARG, "checkpoint_load: data after the payload");
   if (crc32(host_u, (size_t)H.payload_bytes) != H.payload_crc32)
     return set_error(ADV_ERR_INVALID_ARG, "checkpoint_load: payload CRC mismatch");
   return ADV_OK;

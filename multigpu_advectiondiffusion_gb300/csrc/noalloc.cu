@@ -13,21 +13,49 @@ namespace adv {
 // Scratch of adv_heat_run_noalloc. Every GPU that loads this library holds it until exit.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[ADV_NOALLOC_SCRATCH_BYTES];
 
+// Unique id of the calling thread's current CUDA context (0 if none is current), through the
+// driver entry points the runtime exposes (no -lcuda link).
+static unsigned long long current_context_id() {
+  typedef CUresult (*GetCurrentFn)(CUcontext*);
+  typedef CUresult (*GetIdFn)(CUcontext, unsigned long long*);
+  static GetCurrentFn get_current = nullptr;
+  static GetIdFn get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrentFn>(p);
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetIdFn>(p);
+  });
+  CUcontext c = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&c) != CUDA_SUCCESS || !c || get_id(c, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
+
 // Device address of g_noalloc_scratch on the current device. In host code the symbol itself is
-// only a host-side stand-in, so its address is looked up once per device (with that device
-// current) and cached.
+// only a host-side stand-in, so its address is looked up (with that device current) once per
+// device and context, and cached next to the context's unique id: after a cudaDeviceReset the
+// device has a new context, in which the array has a new address, and the lookup is made again.
 static adv_status noalloc_scratch(void** out) {
   static std::mutex mu;
   static void* addr[64] = {};
+  static unsigned long long ctx_of[64] = {};
   int dev = -1;
   ADV_CUDA_TRY(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) return set_error(ADV_ERR_UNSUPPORTED, "heat_run_noalloc: device ordinal out of range");
   std::lock_guard<std::mutex> lk(mu);
-  if (!addr[dev]) {
+  const unsigned long long ctx = current_context_id();
+  if (!addr[dev] || ctx == 0 || ctx != ctx_of[dev]) {
     void* p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return cuda_error(e, "heat_run_noalloc: cudaGetSymbolAddress of the scratch array");
     addr[dev] = p;
+    ctx_of[dev] = current_context_id();  // the lookup made the device's context current
   }
   *out = addr[dev];
   return ADV_OK;

@@ -90,6 +90,10 @@ def test_checkpoint_rejects_damaged_files(native, tmp_path):
     flipped[33] ^= 0x10  # the step count
     assert load(bytes(flipped), "header.bin") == (N.ADV_ERR_INVALID_ARG, "checkpoint_load: header CRC mismatch")
     assert load(raw[:-8], "short.bin") == (N.ADV_ERR_INVALID_ARG, "checkpoint_load: truncated payload")
+    assert load(raw + b"\x00", "appended.bin") == (N.ADV_ERR_INVALID_ARG, "checkpoint_load: data after the payload")
+    assert load(raw + raw, "joined.bin") == (N.ADV_ERR_INVALID_ARG, "checkpoint_load: data after the payload")
+    assert load(raw, "intact.bin")[0] == N.ADV_OK
+    np.testing.assert_array_equal(back, u)
     assert load(raw[:100], "stub.bin") == (N.ADV_ERR_INVALID_ARG, "checkpoint_load: truncated header")
     assert load(b"NOTSTATE" + raw[8:], "magic.bin") == (N.ADV_ERR_INVALID_ARG,
                                                         "checkpoint_load: not a state snapshot")

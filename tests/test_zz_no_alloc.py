@@ -1,8 +1,8 @@
 """adv_heat_run_noalloc through the C ABI, against adv_heat_run.
 
-This entry point serves callers that cannot allocate device memory -- code that records its work
-into its own CUDA graph (cudaMalloc is not allowed during stream capture) and hosts whose device
-memory belongs to another allocator. It keeps its intermediate state in one fixed device array
+This entry point serves callers that cannot allocate device memory -- hosts whose device memory
+belongs to their own allocator, and loops that must not call cudaMalloc/cudaFree because those
+calls may synchronise the device. It keeps its intermediate state in one fixed device array
 instead of a workspace, so it must give exactly the results of adv_heat_run (heat results are
 bit-exact everywhere in these tests), call after call, without allocating. The file sorts last
 so that a run stopping at the first failure has already run every other test.
@@ -45,6 +45,7 @@ def test_noalloc_matches_heat_run_on_consecutive_calls(cuda, native, name, cfg, 
     a = torch.empty_like(u0)
     b = torch.empty_like(u0)
     torch.cuda.synchronize()
+    pool = _default_pool_reserved(cuda)
     for call in range(2):
         a.copy_(u0)
         b.copy_(u0)
@@ -58,6 +59,31 @@ def test_noalloc_matches_heat_run_on_consecutive_calls(cuda, native, name, cfg, 
         assert torch.equal(a, b), f"call {call}: results differ from adv_heat_run"
         if call == 1:  # set-up done on the first call: the second one takes no device memory
             assert free_after >= free_before
+    # nothing came from the stream-ordered allocator's default pool either (cudaMallocAsync); the
+    # pool may only have shrunk (memory an earlier test freed is released at synchronisation)
+    after = _default_pool_reserved(cuda)
+    assert pool is None or after <= pool
+
+
+def _default_pool_reserved(dev):
+    """Reserved bytes of the device's default memory pool (cudaMallocAsync), read through the
+    CUDA runtime the library itself links; None if that runtime cannot be opened."""
+    for name in ("libcudart.so.13", "libcudart.so"):
+        try:
+            rt = C.CDLL(name)
+            break
+        except OSError:
+            rt = None
+    if rt is None:
+        return None
+    pool = C.c_void_p()
+    if rt.cudaDeviceGetDefaultMemPool(C.byref(pool), C.c_int(dev.index or 0)) != 0:
+        return None
+    val = C.c_uint64(0)
+    cudaMemPoolAttrReservedMemCurrent = 5
+    if rt.cudaMemPoolGetAttribute(pool, C.c_int(cudaMemPoolAttrReservedMemCurrent), C.byref(val)) != 0:
+        return None
+    return val.value
 
 
 def test_noalloc_rejects_runs_beyond_its_scratch(cuda, native):
