@@ -24,11 +24,15 @@ linked, unmodified and without their kernels.cu, against the GB300 compatibility
 replaces it (`refmain_<name>`, once multigpu_advectiondiffusion_gb300/_lib is built). Running
 them needs a GPU; the CPU tests check that every symbol resolves.
 
-    python oracle/ref_build.py [--src /root/reference]
+    python oracle/ref_build.py [--src DIR]
+
+DIR defaults to $ADV_REFERENCE_DIR, else /root/reference (where this build's container mounts the
+reference checkout; the GPU hosts have none and use the prebuilt outputs).
 """
 from __future__ import annotations
 
 import argparse
+import os
 import shutil
 import subprocess
 import sys
@@ -119,9 +123,15 @@ def build(src_root: Path) -> list[Path]:
     return made
 
 
+def reference_dir() -> Path | None:
+    """The reference checkout to build from: $ADV_REFERENCE_DIR, else /root/reference; None if absent."""
+    p = Path(os.environ.get("ADV_REFERENCE_DIR", "/root/reference"))
+    return p if p.is_dir() else None
+
+
 def main(argv=None) -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--src", default="/root/reference")
+    ap.add_argument("--src", default=str(reference_dir() or "/root/reference"))
     a = ap.parse_args(argv)
     for p in build(Path(a.src)):
         print(p.relative_to(HERE.parent))

@@ -11,6 +11,7 @@ from __future__ import annotations
 
 import json
 import re
+import os
 import sys
 from pathlib import Path
 
@@ -74,4 +75,4 @@ def main(root: Path) -> None:
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference"))
+    main(Path(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("ADV_REFERENCE_DIR", "/root/reference")))

@@ -20,6 +20,7 @@ from __future__ import annotations
 
 import hashlib
 import re
+import os
 import sys
 from pathlib import Path
 
@@ -146,4 +147,4 @@ def main(root: Path) -> None:
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference"))
+    main(Path(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("ADV_REFERENCE_DIR", "/root/reference")))
