@@ -156,16 +156,24 @@ class ClockSampler:
 
 
 # ----------------------------------------------------------------------------- workloads
-def ic_heat3d_blobs(nx, ny, nz, seed, nblobs=8):
-    """Seeded initial condition from the library's host generator (adv_ic_heat3d_blobs)."""
+def ic_heat3d_blobs(nx, ny, nz, seed, nblobs=8, source="library"):
+    """Seeded initial condition from the library's host generator (adv_ic_heat3d_blobs), or the
+    oracle's (source="oracle", for the CPU arms: equal bit for bit)."""
+    if source == "oracle":
+        from oracle import oracle
+        return oracle.ic_heat3d_blobs(nx, ny, nz, seed, nblobs)
     from multigpu_advectiondiffusion_gb300 import _native as N
     u = np.empty(nx * ny * nz)
     N.check(N.load().adv_ic_heat3d_blobs(nx, ny, nz, seed, nblobs, u.ctypes.data_as(C.POINTER(C.c_double))), "ic")
     return u
 
 
-def ic_burgers_fourier(nx, ny, nz, L, seed, nmodes=16, amax=0.1):
-    """Seeded initial condition from the library's host generator (adv_ic_burgers_fourier)."""
+def ic_burgers_fourier(nx, ny, nz, L, seed, nmodes=16, amax=0.1, source="library"):
+    """Seeded initial condition from the library's host generator (adv_ic_burgers_fourier), or the
+    oracle's (source="oracle")."""
+    if source == "oracle":
+        from oracle import oracle
+        return oracle.ic_burgers_fourier(nx, ny, nz, L, seed, nmodes, amax)
     from multigpu_advectiondiffusion_gb300 import _native as N
     u = np.empty(nx * ny * nz)
     N.check(N.load().adv_ic_burgers_fourier(nx, ny, nz, L, seed, nmodes, amax,
@@ -173,23 +181,62 @@ def ic_burgers_fourier(nx, ny, nz, L, seed, nmodes=16, amax=0.1):
     return u
 
 
-def heat_setup(dtype):
+HEAT3D_WORKLOAD = "heat3d 256^3 f32 o2 euler r=1/8 dirichlet 8 blobs x 2000 steps"
+HEAT2D_WORKLOAD = "heat2d 512^2 f32 o2 euler r=0.2 dirichlet gaussian bump + N(0,1e-3) noise x 1000 steps"
+
+
+def heat_case(workload: str):
+    """(config, time steps per solve) of a heat workload: 3D 256^3 O2 forward Euler at r = 1/8 for
+    2000 steps (the metric's configuration), or 2D 512^2 O2 forward Euler at r = 0.2 for 1000 steps
+    (the plain method, CPU-sized). The configuration object is a plain dataclass (no library load)."""
     from multigpu_advectiondiffusion_gb300.solvers import HeatConfig
-    n = 256
-    cfg = HeatConfig.dirichlet_o2(3, n)
-    u0 = ic_heat3d_blobs(n, n, n, 2).astype(dtype)
-    return cfg, u0, 2000
+    if workload == "heat2d":
+        return HeatConfig.dirichlet_o2(2, 512), 1000
+    return HeatConfig.dirichlet_o2(3, 256), 2000
 
 
-def cpu_heat_rate(cfg, u0, budget_s: float):
-    """Oracle (the reference scheme's CPU restatement) on all host threads: Gcell-updates/s."""
+def heat_initial(workload: str, source: str = "library") -> np.ndarray:
+    """The workload's seeded FP32 initial state, from the library's host generator (the GPU arm) or
+    the oracle's (the CPU arms; the two are equal bit for bit, tests/test_abi.py)."""
+    cfg, _ = heat_case(workload)
+    if source == "oracle":
+        from oracle import oracle
+        u = (oracle.ic_heat2d_gauss_noise(cfg.nx, cfg.ny, 1, 1e-3) if workload == "heat2d"
+             else oracle.ic_heat3d_blobs(cfg.nx, cfg.ny, cfg.nz, 2))
+        return u.astype(np.float32)
+    if workload == "heat2d":
+        from multigpu_advectiondiffusion_gb300 import _native as N
+        u = np.empty(cfg.nx * cfg.ny)
+        N.check(N.load().adv_ic_heat2d_gauss_noise(cfg.nx, cfg.ny, 1, 1e-3, u.ctypes.data_as(C.POINTER(C.c_double))),
+                "ic")
+        return u.astype(np.float32)
+    return ic_heat3d_blobs(cfg.nx, cfg.ny, cfg.nz, 2).astype(np.float32)
+
+
+def heat_config(workload: str, world: int) -> dict:
+    """The `config` object both arms print for a heat workload (identical, so the two lines can be
+    matched)."""
+    if workload == "heat2d":
+        return {"workload": HEAT2D_WORKLOAD, "parallelism": f"replicas{world}",
+                "l2": "1 MiB state fits in L2 (the plain method's size); 252 MiB L2 flush between GPU steps"}
+    return {"workload": HEAT3D_WORKLOAD, "parallelism": f"replicas{world}",
+            "l2": "per time step 64 MiB read + 64 MiB written > 126 MiB L2; 252 MiB L2 flush between GPU steps"}
+
+
+def cpu_heat_rate(cfg, u0, nsteps: int, budget_s: float):
+    """The tuned CPU loop (oracle/cpu_baseline.cpp: the same O2 forward-Euler update, OpenMP) on a
+    bounded sample of one solve: min(nsteps, what fits in about budget_s) time steps from u0.
+    Returns (Gcell-updates/s, time steps, seconds)."""
     from oracle import oracle
+    u = u0.copy()
+    w = np.empty_like(u)
     t0 = time.perf_counter()
-    oracle.heat_run(cfg, u0, 2, 0)
+    oracle.cpu_heat_euler_o2(cfg, u, 2, w)
     one = (time.perf_counter() - t0) / 2
-    steps = int(max(2, min(2000, budget_s / max(one, 1e-6))))
+    steps = int(max(2, min(nsteps, budget_s / max(one, 1e-9))))
+    u[:] = u0
     t0 = time.perf_counter()
-    oracle.heat_run(cfg, u0, steps, 0)
+    oracle.cpu_heat_euler_o2(cfg, u, steps, w)
     dt = time.perf_counter() - t0
     return cfg.numel * steps / dt / 1e9, steps, dt
 
@@ -212,22 +259,23 @@ def cpu_model() -> str:
     return platform.machine()
 
 
-def cpu_baseline_heat(cfg, u0, budget_s: float) -> dict:
-    """The oracle's rate on the heat workload with all host threads, then on one thread (a
-    bounded sample of each: about budget_s and min(budget_s, 3) seconds)."""
+def cpu_baseline_heat(cfg, u0, nsteps: int, budget_s: float) -> dict:
+    """The tuned CPU loop's rate on the heat workload with all host threads, then on one thread
+    (bounded samples of about budget_s and min(budget_s, 3) seconds)."""
     from oracle import oracle
     threads = os.cpu_count() or 1
     oracle.set_threads(threads)
-    r, s, dtc = cpu_heat_rate(cfg, u0, budget_s)
+    r, s, dtc = cpu_heat_rate(cfg, u0, nsteps, budget_s)
     oracle.set_threads(1)
     try:
-        r1, s1, dt1 = cpu_heat_rate(cfg, u0, min(budget_s, 3.0))
+        r1, s1, dt1 = cpu_heat_rate(cfg, u0, nsteps, min(budget_s, 3.0))
     finally:
         oracle.set_threads(threads)
-    n = round(cfg.numel ** (1 / 3)) if cfg.ndim == 3 else cfg.nx
+    size = f"{cfg.nx}^{cfg.ndim}"
     return {"value": r, "unit": "Gcell-updates/s", "cores": threads, "kind": "port",
-            "sample": f"{n}^{cfg.ndim} FP32 O2 Euler, {s} time steps in {dtc:.1f} s (oracle, OpenMP)",
-            "one_core_value": r1, "one_core_sample": f"{s1} time steps in {dt1:.1f} s on one thread",
+            "sample": f"{size} FP32 O2 Euler, {s} of the {nsteps} time steps in {dtc:.2f} s (tuned CPU loop, "
+                      "oracle/cpu_baseline.cpp, OpenMP)",
+            "one_core_value": r1, "one_core_sample": f"{s1} time steps in {dt1:.2f} s on one thread",
             "cpu_model": cpu_model()}
 
 
@@ -236,6 +284,14 @@ BURGERS_FLOPS_PER_CELL_STAGE = 451.4
 
 ENSEMBLE_SEED = 2024
 ENSEMBLE_STEPS = 500
+# WENO weight division of the ensemble's Burgers members: IEEE FP32, whose quotient equals the FP64
+# division's rounded to the FP32 state bit for bit (tests/test_gpu_burgers.py)
+ENSEMBLE_DIV = "f32"
+
+
+def ensemble_workload() -> str:
+    return (f"ensemble 64 heat (n in 64..192, o2 euler r=1/8) + 32 burgers (n in 96..160, weno5-z global-lf "
+            f"periodic cfl 0.4, {ENSEMBLE_DIV} div) x {ENSEMBLE_STEPS} steps, one graph")
 
 
 def ensemble_members():
@@ -250,15 +306,21 @@ def ensemble_members():
         n = int(rng.choice([64, 96, 128, 160, 192]))
         k = float(10 ** rng.uniform(-1, 1))
         heat.append(HeatConfig.dirichlet_o2(3, n, k=k, r=0.125))
-    burgers = [BurgersConfig.periodic(int(rng.choice([96, 112, 128, 144, 160])), weno="z", div="fast")
+    burgers = [BurgersConfig.periodic(int(rng.choice([96, 112, 128, 144, 160])), weno="z", div=ENSEMBLE_DIV)
                for _ in range(32)]
     return heat, burgers
 
 
-def ensemble_initial_states(heat, burgers):
-    hs = [ic_heat3d_blobs(c.nx, c.ny, c.nz, 100 + i).astype(np.float32) for i, c in enumerate(heat)]
-    bs = [ic_burgers_fourier(c.nx, c.ny, c.nz, 2.0, 200 + i).astype(np.float32) for i, c in enumerate(burgers)]
+def ensemble_initial_states(heat, burgers, source="library"):
+    hs = [ic_heat3d_blobs(c.nx, c.ny, c.nz, 100 + i, source=source).astype(np.float32) for i, c in enumerate(heat)]
+    bs = [ic_burgers_fourier(c.nx, c.ny, c.nz, 2.0, 200 + i, source=source).astype(np.float32)
+          for i, c in enumerate(burgers)]
     return hs, bs
+
+
+def ensemble_config(world: int) -> dict:
+    return {"workload": ensemble_workload(), "parallelism": f"replicas{world}",
+            "l2": "1.5 GB heat + 0.9 GB Burgers state > 126 MiB L2; 252 MiB L2 flush between GPU steps"}
 
 
 def bench_ensemble(args, world, rank, dev, stream, flush, lib):
@@ -381,12 +443,9 @@ def bench_ensemble(args, world, rank, dev, stream, flush, lib):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded sizes, diffusivities and Philox4x32-10 initial conditions)",
-            "config": {"workload": f"ensemble 64 heat (n in 64..192, o2 euler r=1/8) + 32 burgers (n in 96..160, "
-                                   f"weno5-z global-lf periodic cfl 0.4, fast div) x {S} steps, one graph",
-                       "parallelism": f"replicas{world}", "heat_cells": heat_cells, "burgers_cells": burg_cells,
-                       "l2": "1.5 GB heat + 0.9 GB Burgers state > 126 MiB L2; 252 MiB L2 flush between steps",
-                       **shape},
-            "roofline": {"bound": "hbm", "kernel": "burgers_batch_kernel<float,Z,FastDiv>", "achieved": achieved,
+            "config": ensemble_config(world),
+            "shape": {"heat_cells": heat_cells, "burgers_cells": burg_cells, **shape},
+            "roofline": {"bound": "hbm", "kernel": f"burgers_batch_kernel<float,Z,{ENSEMBLE_DIV} div>", "achieved": achieved,
                          "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                          "traffic": _traffic("ensemble"), "algorithmic_bytes_per_launch": bytes_per_launch,
                          "avg_launch_us": launch_ms * 1e3},
@@ -531,11 +590,11 @@ def bench_adjoint(args, world, rank, dev, lib):
             "unit": "Gcell-updates/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": t_grad, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded Fourier states and log-normal diffusivity)",
-            "config": {"workload": f"adjoint burgers3d {ADJ_N}^3 f32 weno5-z local-lf periodic, {ADJ_STEPS} steps to "
-                                   f"t={ADJ_T} (cfl {dt * float(u0.abs().max()) / bc.dx:.3f}), checkpoints every "
-                                   f"{ADJ_INTERVAL}; heat k(x) {HEATK_N}^3 f32 {HEATK_STEPS} steps",
-                       "parallelism": f"replicas{world}",
-                       "value_is": "forward cell-stage updates per second of forward + backward (one gradient)"},
+            "config": adjoint_config(world),
+            "value_is": "forward cell-stage updates per second of forward + backward (one gradient)",
+            "scheme_differentiated": (f"WENO5-Z, local Lax-Friedrichs, periodic, fixed dt (CFL "
+                                      f"{dt * float(u0.abs().max()) / bc.dx:.3f} at t = 0), SSP-RK3; the C3 forward "
+                                      "uses global LF, whose max|u| constant the adjoint does not differentiate"),
             "roofline": None,
             "cpu_baseline": None,
             "e2e": None,
@@ -554,8 +613,8 @@ def bench_adjoint(args, world, rank, dev, lib):
 def reference_sg_gpu(workload: str, warmup: int) -> dict | None:
     """The reference's own single-GPU CUDA build on this GPU: its kernels compiled from its sources
     with its flags (-O3, FMA contraction on) into cubins, launched with its launch geometry (run.sh
-    block sizes) in its host loop (oracle/ref_gpu.py). FP64, its only precision. None when the
-    cubins or the GPU are absent."""
+    block sizes) in its host loop (oracle/ref_gpu.py). FP64, its only precision. Inputs come from the
+    oracle's generators (this library is not loaded). None when the cubins or the GPU are absent."""
     try:
         import torch
         from oracle import ref_gpu
@@ -563,7 +622,7 @@ def reference_sg_gpu(workload: str, warmup: int) -> dict | None:
             return None
     except Exception:
         return None
-    from multigpu_advectiondiffusion_gb300.solvers import HeatConfig
+    from oracle import oracle
     dev = torch.device("cuda:0")
     out = {"precision": "f64", "source": "reference kernels.cu compiled -O3 for sm_103a, reference launch geometry"}
 
@@ -577,33 +636,31 @@ def reference_sg_gpu(workload: str, warmup: int) -> dict | None:
         return ev0.elapsed_time(ev1) * 1e-3
 
     n = 256
-    if workload in ("heat3d", "ensemble"):
+    if workload in ("heat3d", "heat2d", "ensemble"):
         mod = ref_gpu.RefModule("heat3d")
+        from multigpu_advectiondiffusion_gb300.solvers import HeatConfig
+        # the reference's constants for a 256^3 node grid on [0,10]^3 (main.cpp:55-62)
         base = HeatConfig.reference_3d(1.0, 10, 10, 10, n, n, n)
-        u = torch.from_numpy(ic_heat3d_blobs(n, n, n, 2)).to(dev)
+        k4, dt = base.kx, base.dt
+        u = torch.from_numpy(oracle.ic_heat3d_blobs(n, n, n, 2)).to(dev)
         for _ in range(max(1, warmup)):
-            ref_gpu.heat3d_run(mod, u, n, n, n, base.kx, base.ky, base.kz, base.dt, 2, block=(32, 4, 4),
-                               scheme="o2-euler")
+            ref_gpu.heat3d_run(mod, u, n, n, n, k4, k4, k4, dt, 2, block=(32, 4, 4), scheme="o2-euler")
         steps = 200
-        t = timed(lambda: ref_gpu.heat3d_run(mod, u, n, n, n, base.kx, base.ky, base.kz, base.dt, steps,
-                                             block=(32, 4, 4), scheme="o2-euler"))
+        t = timed(lambda: ref_gpu.heat3d_run(mod, u, n, n, n, k4, k4, k4, dt, steps, block=(32, 4, 4),
+                                             scheme="o2-euler"))
         out["heat3d_256_o2_euler"] = {"value": n ** 3 * steps / t / 1e9, "unit": "Gcell-updates/s",
                                       "sample": f"{steps} forward-Euler steps (Compute_Laplace3d_O2 + Compute_RK, "
                                                 "uo copy per step)"}
         steps = 20
-        t = timed(lambda: ref_gpu.heat3d_run(mod, u, n, n, n, base.kx, base.ky, base.kz, base.dt, steps,
-                                             block=(32, 4, 4)))
+        t = timed(lambda: ref_gpu.heat3d_run(mod, u, n, n, n, k4, k4, k4, dt, steps, block=(32, 4, 4)))
         out["heat3d_256_o4_rk3"] = {"value": n ** 3 * 3 * steps / t / 1e9, "unit": "Gcell-updates/s",
                                     "sample": f"{steps} SSP-RK3 steps of the baseline code"}
         mod.close()
     if workload in ("burgers3d", "ensemble"):
         mod = ref_gpu.RefModule("burgers3d")
         nb = 256
-        u0 = np.empty(nb ** 3)
-        from multigpu_advectiondiffusion_gb300 import _native as N
         dx = 2.0 / (nb - 1)
-        N.check(N.load().adv_ic_burgers_ref(nb, nb, nb, dx, dx, dx, u0.ctypes.data_as(C.POINTER(C.c_double))), "ic")
-        u = torch.from_numpy(u0).to(dev)
+        u = torch.from_numpy(oracle.ic_burgers_ref(nb, nb, nb, dx, dx, dx)).to(dev)
         ref_gpu.burgers3d_run(mod, u, nb, 2.0, 1.0, 0.3, block=8, max_steps=1)
         steps = 3
         t = timed(lambda: ref_gpu.burgers3d_run(mod, u, nb, 2.0, 1.0, 0.3, block=8, max_steps=steps))
@@ -615,81 +672,87 @@ def reference_sg_gpu(workload: str, warmup: int) -> dict | None:
 
 
 def run_reference_arm(args, world, rank):
+    """--impl reference: the path's CPU implementation on the host cores, for the same workload,
+    metric and config as this library's line. The reference has no CPU code for the path, so this is
+    its scheme restated (the tuned CPU loop for heat, the oracle otherwise), with the inputs from
+    the oracle's generators; the library itself is not loaded. Each benchmark step is a bounded
+    sample of the workload; ms_per_step is its measured wall time."""
     from oracle import oracle
     if rank != 0:
         return
     threads = os.cpu_count() or 1
     oracle.set_threads(threads)
-    if args.workload == "heat3d":
-        cfg, u0, nsteps = heat_setup(np.float32)
-        per_step_budget = 2.0
+    if args.workload in ("heat3d", "heat2d"):
+        cfg, nsteps = heat_case(args.workload)
+        u0 = heat_initial(args.workload, source="oracle")
+        budget = 4.0
         for _ in range(args.warmup):
-            cpu_heat_rate(cfg, u0, 0.2)
-        rates, samples = [], []
+            cpu_heat_rate(cfg, u0, nsteps, 0.2)
+        rates, samples, secs = [], [], []
         for _ in range(args.steps):
-            r, s, dt = cpu_heat_rate(cfg, u0, per_step_budget)
+            r, st, dt = cpu_heat_rate(cfg, u0, nsteps, budget)
             rates.append(r)
-            samples.append(s)
-        value = float(np.median(rates))
-        sample = f"256^3 FP32 O2 Euler, {int(np.median(samples))} of the 2000 time steps per step"
-        config = {"workload": "heat3d 256^3 f32 o2 euler r=1/8 dirichlet 8 blobs x 2000 steps"}
+            samples.append(st)
+            secs.append(dt)
+        sample = (f"{cfg.nx}^{cfg.ndim} FP32 O2 Euler, {int(np.median(samples))} of the {nsteps} time steps per "
+                  "step (tuned CPU loop, oracle/cpu_baseline.cpp, OpenMP)")
+        config = heat_config(args.workload, world)
     elif args.workload == "burgers3d":
         from multigpu_advectiondiffusion_gb300.solvers import BurgersConfig
         n = 256
-        cfg = BurgersConfig.periodic(n, weno="z")
-        u0 = ic_burgers_fourier(n, n, n, 2.0, 3).astype(np.float32)
-        rates = []
+        cfg = BurgersConfig.periodic(n, weno=args.weno, div=args.div)
+        u0 = ic_burgers_fourier(n, n, n, 2.0, 3, source="oracle").astype(np.float32)
+        rates, secs = [], []
         for i in range(args.warmup + args.steps):
             t0 = time.perf_counter()
-            _, _, it = oracle.burgers_run(cfg, u0, 10.0, 0.4, 1, max_steps=1, div64=False)
+            _, _, it = oracle.burgers_run(cfg, u0, 10.0, 0.4, 1, max_steps=1, div64=args.div == "f64")
             dt = time.perf_counter() - t0
             if i >= args.warmup:
                 rates.append(cfg.numel * 3 * it / dt / 1e9)
-        value = float(np.median(rates))
-        sample = "256^3 FP32 WENO5-Z periodic, 1 SSP-RK3 time step per step"
-        config = {"workload": "burgers3d 256^3 f32 weno5-z global-lf periodic cfl 0.4"}
+                secs.append(dt)
+        sample = f"256^3 FP32 WENO5-{args.weno.upper()} periodic, 1 of the 20 SSP-RK3 time steps per step (oracle)"
+        config = burgers_config(args, world)
     elif args.workload == "adjoint":
         # the oracle's adjoint (stored states, OpenMP) on a 48^3 sample of the Burgers problem
-        from multigpu_advectiondiffusion_gb300 import _native as N
         from multigpu_advectiondiffusion_gb300.solvers import BurgersConfig
         n = 48
-        cfg = BurgersConfig(n, n, n, 2.0 / n, 2.0 / n, 2.0 / n, N.ADV_WENO5_Z, N.ADV_LF_LOCAL, N.ADV_BC_PERIODIC,
-                            N.ADV_DIV_F32)
-        u0 = ic_burgers_fourier(n, n, n, 2.0, 5)
-        ut = ic_burgers_fourier(n, n, n, 2.0, 6)
+        cfg = BurgersConfig(n, n, n, 2.0 / n, 2.0 / n, 2.0 / n, 1, 0, 1, 0)  # WENO5-Z, local LF, periodic
+        u0 = ic_burgers_fourier(n, n, n, 2.0, 5, source="oracle")
+        ut = ic_burgers_fourier(n, n, n, 2.0, 6, source="oracle")
         dt = 0.4 * cfg.dx / float(np.abs(u0).max())
-        rates = []
+        rates, secs = [], []
         for i in range(args.warmup + args.steps):
             t0 = time.perf_counter()
             oracle.burgers_loss_and_gradient(cfg, u0, ut, dt, 2)
             dt_ = time.perf_counter() - t0
             if i >= args.warmup:
                 rates.append(n ** 3 * 3 * 2 / dt_ / 1e9)
-        value = float(np.median(rates))
+                secs.append(dt_)
         sample = "48^3 FP64 WENO5-Z local LF periodic, 2 steps forward + adjoint per step (oracle)"
-        config = {"workload": f"adjoint burgers3d {ADJ_N}^3 f32, {ADJ_STEPS} steps"}
+        config = adjoint_config(world)
     else:
         # the ensemble: per step, two heat instances for 4 steps and one Burgers instance for one
         # RK3 step, in proportion to the ensemble's heat / Burgers cell updates
         heat, burgers = ensemble_members()
-        h0, b0 = ensemble_initial_states(heat[:2], burgers[:1])
-        rates = []
+        h0, b0 = ensemble_initial_states(heat[:2], burgers[:1], source="oracle")
+        rates, secs = [], []
         for i in range(args.warmup + args.steps):
             t0 = time.perf_counter()
             cells = 0
             for c, a in zip(heat[:2], h0):
-                oracle.heat_run(c, a, 4, 0)
+                oracle.cpu_heat_euler_o2(c, a.copy(), 4)
                 cells += c.numel * 4
             _, _, it = oracle.burgers_run(burgers[0], b0[0], 1e9, 0.4, 1, max_steps=1, div64=False)
             cells += burgers[0].numel * 3 * it
             dt = time.perf_counter() - t0
             if i >= args.warmup:
                 rates.append(cells / dt / 1e9)
-        value = float(np.median(rates))
+                secs.append(dt)
         sample = "2 heat instances x 4 Euler steps + 1 Burgers instance x 1 SSP-RK3 step of the ensemble"
-        config = {"workload": f"ensemble 64 heat + 32 burgers x {ENSEMBLE_STEPS} steps"}
+        config = ensemble_config(world)
+    value = float(np.median(rates))
     line = {"impl": "reference", "metric": "Gcell-updates/s/RK-stage", "value": value, "unit": "Gcell-updates/s",
-            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(secs)) * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded)", "config": config,
             "cpu_baseline": {"value": value, "unit": "Gcell-updates/s", "cores": threads, "kind": "port",
@@ -699,16 +762,35 @@ def run_reference_arm(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def burgers_workload(args) -> str:
+    return (f"burgers3d 256^3 f32 weno5-{args.weno} global-lf periodic cfl 0.4 x 20 steps, "
+            f"div {args.div}")
+
+
+def burgers_config(args, world: int) -> dict:
+    return {"workload": burgers_workload(args), "parallelism": f"replicas{world}",
+            "l2": "per stage 64 MiB read (+64 MiB for stages 2-3) + 64 MiB written > 126 MiB L2; "
+                  "252 MiB L2 flush between GPU steps"}
+
+
+def adjoint_config(world: int) -> dict:
+    return {"workload": f"adjoint burgers3d {ADJ_N}^3 f32 weno5-z local-lf periodic, {ADJ_STEPS} steps to t={ADJ_T}, "
+                        f"checkpoints every {ADJ_INTERVAL}; heat k(x) {HEATK_N}^3 f32 {HEATK_STEPS} steps",
+            "parallelism": f"replicas{world}"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="heat3d", choices=["heat3d", "burgers3d", "ensemble", "adjoint"])
+    ap.add_argument("--workload", default="heat3d", choices=["heat3d", "heat2d", "burgers3d", "ensemble", "adjoint"])
     ap.add_argument("--cpu-budget", type=float, default=10.0, help="seconds of CPU-baseline work")
-    ap.add_argument("--div", default="fast", choices=["fast", "f32", "f64"],
-                    help="Burgers WENO weight division (FP32 state)")
+    ap.add_argument("--div", default="f32", choices=["fast", "f32", "f64"],
+                    help="Burgers WENO weight division (FP32 state): f32 = IEEE FP32, equal bit for bit to the "
+                         "FP64 division rounded to the state; f64 = computed in FP64; fast = reciprocal-based")
+    ap.add_argument("--weno", default="z", choices=["z", "js"], help="Burgers WENO5 flavour")
     ap.add_argument("--no-tune", action="store_true", help="skip the launch-shape autotuner")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -752,36 +834,35 @@ def main():
         if world > 1:
             dist.destroy_process_group()
         return
-    if args.workload == "heat3d":
-        cfg, u0_np, inner = heat_setup(np.float32)
+    heat = args.workload in ("heat3d", "heat2d")
+    if heat:
+        cfg, inner = heat_case(args.workload)
+        u0_np = heat_initial(args.workload)
         u0 = torch.from_numpy(u0_np).to(dev)
         u = u0.clone()
         ws = heat_workspace(cfg, u)
-        launches_per_step = inner
-        bytes_per_launch = 8 * cfg.numel
         cells_stages_per_step = cfg.numel * inner
 
         def one_step(uu):
             heat_run(cfg, uu, inner, ws, stream=sh)
         tuned = None if args.no_tune else autotune_heat(cfg, u, stream=sh)
-        workload_name = "heat3d 256^3 f32 o2 euler r=1/8 dirichlet 8 blobs x 2000 steps"
-        kernel = "heat_stage_kernel<float,2,3,TMA,stage 1,4 rows,4 warps>"
+        config = heat_config(args.workload, world)
+        kernel = ("heat_stage_kernel<float,2,3,TMA,stage 1,4 rows,4 warps>" if cfg.ndim == 3
+                  else "heat_stage_kernel<float,2,2,TMA,stage 1>")
     else:
         n = 256
-        cfg = BurgersConfig.periodic(n, weno="z", div=args.div)
+        cfg = BurgersConfig.periodic(n, weno=args.weno, div=args.div)
         u0 = torch.from_numpy(ic_burgers_fourier(n, n, n, 2.0, 3).astype(np.float32)).to(dev)
         u = u0.clone()
         ws = burgers_workspace(cfg, u)
         inner = 20
-        launches_per_step = inner * 3  # stage kernels; the per-step dt kernels are timed with them
-        bytes_per_launch = (8 + 12 + 12) / 3 * cfg.numel
         cells_stages_per_step = cfg.numel * 3 * inner
 
         def one_step(uu):
             burgers_run(cfg, uu, 1e9, 0.4, N.ADV_DT_MAXU, max_steps=inner, workspace=ws, stream=sh)
         tuned = None if args.no_tune else autotune_burgers(cfg, u, stream=sh)
-        workload_name = f"burgers3d 256^3 f32 weno5-z global-lf periodic cfl 0.4 x 20 steps, div {args.div}"
-        kernel = f"burgers_stage_kernel<float,Z,{args.div}>"
+        config = burgers_config(args, world)
+        kernel = f"burgers_stage_kernel<float,{args.weno.upper()},{args.div} div>"
 
     def timed(fn, K):
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -815,6 +896,15 @@ def main():
     fl = timed(lambda: None, args.steps)
     ms_max = max_over_ranks(ms, dev)
     value = replica_throughput(cells_stages_per_step * args.steps, ms_max, world)
+    # stage launches of one benchmark step (Burgers: 3 per time step; its per-step dt kernel is
+    # counted by the library but timed with the stages); each stage launch reads and writes the
+    # state once, whatever number of time steps it advances
+    if heat:
+        launches_per_step = max(1, launched // max(1, args.steps))
+        bytes_per_launch = 8 * cfg.numel
+    else:
+        launches_per_step = inner * 3
+        bytes_per_launch = (8 + 12 + 12) / 3 * cfg.numel
     launch_ms = (ms - fl) / max(1, args.steps * launches_per_step)
     achieved = bytes_per_launch / (launch_ms * 1e-3) / 1e9
     peak, peak_kind = _peaks()
@@ -837,7 +927,17 @@ def main():
 
     # ---- accuracy of the FP32 result against FP64 (same device kernels, bit-exact with the oracle)
     extra = {}
-    if args.workload == "heat3d":
+
+    def ev_time(fn):
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        fn()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        return ev0.elapsed_time(ev1) * 1e-3
+
+    if heat:
         u32 = u0.clone()
         u64 = u0.double()
         heat_run(cfg, u32, inner, stream=sh)
@@ -847,15 +947,9 @@ def main():
         ws64 = heat_workspace(cfg, u64)
         for _ in range(2):
             heat_run(cfg, u64, inner, ws64, stream=sh)
-        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        ev0.record(stream)
-        for _ in range(3):
-            heat_run(cfg, u64, inner, ws64, stream=sh)
-        ev1.record(stream)
-        torch.cuda.synchronize()
-        extra["f64_value"] = cells_stages_per_step * 3 / (ev0.elapsed_time(ev1) * 1e-3) / 1e9
-    elif args.workload == "burgers3d":
+        extra["f64_value"] = cells_stages_per_step * 3 / ev_time(
+            lambda: [heat_run(cfg, u64, inner, ws64, stream=sh) for _ in range(3)])
+    else:
         # ALU roofline: the stage is compute-bound. FP32 flops per cell-stage from the ncu
         # instruction mix of the stage kernel (FFMA2 = 4, FADD2/FMUL2/FFMA = 2, FADD/FMUL = 1;
         # profiles/burgers_stage_burgers3d_256_f32_ncu.md); peak = nominal FP32 CUDA-core rate.
@@ -871,33 +965,46 @@ def main():
                                  "unit": "TFLOP/s", "frac": flops / fp32_peak,
                                  "peak_source": f"nominal: {sms} SMs x 128 FP32 lanes x 2 flop x {sm_mhz:.0f} MHz",
                                  "flops_per_cell_stage": BURGERS_FLOPS_PER_CELL_STAGE}
-        # FP32 state after three time steps from the initial state, to compare with the FP64 run
+        # the other WENO weight divisions on the same problem (one benchmark step each)
+        others = {}
+        for dv in ("fast", "f32", "f64"):
+            if dv == args.div:
+                continue
+            c2 = BurgersConfig.periodic(256, weno=args.weno, div=dv)
+            u2 = u0.clone()
+            w2 = burgers_workspace(c2, u2)
+            burgers_run(c2, u2, 1e9, 0.4, N.ADV_DT_MAXU, max_steps=2, workspace=w2, stream=sh)
+            sec = ev_time(lambda: burgers_run(c2, u2, 1e9, 0.4, N.ADV_DT_MAXU, max_steps=inner, workspace=w2,
+                                              stream=sh))
+            others[dv] = cells_stages_per_step / sec / 1e9
+            del u2, w2
+        extra["other_division_values"] = others
+        # the whole C3 run to t = 0.5 (past shock formation) in FP32 with this division and in FP64 in the
+        # reference's operand order (bit-exact with the oracle): steps and relative L2 error
         u32 = u0.clone()
-        burgers_run(cfg, u32, 1e9, 0.4, N.ADV_DT_MAXU, max_steps=3, workspace=burgers_workspace(cfg, u32), stream=sh)
+        t32, it32 = burgers_run(cfg, u32, 0.5, 0.4, N.ADV_DT_MAXU, workspace=ws, stream=sh)
+        c64 = BurgersConfig.periodic(256, weno=args.weno, div="f32")
+        u64 = u0.double()
+        t64, it64 = burgers_run(c64, u64, 0.5, 0.4, N.ADV_DT_MAXU, stream=sh)
+        extra["rel_l2_vs_fp64"] = (torch.linalg.vector_norm(u32.double() - u64) / torch.linalg.vector_norm(u64)).item()
+        extra["rel_l2_vs_fp64_after"] = f"the run to t = 0.5: {it32} FP32 steps, {it64} FP64 steps"
+        del u32
         # FP64 state, same problem: the reference's operand order (bit-exact with the oracle) and
         # the common-denominator form (ADV_DIV_FAST), two steps each
-        for key, div in (("f64_value", N.ADV_DIV_F32), ("f64_fast_value", N.ADV_DIV_FAST)):
-            c64 = dataclasses.replace(cfg, div=div)
+        for key, dv in (("f64_value", "f32"), ("f64_fast_value", "fast")):
+            c64 = BurgersConfig.periodic(256, weno=args.weno, div=dv)
             u64 = u0.double()
             ws64 = burgers_workspace(c64, u64)
             burgers_run(c64, u64, 1e9, 0.4, N.ADV_DT_MAXU, max_steps=1, workspace=ws64, stream=sh)
-            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            torch.cuda.synchronize()
-            ev0.record(stream)
-            burgers_run(c64, u64, 1e9, 0.4, N.ADV_DT_MAXU, max_steps=2, workspace=ws64, stream=sh)
-            ev1.record(stream)
-            torch.cuda.synchronize()
-            extra[key] = cfg.numel * 3 * 2 / (ev0.elapsed_time(ev1) * 1e-3) / 1e9
-            if key == "f64_value":  # u64: three steps in the reference's FP64 arithmetic
-                extra["rel_l2_vs_fp64"] = (torch.linalg.vector_norm(u32.double() - u64) /
-                                           torch.linalg.vector_norm(u64)).item()
-                extra["rel_l2_vs_fp64_after"] = "3 time steps (FP32 with its own max|u| dt)"
+            sec = ev_time(lambda: burgers_run(c64, u64, 1e9, 0.4, N.ADV_DT_MAXU, max_steps=2, workspace=ws64,
+                                              stream=sh))
+            extra[key] = cfg.numel * 3 * 2 / sec / 1e9
             del u64, ws64
 
-    # ---- CPU baseline (oracle on the host cores, rank 0, N = 1 only)
+    # ---- CPU baseline (the tuned CPU loop on the host cores, rank 0, N = 1 only)
     cpu = None
-    if rank == 0 and world == 1 and args.workload == "heat3d":
-        cpu = cpu_baseline_heat(cfg, u0_np, args.cpu_budget)
+    if rank == 0 and world == 1 and heat:
+        cpu = cpu_baseline_heat(cfg, u0_np, inner, args.cpu_budget)
 
     if rank == 0:
         line = {
@@ -905,14 +1012,14 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded Philox4x32-10 initial condition)",
-            "config": {"workload": workload_name, "parallelism": f"replicas{world}",
-                       "l2": "per launch 64 MiB read + 64 MiB written > 126 MiB L2; 252 MiB L2 flush between steps",
-                       "launch_shape": ({"ctas_per_sm": tuned["param_a"], "min_planes_per_cta": tuned["param_b"],
-                                         "tuned_us": tuned["best_us"], "default_us": tuned["default_us"]}
-                                        if tuned else "default")},
+            "config": config,
+            "launch_shape": ({"ctas_per_sm": tuned["param_a"], "min_planes_per_cta": tuned["param_b"],
+                              "tuned_us": tuned["best_us"], "default_us": tuned["default_us"]}
+                             if tuned else "default"),
             "roofline": {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind, "traffic": _traffic(args.workload),
-                         "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_us": launch_ms * 1e3},
+                         "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_us": launch_ms * 1e3,
+                         "launches_per_step": launches_per_step},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "Gcell-updates/s", "h2d_bytes_per_step": nbytes,
                     "d2h_bytes_per_step": nbytes},

@@ -15,6 +15,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 SO = HERE / "_build" / "liboracle.so"
 SRC = HERE / "advdiff_oracle.cpp"
+SOURCES = [SRC, HERE / "cpu_baseline.cpp"]
 
 _lib = None
 _D, _I, _I64, _U32 = C.c_double, C.c_int, C.c_int64, C.c_uint32
@@ -25,11 +26,11 @@ _BURG = [_I, _I, _I, _I, _I, _I, _I, _D, _D, _D, _D, _D, _D]
 
 def build() -> Path:
     """Compiles liboracle.so with g++ (the same flags as oracle/Makefile)."""
-    if not SO.exists() or SO.stat().st_mtime < SRC.stat().st_mtime:
+    if not SO.exists() or any(SO.stat().st_mtime < s.stat().st_mtime for s in SOURCES):
         SO.parent.mkdir(parents=True, exist_ok=True)
         cxx = os.environ.get("CXX", "g++")
         subprocess.run([cxx, "-O3", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
-                        "-o", str(SO), str(SRC)], check=True)
+                        "-o", str(SO), *map(str, SOURCES)], check=True)
     return SO
 
 
@@ -73,6 +74,8 @@ def lib() -> C.CDLL:
             "orc_proto_run_f64": (_I64, [_I, _I, _I, _I, _I, _PD, _D, _D, _I64, C.c_void_p, _PD]),
             "orc_weno7_side_f64": (_D, [_PD]),
             "orc_lsrk54_gain": (None, [_D, _D, _PD, _PD]),
+            "orc_cpu_heat_euler_o2_f32": (None, [_I, _I, _I, _I, _I, _I, _D, _D, _D, _D, _I64, C.c_void_p,
+                                                  C.c_void_p]),
             "orc_num_threads": (_I, []),
             "orc_set_num_threads": (None, [_I]),
         }
@@ -115,6 +118,18 @@ def heat_run(cfg, u: np.ndarray, nsteps: int, time: int, fp32_order: str = "gpu"
         f = lib().orc_heat_run_f32 if fp32_order == "reference" else lib().orc_heat_run_f32_fma
     f(*_heat_args(cfg.ndim, cfg.nx, cfg.ny, cfg.nz, cfg.order, cfg.frozen, cfg.zero_boundary, False,
                   cfg.kx, cfg.ky, cfg.kz, cfg.dt), time, nsteps, _p(u))
+    return u
+
+
+def cpu_heat_euler_o2(cfg, u: np.ndarray, nsteps: int, work: np.ndarray | None = None) -> np.ndarray:
+    """nsteps forward-Euler O2 steps of an FP32 state with the tuned CPU loop of the benchmark's
+    CPU baseline (cpu_baseline.cpp); in place on u, which is returned. Equal bit for bit to
+    heat_run(cfg, u, nsteps, 0, fp32_order="reference")."""
+    assert u.dtype == np.float32 and u.flags.c_contiguous and cfg.order == 2
+    if work is None:
+        work = np.empty_like(u)
+    lib().orc_cpu_heat_euler_o2_f32(cfg.ndim, cfg.nx, cfg.ny, cfg.nz if cfg.ndim == 3 else 1, cfg.frozen,
+                                    int(cfg.zero_boundary), cfg.kx, cfg.ky, cfg.kz, cfg.dt, nsteps, _p(u), _p(work))
     return u
 
 
