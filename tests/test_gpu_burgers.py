@@ -184,6 +184,69 @@ def test_burgers_config_c3_full_size_invariants(cuda, oracle):
     assert u.max().item() <= u0.max() + 1e-3 and u.min().item() >= u0.min() - 1e-3
 
 
+@pytest.mark.parametrize("weno", ["z", "js"])
+def test_fp64_weight_division_equals_ieee_fp32_division(cuda, oracle, weno):
+    """With an FP32 state, ADV_DIV_F64 divides each side's two FP32 weight sums in FP64 and rounds the
+    quotient to FP32; ADV_DIV_F32 divides them in IEEE FP32. Rounding twice is harmless when the
+    wider format carries p >= 2q + 2 bits (53 >= 2*24 + 2; S. Figueroa, "When is double rounding
+    innocuous?", 1995), so the two give the same bits: checked on a stage with partial tiles and on
+    a run past shock formation."""
+    import torch
+    cfg32 = BurgersConfig.periodic(48, weno=weno, div="f32")
+    cfg64 = BurgersConfig.periodic(48, weno=weno, div="f64")
+    u0 = oracle.ic_burgers_fourier(48, 48, 48, 2.0, 3).astype(np.float32)
+    a, b = _t(u0, cuda), _t(u0, cuda)
+    ta, ia = burgers_run(cfg32, a, 0.5, 0.4, N.ADV_DT_MAXU)
+    tb, ib = burgers_run(cfg64, b, 0.5, 0.4, N.ADV_DT_MAXU)
+    assert (ta, ia) == (tb, ib) and torch.equal(a, b)
+    nx, ny, nz = 37, 35, 23
+    for lf in ("global", "local"):
+        c32 = BurgersConfig(nx, ny, nz, 2.0 / nx, 2.0 / ny, 2.0 / nz, cfg32.weno,
+                            N.ADV_LF_GLOBAL if lf == "global" else N.ADV_LF_LOCAL, N.ADV_BC_PERIODIC, N.ADV_DIV_F32)
+        c64 = BurgersConfig(nx, ny, nz, 2.0 / nx, 2.0 / ny, 2.0 / nz, cfg32.weno, c32.lf, N.ADV_BC_PERIODIC,
+                            N.ADV_DIV_F64)
+        x = _t(np.random.default_rng(5).standard_normal(nx * ny * nz).astype(np.float32), cuda)
+        o32, o64 = torch.empty_like(x), torch.empty_like(x)
+        burgers_stage(c32, 1, x, x, o32, 1e-3, float(x.abs().max()))
+        burgers_stage(c64, 1, x, x, o64, 1e-3, float(x.abs().max()))
+        assert torch.equal(o32, o64)
+
+
+_C3_FP64 = {}
+
+
+def _c3_fp64(cuda, oracle, weno):
+    """The C3 problem (256^3 periodic, global LF, CFL 0.4, max|u| dt, t = 0.5) run with FP64 state
+    in the reference's operand order -- the GPU path that equals the FP64 oracle bit for bit
+    (test_burgers_run_fp64_bitwise) -- computed once per WENO flavour."""
+    if weno not in _C3_FP64:
+        n = 256
+        cfg = BurgersConfig.periodic(n, weno=weno)
+        cfg.div = N.ADV_DIV_F32  # FP64 state: the reference's literal form, bit-exact
+        u = _t(oracle.ic_burgers_fourier(n, n, n, 2.0, 3), cuda)
+        t, it = burgers_run(cfg, u, 0.5, 0.4, N.ADV_DT_MAXU)
+        _C3_FP64[weno] = (u.cpu().numpy(), t, it)
+    return _C3_FP64[weno]
+
+
+@pytest.mark.parametrize("weno", ["z", "js"])
+@pytest.mark.parametrize("div", [N.ADV_DIV_FAST, N.ADV_DIV_F64])
+def test_burgers_config_c3_full_size_fp32_vs_fp64(cuda, oracle, weno, div):
+    """C3 at its own size: 256^3 periodic WENO5-Z (and JS), global LF, CFL 0.4, run past shock
+    formation to t = 0.5 in FP32 -- with the FP32 reciprocal division of the benchmark and with the
+    FP64 weight division -- against the same run in FP64: same step count, relative L2 <= 1e-5."""
+    n = 256
+    want, t_w, it_w = _c3_fp64(cuda, oracle, weno)
+    cfg = BurgersConfig.periodic(n, weno=weno)
+    cfg.div = div
+    u = _t(oracle.ic_burgers_fourier(n, n, n, 2.0, 3).astype(np.float32), cuda)
+    t, it = burgers_run(cfg, u, 0.5, 0.4, N.ADV_DT_MAXU)
+    assert it == it_w and t == pytest.approx(t_w, abs=1e-12)
+    got = u.cpu().numpy().astype(np.float64)
+    rel = np.linalg.norm(got - want) / np.linalg.norm(want)
+    assert rel <= 1e-5, rel
+
+
 def test_burgers_run_honours_max_steps(cuda, oracle):
     cfg = BurgersConfig.periodic(16, weno="z")
     u0 = oracle.ic_burgers_fourier(16, 16, 16, 2.0, 3)
