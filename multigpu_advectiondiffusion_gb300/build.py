@@ -30,9 +30,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
               "--expt-relaxed-constexpr", "-I", str(INCLUDE), "-I", str(CSRC)]
 
-LIB_UNITS = ["api.cu", "api_device.cu", "heat_kernels.cu", "heat_f32.cu", "heat_f64.cu", "burgers_f32.cu", "burgers_f64.cu",
+LIB_UNITS = ["api.cu", "api_device.cu", "heat_kernels.cu", "heat_f32.cu", "heat_f64.cu", "heat2_f32.cu", "burgers_f32.cu", "burgers_f64.cu",
              "ref_ops.cu", "noalloc.cu", "heat_batch.cu", "burgers_batch_f32.cu", "burgers_batch_f64.cu", "ensemble.cu",
-             "heatk.cu", "burgers_adjoint.cu", "autotune.cu",
+             "heatk.cu", "burgers_adjoint.cu", "autotune.cu", "weno7.cu",
              "formats.cpp"]
 # library -> (source, extra defines)
 COMPAT = {

@@ -88,6 +88,11 @@ adv_status heat_prepare(const adv_heat_desc& d, const void* u_in, HeatLaunch* L,
 adv_status heat_launch(const adv_heat_desc& d, const HeatLaunch& L, int stage, const void* u_in,
                        const void* u_n, void* u_out, cudaStream_t s);
 adv_status heat_validate(const adv_heat_desc* d);
+// Two forward-Euler steps per launch (FP32 3D O2, rows of whole 16-byte vectors, TMA path):
+// u_out = E(E(u_in)), bit for bit two heat_launch stage-1 steps.
+bool heat2_eligible(const adv_heat_desc& d, const void* u_in);
+adv_status heat2_prepare(const adv_heat_desc& d, const void* u_in, HeatLaunch* L);
+adv_status heat2_launch(const adv_heat_desc& d, const HeatLaunch& L, const void* u_in, void* u_out, cudaStream_t s);
 int heat_tune_variant(const adv_heat_desc& d);
 
 // --------------------------------------------------------------- Burgers launchers

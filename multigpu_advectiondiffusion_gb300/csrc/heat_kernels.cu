@@ -120,6 +120,62 @@ adv_status heat_prepare(const adv_heat_desc& d, const void* u_in, HeatLaunch* L,
   return ADV_OK;
 }
 
+// ------------------------------------------------------------- two Euler steps per launch
+void* heat_twostep_kernel_ptr();
+size_t heat_twostep_smem();
+
+bool heat2_eligible(const adv_heat_desc& d, const void* u_in) {
+  return d.dtype == ADV_F32 && d.ndim == 3 && d.order == 2 && d.nx % 4 == 0 && (uintptr_t)u_in % 16 == 0 &&
+         d.nx >= 2 * d.frozen + 1 && d.ny >= 2 * d.frozen + 1 && d.nz >= 2 * d.frozen + 1;
+}
+
+adv_status heat2_prepare(const adv_heat_desc& d, const void* u_in, HeatLaunch* L) {
+  if (!heat2_eligible(d, u_in)) return set_error(ADV_ERR_UNSUPPORTED, "heat: no two-step kernel for this problem");
+  DeviceInfo di;
+  adv_status st = device_info(&di);
+  if (st != ADV_OK) return st;
+  constexpr int BX = 128, BY = 16, SW = 136, SHU = 20;
+  void* k = heat_twostep_kernel_ptr();
+  const size_t smem = heat_twostep_smem();
+  ADV_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int occ = 0;
+  ADV_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, 128, smem));
+  occ = std::max(occ, 1);
+  L->tma = true;
+  L->occ = occ;
+  L->rows = 4;
+  L->warps = 4;
+  L->lanes = 32;
+  L->block = dim3(32, 4, 1);
+  L->tiles_x = (d.nx + BX - 1) / BX;
+  L->tiles_y = (d.ny + BY - 1) / BY;
+  // one wave of CTAs with equal shares of the (tile, plane) pairs, at least 8 planes each
+  const int64_t total = (int64_t)L->tiles_x * L->tiles_y * d.nz;
+  const int64_t ctas = std::max<int64_t>(1, std::min<int64_t>((int64_t)di.sms * occ, total / 8));
+  L->grid = dim3((unsigned)ctas, 1, 1);
+  L->smem = smem;
+  std::memset(&L->tmap_in, 0, sizeof(L->tmap_in));
+  EncodeTiledFn enc = encode_tiled_fn();
+  if (!enc) return set_error(ADV_ERR_CUDA, "heat: cuTensorMapEncodeTiled unavailable");
+  cuuint64_t gdim[3] = {(cuuint64_t)d.nx, (cuuint64_t)d.ny, (cuuint64_t)d.nz};
+  cuuint64_t gstride[2] = {(cuuint64_t)d.nx * 4, (cuuint64_t)d.nx * d.ny * 4};
+  cuuint32_t box[3] = {(cuuint32_t)SW, (cuuint32_t)SHU, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult cr = enc(&L->tmap_in, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void*>(u_in), gdim, gstride, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (cr != CUDA_SUCCESS) return set_error(ADV_ERR_CUDA, "heat: cuTensorMapEncodeTiled failed");
+  return ADV_OK;
+}
+
+adv_status heat2_launch(const adv_heat_desc& d, const HeatLaunch& L, const void* u_in, void* u_out, cudaStream_t s) {
+  HeatParams<float> p = heat_params<float>(d, L, 1, u_in, u_in, u_out);
+  void* args[] = {const_cast<CUtensorMap*>(&L.tmap_in), &p};
+  ADV_CUDA_TRY(cudaLaunchKernel(heat_twostep_kernel_ptr(), L.grid, L.block, args, L.smem, s));
+  count_launches(1);
+  return ADV_OK;
+}
+
 template <class T>
 static adv_status heat_launch_t(const adv_heat_desc& d, const HeatLaunch& L, int stage, const void* u_in,
                                 const void* u_n, void* u_out, cudaStream_t s) {

@@ -466,8 +466,12 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
     }
     __syncthreads();  // every read of stream entry q - RZ is done: its slot can be refilled
     if (*abort_flag) {
-      // A wait expired: let the copies already issued land (bounded) before the CTA exits.
+      // A wait expired: let every copy already issued land (bounded) before the CTA exits -- plane
+      // q itself unless its copy was withheld (its slot's parity bit was already advanced), and
+      // the planes prefetched after it.
       if (TMA && tid == 0) {
+        const int s_q = s_wait == 0 ? C::NS - 1 : s_wait - 1;
+        if (p0 + q != p.withheld_plane) mbar_wait_bounded(&bars[s_q], ((parity >> s_q) & 1u) ^ 1u, p.status);
         int s = s_wait;
         for (int m = q + 1; m < Q && m <= q + C::P; ++m) {
           mbar_wait_bounded(&bars[s], (parity >> s) & 1u, p.status);
