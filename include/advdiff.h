@@ -193,6 +193,33 @@ adv_status adv_burgers_resume(const adv_burgers_desc* d, void* u, void* workspac
                               int64_t step0, double tEnd, double cfl, int dt_rule, double C,
                               int64_t max_steps, double* t_out, int64_t* steps_out, void* stream);
 
+/* ----------------------------------------------------------------- WENO7 Burgers (prototype)
+ * The reference's seventh-order prototype solver of u_t + (u^2/2)_x + (u^2/2)_y (+ (u^2/2)_z) = 0
+ * (Matlab_Prototipes/InviscidBurgersNd/WENO7resAdv_{X,Y,Z}.m, LFWENO7FDM{2,3}d.m:65-104): local
+ * Lax-Friedrichs split, every line extended past its ends by copies of its end values with the
+ * face left of its first node taken as 0, the Balsara-Shu WENO7 reconstruction with the
+ * prototype's integer smoothness indicators, the residuals summed in axis order, and the
+ * Carpenter-Kennedy five-stage fourth-order 2N-storage Runge-Kutta step with dt = CFL dx /
+ * max|u| trimmed to land on tEnd. An FP64 state reproduces the prototypes' arithmetic operand for
+ * operand; an FP32 state runs the same operations in FP32. 2D (nz == 1) and 3D grids, node (i,j,k)
+ * at i + nx*j + nx*ny*k. */
+typedef struct adv_weno7_desc {
+  int32_t nx, ny, nz;
+  int32_t dtype; /* adv_dtype */
+  double dx, dy, dz;
+} adv_weno7_desc;
+
+/* Workspace of adv_weno7_rhs / adv_weno7_run: four state arrays and a loop state. */
+adv_status adv_weno7_workspace_bytes(const adv_weno7_desc* d, size_t* bytes);
+/* L = the summed prototype residuals (df/dx + df/dy (+ df/dz), the sign of the prototypes' res).
+ * Asynchronous. */
+adv_status adv_weno7_rhs(const adv_weno7_desc* d, const void* u, void* L, void* workspace, void* stream);
+/* The prototype's time loop to tEnd (at most max_steps steps) in place on u, as one CUDA graph with
+ * a device-driven loop. Synchronises the stream (reads t and the step count back); inside a stream
+ * capture it returns ADV_ERR_UNSUPPORTED. */
+adv_status adv_weno7_run(const adv_weno7_desc* d, void* u, void* workspace, double tEnd, double cfl,
+                         int64_t max_steps, double* t_out, int64_t* steps_out, void* stream);
+
 /* ------------------------------------------- heat with a diffusivity field k(x), and its adjoint
  * u_t = div(k grad u) on a 3D node grid: conservative 7-point form with arithmetic face averages
  * k_{i+1/2} = (k_i + k_{i+1})/2, forward Euler, c_a = dt / h_a^2:

@@ -39,6 +39,12 @@ class BurgersDesc(C.Structure):
                 ("kx", C.c_double), ("ky", C.c_double), ("kz", C.c_double)]
 
 
+class Weno7Desc(C.Structure):
+    """adv_weno7_desc (include/advdiff.h)."""
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("dtype", C.c_int32),
+                ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double)]
+
+
 class HeatKDesc(C.Structure):
     """adv_heatk_desc (include/advdiff.h)."""
     _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("dtype", C.c_int32),
@@ -85,6 +91,9 @@ SIGNATURES = [
     ("adv_burgers_workspace_bytes", _I, [C.POINTER(BurgersDesc), C.POINTER(C.c_size_t)]),
     ("adv_burgers_run", _I, [C.POINTER(BurgersDesc), _VP, _VP, _D, _D, _I, _D, _I64, _PD,
                              C.POINTER(C.c_int64), _VP]),
+    ("adv_weno7_workspace_bytes", _I, [C.POINTER(Weno7Desc), C.POINTER(C.c_size_t)]),
+    ("adv_weno7_rhs", _I, [C.POINTER(Weno7Desc), _VP, _VP, _VP, _VP]),
+    ("adv_weno7_run", _I, [C.POINTER(Weno7Desc), _VP, _VP, _D, _D, _I64, _PD, C.POINTER(C.c_int64), _VP]),
     ("adv_heatk_step", _I, [C.POINTER(HeatKDesc), _VP, _VP, _VP, _VP]),
     ("adv_heatk_adjoint_step", _I, [C.POINTER(HeatKDesc), _VP, _VP, _VP, _VP, _VP, _VP]),
     ("adv_heatk_checkpoint_bytes", _I, [C.POINTER(HeatKDesc), _I64, _I64, C.POINTER(C.c_size_t),

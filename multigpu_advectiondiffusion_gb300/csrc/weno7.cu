@@ -1,0 +1,396 @@
+// weno7.cu -- the seventh-order WENO Burgers solver of the reference's MATLAB prototypes on the GPU
+// (Matlab_Prototipes/InviscidBurgersNd/WENO7resAdv_{X,Y,Z}.m, LFWENO7FDM{2,3}d.m:65-104).
+//
+// Scheme (per axis, on every line of the grid):
+//   * local Lax-Friedrichs split f+- = (f +- |u| u)/2 of f = u^2/2 at every node;
+//   * the line extended past its ends by copies of its end values (a clamped index), faces at
+//     i+1/2 for i = 0..N-1, the face left of node 0 taken as 0;
+//   * the seven-point WENO of Balsara & Shu (J. Comput. Phys. 160 (2000) 405-452): four cubic
+//     candidates, linear weights 1/35, 12/35, 18/35, 4/35, weights d_k / (eps + beta_k)^2,
+//     eps = 1e-6, the prototype's integer quadratic-form smoothness indicators
+//     (WENO7resAdv_X.m:75-82);
+//   * res_i = (((hp_{i+1/2} + hn_{i+1/2}) - hp_{i-1/2}) - hn_{i-1/2}) / h, summed over the axes in
+//     axis order;
+//   * time: dt = CFL dx / max|u| trimmed to land on tEnd, the five-stage fourth-order 2N-storage
+//     Runge-Kutta scheme of Carpenter & Kennedy (NASA TM-109112, 1994): r = A_s r + dt R(u),
+//     u = u - B_s r.
+// Every operation is evaluated in the prototypes' operand order with correctly rounded
+// intrinsics (no contraction), so the FP64 results are those of the prototypes -- and of the CPU
+// oracle that restates them -- bit for bit; the FP32 state runs the same operations in FP32.
+//
+// Kernels. Per stage and axis: a face kernel (one thread per face i+1/2, the two split parts'
+// reconstructions hp and hn into two face arrays) and a residual kernel (one thread per node,
+// accumulating the axis's residual into the stage's right-hand side); the last axis's residual
+// kernel also applies the Runge-Kutta update in place and, at the last stage, reduces max|u| for
+// the next step's dt. Threads run along x, so every access of every axis is coalesced. The time
+// loop is one CUDA graph with a device-driven while node (the step-start kernel of the Burgers
+// loop: dt rule, trim, t in FP64).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+
+#include "adv_device.cuh"
+#include "adv_internal.h"
+#include "adv_math.cuh"
+#include "nvtx_range.h"
+
+namespace adv {
+namespace {
+
+// Smoothness indicator of WENO7 candidate k over its cells x0..x3, in the prototype's order:
+//   x2 (k0 x2 + k1 x3) + x0 (((k2 xb + k3 xc) + k4 xd) + k5 x3) + k6 x3 x3 + x1 ((k7 xs + k8 xt) + k9 x3)
+// (the same table as the oracle's kW7Beta).
+struct W7B {
+  int b, c, d, s, t;
+  double k[10];
+};
+__device__ constexpr W7B kBeta[4] = {
+    {2, 1, 0, 2, 1, {134241, -114894, 56694, -47214, 6649, -22778, 25729, -210282, 85641, 86214}},
+    {1, 0, 2, 1, 2, {41001, -30414, -19374, 3169, 19014, -5978, 6649, 33441, -70602, 23094}},
+    {0, 1, 2, 1, 2, {33441, -19374, 6649, -30414, 23094, -5978, 3169, 41001, -70602, 19014}},
+    {0, 1, 2, 1, 2, {85641, -47214, 25729, -114894, 86214, -22778, 6649, 134241, -210282, 56694}},
+};
+// candidates (c0 x0 + c1 x1 + c2 x2 + c3 x3)/12: the part moving towards +x (cells i-3+k .. i+k)
+// and towards -x (cells i-2+k .. i+1+k); linear weights of each
+__device__ constexpr double kPolyP[4][4] = {{-3, 13, -23, 25}, {1, -5, 13, 3}, {-1, 7, 7, -1}, {3, 13, -5, 1}};
+__device__ constexpr double kPolyM[4][4] = {{1, -5, 13, 3}, {-1, 7, 7, -1}, {3, 13, -5, 1}, {25, -23, 13, -3}};
+__device__ constexpr double kLinP[4] = {1. / 35., 12. / 35., 18. / 35., 4. / 35.};
+__device__ constexpr double kLinM[4] = {4. / 35., 18. / 35., 12. / 35., 1. / 35.};
+
+// Carpenter & Kennedy LSRK(5,4) coefficients (the published rational values).
+__device__ constexpr double kA[5] = {0.0, -567301805773.0 / 1357537059087.0, -2404267990393.0 / 2016746695238.0,
+                                     -3550918686646.0 / 2091501179385.0, -1275806237668.0 / 842570457699.0};
+__device__ constexpr double kB[5] = {1432997174477.0 / 9575080441755.0, 5161836677717.0 / 13612068292357.0,
+                                     1720146321549.0 / 2090206949498.0, 3134564353537.0 / 4481467310338.0,
+                                     2277821191437.0 / 14882151754819.0};
+
+// One split part's face value from its seven cells f[0..6] (candidate k uses f[k..k+3]).
+template <class T, bool PLUS>
+__device__ __forceinline__ T weno7_part(const T (&f)[7]) {
+  const T eps = T(1e-6);
+  T a[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const T* x = f + k;
+    const W7B& B = kBeta[k];
+    const T t1 = mul_rn(x[2], add_rn(mul_rn(T(B.k[0]), x[2]), mul_rn(T(B.k[1]), x[3])));
+    const T t2 = mul_rn(x[0], add_rn(add_rn(add_rn(mul_rn(T(B.k[2]), x[B.b]), mul_rn(T(B.k[3]), x[B.c])),
+                                            mul_rn(T(B.k[4]), x[B.d])),
+                                     mul_rn(T(B.k[5]), x[3])));
+    const T t3 = mul_rn(T(B.k[6]), mul_rn(x[3], x[3]));
+    const T t4 = mul_rn(x[1], add_rn(add_rn(mul_rn(T(B.k[7]), x[B.s]), mul_rn(T(B.k[8]), x[B.t])),
+                                     mul_rn(T(B.k[9]), x[3])));
+    const T beta = add_rn(add_rn(add_rn(t1, t2), t3), t4);
+    const T e = add_rn(eps, beta);
+    a[k] = div_rn(T(PLUS ? kLinP[k] : kLinM[k]), mul_rn(e, e));
+  }
+  const T sum = add_rn(add_rn(add_rn(a[0], a[1]), a[2]), a[3]);
+  T h = T(0);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const T* x = f + k;
+    const double* c = PLUS ? kPolyP[k] : kPolyM[k];
+    const T cand = add_rn(add_rn(add_rn(mul_rn(T(c[0]), x[0]), mul_rn(T(c[1]), x[1])), mul_rn(T(c[2]), x[2])),
+                          mul_rn(T(c[3]), x[3]));
+    const T term = div_rn(mul_rn(div_rn(a[k], sum), cand), T(12));
+    h = k == 0 ? term : add_rn(h, term);
+  }
+  return h;
+}
+
+// f+- of one node value (WENO7resAdv_X.m's split with a = |u|).
+template <class T>
+__device__ __forceinline__ void split(T v, T& fp, T& fm) {
+  const T f = div_rn(mul_rn(v, v), T(2));
+  const T av = mul_rn(fabs(v), v);
+  fp = mul_rn(T(0.5), add_rn(f, av));
+  fm = mul_rn(T(0.5), sub_rn(f, av));
+}
+
+struct W7Geom {
+  int nx, ny, nz;
+  int64_t n;
+};
+
+// Face kernel of axis AX: for every node (the face i+1/2 on its right along AX) the two parts'
+// reconstructions into hp / hn.
+template <class T, int AX>
+__global__ void __launch_bounds__(256) weno7_face_kernel(const T* __restrict__ u, T* __restrict__ hp,
+                                                         T* __restrict__ hn, W7Geom g) {
+  const int64_t stride = AX == 0 ? 1 : AX == 1 ? (int64_t)g.nx : (int64_t)g.nx * g.ny;
+  const int N = AX == 0 ? g.nx : AX == 1 ? g.ny : g.nz;
+  for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < g.n; o += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t line_pos = AX == 0 ? o % g.nx : AX == 1 ? (o / g.nx) % g.ny : o / ((int64_t)g.nx * g.ny);
+    const int i = (int)line_pos;
+    const T* line = u + (o - (int64_t)i * stride);
+    T fp[8], fm[8];  // cells i-3 .. i+4 (clamped)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int c = min(max(i + j - 3, 0), N - 1);
+      split<T>(line[(int64_t)c * stride], fp[j], fm[j]);
+    }
+    T p[7], m[7];
+#pragma unroll
+    for (int j = 0; j < 7; ++j) {
+      p[j] = fp[j];      // cells i-3 .. i+3
+      m[j] = fm[j + 1];  // cells i-2 .. i+4
+    }
+    hn[o] = weno7_part<T, true>(p);
+    hp[o] = weno7_part<T, false>(m);
+  }
+}
+
+// Residual kernel of axis AX: res_i = (((hp_i + hn_i) - hp_{i-1}) - hn_{i-1}) / h (0 for the face
+// left of node 0), accumulated into acc (FIRST: acc = res). LAST: then the Runge-Kutta update
+// r = A r + dt acc, u = u - B r in place, and (REDUCE) max|u_new| into *maxkey.
+template <class T, int AX, bool FIRST, bool LAST>
+__global__ void __launch_bounds__(256) weno7_residual_kernel(const T* __restrict__ hp, const T* __restrict__ hn,
+                                                             T* __restrict__ acc, T* __restrict__ r, T* __restrict__ u,
+                                                             W7Geom g, T h, int stage, const double* dt_dev,
+                                                             typename KeyOf<T>::type* maxkey, const int* active) {
+  using K = typename KeyOf<T>::type;
+  if (active && *active == 0) return;
+  const int64_t stride = AX == 0 ? 1 : AX == 1 ? (int64_t)g.nx : (int64_t)g.nx * g.ny;
+  const T A = T(kA[stage]), B = T(kB[stage]);
+  const T dt = LAST ? T(*dt_dev) : T(0);
+  K kmax = 0;
+  for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < g.n; o += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = AX == 0 ? o % g.nx : AX == 1 ? (o / g.nx) % g.ny : o / ((int64_t)g.nx * g.ny);
+    const T hp0 = i > 0 ? hp[o - stride] : T(0), hn0 = i > 0 ? hn[o - stride] : T(0);
+    const T res = div_rn(sub_rn(sub_rn(add_rn(hp[o], hn[o]), hp0), hn0), h);
+    const T L = FIRST ? res : add_rn(acc[o], res);
+    if (!LAST) {
+      acc[o] = L;
+    } else {
+      const T rn = add_rn(mul_rn(A, r[o]), mul_rn(dt, L));
+      r[o] = rn;
+      const T un = sub_rn(u[o], mul_rn(B, rn));
+      u[o] = un;
+      if (maxkey) {
+        const K k = abs_key(un);
+        kmax = k > kmax ? k : kmax;
+      }
+    }
+  }
+  if (LAST && maxkey) {
+    kmax = warp_max(kmax);
+    if ((threadIdx.x & 31) == 0 && kmax) atomicMax(maxkey, kmax);
+  }
+}
+
+adv_status weno7_validate(const adv_weno7_desc* d) {
+  if (!d) return set_error(ADV_ERR_INVALID_ARG, "weno7: null descriptor");
+  if (d->dtype != ADV_F32 && d->dtype != ADV_F64) return set_error(ADV_ERR_INVALID_ARG, "weno7: bad dtype");
+  if (d->nx < 1 || d->ny < 1 || d->nz < 1) return set_error(ADV_ERR_INVALID_ARG, "weno7: empty grid");
+  if (d->ny < 2) return set_error(ADV_ERR_UNSUPPORTED, "weno7: 2D and 3D grids only (ny >= 2)");
+  if ((int64_t)d->nx * d->ny * d->nz > ((int64_t)1 << 36)) return set_error(ADV_ERR_INVALID_ARG, "weno7: grid too large");
+  if (!(d->dx > 0) || !(d->dy > 0) || !(d->dz > 0)) return set_error(ADV_ERR_INVALID_ARG, "weno7: spacing must be > 0");
+  return ADV_OK;
+}
+
+size_t weno7_array_bytes(const adv_weno7_desc& d) {
+  const size_t n = (size_t)d.nx * d.ny * d.nz;
+  return (n * (d.dtype == ADV_F32 ? 4 : 8) + 255) / 256 * 256;
+}
+
+int weno7_ndim(const adv_weno7_desc& d) { return d.nz > 1 ? 3 : 2; }
+
+// Workspace: hp, hn, acc, r, then the loop state.
+struct W7Work {
+  char *hp, *hn, *acc, *r;
+  BurgersLoopState* st;
+};
+W7Work weno7_work(const adv_weno7_desc& d, void* ws) {
+  const size_t one = weno7_array_bytes(d);
+  char* b = static_cast<char*>(ws);
+  return W7Work{b, b + one, b + 2 * one, b + 3 * one, reinterpret_cast<BurgersLoopState*>(b + 4 * one)};
+}
+
+int weno7_grid(const adv_weno7_desc& d) {
+  DeviceInfo di;
+  const int sms = device_info(&di) == ADV_OK ? di.sms : 152;
+  const int64_t n = (int64_t)d.nx * d.ny * d.nz;
+  return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)sms * 16));
+}
+
+// The face + residual launches of one stage (stage 0..4), the update fused into the last axis.
+template <class T>
+adv_status weno7_stage_t(const adv_weno7_desc& d, T* u, const W7Work& w, int stage, const double* dt_dev,
+                         void* maxkey, const int* active, bool count, cudaStream_t s) {
+  using K = typename KeyOf<T>::type;
+  const W7Geom g{d.nx, d.ny, d.nz, (int64_t)d.nx * d.ny * d.nz};
+  const int grid = weno7_grid(d);
+  const int nd = weno7_ndim(d);
+  T* hp = reinterpret_cast<T*>(w.hp);
+  T* hn = reinterpret_cast<T*>(w.hn);
+  T* acc = reinterpret_cast<T*>(w.acc);
+  T* r = reinterpret_cast<T*>(w.r);
+  K* mk = static_cast<K*>(maxkey);
+  const T hx = T(d.dx), hy = T(d.dy), hz = T(d.dz);
+  weno7_face_kernel<T, 0><<<grid, 256, 0, s>>>(u, hp, hn, g);
+  weno7_residual_kernel<T, 0, true, false><<<grid, 256, 0, s>>>(hp, hn, acc, r, u, g, hx, stage, dt_dev, mk, active);
+  weno7_face_kernel<T, 1><<<grid, 256, 0, s>>>(u, hp, hn, g);
+  if (nd == 2) {
+    weno7_residual_kernel<T, 1, false, true><<<grid, 256, 0, s>>>(hp, hn, acc, r, u, g, hy, stage, dt_dev, mk, active);
+  } else {
+    weno7_residual_kernel<T, 1, false, false><<<grid, 256, 0, s>>>(hp, hn, acc, r, u, g, hy, stage, dt_dev, mk,
+                                                                   active);
+    weno7_face_kernel<T, 2><<<grid, 256, 0, s>>>(u, hp, hn, g);
+    weno7_residual_kernel<T, 2, false, true><<<grid, 256, 0, s>>>(hp, hn, acc, r, u, g, hz, stage, dt_dev, mk, active);
+  }
+  ADV_CUDA_TRY(cudaGetLastError());
+  if (count) count_launches(2 * nd);
+  return ADV_OK;
+}
+
+adv_status weno7_stage(const adv_weno7_desc& d, void* u, const W7Work& w, int stage, const double* dt_dev,
+                       void* maxkey, const int* active, bool count, cudaStream_t s) {
+  if (d.dtype == ADV_F32)
+    return weno7_stage_t<float>(d, static_cast<float*>(u), w, stage, dt_dev, maxkey, active, count, s);
+  return weno7_stage_t<double>(d, static_cast<double*>(u), w, stage, dt_dev, maxkey, active, count, s);
+}
+
+// The right-hand side alone (the summed residuals, no update): RHS kernels into acc, then copied
+// to the caller's L.
+template <class T>
+adv_status weno7_rhs_t(const adv_weno7_desc& d, const T* u, T* L, const W7Work& w, cudaStream_t s) {
+  const W7Geom g{d.nx, d.ny, d.nz, (int64_t)d.nx * d.ny * d.nz};
+  const int grid = weno7_grid(d);
+  const int nd = weno7_ndim(d);
+  T* hp = reinterpret_cast<T*>(w.hp);
+  T* hn = reinterpret_cast<T*>(w.hn);
+  weno7_face_kernel<T, 0><<<grid, 256, 0, s>>>(u, hp, hn, g);
+  weno7_residual_kernel<T, 0, true, false><<<grid, 256, 0, s>>>(hp, hn, L, nullptr, nullptr, g, T(d.dx), 0, nullptr,
+                                                                 nullptr, nullptr);
+  weno7_face_kernel<T, 1><<<grid, 256, 0, s>>>(u, hp, hn, g);
+  weno7_residual_kernel<T, 1, false, false><<<grid, 256, 0, s>>>(hp, hn, L, nullptr, nullptr, g, T(d.dy), 0, nullptr,
+                                                                 nullptr, nullptr);
+  if (nd == 3) {
+    weno7_face_kernel<T, 2><<<grid, 256, 0, s>>>(u, hp, hn, g);
+    weno7_residual_kernel<T, 2, false, false><<<grid, 256, 0, s>>>(hp, hn, L, nullptr, nullptr, g, T(d.dz), 0,
+                                                                   nullptr, nullptr, nullptr);
+  }
+  ADV_CUDA_TRY(cudaGetLastError());
+  count_launches(2 * nd);
+  return ADV_OK;
+}
+
+}  // namespace
+}  // namespace adv
+
+using namespace adv;
+
+extern "C" {
+
+adv_status adv_weno7_workspace_bytes(const adv_weno7_desc* d, size_t* bytes) {
+  adv_status st = weno7_validate(d);
+  if (st != ADV_OK) return st;
+  if (!bytes) return set_error(ADV_ERR_INVALID_ARG, "weno7: null output");
+  *bytes = 4 * weno7_array_bytes(*d) + (sizeof(BurgersLoopState) + 255) / 256 * 256;
+  return ADV_OK;
+}
+
+adv_status adv_weno7_rhs(const adv_weno7_desc* d, const void* u, void* L, void* workspace, void* stream) {
+  ADV_NVTX_RANGE("adv_weno7_rhs");
+  adv_status st = weno7_validate(d);
+  if (st != ADV_OK) return st;
+  if (!u || !L || !workspace) return set_error(ADV_ERR_INVALID_ARG, "weno7: null buffer");
+  if (u == L) return set_error(ADV_ERR_INVALID_ARG, "weno7: u and L must not alias");
+  const W7Work w = weno7_work(*d, workspace);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (d->dtype == ADV_F32) return weno7_rhs_t<float>(*d, static_cast<const float*>(u), static_cast<float*>(L), w, s);
+  return weno7_rhs_t<double>(*d, static_cast<const double*>(u), static_cast<double*>(L), w, s);
+}
+
+adv_status adv_weno7_run(const adv_weno7_desc* d, void* u, void* workspace, double tEnd, double cfl,
+                         int64_t max_steps, double* t_out, int64_t* steps_out, void* stream) {
+  ADV_NVTX_RANGE("adv_weno7_run");
+  adv_status st = weno7_validate(d);
+  if (st != ADV_OK) return st;
+  if (!u || !workspace) return set_error(ADV_ERR_INVALID_ARG, "weno7: null buffer");
+  if (!(cfl > 0) || !std::isfinite(tEnd) || max_steps < 0) return set_error(ADV_ERR_INVALID_ARG, "weno7: bad cfl/tEnd/max_steps");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if ((st = reject_capture(s, "weno7 run")) != ADV_OK) return st;
+  const W7Work w = weno7_work(*d, workspace);
+  const size_t n = (size_t)d->nx * d->ny * d->nz;
+  const size_t es = d->dtype == ADV_F32 ? 4 : 8;
+  // loop state: the Burgers loop's dt rule MAXU (dt = CFL dx / max|u|, trimmed to tEnd)
+  adv_burgers_desc bd{};
+  bd.nx = d->nx; bd.ny = d->ny; bd.nz = d->nz;
+  bd.dx = d->dx; bd.dy = d->dy; bd.dz = d->dz;
+  BurgersLoopState h = burgers_loop_state(bd, tEnd, cfl, ADV_DT_MAXU, 0.0, max_steps);
+  ADV_CUDA_TRY(cudaMemcpyAsync(w.st, &h, sizeof(h), cudaMemcpyHostToDevice, s));
+  ADV_CUDA_TRY(cudaMemsetAsync(w.r, 0, n * es, s));  // the 2N-storage register starts at zero
+  void* key0 = d->dtype == ADV_F32 ? (void*)&w.st->maxbits[0] : (void*)&w.st->maxbits64[0];
+  if ((st = max_abs_launch(d->dtype, u, (int64_t)n, key0, s)) != ADV_OK) return st;
+  // one time step: the step-start kernel (dt, t, loop condition), then five stages; the last one
+  // reduces max|u| for the next step into slot 0
+  const int nd = weno7_ndim(*d);
+  auto body = [&](cudaStream_t cs, unsigned long long cond, int use_cond) -> adv_status {
+    adv_status r = burgers_loop_begin_step(w.st, d->dtype, cond, use_cond, cs);
+    for (int stg = 0; stg < 5 && r == ADV_OK; ++stg)
+      r = weno7_stage(*d, u, w, stg, &w.st->dt, stg == 4 ? key0 : nullptr, &w.st->active, !use_cond, cs);
+    return r;
+  };
+  const int64_t launched_per_step = 1 + 5 * 2 * nd;
+  bool graph_ran = false;
+  if (max_steps > 0 && tEnd > 0.0) {
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    cudaStream_t cs;
+    ADV_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    cudaError_t e = cudaGraphCreate(&g, 0);
+    cudaGraphConditionalHandle h_cond = 0;
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h_cond, g, 1, cudaGraphCondAssignDefault);
+    cudaGraphNode_t node;
+    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+    cp.conditional.handle = h_cond;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    if (e == cudaSuccess) e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp);
+    adv_status bst = ADV_OK;
+    if (e == cudaSuccess) {
+      e = cudaStreamBeginCaptureToGraph(cs, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                        cudaStreamCaptureModeThreadLocal);
+      if (e == cudaSuccess) {
+        bst = body(cs, (unsigned long long)h_cond, 1);
+        cudaGraph_t outg = nullptr;
+        e = cudaStreamEndCapture(cs, &outg);
+      }
+      if (e == cudaSuccess && bst == ADV_OK) e = cudaGraphInstantiate(&ge, g, 0);
+    }
+    if (g) cudaGraphDestroy(g);
+    cudaStreamDestroy(cs);
+    if (bst != ADV_OK) {
+      if (ge) cudaGraphExecDestroy(ge);
+      return bst;
+    }
+    if (e == cudaSuccess && ge) {
+      graph_ran = true;
+      e = cudaGraphLaunch(ge, s);
+      cudaError_t e2 = cudaStreamSynchronize(s);
+      cudaGraphExecDestroy(ge);
+      if (e != cudaSuccess) return cuda_error(e, "weno7: graph launch");
+      if (e2 != cudaSuccess) return cuda_error(e2, "weno7: run");
+    } else {
+      cudaGetLastError();  // conditional nodes unavailable: one step at a time from the host
+      if (ge) cudaGraphExecDestroy(ge);
+      for (int64_t i = 0; i < max_steps; ++i) {
+        if ((st = body(s, 0, 0)) != ADV_OK) return st;
+        int active = 0;
+        ADV_CUDA_TRY(cudaMemcpyAsync(&active, &w.st->active, sizeof(int), cudaMemcpyDeviceToHost, s));
+        ADV_CUDA_TRY(cudaStreamSynchronize(s));
+        if (!active) break;
+      }
+    }
+  }
+  ADV_CUDA_TRY(cudaMemcpyAsync(&h, w.st, sizeof(h), cudaMemcpyDeviceToHost, s));
+  ADV_CUDA_TRY(cudaStreamSynchronize(s));
+  if (graph_ran) count_launches(launched_per_step * h.step);  // (the host loop counted its own)
+  if (t_out) *t_out = h.t;
+  if (steps_out) *steps_out = h.step;
+  return read_and_clear_device_status(s);
+}
+
+}  // extern "C"

@@ -254,6 +254,57 @@ def max_abs(u, stream=None) -> float:
 
 
 @dataclass
+class Weno7Config:
+    """The seventh-order WENO prototype solver (adv_weno7_desc): a 2D (nz = 1) or 3D node grid with
+    spacings dx, dy, dz."""
+    nx: int
+    ny: int
+    nz: int
+    dx: float
+    dy: float
+    dz: float
+
+    def desc(self, dtype: int) -> N.Weno7Desc:
+        return N.Weno7Desc(self.nx, self.ny, self.nz, dtype, self.dx, self.dy, self.dz)
+
+    @property
+    def numel(self) -> int:
+        return self.nx * self.ny * self.nz
+
+
+def _weno7_workspace_bytes(cfg: Weno7Config, code: int) -> int:
+    nb = C.c_size_t(0)
+    N.check(N.load().adv_weno7_workspace_bytes(C.byref(cfg.desc(code)), C.byref(nb)), "adv_weno7_workspace_bytes")
+    return nb.value
+
+
+def weno7_workspace(cfg: Weno7Config, like):
+    import torch
+    return torch.empty(_weno7_workspace_bytes(cfg, _dtype_code(like)), dtype=torch.uint8, device=like.device)
+
+
+def weno7_rhs(cfg: Weno7Config, u, L, workspace=None, stream=None) -> None:
+    """L = the summed prototype residuals of u (adv_weno7_rhs)."""
+    code = _fields(cfg.numel, u, L)
+    ws = weno7_workspace(cfg, u) if workspace is None else workspace
+    wp = _buffer(ws, _weno7_workspace_bytes(cfg, code), "the WENO7 workspace")
+    N.check(N.load().adv_weno7_rhs(C.byref(cfg.desc(code)), _ptr(u), _ptr(L), wp, _stream(stream, u)), "adv_weno7_rhs")
+
+
+def weno7_run(cfg: Weno7Config, u, tEnd: float, cfl: float, max_steps: int = 1 << 40, workspace=None,
+              stream=None) -> tuple[float, int]:
+    """The prototype's LSRK(5,4) time loop to tEnd in place on u (adv_weno7_run); returns (t, steps)."""
+    code = _fields(cfg.numel, u)
+    ws = weno7_workspace(cfg, u) if workspace is None else workspace
+    wp = _buffer(ws, _weno7_workspace_bytes(cfg, code), "the WENO7 workspace")
+    t = C.c_double(0.0)
+    steps = C.c_int64(0)
+    N.check(N.load().adv_weno7_run(C.byref(cfg.desc(code)), _ptr(u), wp, float(tEnd), float(cfl), int(max_steps),
+                                   C.byref(t), C.byref(steps), _stream(stream, u)), "adv_weno7_run")
+    return t.value, steps.value
+
+
+@dataclass
 class HeatKConfig:
     """3D heat with a diffusivity field (adv_heatk_desc): c_a = dt / h_a^2."""
     nx: int

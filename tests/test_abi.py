@@ -229,6 +229,7 @@ def _ctype_ok(decl: str, ct) -> bool:
     if "*" in decl:
         base = decl.split("*")[0].split()[0]
         structs = {"adv_heat_desc": N.HeatDesc, "adv_burgers_desc": N.BurgersDesc, "adv_heatk_desc": N.HeatKDesc,
+                   "adv_weno7_desc": N.Weno7Desc,
                    "adv_heat_member": N.HeatMember, "adv_burgers_member": N.BurgersMember,
                    "adv_tune_result": N.TuneResult, "adv_checkpoint_header": N.CheckpointHeader}
         if base == "char":
@@ -272,6 +273,7 @@ def test_ctypes_structures_match_the_c_layout(tmp_path):
     if shutil.which("gcc") is None:
         pytest.skip("no host compiler")
     structs = {"adv_heat_desc": N.HeatDesc, "adv_burgers_desc": N.BurgersDesc, "adv_heatk_desc": N.HeatKDesc,
+               "adv_weno7_desc": N.Weno7Desc,
                "adv_heat_member": N.HeatMember, "adv_burgers_member": N.BurgersMember,
                "adv_tune_result": N.TuneResult, "adv_checkpoint_header": N.CheckpointHeader}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "advdiff.h"', "int main(void) {"]
