@@ -19,10 +19,11 @@ The same programs' host tools (SingleGPU/<program>/tools.cpp: initial conditions
 are compiled with g++ together with oracle/ref_tools_shim.cpp into host libraries
 `libref_tools_<name>.so` (-ffp-contract=off, as the library's host code), for the CPU tests.
 
-Drop-in link check: each program's own main.cpp + tools.cpp (dense and pitched variants) are
-linked, unmodified and without their kernels.cu, against the GB300 compatibility library that
-replaces it (`refmain_<name>`, once multigpu_advectiondiffusion_gb300/_lib is built). Running
-them needs a GPU; the CPU tests check that every symbol resolves.
+Drop-in programs: each program's own main.cpp + tools.cpp (dense and pitched variants) are linked,
+unmodified and without their kernels.cu, against the GB300 compatibility library that replaces it
+(`refmain_<name>`, once multigpu_advectiondiffusion_gb300/_lib is built). They are linked from
+copies staged under oracle/_ref/src/ (git-ignored), so a GPU host of another architecture links
+them too (build_mains). The CPU tests check that every symbol resolves; the GPU tests run them.
 
     python oracle/ref_build.py [--src DIR]
 
@@ -99,24 +100,65 @@ def build(src_root: Path) -> list[Path]:
         cmd = [cxx, "-O2", "-fPIC", "-shared", "-ffp-contract=off", f"-D{define}", "-I", str(src_root / rel),
                "-I", str(_cuda_include()), "-w", "-o", str(out), str(shim), str(src), "-lm"]
         jobs.append((out, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)))
-    for name, (rel, compat) in MAINS.items():
-        lib = LIBDIR / f"lib{compat}.so"
-        srcs = [src_root / rel / "main.cpp", src_root / rel / "tools.cpp"]
-        if not lib.exists() or not all(x.exists() for x in srcs):
-            continue
-        out = OUT / f"refmain_{name}"
-        if out.exists() and out.stat().st_mtime >= max(x.stat().st_mtime for x in srcs + [lib]):
-            made.append(out)
-            continue
-        cmd = [nvcc, *ARCH, "-O3", "-w", "-o", str(out), *map(str, srcs), "-L", str(LIBDIR), f"-l{compat}",
-               "-ladvdiff", "-Xlinker", f"-rpath,{LIBDIR}"]
-        jobs.append((out, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)))
+    stage_sources(src_root)
+    jobs += _main_jobs(made)
     for out, p in jobs:
         log, _ = p.communicate()
         if p.returncode != 0:
             if out.suffix == ".cubin":
                 raise RuntimeError(f"reference build failed for {out.name}:\n{log}")
             # host tools and linked mains are checks of their own: their tests skip without them
+            print(f"warning: {out.name} not built:\n{log[-2000:]}", file=sys.stderr)
+            continue
+        made.append(out)
+    return made
+
+
+def stage_sources(src_root: Path) -> None:
+    """Copies each linked program's own main.cpp, tools.cpp and headers, unmodified, into
+    oracle/_ref/src/<name>/ (git-ignored like the rest of oracle/_ref, never committed). The GPU
+    hosts are another architecture and have no reference checkout: build() links the programs
+    there from these copies."""
+    for name, (rel, _) in MAINS.items():
+        d = src_root / rel
+        if not (d / "main.cpp").exists():
+            continue
+        dst = OUT / "src" / name
+        dst.mkdir(parents=True, exist_ok=True)
+        for f in [d / "main.cpp", d / "tools.cpp", *sorted(d.glob("*.h"))]:
+            t = dst / f.name
+            if not t.exists() or t.stat().st_mtime < f.stat().st_mtime:
+                shutil.copy2(f, t)
+
+
+def _main_jobs(made: list) -> list:
+    """Compile jobs linking each staged program against the compatibility library that replaces
+    its kernels.cu (refmain_<name>); up-to-date outputs go straight to `made`."""
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    jobs = []
+    for name, (_, compat) in MAINS.items():
+        lib = LIBDIR / f"lib{compat}.so"
+        stage = OUT / "src" / name
+        srcs = [stage / "main.cpp", stage / "tools.cpp"]
+        if not lib.exists() or not all(x.exists() for x in srcs):
+            continue
+        out = OUT / f"refmain_{name}"
+        if out.exists() and out.stat().st_mtime >= max(x.stat().st_mtime for x in srcs + [lib]):
+            made.append(out)
+            continue
+        rpath = "-rpath,$ORIGIN/../../multigpu_advectiondiffusion_gb300/_lib"
+        cmd = [nvcc, *ARCH, "-O3", "-w", "-o", str(out), *map(str, srcs), "-L", str(LIBDIR), f"-l{compat}",
+               "-ladvdiff", "-Xlinker", rpath]
+        jobs.append((out, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)))
+    return jobs
+
+
+def build_mains() -> list[Path]:
+    """Links the staged reference programs on this host (no reference checkout needed)."""
+    made: list[Path] = []
+    for out, p in _main_jobs(made):
+        log, _ = p.communicate()
+        if p.returncode != 0:
             print(f"warning: {out.name} not built:\n{log[-2000:]}", file=sys.stderr)
             continue
         made.append(out)
