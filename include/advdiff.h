@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define ADV_ABI_VERSION 1
+#define ADV_ABI_VERSION 2
 
 typedef enum adv_status {
   ADV_OK = 0,
@@ -86,6 +86,15 @@ typedef struct adv_heat_desc {
   int32_t zero_boundary; /* 0 or 1 */
   double kx, ky, kz;     /* per-axis coefficients (kz ignored in 2D) */
   double dt;
+  /* FP64 evaluation form. 0: the reference's operand order, every operation rounded on its own
+   * (bit-exact with the reference's kernels built without contraction); 1: the fused
+   * multiply-add pattern the FP32 state always uses (per axis O2 fma(-2, c, p1) + m1, O4
+   * fma(16, far1, fma(-30, c, fma(16, near1, -near2))) - far2; L = fma(kz, Sz, fma(ky, Sy,
+   * kx Sx)); stages fma(dt, L, un) | fma(0.25, fma(dt, L, uin), 0.75 un) | fma(2, fma(dt, L,
+   * uin), un) / 3): six fewer FP64 operations per node on the O2 stencil, a few ulps from form
+   * 0. Ignored for FP32. */
+  int32_t contract;
+  int32_t pad0;
 } adv_heat_desc;
 
 /* u_in and u_out must not alias; u_n may alias u_out (it is read at the written node only). */

@@ -27,7 +27,8 @@ class HeatDesc(C.Structure):
     """adv_heat_desc (include/advdiff.h)."""
     _fields_ = [("ndim", C.c_int32), ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32),
                 ("dtype", C.c_int32), ("order", C.c_int32), ("frozen", C.c_int32), ("zero_boundary", C.c_int32),
-                ("kx", C.c_double), ("ky", C.c_double), ("kz", C.c_double), ("dt", C.c_double)]
+                ("kx", C.c_double), ("ky", C.c_double), ("kz", C.c_double), ("dt", C.c_double),
+                ("contract", C.c_int32), ("pad0", C.c_int32)]
 
 
 class BurgersDesc(C.Structure):

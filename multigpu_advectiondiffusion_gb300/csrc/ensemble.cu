@@ -289,6 +289,8 @@ adv_status create_impl(const adv_heat_member* heat, int n_heat, int scheme, cons
     if (!m.u || !m.work) return set_error(ADV_ERR_INVALID_ARG, "ensemble: null heat buffer");
     if (m.desc.dtype != heat[0].desc.dtype || m.desc.order != heat[0].desc.order)
       return set_error(ADV_ERR_INVALID_ARG, "ensemble: heat members must share dtype and order");
+    if (m.desc.dtype == ADV_F64 && m.desc.contract)
+      return set_error(ADV_ERR_UNSUPPORTED, "ensemble: FP64 heat members take the reference's rounding (contract 0)");
   }
   for (int i = 0; i < n_burgers; ++i) {
     const adv_burgers_member& m = burgers[i];

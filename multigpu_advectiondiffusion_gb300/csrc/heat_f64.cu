@@ -3,10 +3,11 @@
 
 namespace adv {
 
-// Kernel for (order, ndim, TMA or cp.async loads, stage specialisation).
-void* heat_kernel_f64(int order, int ndim, bool tma, int stage_kind, int rows, int warps, int lanes) {
-  if (rows != 2 || warps != 8 || lanes != 32) return nullptr;
-#define HK(O, N, M, S) reinterpret_cast<void*>(&heat_stage_kernel<double, O, N, M, S>)
+// Kernel for (order, ndim, TMA or cp.async loads, stage specialisation, the reference's rounding
+// or the fused multiply-add form).
+template <bool CT>
+static void* heat_kernel_f64_t(int order, int ndim, bool tma, int stage_kind) {
+#define HK(O, N, M, S) reinterpret_cast<void*>(&heat_stage_kernel<double, O, N, M, S, 2, 8, 32, CT>)
 #define HS(O, N, M)                                            \
   switch (stage_kind) {                                        \
     case 1: return HK(O, N, M, 1);                             \
@@ -21,6 +22,12 @@ void* heat_kernel_f64(int order, int ndim, bool tma, int stage_kind, int rows, i
 #undef HS
 #undef HK
   return nullptr;
+}
+
+void* heat_kernel_f64(int order, int ndim, bool tma, int stage_kind, int rows, int warps, int lanes, bool contract) {
+  if (rows != 2 || warps != 8 || lanes != 32) return nullptr;
+  return contract ? heat_kernel_f64_t<true>(order, ndim, tma, stage_kind)
+                  : heat_kernel_f64_t<false>(order, ndim, tma, stage_kind);
 }
 
 }  // namespace adv

@@ -8,7 +8,7 @@
 namespace adv {
 
 void* heat_kernel_f32(int order, int ndim, bool tma, int stage_kind, int rows, int warps, int lanes);
-void* heat_kernel_f64(int order, int ndim, bool tma, int stage_kind, int rows, int warps, int lanes);
+void* heat_kernel_f64(int order, int ndim, bool tma, int stage_kind, int rows, int warps, int lanes, bool contract);
 
 adv_status heat_validate(const adv_heat_desc* d) {
   if (!d) return set_error(ADV_ERR_INVALID_ARG, "heat: null descriptor");
@@ -21,6 +21,7 @@ adv_status heat_validate(const adv_heat_desc* d) {
   if (d->frozen < d->order / 2)
     return set_error(ADV_ERR_INVALID_ARG, "heat: frozen layers must cover the stencil radius");
   if ((int64_t)d->nx * d->ny * nzv > (int64_t)1 << 40) return set_error(ADV_ERR_INVALID_ARG, "heat: grid too large");
+  if (d->contract != 0 && d->contract != 1) return set_error(ADV_ERR_INVALID_ARG, "heat: contract must be 0 or 1");
   if (d->nx > (1 << 30) || d->ny > (1 << 30) || nzv > (1 << 30))
     return set_error(ADV_ERR_INVALID_ARG, "heat: dimension too large");
   return ADV_OK;
@@ -28,9 +29,10 @@ adv_status heat_validate(const adv_heat_desc* d) {
 
 namespace {
 
-void* pick_kernel(int dtype, int order, int ndim, bool tma, int stage_kind, const HeatLaunch& L) {
-  return dtype == ADV_F32 ? heat_kernel_f32(order, ndim, tma, stage_kind, L.rows, L.warps, L.lanes)
-                          : heat_kernel_f64(order, ndim, tma, stage_kind, L.rows, L.warps, L.lanes);
+void* pick_kernel(const adv_heat_desc& d, bool tma, int stage_kind, const HeatLaunch& L) {
+  return d.dtype == ADV_F32 ? heat_kernel_f32(d.order, d.ndim, tma, stage_kind, L.rows, L.warps, L.lanes)
+                            : heat_kernel_f64(d.order, d.ndim, tma, stage_kind, L.rows, L.warps, L.lanes,
+                                              d.contract != 0);
 }
 
 template <class T, int ORDER, int NDIM, int ROWS, int WARPS = 8, int LANES = 32>
@@ -51,7 +53,9 @@ void tile_for(int dtype, int order, int ndim, int rows, int lanes, int* bx, int*
 
 }  // namespace
 
-int heat_tune_variant(const adv_heat_desc& d) { return d.dtype * 100 + d.order * 10 + d.ndim; }
+int heat_tune_variant(const adv_heat_desc& d) {
+  return (d.dtype == ADV_F64 && d.contract ? 1000 : 0) + d.dtype * 100 + d.order * 10 + d.ndim;
+}
 
 // Fraction of a row's lanes that hold grid nodes when rows of nx nodes are cut into tiles bx wide.
 static double tile_use(int nx, int bx) { return (double)nx / ((double)((nx + bx - 1) / bx) * bx); }
@@ -80,11 +84,11 @@ adv_status heat_prepare(const adv_heat_desc& d, const void* u_in, HeatLaunch* L,
   L->block = dim3((unsigned)L->lanes, (unsigned)(32 * L->warps / L->lanes), 1);
   const int tiles_x = (d.nx + bx - 1) / bx, tiles_y = (d.ny + by - 1) / by;
   for (int sk = 0; sk <= 3; ++sk) {
-    void* k = pick_kernel(d.dtype, d.order, d.ndim, L->tma, sk, *L);
+    void* k = pick_kernel(d, L->tma, sk, *L);
     if (!k) return set_error(ADV_ERR_UNSUPPORTED, "heat: no kernel for this configuration");
     ADV_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   }
-  void* k0 = pick_kernel(d.dtype, d.order, d.ndim, L->tma, 1, *L);
+  void* k0 = pick_kernel(d, L->tma, 1, *L);
   int occ = 0;
   ADV_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k0, 32 * L->warps, smem));
   occ = std::max(occ, 1);
@@ -181,7 +185,7 @@ static adv_status heat_launch_t(const adv_heat_desc& d, const HeatLaunch& L, int
                                 const void* u_n, void* u_out, cudaStream_t s) {
   HeatParams<T> p = heat_params<T>(d, L, stage, u_in, u_n, u_out);
   const int stage_kind = (stage == 1 && u_n != u_in) ? 0 : stage;
-  void* k = pick_kernel(d.dtype, d.order, d.ndim, L.tma, stage_kind, L);
+  void* k = pick_kernel(d, L.tma, stage_kind, L);
   void* args[] = {const_cast<CUtensorMap*>(&L.tmap_in), &p};
   ADV_CUDA_TRY(cudaLaunchKernel(k, L.grid, L.block, args, L.smem, s));
   count_launches(1);

@@ -185,13 +185,16 @@ __device__ __forceinline__ int* heat_abort_flag() {
 // 0 = stage taken at run time with a separate u_n. Returns the pipeline state for the next
 // segment (by value, so it stays in registers), with s_issue = -1 if a wait timed out (the CTA
 // must then return).
-template <class T, int ORDER, int NDIM, bool TMA, int STAGE, int ROWS = 2, int WARPS = 8, int LANES = 32>
+template <class T, int ORDER, int NDIM, bool TMA, int STAGE, int ROWS = 2, int WARPS = 8, int LANES = 32,
+          bool CONTRACT = false>
 __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const HeatParams<T>& p, int x0, int y0, int zs,
                                              int ze, HeatPipe pipe) {
   using C = HeatTile<T, ORDER, NDIM, ROWS, WARPS, LANES>;
   constexpr int RY = C::RY;
   using V = typename Vec16<T>::type;
-  constexpr bool FAST = sizeof(T) == 4;
+  // FP32 always, FP64 on request: the fused multiply-add pattern instead of the reference's
+  // separately rounded operations
+  constexpr bool FAST = sizeof(T) == 4 || CONTRACT;
   constexpr int R = C::R, RZ = C::RZ, VX = C::VX, SW = C::SW;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   T* ring = reinterpret_cast<T*>(smem_raw);
@@ -354,7 +357,7 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
       // Every lane evaluates the stencil (halo values outside the grid are finite zero fill);
       // nodes that are not updated are fixed up afterwards with warp-uniform branches.
       T res[RY][VX];
-      if constexpr (FAST && ORDER == 2) {
+      if constexpr (sizeof(T) == 4 && ORDER == 2) {
         // FP32 O2: node pairs (e, e+1) in paired instructions, the same operations lane by lane
         // (the O4 stencil stays scalar: paired it needs more registers than its occupancy allows)
         static_assert(VX % 2 == 0, "node pairs");
@@ -512,7 +515,8 @@ constexpr int heat_min_ctas() {
   return ROWS > 2 ? 16 / WARPS : (ORDER == 2 ? 4 : (sizeof(T) == 4 ? 3 : 2));
 }
 
-template <class T, int ORDER, int NDIM, bool TMA, int STAGE, int ROWS = 2, int WARPS = 8, int LANES = 32>
+template <class T, int ORDER, int NDIM, bool TMA, int STAGE, int ROWS = 2, int WARPS = 8, int LANES = 32,
+          bool CONTRACT = false>
 __global__ void __launch_bounds__(32 * WARPS, heat_min_ctas<T, ORDER, ROWS, WARPS>())
 heat_stage_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ HeatParams<T> p) {
   using C = HeatTile<T, ORDER, NDIM, ROWS, WARPS, LANES>;
@@ -539,7 +543,7 @@ heat_stage_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constan
     const int ze = (int)min((int64_t)p.nz, zs + (seg_b - pos));
     pos += ze - zs;
     const int x0 = (int)(tile % p.tiles_x) * C::BX, y0 = (int)(tile / p.tiles_x) * C::BY;
-    pipe = heat_segment<T, ORDER, NDIM, TMA, STAGE, ROWS, WARPS, LANES>(&tmap, p, x0, y0, zs, ze, pipe);
+    pipe = heat_segment<T, ORDER, NDIM, TMA, STAGE, ROWS, WARPS, LANES, CONTRACT>(&tmap, p, x0, y0, zs, ze, pipe);
     if (pipe.s_issue < 0) return;
   }
 }

@@ -83,6 +83,7 @@ class HeatConfig:
     kz: float = 0.0
     dt: float = 0.0
     time: int = N.ADV_SSPRK3
+    contract: bool = False  # FP64 only: the fused multiply-add form instead of the reference's rounding
 
     @classmethod
     def reference_3d(cls, C: float, L: int, W: int, H: int, nx: int, ny: int, nz: int) -> "HeatConfig":
@@ -112,7 +113,8 @@ class HeatConfig:
 
     def desc(self, dtype: int) -> N.HeatDesc:
         return N.HeatDesc(self.ndim, self.nx, self.ny, self.nz if self.ndim == 3 else 1, dtype, self.order,
-                          self.frozen, int(self.zero_boundary), self.kx, self.ky, self.kz, self.dt)
+                          self.frozen, int(self.zero_boundary), self.kx, self.ky, self.kz, self.dt,
+                          int(self.contract), 0)
 
     @property
     def numel(self) -> int:

@@ -146,16 +146,17 @@ void heat_stage(const HeatCfg& c, int stage, const T* uin, const T* un, T* out) 
       }
 }
 
-// FP32 evaluation order of the GPU path (fused multiply-adds in a fixed pattern; see the
-// product's heat_stage.cuh). Mathematically the same stencil and stage update as heat_stage();
-// used to check the FP32 kernels bit for bit.
+// The GPU path's fused multiply-add evaluation order (FP32 always, FP64 with the descriptor's
+// `contract`; see the product's heat_stage.cuh). Mathematically the same stencil and stage update
+// as heat_stage(); used to check those kernels bit for bit.
 //   O2 per axis: fma(-2, c, p1) + m1;  O4 per axis: fma(16, far1, fma(-30, c, fma(16, near1,
 //   -near2))) - far2 with near = +1 in 3D and -1 in 2D;  L = fma(kz, Sz, fma(ky, Sy, kx*Sx));
 //   stages: fma(dt, L, un) | fma(0.25, fma(dt, L, uin), 0.75*un) | fma(2, fma(dt, L, uin), un)/3.
-void heat_stage_fma32(const HeatCfg& c, int stage, const float* uin, const float* un, float* out) {
+template <class T>
+void heat_stage_fma(const HeatCfg& c, int stage, const T* uin, const T* un, T* out) {
   const int64_t nx = c.nx, ny = c.ny, nz = (c.ndim == 3) ? c.nz : 1;
   const int64_t sz = nx * ny;
-  const float kx = (float)c.kx, ky = (float)c.ky, kz = (float)c.kz, dt = (float)c.dt;
+  const T kx = (T)c.kx, ky = (T)c.ky, kz = (T)c.kz, dt = (T)c.dt;
   const int F = c.frozen;
 #pragma omp parallel for collapse(2) schedule(static)
   for (int64_t k = 0; k < nz; ++k)
@@ -167,39 +168,40 @@ void heat_stage_fma32(const HeatCfg& c, int stage, const float* uin, const float
         if (!interior) {
           bool outer = i == 0 || i == nx - 1 || j == 0 || j == ny - 1;
           if (c.ndim == 3) outer = outer || k == 0 || k == nz - 1;
-          out[o] = (c.zero_boundary && outer) ? 0.0f : uin[o];
+          out[o] = (c.zero_boundary && outer) ? T(0) : uin[o];
           continue;
         }
-        const float ce = uin[o];
-        auto axis = [&](int64_t s) -> float {
-          const float p1 = uin[o + s], m1 = uin[o - s];
-          if (c.order == 2) return std::fma(-2.0f, ce, p1) + m1;
-          const float p2 = uin[o + 2 * s], m2 = uin[o - 2 * s];
+        const T ce = uin[o];
+        auto axis = [&](int64_t s) -> T {
+          const T p1 = uin[o + s], m1 = uin[o - s];
+          if (c.order == 2) return std::fma(T(-2), ce, p1) + m1;
+          const T p2 = uin[o + 2 * s], m2 = uin[o - 2 * s];
           const bool plus_first = c.ndim == 3;
-          const float a1 = plus_first ? p1 : m1, a2 = plus_first ? p2 : m2;
-          const float b1 = plus_first ? m1 : p1, b2 = plus_first ? m2 : p2;
-          return std::fma(16.0f, b1, std::fma(-30.0f, ce, std::fma(16.0f, a1, -a2))) - b2;
+          const T a1 = plus_first ? p1 : m1, a2 = plus_first ? p2 : m2;
+          const T b1 = plus_first ? m1 : p1, b2 = plus_first ? m2 : p2;
+          return std::fma(T(16), b1, std::fma(T(-30), ce, std::fma(T(16), a1, -a2))) - b2;
         };
-        float L = std::fma(ky, axis(nx), kx * axis(1));
+        T L = std::fma(ky, axis(nx), kx * axis(1));
         if (c.ndim == 3) L = std::fma(kz, axis(sz), L);
-        float v;
-        if (stage == 2) v = std::fma(0.25f, std::fma(dt, L, ce), 0.75f * un[o]);
-        else if (stage == 3) v = std::fma(2.0f, std::fma(dt, L, ce), un[o]) / 3.0f;
+        T v;
+        if (stage == 2) v = std::fma(T(0.25), std::fma(dt, L, ce), T(0.75) * un[o]);
+        else if (stage == 3) v = std::fma(T(2), std::fma(dt, L, ce), un[o]) / T(3);
         else v = std::fma(dt, L, un[o]);
         out[o] = v;
       }
 }
 
-void heat_run_fma32(const HeatCfg& c, int time, int64_t nsteps, float* u) {
+template <class T>
+void heat_run_fma(const HeatCfg& c, int time, int64_t nsteps, T* u) {
   const size_t n = (size_t)c.nx * c.ny * (c.ndim == 3 ? c.nz : 1);
-  std::vector<float> a(n), b(n);
+  std::vector<T> a(n), b(n);
   for (int64_t s = 0; s < nsteps; ++s) {
-    heat_stage_fma32(c, 1, u, u, a.data());
+    heat_stage_fma<T>(c, 1, u, u, a.data());
     if (time != 0) {
-      heat_stage_fma32(c, 2, a.data(), u, b.data());
-      heat_stage_fma32(c, 3, b.data(), u, a.data());
+      heat_stage_fma<T>(c, 2, a.data(), u, b.data());
+      heat_stage_fma<T>(c, 3, b.data(), u, a.data());
     }
-    std::memcpy(u, a.data(), n * sizeof(float));
+    std::memcpy(u, a.data(), n * sizeof(T));
   }
 }
 
@@ -875,12 +877,22 @@ void orc_heat_run_f32(int ndim, int nx, int ny, int nz, int order, int frozen, i
 void orc_heat_stage_f32_fma(int ndim, int nx, int ny, int nz, int order, int frozen, int zero_boundary,
                             int periodic, double kx, double ky, double kz, double dt, int stage,
                             const float* uin, const float* un, float* out) {
-  HEAT_CFG heat_stage_fma32(c, stage, uin, un, out);
+  HEAT_CFG heat_stage_fma<float>(c, stage, uin, un, out);
 }
 void orc_heat_run_f32_fma(int ndim, int nx, int ny, int nz, int order, int frozen, int zero_boundary,
                           int periodic, double kx, double ky, double kz, double dt, int time,
                           int64_t nsteps, float* u) {
-  HEAT_CFG heat_run_fma32(c, time, nsteps, u);
+  HEAT_CFG heat_run_fma<float>(c, time, nsteps, u);
+}
+void orc_heat_stage_f64_fma(int ndim, int nx, int ny, int nz, int order, int frozen, int zero_boundary,
+                            int periodic, double kx, double ky, double kz, double dt, int stage,
+                            const double* uin, const double* un, double* out) {
+  HEAT_CFG heat_stage_fma<double>(c, stage, uin, un, out);
+}
+void orc_heat_run_f64_fma(int ndim, int nx, int ny, int nz, int order, int frozen, int zero_boundary,
+                          int periodic, double kx, double ky, double kz, double dt, int time,
+                          int64_t nsteps, double* u) {
+  HEAT_CFG heat_run_fma<double>(c, time, nsteps, u);
 }
 
 // Reference heat dt and final time (SingleGPU/Diffusion3d_baselineCode/main.cpp:55-63,

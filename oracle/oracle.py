@@ -46,6 +46,8 @@ def lib() -> C.CDLL:
             "orc_heat_run_f32": (None, _HEAT + [_I, _I64, C.c_void_p]),
             "orc_heat_stage_f32_fma": (None, _HEAT + [_I, C.c_void_p, C.c_void_p, C.c_void_p]),
             "orc_heat_run_f32_fma": (None, _HEAT + [_I, _I64, C.c_void_p]),
+            "orc_heat_stage_f64_fma": (None, _HEAT + [_I, C.c_void_p, C.c_void_p, C.c_void_p]),
+            "orc_heat_run_f64_fma": (None, _HEAT + [_I, _I64, C.c_void_p]),
             "orc_heat_ref_constants": (None, [_I, _D, _I, _I, _I, _I, _I, _I, _I] + [_PD] * 8),
             "orc_ic_heat_ref": (None, [_I, _I, _I, _I, _D, _D, _D, C.c_void_p]),
             "orc_heat_accuracy": (_I, [_I, _I, _D, _D, _PD, _PD, _PD]),
@@ -99,10 +101,11 @@ def _heat_args(ndim, nx, ny, nz, order, frozen, zero_boundary, periodic, kx, ky,
 def heat_stage(cfg, stage: int, uin: np.ndarray, un: np.ndarray, periodic: bool = False,
                fp32_order: str = "gpu") -> np.ndarray:
     """One stage with the scheme of a solvers.HeatConfig-like object (ndim, nx.., order, ...).
-    FP32 inputs use the GPU path's fused-multiply-add order unless fp32_order == "reference"."""
+    FP32 inputs use the GPU path's fused-multiply-add order unless fp32_order == "reference"; FP64
+    inputs use it when the configuration asks for the contracted form (cfg.contract)."""
     out = np.empty_like(uin)
     if uin.dtype == np.float64:
-        f = lib().orc_heat_stage_f64
+        f = lib().orc_heat_stage_f64_fma if getattr(cfg, "contract", False) else lib().orc_heat_stage_f64
     else:
         f = lib().orc_heat_stage_f32 if fp32_order == "reference" else lib().orc_heat_stage_f32_fma
     f(*_heat_args(cfg.ndim, cfg.nx, cfg.ny, cfg.nz, cfg.order, cfg.frozen, cfg.zero_boundary, periodic,
@@ -113,7 +116,7 @@ def heat_stage(cfg, stage: int, uin: np.ndarray, un: np.ndarray, periodic: bool 
 def heat_run(cfg, u: np.ndarray, nsteps: int, time: int, fp32_order: str = "gpu") -> np.ndarray:
     u = np.ascontiguousarray(u).copy()
     if u.dtype == np.float64:
-        f = lib().orc_heat_run_f64
+        f = lib().orc_heat_run_f64_fma if getattr(cfg, "contract", False) else lib().orc_heat_run_f64
     else:
         f = lib().orc_heat_run_f32 if fp32_order == "reference" else lib().orc_heat_run_f32_fma
     f(*_heat_args(cfg.ndim, cfg.nx, cfg.ny, cfg.nz, cfg.order, cfg.frozen, cfg.zero_boundary, False,

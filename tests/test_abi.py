@@ -50,7 +50,7 @@ def test_compat_exports_reference_names(native, lib, header, names, pitched):
 
 
 def test_abi_version_and_strings(native):
-    assert native.adv_abi_version() == 1
+    assert native.adv_abi_version() == 2
     assert native.adv_status_string(N.ADV_ERR_TIMEOUT) == b"ADV_ERR_TIMEOUT"
 
 
@@ -189,7 +189,7 @@ def test_c_host_links_and_calls_the_library(native, tmp_path):
 int main(int argc, char** argv) {
   enum { NX = 9, NY = 8, NZ = 7, N = NX * NY * NZ };
   double u[N], back[N];
-  if (adv_abi_version() != 1) return 2;
+  if (adv_abi_version() != ADV_ABI_VERSION) return 2;
   if (adv_ic_heat_ref(3, NX, NY, NZ, 0.5, 0.5, 0.5, u) != ADV_OK) return 3;
   if (adv_write_result_bin(argv[1], ADV_F64, u, N) != ADV_OK) return 4;
   if (adv_read_result_bin(argv[1], N, back) != ADV_OK) return 5;
