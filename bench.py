@@ -730,6 +730,23 @@ def run_reference_arm(args, world, rank):
                 secs.append(dt_)
         sample = "48^3 FP64 WENO5-Z local LF periodic, 2 steps forward + adjoint per step (oracle)"
         config = adjoint_config(world)
+    elif args.workload == "weno7":
+        # the oracle's restatement of the prototype loop (FP64, OpenMP over lines) on a 96^3 sample,
+        # one LSRK(5,4) step per benchmark step
+        n = 96
+        _, u0 = weno7_case(n)
+        u0 = u0.reshape(n, n, n)
+        h = 2.0 / (n - 1)
+        rates, secs = [], []
+        for i in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            _, _, it = oracle.proto_run(7, u0, [h, h, h], 0.4, 1e9, max_steps=1)
+            dt = time.perf_counter() - t0
+            if i >= args.warmup:
+                rates.append(n ** 3 * 5 * it / dt / 1e9)
+                secs.append(dt)
+        sample = "96^3 FP64 WENO7 prototype scheme, 1 LSRK(5,4) step per step (oracle)"
+        config = weno7_config(world)
     else:
         # the ensemble: per step, two heat instances for 4 steps and one Burgers instance for one
         # RK3 step, in proportion to the ensemble's heat / Burgers cell updates
@@ -762,6 +779,102 @@ def run_reference_arm(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+WENO7_N, WENO7_STEPS = 256, 10
+
+
+def weno7_case(n: int = WENO7_N):
+    """The WENO7 prototype's problem (LFWENO7FDM3d.m): u0 = exp(-(x^2+y^2+z^2)/0.1) on the node grid
+    of [-1,1]^3, CFL 0.4, here at n^3 FP32; (config, u0)."""
+    from multigpu_advectiondiffusion_gb300.solvers import Weno7Config
+    x = np.linspace(-1.0, 1.0, n)
+    h = 2.0 / (n - 1)
+    u0 = np.exp(-(x[None, None, :] ** 2 + x[None, :, None] ** 2 + x[:, None, None] ** 2) / 0.1).ravel()
+    return Weno7Config(n, n, n, h, h, h), u0
+
+
+def weno7_config(world: int) -> dict:
+    return {"workload": f"weno7 {WENO7_N}^3 f32 (prototype scheme: local LF, clamped ends, LSRK(5,4)), gaussian, "
+                        f"cfl 0.4 x {WENO7_STEPS} steps",
+            "parallelism": f"replicas{world}",
+            "l2": "per stage 4 sweeps of 64 MiB arrays > 126 MiB L2; 252 MiB L2 flush between GPU steps"}
+
+
+def bench_weno7(args, world, rank, dev, stream, flush, lib):
+    """The WENO7 prototype solver at 256^3 FP32: one benchmark step = 10 LSRK(5,4) time steps (50
+    stages) through adv_weno7_run; rel-L2 of a 0.05-time-unit run against the same run in FP64."""
+    import torch
+    from multigpu_advectiondiffusion_gb300.solvers import weno7_run, weno7_workspace
+    cfg, u0n = weno7_case()
+    u0 = torch.from_numpy(u0n.astype(np.float32)).to(dev)
+    u = u0.clone()
+    ws = weno7_workspace(cfg, u)
+    sh = stream.cuda_stream
+    S = WENO7_STEPS
+
+    def one_step():
+        weno7_run(cfg, u, 1e9, 0.4, max_steps=S, workspace=ws, stream=sh)
+
+    def timed(fn, K):
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(K):
+            with torch.cuda.stream(stream):
+                flush.fill_(1.0)
+            fn()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        return ev0.elapsed_time(ev1)
+
+    for _ in range(args.warmup):
+        u.copy_(u0)
+        one_step()
+    uuid = None
+    try:
+        uuid = "GPU-" + str(torch.cuda.get_device_properties(dev).uuid)
+    except Exception:
+        pass
+    u.copy_(u0)
+    with ClockSampler(uuid) as clk:
+        launches0 = lib.adv_kernel_launch_count()
+        ms = timed(one_step, args.steps)
+        launched = lib.adv_kernel_launch_count() - launches0
+    ms_max = max_over_ranks(ms, dev)
+    work = cfg.numel * 5 * S
+    value = replica_throughput(work * args.steps, ms_max, world)
+    # accuracy: FP32 vs FP64 over a short run from the initial state
+    a32 = u0.clone()
+    a64 = torch.from_numpy(u0n).to(dev)
+    t32, it32 = weno7_run(cfg, a32, 0.05, 0.4, stream=sh)
+    t64, it64 = weno7_run(cfg, a64, 0.05, 0.4, stream=sh)
+    rel = (torch.linalg.vector_norm(a32.double() - a64) / torch.linalg.vector_norm(a64)).item()
+    host_in = u0.cpu().pin_memory()
+    host_out = torch.empty_like(host_in).pin_memory()
+
+    def e2e_step():
+        with torch.cuda.stream(stream):
+            u.copy_(host_in, non_blocking=True)
+        one_step()
+        with torch.cuda.stream(stream):
+            host_out.copy_(u, non_blocking=True)
+    e2e_step()
+    ems = max_over_ranks(timed(e2e_step, args.steps), dev)
+    nbytes = u.numel() * u.element_size()
+    if rank == 0:
+        line = {
+            "metric": "Gcell-updates/s/RK-stage", "value": value, "unit": "Gcell-updates/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (the prototype's Gaussian initial state)", "config": weno7_config(world),
+            "roofline": None, "cpu_baseline": None,
+            "e2e": {"value": replica_throughput(work * args.steps, ems, world), "unit": "Gcell-updates/s",
+                    "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
+            "gpu_launches": int(launched), "clocks": clk.summary(),
+            "rel_l2_vs_fp64": rel, "rel_l2_vs_fp64_after": f"t = 0.05: {it32} FP32 steps, {it64} FP64 steps",
+        }
+        print(json.dumps(line), flush=True)
+
+
 def burgers_workload(args) -> str:
     return (f"burgers3d 256^3 f32 weno5-{args.weno} global-lf periodic cfl 0.4 x 20 steps, "
             f"div {args.div}")
@@ -785,7 +898,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="heat3d", choices=["heat3d", "heat2d", "burgers3d", "ensemble", "adjoint"])
+    ap.add_argument("--workload", default="heat3d",
+                    choices=["heat3d", "heat2d", "burgers3d", "weno7", "ensemble", "adjoint"])
     ap.add_argument("--cpu-budget", type=float, default=10.0, help="seconds of CPU-baseline work")
     ap.add_argument("--div", default="f32", choices=["fast", "f32", "f64"],
                     help="Burgers WENO weight division (FP32 state): f32 = IEEE FP32, equal bit for bit to the "
@@ -826,9 +940,11 @@ def main():
     sh = stream.cuda_stream
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
 
-    if args.workload in ("ensemble", "adjoint"):
+    if args.workload in ("ensemble", "adjoint", "weno7"):
         if args.workload == "ensemble":
             bench_ensemble(args, world, rank, dev, stream, flush, lib)
+        elif args.workload == "weno7":
+            bench_weno7(args, world, rank, dev, stream, flush, lib)
         else:
             bench_adjoint(args, world, rank, dev, lib)
         if world > 1:

@@ -254,13 +254,19 @@ adv_status adv_heatk_adjoint_step(const adv_heatk_desc* d, const void* k, const 
  * (interval arrays) and sweeps the adjoint through it. Sizes in bytes. */
 adv_status adv_heatk_checkpoint_bytes(const adv_heatk_desc* d, int64_t nsteps, int64_t interval,
                                       size_t* ckpt_bytes, size_t* work_bytes);
-/* nsteps steps in place on u; ckpt may be NULL (no checkpoints kept). */
+/* nsteps steps in place on u; ckpt may be NULL (no checkpoints kept). With checkpoints, the run
+ * also leaves the states of its last checkpoint interval (u^{n0+1} .. u^{nsteps-1}) in work, where
+ * adv_heatk_backward would recompute them. */
 adv_status adv_heatk_forward(const adv_heatk_desc* d, const void* k, void* u, int64_t nsteps,
                              int64_t interval, void* ckpt, void* work, void* stream);
-/* lam: in dJ/du at step nsteps, out dJ/du at step 0. grad_k += dJ/dk. */
+/* lam: in dJ/du at step nsteps, out dJ/du at step 0. grad_k += dJ/dk. flags:
+ * ADV_HEATK_LAST_INTERVAL_IN_WORK when work still holds what adv_heatk_forward left there (the
+ * same nsteps, interval and ckpt, nothing written to work since): the last interval is then not
+ * recomputed. */
+#define ADV_HEATK_LAST_INTERVAL_IN_WORK 1
 adv_status adv_heatk_backward(const adv_heatk_desc* d, const void* k, int64_t nsteps,
                               int64_t interval, const void* ckpt, void* lam, void* grad_k,
-                              void* work, void* stream);
+                              void* work, int flags, void* stream);
 
 /* --------------------------------------------------------------- Burgers discrete adjoint
  * Exact transpose of the fixed-dt SSP-RK3 step of the periodic, local Lax-Friedrichs, inviscid

@@ -21,6 +21,7 @@ ADV_BC_FROZEN, ADV_BC_PERIODIC = 0, 1
 ADV_DIV_F32, ADV_DIV_F64, ADV_DIV_FAST = 0, 1, 2
 ADV_DT_FIXED, ADV_DT_MAXU = 0, 1
 ADV_ENSEMBLE_DIRECT = 1
+ADV_HEATK_LAST_INTERVAL_IN_WORK = 1
 
 
 class HeatDesc(C.Structure):
@@ -100,7 +101,7 @@ SIGNATURES = [
     ("adv_heatk_checkpoint_bytes", _I, [C.POINTER(HeatKDesc), _I64, _I64, C.POINTER(C.c_size_t),
                                         C.POINTER(C.c_size_t)]),
     ("adv_heatk_forward", _I, [C.POINTER(HeatKDesc), _VP, _VP, _I64, _I64, _VP, _VP, _VP]),
-    ("adv_heatk_backward", _I, [C.POINTER(HeatKDesc), _VP, _I64, _I64, _VP, _VP, _VP, _VP, _VP]),
+    ("adv_heatk_backward", _I, [C.POINTER(HeatKDesc), _VP, _I64, _I64, _VP, _VP, _VP, _VP, _I, _VP]),
     ("adv_burgers_adjoint_step", _I, [C.POINTER(BurgersDesc), _VP, _VP, _VP, _D, _VP, _VP, _VP]),
     ("adv_burgers_checkpoint_bytes", _I, [C.POINTER(BurgersDesc), _I64, _I64, C.POINTER(C.c_size_t),
                                           C.POINTER(C.c_size_t)]),

@@ -479,23 +479,40 @@ adv_status adv_heatk_forward(const adv_heatk_desc* d, const void* k, void* u, in
   const size_t nb = (size_t)d->nx * d->ny * d->nz * (d->dtype == ADV_F32 ? 4 : 8);
   char* a = static_cast<char*>(u);
   char* b = static_cast<char*>(work);
-  for (int64_t n = 0; n < nsteps; ++n) {
+  // With checkpoints, the last interval runs from its checkpoint through work's slots (the states
+  // u^{n0+1} .. u^{nsteps-1}, where adv_heatk_backward would recompute them) into u.
+  const int64_t m = (nsteps + interval - 1) / interval;
+  const int64_t n_last = ckpt && nsteps > 0 ? (m - 1) * interval : nsteps;
+  for (int64_t n = 0; n < n_last; ++n) {
     if (ckpt && n % interval == 0)
       ADV_CUDA_TRY(cudaMemcpyAsync(static_cast<char*>(ckpt) + (n / interval) * one, a, nb, cudaMemcpyDeviceToDevice, s));
     if ((st = heatk_step_launch(*d, k, a, b, s)) != ADV_OK) return st;
     std::swap(a, b);
   }
-  if (a != static_cast<char*>(u)) ADV_CUDA_TRY(cudaMemcpyAsync(u, a, nb, cudaMemcpyDeviceToDevice, s));
+  if (n_last < nsteps) {
+    char* c = static_cast<char*>(ckpt) + (m - 1) * one;
+    ADV_CUDA_TRY(cudaMemcpyAsync(c, a, nb, cudaMemcpyDeviceToDevice, s));
+    const char* src = c;
+    char* states = static_cast<char*>(work);
+    for (int64_t n = n_last; n < nsteps; ++n) {
+      char* dst = n + 1 < nsteps ? states + (n - n_last) * one : static_cast<char*>(u);
+      if ((st = heatk_step_launch(*d, k, src, dst, s)) != ADV_OK) return st;
+      src = dst;
+    }
+  } else if (a != static_cast<char*>(u)) {
+    ADV_CUDA_TRY(cudaMemcpyAsync(u, a, nb, cudaMemcpyDeviceToDevice, s));
+  }
   return ADV_OK;
 }
 
 adv_status adv_heatk_backward(const adv_heatk_desc* d, const void* k, int64_t nsteps, int64_t interval,
-                              const void* ckpt, void* lam, void* grad_k, void* work, void* stream) {
+                              const void* ckpt, void* lam, void* grad_k, void* work, int flags, void* stream) {
   ADV_NVTX_RANGE("adv_heatk_backward");
   adv_status st = heatk_validate(d);
   if (st != ADV_OK) return st;
   if (!k || !ckpt || !lam || !grad_k || !work) return set_error(ADV_ERR_INVALID_ARG, "heatk: null buffer");
   if (nsteps < 0 || interval < 1) return set_error(ADV_ERR_INVALID_ARG, "heatk: bad nsteps/interval");
+  if (flags & ~ADV_HEATK_LAST_INTERVAL_IN_WORK) return set_error(ADV_ERR_INVALID_ARG, "heatk: unknown flags");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const size_t one = array_bytes(*d);
   const size_t nb = (size_t)d->nx * d->ny * d->nz * (d->dtype == ADV_F32 ? 4 : 8);
@@ -508,7 +525,8 @@ adv_status adv_heatk_backward(const adv_heatk_desc* d, const void* k, int64_t ns
     const int64_t n0 = seg * interval, n1 = std::min(nsteps, n0 + interval);
     const char* base = static_cast<const char*>(ckpt) + seg * one;
     auto state = [&](int64_t n) -> const char* { return n == n0 ? base : states + (n - n0 - 1) * one; };
-    for (int64_t n = n0; n + 1 < n1; ++n)
+    const bool kept = seg == m - 1 && (flags & ADV_HEATK_LAST_INTERVAL_IN_WORK);
+    for (int64_t n = n0; !kept && n + 1 < n1; ++n)
       if ((st = heatk_step_launch(*d, k, state(n), states + (n - n0) * one, s)) != ADV_OK) return st;
     for (int64_t n = n1 - 1; n >= n0; --n) {
       if ((st = heatk_adjoint_launch(*d, k, state(n), la, lb, grad_k, s)) != ADV_OK) return st;

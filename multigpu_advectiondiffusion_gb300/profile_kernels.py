@@ -1,9 +1,12 @@
 """Direct launches of one hot kernel for profilers (ncu): no CUDA graph, no host loop logic.
 
     python -m multigpu_advectiondiffusion_gb300.profile_kernels heat3d   [--n 256] [--launches 6]
+    python -m multigpu_advectiondiffusion_gb300.profile_kernels heat3d2  [--n 256] [--launches 6]
     python -m multigpu_advectiondiffusion_gb300.profile_kernels burgers3d [--n 256] [--launches 4]
 
 heat3d: the 3D O2 forward-Euler stage on an n^3 FP32 grid (ping-pong between two buffers).
+heat3d2: the same problem through adv_heat_run, whose launches each advance two Euler steps
+(2 x launches time steps).
 burgers3d: the periodic WENO5-Z global-Lax-Friedrichs SSP-RK3 stage 1 on an n^3 FP32 grid.
 Inputs are the seeded initial conditions of the benchmark workloads, generated on the host.
 """
@@ -18,7 +21,7 @@ import numpy as np
 
 def main(argv=None) -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("kernel", choices=["heat3d", "burgers3d"])
+    ap.add_argument("kernel", choices=["heat3d", "heat3d2", "burgers3d"])
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--launches", type=int, default=6)
     ap.add_argument("--dtype", default="f32", choices=["f32", "f64"])
@@ -27,13 +30,19 @@ def main(argv=None) -> None:
     import torch
 
     from . import _native as N
-    from .solvers import BurgersConfig, HeatConfig, burgers_stage, heat_stage
+    from .solvers import BurgersConfig, HeatConfig, burgers_stage, heat_run, heat_stage
 
     dev = torch.device("cuda:0")
     lib = N.load()
     npdt = np.float32 if a.dtype == "f32" else np.float64
     n = a.n
-    if a.kernel == "heat3d":
+    if a.kernel == "heat3d2":
+        cfg = HeatConfig.dirichlet_o2(3, n)
+        u0 = np.empty(n ** 3)
+        N.check(lib.adv_ic_heat3d_blobs(n, n, n, 2, 8, u0.ctypes.data_as(N.C.POINTER(N.C.c_double))), "ic")
+        u = torch.from_numpy(u0.astype(npdt)).to(dev)
+        heat_run(cfg, u, 2 * a.launches)
+    elif a.kernel == "heat3d":
         cfg = HeatConfig.dirichlet_o2(3, n)
         u0 = np.empty(n ** 3)
         N.check(lib.adv_ic_heat3d_blobs(n, n, n, 2, 8, u0.ctypes.data_as(N.C.POINTER(N.C.c_double))), "ic")

@@ -383,8 +383,10 @@ def _autograd():
             lam = grad_u.detach().clone().contiguous()
             gk = torch.zeros_like(k)
             d = ctx.cfg.desc(_fields(ctx.cfg.numel, lam, k, gk))
+            # the forward run left its last interval's states in ctx.work, untouched since
             N.check(N.load().adv_heatk_backward(C.byref(d), _ptr(k), int(ctx.nsteps), int(ctx.interval),
                                                 _ptr(ctx.ckpt), _ptr(lam), _ptr(gk), _ptr(ctx.work),
+                                                N.ADV_HEATK_LAST_INTERVAL_IN_WORK,
                                                 N.stream_handle(torch.cuda.current_stream())), "adv_heatk_backward")
             return gk, lam, None, None, None
 

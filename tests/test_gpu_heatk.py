@@ -145,3 +145,38 @@ def test_backward_rejects_bad_interval(cuda, native):
     assert native.adv_heatk_checkpoint_bytes(N.C.byref(d), 10, 4, N.C.byref(cb), N.C.byref(wb)) == N.ADV_OK
     one = (8 * 8 * 8 * 4 + 255) // 256 * 256
     assert cb.value == 3 * one and wb.value == 4 * one
+
+
+@pytest.mark.parametrize("steps,interval", [(10, 4), (12, 4), (7, 7), (9, 1), (1, 3)])
+def test_backward_with_and_without_the_kept_interval(cuda, native, oracle, steps, interval):
+    """adv_heatk_forward leaves its last interval's states in work; the backward run that takes
+    them (ADV_HEATK_LAST_INTERVAL_IN_WORK) and the one that recomputes them (flags 0) give the same
+    bits, for last intervals of every length, and the forward's result is the plain run's."""
+    import torch
+    shape = (24, 20, 18)
+    cfg, k, u0, target = _case(shape, np.float32, 2)
+    d = cfg.desc(N.ADV_F32)
+    cb, wb = N.C.c_size_t(0), N.C.c_size_t(0)
+    assert native.adv_heatk_checkpoint_bytes(N.C.byref(d), steps, interval, N.C.byref(cb), N.C.byref(wb)) == N.ADV_OK
+    kk = _t(k, cuda)
+    res = []
+    for flags in (N.ADV_HEATK_LAST_INTERVAL_IN_WORK, 0):
+        u = _t(u0, cuda)
+        ckpt = torch.empty(cb.value, dtype=torch.uint8, device=cuda)
+        work = torch.empty(wb.value, dtype=torch.uint8, device=cuda)
+        assert native.adv_heatk_forward(N.C.byref(d), kk.data_ptr(), u.data_ptr(), steps, interval, ckpt.data_ptr(),
+                                        work.data_ptr(), None) == N.ADV_OK
+        plain = _t(u0, cuda)
+        w2 = torch.empty_like(plain)
+        assert native.adv_heatk_forward(N.C.byref(d), kk.data_ptr(), plain.data_ptr(), steps, interval, None,
+                                        w2.data_ptr(), None) == N.ADV_OK
+        assert torch.equal(u, plain)
+        lam = u - _t(target, cuda)
+        gk = torch.zeros_like(kk)
+        assert native.adv_heatk_backward(N.C.byref(d), kk.data_ptr(), steps, interval, ckpt.data_ptr(),
+                                         lam.data_ptr(), gk.data_ptr(), work.data_ptr(), flags, None) == N.ADV_OK
+        torch.cuda.synchronize()
+        res.append((lam.cpu().numpy(), gk.cpu().numpy()))
+    assert np.array_equal(res[0][0], res[1][0]) and np.array_equal(res[0][1], res[1][1])
+    assert native.adv_heatk_backward(N.C.byref(d), kk.data_ptr(), steps, interval, ckpt.data_ptr(), lam.data_ptr(),
+                                     gk.data_ptr(), work.data_ptr(), 2, None) == N.ADV_ERR_INVALID_ARG
