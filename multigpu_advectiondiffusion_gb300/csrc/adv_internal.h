@@ -66,6 +66,8 @@ void tune_clear();
 void graph_cache_clear();  // cached CUDA graphs hold launch shapes: drop them when tuning changes
 
 // ------------------------------------------------------------------ heat launchers
+// "No plane withheld": below every plane a stream can visit (halo planes reach z = -2).
+constexpr int kNoWithheldPlane = -2147483647 - 1;
 struct HeatLaunch {
   // resolved per plan: whether the TMA path applies and the chosen z-chunk
   bool tma = false;
@@ -78,8 +80,9 @@ struct HeatLaunch {
   size_t smem = 0;
   CUtensorMap tmap_in;  // tensor map of u_in (re-encoded when the pointer changes)
   // failure-path testing only (adv_test_heat_stage_withheld): a z plane whose copy is never
-  // issued, and the wait limit for planes (0: the normal limit)
-  int withheld_plane = -1;
+  // issued (kNoWithheldPlane: none -- negative planes are real halo planes), and the wait limit
+  // for planes (0: the normal limit)
+  int withheld_plane = kNoWithheldPlane;
   unsigned long long wait_limit_ns = 0;
 };
 // rows: rows per thread of the stage kernel (2 or 4), lanes: lanes per row (32 or 16); 0 = the

@@ -78,8 +78,8 @@ struct HeatParams {
   T kx, ky, kz, dt;
   int* status;  // device status word
   // Failure-path testing only (adv_test_heat_stage_withheld): the TMA copy of z plane
-  // `withheld_plane` is never issued (-1: none), and the waits for planes give up after
-  // `wait_limit_ns` (the normal limit otherwise).
+  // `withheld_plane` is never issued (INT_MIN: none; halo planes below the grid have negative z),
+  // and the waits for planes give up after `wait_limit_ns` (the normal limit otherwise).
   int withheld_plane;
   unsigned long long wait_limit_ns;
 };

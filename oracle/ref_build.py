@@ -147,8 +147,11 @@ def _main_jobs(made: list) -> list:
             made.append(out)
             continue
         rpath = "-rpath,$ORIGIN/../../multigpu_advectiondiffusion_gb300/_lib"
-        cmd = [nvcc, *ARCH, "-O3", "-w", "-o", str(out), *map(str, srcs), "-L", str(LIBDIR), f"-l{compat}",
-               "-ladvdiff", "-Xlinker", rpath]
+        # -ffp-contract=off: the programs' host arithmetic (their initial conditions) rounds as written
+        # on every host, as the oracle and the library's host code do; g++ would otherwise fuse
+        # multiply-adds on Arm hosts (FMA is in the base ISA there, not on x86-64)
+        cmd = [nvcc, *ARCH, "-O3", "-w", "-Xcompiler", "-ffp-contract=off", "-o", str(out), *map(str, srcs),
+               "-L", str(LIBDIR), f"-l{compat}", "-ladvdiff", "-Xlinker", rpath]
         jobs.append((out, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)))
     return jobs
 

@@ -77,7 +77,7 @@ def test_weno7_rhs_and_run_equal_the_oracle(cuda, oracle, shape):
     L = torch.empty_like(a)
     weno7_rhs(cfg, a, L)
     np.testing.assert_array_equal(L.cpu().numpy().reshape(u0.shape), want)
-    uw, tw, itw = oracle.proto_run(7, u0, [h[0]] * len(shape), 0.4, 0.05)
+    uw, tw, itw = oracle.proto_run(7, u0, h, 0.4, 0.05)
     t, it = weno7_run(cfg, a, 0.05, 0.4)
     assert (it, t) == (itw, tw)
     np.testing.assert_array_equal(a.cpu().numpy().reshape(u0.shape), uw)
