@@ -348,6 +348,11 @@ adv_status adv_ensemble_destroy(adv_ensemble* e);
  *   heat / Burgers stages: param_a = CTAs per SM (up to the kernel's occupancy), param_b =
  *     minimum z planes per CTA share (the z-halo re-reads vs tail balance trade-off);
  *   heat with k(x), step and adjoint kernels: param_a = block height, param_b = z planes per CTA.
+ * adv_autotune_heat also times, for FP32 3D O2 problems with rows of whole 16-byte vectors, one
+ * launch of the two-step kernel (two forward-Euler steps per pass over HBM) against two tuned
+ * single-step launches; adv_heat_run's forward-Euler loop takes two-step launches for that problem
+ * only if they were more than 2% faster (table kind 5, a = steps per launch). Its result (out)
+ * describes the single-step shape.
  * Synchronises the stream. */
 typedef struct adv_tune_result {
   int32_t kind;

@@ -55,7 +55,9 @@ int* device_status_ptr();
 // problem was never tuned (launchers then use their defaults). Kinds and parameters:
 //   TUNE_HEAT, TUNE_BURGERS: a = CTAs per SM (<= occupancy), b = minimum planes per CTA share
 //   TUNE_HEATK_STEP, TUNE_HEATK_ADJ: a = block height (threads in y), b = z planes per CTA
-enum TuneKind { TUNE_HEAT = 1, TUNE_BURGERS = 2, TUNE_HEATK_STEP = 3, TUNE_HEATK_ADJ = 4 };
+//   TUNE_HEAT_STEPS: a = forward-Euler time steps per launch of adv_heat_run (1, or 2 with the
+//     two-step kernel where it measured faster), b = 1
+enum TuneKind { TUNE_HEAT = 1, TUNE_BURGERS = 2, TUNE_HEATK_STEP = 3, TUNE_HEATK_ADJ = 4, TUNE_HEAT_STEPS = 5 };
 struct TuneParams {
   int a = 0, b = 0;
   bool set = false;

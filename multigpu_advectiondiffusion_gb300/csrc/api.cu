@@ -350,9 +350,12 @@ adv_status adv_heat_run(const adv_heat_desc* d, int time_scheme, int64_t nsteps,
   const size_t one = (n * es + 255) / 256 * 256;
   char* w1 = static_cast<char*>(workspace);
   char* w2 = w1 + one;
-  if (time_scheme == ADV_EULER && nsteps >= 2 && heat2_eligible(*d, u) && heat2_eligible(*d, w1)) {
-    // Two steps per launch (one pass over HBM per two updates): u -(2)-> w1 -(2)-> u, a chunk of
-    // 4*C steps captured once and replayed; 2 or 3 remaining steps end with single-step launches.
+  const TuneParams steps = tune_lookup(TUNE_HEAT_STEPS, heat_tune_variant(*d), d->nx, d->ny, d->ndim == 3 ? d->nz : 1);
+  if (time_scheme == ADV_EULER && nsteps >= 2 && steps.set && steps.a == 2 && heat2_eligible(*d, u) &&
+      heat2_eligible(*d, w1)) {
+    // Two steps per launch, where the autotuner measured it faster (one pass over HBM per two
+    // updates): u -(2)-> w1 -(2)-> u, a chunk of 4*C steps captured once and replayed; 2 or 3
+    // remaining steps end with single-step launches.
     HeatLaunch Ta, Tb, La, Lb;
     if ((st = heat2_prepare(*d, u, &Ta)) != ADV_OK) return st;
     if ((st = heat2_prepare(*d, w1, &Tb)) != ADV_OK) return st;

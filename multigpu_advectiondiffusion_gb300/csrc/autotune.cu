@@ -175,6 +175,7 @@ bool tune_allowed(int kind, long long a, long long b) {
     case TUNE_BURGERS: return a >= 1 && a <= 32 && in(b, {4, 8, 16, 32});
     case TUNE_HEATK_STEP:
     case TUNE_HEATK_ADJ: return in(a, {4, 8, 16}) && in(b, {4, 8, 16, 32});
+    case TUNE_HEAT_STEPS: return in(a, {1, 2}) && b == 1;
     default: return false;
   }
 }
@@ -353,7 +354,32 @@ adv_status adv_autotune_heat(const adv_heat_desc* d, const void* u, void* stream
     flip ^= 1;
     return flip ? heat_launch(*d, La, 1, tmp2.p, tmp2.p, tmp.p, s) : heat_launch(*d, Lb, 1, tmp.p, tmp.p, tmp2.p, s);
   };
-  return sweep(TUNE_HEAT, heat_tune_variant(*d), d->nx, d->ny, nz, cands, dflt, prep, run, reps, s, out);
+  st = sweep(TUNE_HEAT, heat_tune_variant(*d), d->nx, d->ny, nz, cands, dflt, prep, run, reps, s, out);
+  if (st != ADV_OK) return st;
+  // Forward Euler can also advance two steps per launch (one pass over HBM for two updates, but
+  // about twice the instructions per pass): time two tuned single-step launches against one
+  // two-step launch and let adv_heat_run take the two-step kernel only where it is clearly faster.
+  tune_store(TUNE_HEAT_STEPS, heat_tune_variant(*d), d->nx, d->ny, nz, TuneParams{1, 1, true});
+  if (!heat2_eligible(*d, tmp.p) || !heat2_eligible(*d, tmp2.p)) return ADV_OK;
+  double one_us = 0.0, two_us = 0.0;
+  if ((st = prep()) != ADV_OK) return st;
+  auto pair = [&]() {
+    adv_status r = run();
+    return r == ADV_OK ? run() : r;
+  };
+  if ((st = time_us(pair, reps, s, &one_us)) != ADV_OK) return st;
+  HeatLaunch Ta, Tb;
+  if ((st = heat2_prepare(*d, tmp2.p, &Ta)) != ADV_OK) return st;
+  if ((st = heat2_prepare(*d, tmp.p, &Tb)) != ADV_OK) return st;
+  auto run2 = [&]() {
+    flip ^= 1;
+    return flip ? heat2_launch(*d, Ta, tmp2.p, tmp.p, s) : heat2_launch(*d, Tb, tmp.p, tmp2.p, s);
+  };
+  if ((st = time_us(run2, reps, s, &two_us)) != ADV_OK) return st;
+  if (two_us < 0.98 * one_us)
+    tune_store(TUNE_HEAT_STEPS, heat_tune_variant(*d), d->nx, d->ny, nz, TuneParams{2, 1, true});
+  graph_cache_clear();
+  return ADV_OK;
 }
 
 adv_status adv_autotune_burgers(const adv_burgers_desc* d, const void* u, void* stream, adv_tune_result* out) {

@@ -52,6 +52,8 @@ def test_import_then_export_round_trip(tmp_path):
     _table((2, 1, 64, 64, 64, 4, 3)),            # Burgers share outside {4, 8, 16, 32}
     _table((1, 1, 64, 64, 64, 0, 8)),            # no CTAs
     _table((9, 1, 64, 64, 64, 1, 8)),            # unknown kind
+    _table((5, 23, 64, 64, 64, 3, 1)),           # steps per launch outside {1, 2}
+    _table((5, 23, 64, 64, 64, 2, 8)),           # steps per launch with b != 1
     _table((1, 1, 0, 64, 64, 1, 8)),             # empty grid
     _table((1, 1, 64, 64, 64, 1, 8), version=2),
     '{"advdiff_autotune": 1, "entries": [{"kind": 1, "variant": 1, "nx": 8, "ny": 8, "nz": 8, "a": 1}]}',
@@ -85,3 +87,11 @@ def test_export_buffer_size_contract(native):
     assert native.adv_autotune_export(small, n.value - 1, C.byref(n)) == N.ADV_ERR_INVALID_ARG
     assert native.adv_autotune_export(None, 0, None) == N.ADV_ERR_INVALID_ARG
     assert native.adv_autotune_import(None) == N.ADV_ERR_INVALID_ARG
+
+
+def test_steps_per_launch_entries_round_trip():
+    """Table kind 5 (forward-Euler steps per launch of adv_heat_run) takes 1 or 2."""
+    S.autotune_clear()
+    S.autotune_import(_table((5, 23, 256, 256, 256, 2, 1), (5, 23, 96, 96, 96, 1, 1)))
+    assert sorted(_entries()) == sorted([(5, 23, 256, 256, 256, 2, 1), (5, 23, 96, 96, 96, 1, 1)])
+    S.autotune_clear()
