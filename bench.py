@@ -1066,7 +1066,7 @@ def main():
         for _ in range(2):
             heat_run(cfg, u64, inner, ws64, stream=sh)
         extra["f64_value"] = cells_stages_per_step * 3 / ev_time(
-            lambda: [heat_run(cfg, u64, inner, ws64, stream=sh) for _ in range(3)])
+            lambda: [heat_run(cfg, u64, inner, ws64, stream=sh) for _ in range(3)]) / 1e9
     else:
         # ALU roofline: the stage is compute-bound. FP32 flops per cell-stage from the ncu
         # instruction mix of the stage kernel (FFMA2 = 4, FADD2/FMUL2/FFMA = 2, FADD/FMUL = 1;

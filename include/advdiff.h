@@ -145,9 +145,10 @@ adv_status adv_device_status(void* stream);
  * of z plane `plane` is never issued, and the waits for planes give up after wait_limit_ns
  * (1e5 .. 2e9 ns). Every CTA that streams that plane then waits until its limit runs out,
  * records ADV_ERR_TIMEOUT in the status word, lets its copies already in flight land, and
- * returns; the output is left incomplete. Nothing faults or waits without limit. Needs the TMA
- * load path (16-byte aligned buffer and rows); ADV_ERR_UNSUPPORTED otherwise. No counterpart in
- * the reference. */
+ * returns; the output is left incomplete. Nothing faults or waits without limit. Takes stage 1
+ * (u_n == u_in) of an FP32 3D O2 problem on the TMA load path (16-byte aligned buffer and rows);
+ * ADV_ERR_UNSUPPORTED otherwise. It runs its own build of the stage kernel: the kernels every other
+ * call launches carry none of this test's code. No counterpart in the reference. */
 adv_status adv_test_heat_stage_withheld(const adv_heat_desc* d, int stage, const void* u_in,
                                         const void* u_n, void* u_out, int plane, uint64_t wait_limit_ns,
                                         void* stream);

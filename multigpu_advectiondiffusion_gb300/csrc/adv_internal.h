@@ -93,6 +93,10 @@ adv_status heat_prepare(const adv_heat_desc& d, const void* u_in, HeatLaunch* L,
 adv_status heat_launch(const adv_heat_desc& d, const HeatLaunch& L, int stage, const void* u_in,
                        const void* u_n, void* u_out, cudaStream_t s);
 adv_status heat_validate(const adv_heat_desc* d);
+// One stage-1 launch of the failure-path test's kernel variant (FP32 3D O2, TMA, L's withheld plane
+// and wait limit); ADV_ERR_UNSUPPORTED for other problems.
+adv_status heat_launch_test_hook(const adv_heat_desc& d, const HeatLaunch& L, const void* u_in, void* u_out,
+                                 cudaStream_t s);
 // Two forward-Euler steps per launch (FP32 3D O2, rows of whole 16-byte vectors, TMA path):
 // u_out = E(E(u_in)), bit for bit two heat_launch stage-1 steps.
 bool heat2_eligible(const adv_heat_desc& d, const void* u_in);

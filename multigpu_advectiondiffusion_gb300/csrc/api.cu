@@ -311,10 +311,10 @@ adv_status adv_test_heat_stage_withheld(const adv_heat_desc* d, int stage, const
     return set_error(ADV_ERR_INVALID_ARG, "heat test: wait limit must lie in [1e5, 2e9] ns");
   HeatLaunch L;
   if ((st = heat_prepare(*d, u_in, &L)) != ADV_OK) return st;
-  if (!L.tma) return set_error(ADV_ERR_UNSUPPORTED, "heat test: the withheld-copy test needs the TMA load path");
+  if (stage != 1 || u_n != u_in) return set_error(ADV_ERR_UNSUPPORTED, "heat test: the withheld-copy test runs stage 1");
   L.withheld_plane = plane;
   L.wait_limit_ns = wait_limit_ns;
-  return heat_launch(*d, L, stage, u_in, u_n, u_out, static_cast<cudaStream_t>(stream));
+  return heat_launch_test_hook(*d, L, u_in, u_out, static_cast<cudaStream_t>(stream));
 }
 
 adv_status adv_device_status(void* stream) {

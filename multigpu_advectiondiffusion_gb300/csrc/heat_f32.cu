@@ -38,4 +38,12 @@ void* heat_kernel_f32(int order, int ndim, bool tma, int stage_kind, int rows, i
   return nullptr;
 }
 
+// The failure-path test's variant of the FP32 3D O2 stage-1 kernel with TMA loads (4 rows, 4 warps,
+// rows of `lanes` lanes): it withholds one plane's copy and takes the wait limit from its
+// parameters (HeatParams::withheld_plane, wait_limit_ns).
+void* heat_test_hook_kernel_f32(int lanes) {
+  return lanes == 16 ? reinterpret_cast<void*>(&heat_stage_kernel<float, 2, 3, true, 1, 4, 4, 16, false, true>)
+                     : reinterpret_cast<void*>(&heat_stage_kernel<float, 2, 3, true, 1, 4, 4, 32, false, true>);
+}
+
 }  // namespace adv

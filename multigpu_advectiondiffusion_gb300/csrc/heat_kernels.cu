@@ -192,6 +192,21 @@ static adv_status heat_launch_t(const adv_heat_desc& d, const HeatLaunch& L, int
   return ADV_OK;
 }
 
+void* heat_test_hook_kernel_f32(int lanes);
+
+adv_status heat_launch_test_hook(const adv_heat_desc& d, const HeatLaunch& L, const void* u_in, void* u_out,
+                                 cudaStream_t s) {
+  if (d.dtype != ADV_F32 || d.ndim != 3 || d.order != 2 || !L.tma || L.rows != 4 || L.warps != 4)
+    return set_error(ADV_ERR_UNSUPPORTED, "heat test: the withheld-copy test takes FP32 3D O2 on the TMA path");
+  HeatParams<float> p = heat_params<float>(d, L, 1, u_in, u_in, u_out);
+  void* k = heat_test_hook_kernel_f32(L.lanes);
+  ADV_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem));
+  void* args[] = {const_cast<CUtensorMap*>(&L.tmap_in), &p};
+  ADV_CUDA_TRY(cudaLaunchKernel(k, L.grid, L.block, args, L.smem, s));
+  count_launches(1);
+  return ADV_OK;
+}
+
 adv_status heat_launch(const adv_heat_desc& d, const HeatLaunch& L, int stage, const void* u_in, const void* u_n,
                        void* u_out, cudaStream_t s) {
   if (stage < 1 || stage > 3) return set_error(ADV_ERR_INVALID_ARG, "heat: stage must be 1, 2 or 3");

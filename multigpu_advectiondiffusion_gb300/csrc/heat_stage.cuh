@@ -77,9 +77,10 @@ struct HeatParams {
   int vec_ok;  // output rows 16-byte aligned: vector stores
   T kx, ky, kz, dt;
   int* status;  // device status word
-  // Failure-path testing only (adv_test_heat_stage_withheld): the TMA copy of z plane
-  // `withheld_plane` is never issued (INT_MIN: none; halo planes below the grid have negative z),
-  // and the waits for planes give up after `wait_limit_ns` (the normal limit otherwise).
+  // Failure-path testing only (adv_test_heat_stage_withheld; read only by the kernels built with
+  // HOOK = true): the TMA copy of z plane `withheld_plane` is never issued (INT_MIN: none; halo
+  // planes below the grid have negative z), and the waits for planes give up after
+  // `wait_limit_ns`.
   int withheld_plane;
   unsigned long long wait_limit_ns;
 };
@@ -186,7 +187,7 @@ __device__ __forceinline__ int* heat_abort_flag() {
 // segment (by value, so it stays in registers), with s_issue = -1 if a wait timed out (the CTA
 // must then return).
 template <class T, int ORDER, int NDIM, bool TMA, int STAGE, int ROWS = 2, int WARPS = 8, int LANES = 32,
-          bool CONTRACT = false>
+          bool CONTRACT = false, bool HOOK = false>
 __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const HeatParams<T>& p, int x0, int y0, int zs,
                                              int ze, HeatPipe pipe) {
   using C = HeatTile<T, ORDER, NDIM, ROWS, WARPS, LANES>;
@@ -216,7 +217,7 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
     T* dst = ring + s_issue * C::SLOT_ELEMS;
     const int z = p0 + q;
     if (TMA) {
-      if (tid == 0 && z != p.withheld_plane) {
+      if (tid == 0 && (!HOOK || z != p.withheld_plane)) {
         mbar_arrive_expect_tx(&bars[s_issue], C::PLANE_BYTES);
         tma_load_3d(dst, tmap, x0 - C::PADX, y0 - R, z, &bars[s_issue]);
       }
@@ -297,7 +298,7 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
     bool ok = true;
     if (TMA) {
       // every lane waits on the barrier itself (converged: same barrier, same phase)
-      ok = mbar_wait_bounded(&bars[s_wait], (parity >> s_wait) & 1u, p.status, p.wait_limit_ns);
+      ok = mbar_wait_bounded(&bars[s_wait], (parity >> s_wait) & 1u, p.status, HOOK ? p.wait_limit_ns : kWaitLimitNs);
       if (!ok) *abort_flag = 1;
     } else {
       cp_async_wait<C::P>();
@@ -474,7 +475,7 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
       // the planes prefetched after it.
       if (TMA && tid == 0) {
         const int s_q = s_wait == 0 ? C::NS - 1 : s_wait - 1;
-        if (p0 + q != p.withheld_plane) mbar_wait_bounded(&bars[s_q], ((parity >> s_q) & 1u) ^ 1u, p.status);
+        if (!HOOK || p0 + q != p.withheld_plane) mbar_wait_bounded(&bars[s_q], ((parity >> s_q) & 1u) ^ 1u, p.status);
         int s = s_wait;
         for (int m = q + 1; m < Q && m <= q + C::P; ++m) {
           mbar_wait_bounded(&bars[s], (parity >> s) & 1u, p.status);
@@ -515,8 +516,10 @@ constexpr int heat_min_ctas() {
   return ROWS > 2 ? 16 / WARPS : (ORDER == 2 ? 4 : (sizeof(T) == 4 ? 3 : 2));
 }
 
+// HOOK: the failure-path test's variant (adv_test_heat_stage_withheld); every other launch runs the
+// kernels without it.
 template <class T, int ORDER, int NDIM, bool TMA, int STAGE, int ROWS = 2, int WARPS = 8, int LANES = 32,
-          bool CONTRACT = false>
+          bool CONTRACT = false, bool HOOK = false>
 __global__ void __launch_bounds__(32 * WARPS, heat_min_ctas<T, ORDER, ROWS, WARPS>())
 heat_stage_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ HeatParams<T> p) {
   using C = HeatTile<T, ORDER, NDIM, ROWS, WARPS, LANES>;
@@ -543,7 +546,7 @@ heat_stage_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constan
     const int ze = (int)min((int64_t)p.nz, zs + (seg_b - pos));
     pos += ze - zs;
     const int x0 = (int)(tile % p.tiles_x) * C::BX, y0 = (int)(tile / p.tiles_x) * C::BY;
-    pipe = heat_segment<T, ORDER, NDIM, TMA, STAGE, ROWS, WARPS, LANES, CONTRACT>(&tmap, p, x0, y0, zs, ze, pipe);
+    pipe = heat_segment<T, ORDER, NDIM, TMA, STAGE, ROWS, WARPS, LANES, CONTRACT, HOOK>(&tmap, p, x0, y0, zs, ze, pipe);
     if (pipe.s_issue < 0) return;
   }
 }
