@@ -875,6 +875,49 @@ def bench_weno7(args, world, rank, dev, stream, flush, lib):
         print(json.dumps(line), flush=True)
 
 
+def compat_program_rates(n: int = 256) -> dict | None:
+    """The reference's own single-GPU programs (their main.cpp + tools.cpp, unmodified) linked
+    against this library's compatibility libraries (oracle/_ref/refmain_*), run on an n^3 grid with
+    the reference's command line: the rate from the wall-time difference of two run lengths, so
+    process start-up, the host initial condition and the copies cancel. FP64 (the programs' REAL).
+    None when the programs were not built."""
+    ref = ROOT / "oracle" / "_ref"
+    out = {}
+
+    def wall(argv):
+        t0 = time.perf_counter()
+        r = subprocess.run(argv, capture_output=True, text=True, timeout=600, cwd=str(ref))
+        return time.perf_counter() - t0, r
+
+    exe = ref / "refmain_burgers3d"
+    if exe.exists():
+        its, ts = [], []
+        for tend in (0.005, 0.02):
+            t, r = wall([str(exe), str(tend), "0.3", "2", "2", "2", str(n), str(n), str(n), "8", "8", "8"])
+            m = re.search(r"iterations: (\S+)", r.stdout)
+            if r.returncode != 0 or not m:
+                return None
+            its.append(int(float(m.group(1))))
+            ts.append(t)
+        out["burgers3d"] = {"value": n ** 3 * 3 * (its[1] - its[0]) / (ts[1] - ts[0]) / 1e9, "unit": "Gcell-updates/s",
+                            "sample": f"{n}^3, {its[0]} vs {its[1]} SSP-RK3 steps of the reference scheme (local LF "
+                                      "WENO5-Z + viscous term, frozen layers), FP64"}
+    exe = ref / "refmain_heat3d"
+    if exe.exists():
+        ts = []
+        for iters in (20, 60):
+            t, r = wall([str(exe), "1.0", "10", "10", "10", str(n), str(n), str(n), str(iters), "32", "4", "4"])
+            if r.returncode != 0:
+                return None
+            ts.append(t)
+        out["heat3d_o4_rk3"] = {"value": n ** 3 * 3 * 40 / (ts[1] - ts[0]) / 1e9, "unit": "Gcell-updates/s",
+                                "sample": f"{n}^3, 20 vs 60 SSP-RK3 steps of the reference's O4 heat scheme, FP64"}
+    if out:
+        out["how"] = ("the reference's main.cpp + tools.cpp linked unmodified against libadvdiff_compat_*; "
+                      "compare with the reference arm's sg_gpu (its own kernels.cu on this GPU)")
+    return out or None
+
+
 def burgers_workload(args) -> str:
     return (f"burgers3d 256^3 f32 weno5-{args.weno} global-lf periodic cfl 0.4 x 20 steps, "
             f"div {args.div}")
@@ -1062,11 +1105,23 @@ def main():
         heat_run(cfg, u64, inner, stream=sh)
         torch.cuda.synchronize()
         extra["rel_l2_vs_fp64"] = (torch.linalg.vector_norm(u32.double() - u64) / torch.linalg.vector_norm(u64)).item()
+        u64_ref = u64.clone()
         ws64 = heat_workspace(cfg, u64)
         for _ in range(2):
             heat_run(cfg, u64, inner, ws64, stream=sh)
         extra["f64_value"] = cells_stages_per_step * 3 / ev_time(
             lambda: [heat_run(cfg, u64, inner, ws64, stream=sh) for _ in range(3)]) / 1e9
+        # FP64 in the fused multiply-add form (adv_heat_desc.contract = 1), and its distance from the
+        # reference's rounding after the whole solve
+        cfg_c = dataclasses.replace(cfg, contract=True)
+        u64c = u0.double()
+        heat_run(cfg_c, u64c, inner, ws64, stream=sh)
+        torch.cuda.synchronize()
+        extra["f64_contracted_rel_l2_vs_f64"] = (torch.linalg.vector_norm(u64c - u64_ref) /
+                                                 torch.linalg.vector_norm(u64_ref)).item()
+        extra["f64_contracted_after"] = f"{inner} time steps from the same initial state"
+        extra["f64_fast_value"] = cells_stages_per_step * 3 / ev_time(
+            lambda: [heat_run(cfg_c, u64c, inner, ws64, stream=sh) for _ in range(3)]) / 1e9
     else:
         # ALU roofline: the stage is compute-bound. FP32 flops per cell-stage from the ncu
         # instruction mix of the stage kernel (FFMA2 = 4, FADD2/FMUL2/FFMA = 2, FADD/FMUL = 1;
@@ -1097,6 +1152,7 @@ def main():
             others[dv] = cells_stages_per_step / sec / 1e9
             del u2, w2
         extra["other_division_values"] = others
+        extra["compat_reference_programs"] = compat_program_rates()
         # the whole C3 run to t = 0.5 (past shock formation) in FP32 with this division and in FP64 in the
         # reference's operand order (bit-exact with the oracle): steps and relative L2 error
         u32 = u0.clone()

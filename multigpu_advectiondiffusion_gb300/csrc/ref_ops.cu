@@ -81,34 +81,50 @@ __global__ void ref_rk_kernel(Grid3 g, int ndim, int lo, int step, T dt, T* __re
   }
 }
 
+// One directional sweep (Compute_dF / dG / dH, SG/Burgers3d_WENO5/kernels.cu:197-394): for every
+// node with a in [2, na-4] along the axis and the other two indices in [3, n-4], the face flux
+// F(a+1/2) from f+ at a-2..a+2 and f- at a-1..a+3 (local Lax-Friedrichs split), and
+// Lu = -(F(a+1/2) - F(a-1/2)) / h (x: assigned; y, z: accumulated), with F(2-1/2) taken as 0.
+// One thread per line walks a upwards as the reference's sweeps do: each face is reconstructed
+// once (the previous one is kept in a register) and each node split once (a sliding window of six
+// split values). Threads of a warp take neighbouring x positions for the y and z sweeps
+// (coalesced); the x sweep's lines are rows, read through L1.
 template <class T, bool Z>
-__device__ __forceinline__ T sweep_face(const T* __restrict__ u, int64_t o, int64_t s) {
-  // face at o + 1/2 along stride s: f+ at o-2s..o+2s, f- at o-s..o+3s (local LF)
-  T fp[6], fm[6];
+__global__ void __launch_bounds__(256) ref_sweep_kernel(Grid3 g, int axis, T h, const T* __restrict__ u,
+                                                        T* __restrict__ Lu) {
+  const int na = axis == 0 ? g.nx : axis == 1 ? g.ny : g.nz;
+  const int nb = axis == 0 ? g.ny : g.nx, nc = axis == 2 ? g.ny : g.nz;
+  const int lb = nb - 6, lc = nc - 6;  // the other indices run over [3, n-4]
+  if (na < 6 || lb <= 0 || lc <= 0) return;
+  const int64_t s = axis == 0 ? 1 : axis == 1 ? g.pitch : g.pitch * g.ny;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < (int64_t)lb * lc;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int b = 3 + (int)(t % lb), c = 3 + (int)(t / lb);
+    const int i = axis == 0 ? 0 : b, j = axis == 0 ? b : (axis == 1 ? 0 : c), k = axis == 2 ? 0 : c;
+    const int64_t o0 = g.at(i, j, k);  // node a = 0 of this line
+    T fp[6], fm[6];                    // split values of nodes a-2 .. a+3
 #pragma unroll
-  for (int q = 0; q < 6; ++q) {
-    const T v = u[o + (q - 2) * s];
-    lf_split<T>(v, fabs(v), fp[q], fm[q]);
-  }
-  return weno_face_ref<Z, T>(fp[0], fp[1], fp[2], fp[3], fp[4], fm[1], fm[2], fm[3], fm[4], fm[5]);
-}
-
-template <class T, bool Z>
-__global__ void ref_sweep_kernel(Grid3 g, int axis, T h, const T* __restrict__ u, T* __restrict__ Lu) {
-  for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < g.count(); f += (int64_t)gridDim.x * blockDim.x) {
-    int i, j, k;
-    g.ijk(f, i, j, k);
-    const int a = axis == 0 ? i : axis == 1 ? j : k;
-    const int na = axis == 0 ? g.nx : axis == 1 ? g.ny : g.nz;
-    const int b = axis == 0 ? j : i, nb = axis == 0 ? g.ny : g.nx;
-    const int c = axis == 2 ? j : k, nc = axis == 2 ? g.ny : g.nz;
-    if (a < 2 || a > na - 4 || b < 3 || b > nb - 4 || c < 3 || c > nc - 4) continue;
-    const int64_t o = g.at(i, j, k);
-    const int64_t s = axis == 0 ? 1 : axis == 1 ? g.pitch : g.pitch * g.ny;
-    const T fu = sweep_face<T, Z>(u, o, s);
-    const T fu_old = a == 2 ? T(0) : sweep_face<T, Z>(u, o - s, s);
-    if (axis == 0) Lu[o] = div_rn(-sub_rn(fu, fu_old), h);
-    else Lu[o] = sub_rn(Lu[o], div_rn(sub_rn(fu, fu_old), h));
+    for (int q = 0; q < 6; ++q) {
+      const T v = u[o0 + q * s];
+      lf_split<T>(v, fabs(v), fp[q], fm[q]);
+    }
+    T fu_old = T(0);
+    for (int a = 2; a <= na - 4; ++a) {
+      const T fu = weno_face_ref<Z, T>(fp[0], fp[1], fp[2], fp[3], fp[4], fm[1], fm[2], fm[3], fm[4], fm[5]);
+      const int64_t o = o0 + (int64_t)a * s;
+      if (axis == 0) Lu[o] = div_rn(-sub_rn(fu, fu_old), h);
+      else Lu[o] = sub_rn(Lu[o], div_rn(sub_rn(fu, fu_old), h));
+      fu_old = fu;
+#pragma unroll
+      for (int q = 0; q < 5; ++q) {
+        fp[q] = fp[q + 1];
+        fm[q] = fm[q + 1];
+      }
+      if (a + 4 < na) {
+        const T v = u[o0 + (int64_t)(a + 4) * s];
+        lf_split<T>(v, fabs(v), fp[5], fm[5]);
+      }
+    }
   }
 }
 
@@ -200,7 +216,8 @@ adv_status adv_ref_burgers_sweep(int dtype, int axis, int weno, int64_t pitch, i
     return set_error(ADV_ERR_INVALID_ARG, "ref_burgers_sweep: bad arguments");
   Grid3 g{nx, ny, nz, pitch};
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const dim3 grid = flat_grid((int64_t)nx * ny * nz);
+  const int nb = axis == 0 ? ny : nx, nc = axis == 2 ? ny : nz;
+  const dim3 grid = flat_grid((int64_t)std::max(nb - 6, 1) * std::max(nc - 6, 1));  // one thread per line
   const bool z = weno == ADV_WENO5_Z;
   if (dtype == ADV_F64) {
     if (z) ref_sweep_kernel<double, true><<<grid, 256, 0, s>>>(g, axis, h, (const double*)u, (double*)Lu);
