@@ -405,6 +405,21 @@ def bench_ensemble(args, world, rank, dev, stream, flush, lib):
     heat_shape = ens_h.shape()
     ens_h.close()
 
+    # launch floor: the same graph (64 heat + 32 Burgers members, S steps, the same per-step
+    # kernels and stage launches) over 16^3 heat and 32^3 Burgers members, whose launches carry
+    # almost no work. What this run costs bounds what fusing the loop into one persistent kernel
+    # could remove (launch gaps, graph node overhead and the per-step kernels).
+    from multigpu_advectiondiffusion_gb300.solvers import BurgersConfig, HeatConfig
+    gen = torch.Generator(device="cpu").manual_seed(ENSEMBLE_SEED)
+    th = [HeatConfig.dirichlet_o2(3, 16, r=0.125) for _ in heat]
+    tb = [BurgersConfig.periodic(32, weno="z", div=ENSEMBLE_DIV) for _ in burgers]
+    thu = [torch.rand(c.numel, generator=gen).to(dev) for c in th]
+    tbu = [(0.5 + 0.1 * torch.rand(c.numel, generator=gen)).to(dev) for c in tb]
+    ens_t = Ensemble(heat=list(zip(th, thu)), burgers=[(c, u, 1e9, 0.4, N.ADV_DT_MAXU, S) for c, u in zip(tb, tbu)])
+    ens_t.run(S, stream=sh)
+    floor_ms = timed(lambda: ens_t.run(S, stream=sh), 1) - fl
+    ens_t.close()
+
     # plain per-instance loop over the same instances (each instance its own heat_run /
     # burgers_run: one-wave grids per instance, one graph per instance)
     hws = [heat_workspace(c, u) for c, u in zip(heat, hu)]
@@ -454,6 +469,9 @@ def bench_ensemble(args, world, rank, dev, stream, flush, lib):
                     "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
             "gpu_launches": int(launched),
             "clocks": clk.summary(),
+            "launch_floor": {"ms_per_run": floor_ms, "share_of_run": floor_ms / (ms_max / args.steps),
+                             "measured_as": "the same graph over 64 heat 16^3 + 32 Burgers 32^3 members, "
+                                            f"{S} steps: launches carrying almost no work"},
             "per_instance_loop_value": loop_value,
             "speedup_vs_per_instance_loop": value / loop_value,
             "roofline_heat_batch": {"bound": "hbm", "kernel": "heat_batch_kernel<float,2,TMA,stage 1>",
@@ -505,7 +523,7 @@ def adjoint_setup():
 
 def bench_adjoint(args, world, rank, dev, lib):
     import torch
-    from multigpu_advectiondiffusion_gb300.solvers import burgers_run_fixed, heatk_run
+    from multigpu_advectiondiffusion_gb300.solvers import burgers_run_fixed, default_interval, heatk_run
     bc, u0n, utn, dt, hc, kn, k2n, h0n = adjoint_setup()
     u0 = torch.from_numpy(u0n.astype(np.float32)).to(dev)
     with torch.no_grad():
@@ -572,17 +590,22 @@ def bench_adjoint(args, world, rank, dev, lib):
         from multigpu_advectiondiffusion_gb300.solvers import autotune_heatk
         autotune_heatk(hc, k, h0)
 
-    def grad_heat():
+    def grad_heat(interval=None):
         kk = k.clone().requires_grad_(True)
         hh = h0.clone().requires_grad_(True)
-        tfh, uT = ev(lambda: heatk_run(hc, kk, hh, HEATK_STEPS))
+        tfh, uT = ev(lambda: heatk_run(hc, kk, hh, HEATK_STEPS, interval))
         loss = 0.5 * ((uT - htarget) ** 2).sum()
         tbh, _ = ev(loss.backward)
         return tfh, tbh
-    for _ in range(2):
-        grad_heat()
-    hts = [grad_heat() for _ in range(3)]
-    tfh, tbh = float(np.median([h[0] for h in hts])), float(np.median([h[1] for h in hts]))
+
+    def median_grad(interval=None):
+        for _ in range(2):
+            grad_heat(interval)
+        hts = [grad_heat(interval) for _ in range(3)]
+        return float(np.median([h[0] for h in hts])), float(np.median([h[1] for h in hts]))
+    tfh, tbh = median_grad()
+    # every state kept (interval 1: 200 states of 192^3 FP32, 5.7 GB of HBM): no recompute
+    tfh1, tbh1 = median_grad(1)
     t_grad = max_over_ranks(tf + tb, dev)
     if rank == 0:
         line = {
@@ -605,7 +628,12 @@ def bench_adjoint(args, world, rank, dev, lib):
                         "fd_rel_err_max_16_dirs": max(fd_err), "fd_rel_err_median": float(np.median(fd_err)),
                         "fd": "central differences of the FP64 forward run, step 1e-8, 16 seeded directions"},
             "heat_k": {"forward_ms": tfh, "backward_ms": tbh, "backward_over_forward": tbh / tfh,
-                       "forward_value": HEATK_N ** 3 * HEATK_STEPS / (tfh * 1e-3) / 1e9},
+                       "forward_value": HEATK_N ** 3 * HEATK_STEPS / (tfh * 1e-3) / 1e9,
+                       "checkpoints": f"every {default_interval(HEATK_STEPS)} steps (sqrt N)"},
+            "heat_k_every_state": {"forward_ms": tfh1, "backward_ms": tbh1, "backward_over_forward": tbh1 / tfh1,
+                                   "forward_value": HEATK_N ** 3 * HEATK_STEPS / (tfh1 * 1e-3) / 1e9,
+                                   "checkpoints": "every step (interval 1): no recompute",
+                                   "checkpoint_bytes": HEATK_STEPS * HEATK_N ** 3 * 4},
         }
         print(json.dumps(line), flush=True)
 
@@ -894,7 +922,7 @@ def compat_program_rates(n: int = 256) -> dict | None:
         its, ts = [], []
         for tend in (0.005, 0.02):
             t, r = wall([str(exe), str(tend), "0.3", "2", "2", "2", str(n), str(n), str(n), "8", "8", "8"])
-            m = re.search(r"iterations: (\S+)", r.stdout)
+            m = re.search(r"iterations: ([0-9.eE+-]+)", r.stdout)
             if r.returncode != 0 or not m:
                 return None
             its.append(int(float(m.group(1))))

@@ -250,9 +250,11 @@ adv_status adv_heatk_step(const adv_heatk_desc* d, const void* k, const void* u_
                           void* stream);
 adv_status adv_heatk_adjoint_step(const adv_heatk_desc* d, const void* k, const void* u_n,
                                   const void* lam_next, void* lam_out, void* grad_k, void* stream);
-/* sqrt(N) checkpointing: the forward run stores u every `interval` steps (ceil(nsteps/interval)
- * arrays in ckpt); the backward run recomputes each interval from its checkpoint into `work`
- * (interval arrays) and sweeps the adjoint through it. Sizes in bytes. */
+/* Checkpointing: the forward run stores u every `interval` steps (ceil(nsteps/interval) arrays in
+ * ckpt; each stored state is written there by the step that makes it); the backward run
+ * recomputes each interval from its checkpoint into `work` (interval arrays) and sweeps the
+ * adjoint through it. interval ~ sqrt(nsteps) keeps memory at ~2 sqrt(nsteps) arrays; interval 1
+ * keeps every state (nsteps arrays) and the backward run recomputes nothing. Sizes in bytes. */
 adv_status adv_heatk_checkpoint_bytes(const adv_heatk_desc* d, int64_t nsteps, int64_t interval,
                                       size_t* ckpt_bytes, size_t* work_bytes);
 /* nsteps steps in place on u; ckpt may be NULL (no checkpoints kept). With checkpoints, the run

@@ -90,6 +90,9 @@ struct HeatLaunch {
 // rows: rows per thread of the stage kernel (2 or 4), lanes: lanes per row (32 or 16); 0 = the
 // library's choice.
 adv_status heat_prepare(const adv_heat_desc& d, const void* u_in, HeatLaunch* L, int rows = 0, int lanes = 0);
+// Lanes per row of the 4-row FP32 tile for rows of nx nodes: 16 (64-wide tiles) where 128-wide
+// tiles leave clearly more lanes idle, else 32.
+int heat_row_lanes(int nx);
 adv_status heat_launch(const adv_heat_desc& d, const HeatLaunch& L, int stage, const void* u_in,
                        const void* u_n, void* u_out, cudaStream_t s);
 adv_status heat_validate(const adv_heat_desc* d);

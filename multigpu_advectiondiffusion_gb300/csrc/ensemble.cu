@@ -21,6 +21,7 @@
 
 namespace adv {
 void* heat_batch_kernel_for(int dtype, int order, bool tma, int stage_kind, int rows, int lanes);
+void* heat_batch_mixed_kernel_for(int stage_kind);
 template <class T>
 void* burgers_batch_kernel_for(const adv_burgers_desc& d);
 size_t burgers_smem_f32();
@@ -40,6 +41,12 @@ struct adv_ensemble {
   int64_t heat_units = 0;
   int heat_ctas = 0;
   int heat_rows = 2, heat_warps = 8, heat_lanes = 32;  // tile of the batched heat kernel
+  // 4-row tiles of two widths (heat_batch_mixed_kernel): the table's first heat_n_wide members
+  // (units [0, heat_units_wide)) take rows of 32 lanes and CTAs [0, heat_ctas_wide), the rest
+  // rows of 16 lanes
+  bool heat_mixed = false;
+  int heat_n_wide = 0, heat_ctas_wide = 0;
+  int64_t heat_units_wide = 0;
   size_t heat_smem = 0;
   void* heat_k[3] = {nullptr, nullptr, nullptr};
   // Burgers members
@@ -93,27 +100,46 @@ int heat_slots_of(const adv_heat_member& m, int scheme, HeatSlot* sl) {
 
 template <class T>
 adv_status build_heat_table(adv_ensemble* e, std::vector<unsigned char>& bytes) {
-  std::vector<HeatBatchInst<T>> tab((size_t)e->n_heat);
-  int64_t units = 0;
-  bool tma = true;
+  // Table order: with 4-row tiles each member takes the row width a single grid of its size
+  // would (heat_row_lanes), members of 128-wide tiles first; the kernels only see the table, so
+  // its order is free.
+  std::vector<int> order((size_t)e->n_heat), lanes((size_t)e->n_heat, 32);
   for (int i = 0; i < e->n_heat; ++i) {
-    const adv_heat_member& m = e->heat[i];
+    order[(size_t)i] = i;
+    if (e->heat_rows == 4) lanes[(size_t)i] = heat_row_lanes(e->heat[(size_t)i].desc.nx);
+  }
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return lanes[(size_t)a] > lanes[(size_t)b]; });
+  std::vector<HeatBatchInst<T>> tab((size_t)e->n_heat);
+  int64_t units = 0, units_wide = 0;
+  int n_wide = 0;
+  bool tma = true;
+  for (int j = 0; j < e->n_heat; ++j) {
+    const int i = order[(size_t)j];
+    const adv_heat_member& m = e->heat[(size_t)i];
     HeatSlot sl[3];
     const int ns = heat_slots_of(m, e->heat_scheme, sl);
     HeatLaunch L;
     for (int s = 0; s < ns; ++s) {
-      adv_status st = heat_prepare(m.desc, sl[s].in, &L, e->heat_rows, e->heat_lanes);  // the batched tile
+      adv_status st = heat_prepare(m.desc, sl[s].in, &L, e->heat_rows, lanes[(size_t)i]);  // the batched tile
       if (st != ADV_OK) return st;
       tma = tma && L.tma;
-      tab[i].tmap[s] = L.tmap_in;
-      tab[i].p[s] = heat_params<T>(m.desc, L, sl[s].stage, sl[s].in, sl[s].un, sl[s].out);
+      tab[(size_t)j].tmap[s] = L.tmap_in;
+      tab[(size_t)j].p[s] = heat_params<T>(m.desc, L, sl[s].stage, sl[s].in, sl[s].un, sl[s].out);
     }
-    tab[i].unit_begin = units;
+    tab[(size_t)j].unit_begin = units;
     units += (int64_t)L.tiles_x * L.tiles_y * m.desc.nz;
+    if (lanes[(size_t)i] == 32) {
+      ++n_wide;
+      units_wide = units;
+    }
     e->heat_smem = L.smem;
   }
   e->heat_tma = tma;
   e->heat_units = units;
+  e->heat_n_wide = n_wide;
+  e->heat_units_wide = units_wide;
+  e->heat_mixed = n_wide > 0 && n_wide < e->n_heat;
+  e->heat_lanes = n_wide > 0 ? 32 : 16;
   bytes.resize(tab.size() * sizeof(HeatBatchInst<T>));
   std::memcpy(bytes.data(), tab.data(), bytes.size());
   return ADV_OK;
@@ -183,9 +209,17 @@ adv_status launch_heat_slot(adv_ensemble* e, int slot, const int* active, cudaSt
   const void* tab = e->heat_tab;
   int n = e->n_heat;
   int64_t units = e->heat_units;
-  void* args[] = {&tab, &n, &units, &slot, &active};
-  const dim3 block((unsigned)e->heat_lanes, (unsigned)(32 * e->heat_warps / e->heat_lanes), 1);
-  ADV_CUDA_TRY(cudaLaunchKernel(e->heat_k[slot], dim3((unsigned)e->heat_ctas), block, args, e->heat_smem, s));
+  if (e->heat_mixed) {
+    int n_wide = e->heat_n_wide, ctas_wide = e->heat_ctas_wide;
+    int64_t units_wide = e->heat_units_wide;
+    void* args[] = {&tab, &n_wide, &n, &units_wide, &units, &ctas_wide, &slot, &active};
+    ADV_CUDA_TRY(cudaLaunchKernel(e->heat_k[slot], dim3((unsigned)e->heat_ctas), dim3(128, 1, 1), args, e->heat_smem,
+                                  s));
+  } else {
+    void* args[] = {&tab, &n, &units, &slot, &active};
+    const dim3 block((unsigned)e->heat_lanes, (unsigned)(32 * e->heat_warps / e->heat_lanes), 1);
+    ADV_CUDA_TRY(cudaLaunchKernel(e->heat_k[slot], dim3((unsigned)e->heat_ctas), block, args, e->heat_smem, s));
+  }
   count_launches(1);
   return ADV_OK;
 }
@@ -339,9 +373,8 @@ adv_status create_impl(const adv_heat_member* heat, int n_heat, int scheme, cons
 
   if (n_heat > 0) {
     std::vector<unsigned char> bytes;
-    // the 4-row tile when every member's stage takes it (FP32 O2 with TMA loads), else 2 rows.
-    // Rows of 32 lanes: measured faster on a mixed-size ensemble than rows of 16 even where those
-    // leave fewer lanes idle (a single grid picks per its width).
+    // the 4-row tile when every member's stage takes it (FP32 O2 with TMA loads; rows of 32 or 16
+    // lanes per member), else 2 rows of 32 lanes.
     e->heat_rows = 4;
     e->heat_warps = 4;
     e->heat_lanes = 32;
@@ -356,8 +389,10 @@ adv_status create_impl(const adv_heat_member* heat, int n_heat, int scheme, cons
     if (st != ADV_OK) return st;
     ADV_CUDA_TRY(cudaMemcpy(e->heat_tab, bytes.data(), bytes.size(), cudaMemcpyHostToDevice));
     for (int k = 0; k < e->heat_slots; ++k) {
-      e->heat_k[k] = heat_batch_kernel_for(e->heat_dtype, e->heat_order, e->heat_tma,
-                                           scheme == ADV_EULER ? 1 : k + 1, e->heat_rows, e->heat_lanes);
+      const int sk = scheme == ADV_EULER ? 1 : k + 1;
+      e->heat_k[k] = e->heat_mixed ? heat_batch_mixed_kernel_for(sk)
+                                   : heat_batch_kernel_for(e->heat_dtype, e->heat_order, e->heat_tma, sk, e->heat_rows,
+                                                           e->heat_lanes);
       if (!e->heat_k[k]) return set_error(ADV_ERR_UNSUPPORTED, "ensemble: no batched heat kernel");
       ADV_CUDA_TRY(cudaFuncSetAttribute(e->heat_k[k], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->heat_smem));
     }
@@ -366,6 +401,13 @@ adv_status create_impl(const adv_heat_member* heat, int n_heat, int scheme, cons
     // two waves of equal shares instead of one: CTAs whose segments finish early leave their SM
     // to the second wave (measured 2-6% faster on the mixed-size ensemble)
     e->heat_ctas = (int)std::max<int64_t>(1, std::min<int64_t>(2 * (int64_t)e->heat_ctas, e->heat_units / 4));
+    if (e->heat_mixed) {
+      // CTAs per width group in proportion to its units (a unit costs the same in both), at
+      // least one each
+      e->heat_ctas = std::max(e->heat_ctas, 2);
+      const double f = (double)e->heat_units_wide / (double)e->heat_units;
+      e->heat_ctas_wide = std::min(e->heat_ctas - 1, std::max(1, (int)std::lround(f * e->heat_ctas)));
+    }
   }
   if (n_burgers > 0) {
     std::vector<unsigned char> bytes[3];

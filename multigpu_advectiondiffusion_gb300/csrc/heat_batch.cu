@@ -45,6 +45,16 @@ void* heat_batch_kernel_for(int dtype, int order, bool tma, int stage_kind, int 
   return nullptr;
 }
 
+// The two-width kernel (4-row FP32 O2 tiles of 128 and 64 nodes, TMA loads) for stage 1..3.
+void* heat_batch_mixed_kernel_for(int stage_kind) {
+  switch (stage_kind) {
+    case 1: return reinterpret_cast<void*>(&heat_batch_mixed_kernel<1>);
+    case 2: return reinterpret_cast<void*>(&heat_batch_mixed_kernel<2>);
+    case 3: return reinterpret_cast<void*>(&heat_batch_mixed_kernel<3>);
+    default: return nullptr;
+  }
+}
+
 size_t heat_batch_inst_bytes(int dtype) {
   return dtype == ADV_F32 ? sizeof(HeatBatchInst<float>) : sizeof(HeatBatchInst<double>);
 }

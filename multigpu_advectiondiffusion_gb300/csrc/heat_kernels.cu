@@ -60,6 +60,9 @@ int heat_tune_variant(const adv_heat_desc& d) {
 // Fraction of a row's lanes that hold grid nodes when rows of nx nodes are cut into tiles bx wide.
 static double tile_use(int nx, int bx) { return (double)nx / ((double)((nx + bx - 1) / bx) * bx); }
 
+// rows of 16 lanes (tile 64 wide) where they waste clearly fewer lanes than rows of 32
+int heat_row_lanes(int nx) { return tile_use(nx, 64) > tile_use(nx, 128) + 0.02 ? 16 : 32; }
+
 adv_status heat_prepare(const adv_heat_desc& d, const void* u_in, HeatLaunch* L, int rows, int lanes) {
   DeviceInfo di;
   adv_status st = device_info(&di);
@@ -76,8 +79,7 @@ adv_status heat_prepare(const adv_heat_desc& d, const void* u_in, HeatLaunch* L,
   if (rows == 4 && !rows4_ok) return set_error(ADV_ERR_UNSUPPORTED, "heat: 4 rows per thread need FP32 3D O2 with TMA");
   L->rows = rows == 0 ? (rows4_ok ? 4 : 2) : rows;
   L->warps = L->rows == 4 ? 4 : 8;
-  // rows of 16 lanes (tile 64 wide) where they waste clearly fewer lanes than rows of 32
-  L->lanes = L->rows == 4 ? (lanes != 0 ? lanes : (tile_use(d.nx, 64) > tile_use(d.nx, 128) + 0.02 ? 16 : 32)) : 32;
+  L->lanes = L->rows == 4 ? (lanes != 0 ? lanes : heat_row_lanes(d.nx)) : 32;
   int bx, by, sw, sh, padx, r;
   size_t smem;
   tile_for(d.dtype, d.order, d.ndim, L->rows, L->lanes, &bx, &by, &sw, &sh, &padx, &r, &smem);

@@ -203,7 +203,10 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
   int* abort_flag = heat_abort_flag();
   int s_issue = pipe.s_issue, s_wait = pipe.s_wait;
   unsigned parity = pipe.parity;
-  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * C::TX + tx;
+  // thread coordinates in the tile from the linear thread index: a (TX, TY) block or a 1D block
+  // of the same size (the mixed-width batched kernel) give the same layout
+  const int tid = threadIdx.y * C::TX + threadIdx.x;
+  const int tx = (int)((unsigned)tid % C::TX), ty = (int)((unsigned)tid / C::TX);
   const int nx = p.nx, ny = p.ny, nz = p.nz;
   const size_t sxy = (size_t)nx * ny;
   const int stage = STAGE == 0 ? p.stage : STAGE;
@@ -562,28 +565,15 @@ struct alignas(64) HeatBatchInst {
   int64_t pad[7];
 };
 
-// Batched stage over many 3D instances (slot `slot` of each): the units (instance, tile,
-// z-plane) of all instances, instance-major then tile-major, are cut into gridDim.x equal
-// contiguous ranges. Returns at once when *active == 0 (predicated steps of a device-driven
-// loop).
-template <class T, int ORDER, bool TMA, int STAGE, int ROWS = 2, int WARPS = 8, int LANES = 32>
-__global__ void __launch_bounds__(32 * WARPS, heat_min_ctas<T, ORDER, ROWS, WARPS>())
-heat_batch_kernel(const HeatBatchInst<T>* __restrict__ inst, int n_inst, int64_t total_units, int slot,
-                  const int* active) {
+// A CTA's share of a batched stage: units [u0 + units*cta/ctas, u0 + units*(cta+1)/ctas) of the
+// instances inst[0 .. n_inst), whose units (instance, tile, z-plane), instance-major then
+// tile-major, run from u0 (inst[0].unit_begin) to u0 + units.
+template <class T, int ORDER, bool TMA, int STAGE, int ROWS, int WARPS, int LANES>
+__device__ __forceinline__ void heat_batch_share(const HeatBatchInst<T>* __restrict__ inst, int n_inst, int64_t u0,
+                                                 int64_t units, int cta, int ctas, int slot) {
   using C = HeatTile<T, ORDER, 3, ROWS, WARPS, LANES>;
-  if (active && *active == 0) return;
-  uint64_t* bars = heat_bars<T, ORDER, 3>();
-  int& abort_flag = *heat_abort_flag();
   const int tid = threadIdx.y * C::TX + threadIdx.x;
-  const int64_t seg_a = total_units * blockIdx.x / gridDim.x, seg_b = total_units * (blockIdx.x + 1) / gridDim.x;
-  if (tid == 0) {
-    if (TMA) {
-      for (int s = 0; s < C::NS; ++s) mbar_init(&bars[s], 1);
-      mbar_fence_init();
-    }
-    abort_flag = 0;
-  }
-  __syncthreads();
+  const int64_t seg_a = u0 + units * cta / ctas, seg_b = u0 + units * (cta + 1) / ctas;
   HeatPipe pipe{0, 0, 0u};
   // instance of the first unit (binary search on unit_begin)
   int i = 0;
@@ -599,7 +589,7 @@ heat_batch_kernel(const HeatBatchInst<T>* __restrict__ inst, int n_inst, int64_t
     while (i + 1 < n_inst && inst[i + 1].unit_begin <= pos) ++i;
     const HeatParams<T> p = inst[i].p[slot];  // a copy: registers, not reloads from the table
     const int64_t local = pos - inst[i].unit_begin;
-    const int64_t inst_end = i + 1 < n_inst ? inst[i + 1].unit_begin : total_units;
+    const int64_t inst_end = i + 1 < n_inst ? inst[i + 1].unit_begin : u0 + units;
     const int64_t tile = local / p.nz;
     const int zs = (int)(local - tile * p.nz);
     const int64_t stop = min(seg_b, inst_end);
@@ -611,6 +601,54 @@ heat_batch_kernel(const HeatBatchInst<T>* __restrict__ inst, int n_inst, int64_t
     pipe = heat_segment<T, ORDER, 3, TMA, STAGE, ROWS, WARPS, LANES>(tm, p, x0, y0, zs, ze, pipe);
     if (pipe.s_issue < 0) return;
   }
+}
+
+template <class T, int ORDER, bool TMA>
+__device__ __forceinline__ void heat_batch_prologue() {
+  uint64_t* bars = heat_bars<T, ORDER, 3>();
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    if (TMA) {
+      for (int s = 0; s < HeatTile<T, ORDER, 3>::NS; ++s) mbar_init(&bars[s], 1);
+      mbar_fence_init();
+    }
+    *heat_abort_flag() = 0;
+  }
+  __syncthreads();
+}
+
+// Batched stage over many 3D instances (slot `slot` of each): the units (instance, tile,
+// z-plane) of all instances, instance-major then tile-major, are cut into gridDim.x equal
+// contiguous ranges. Returns at once when *active == 0 (predicated steps of a device-driven
+// loop).
+template <class T, int ORDER, bool TMA, int STAGE, int ROWS = 2, int WARPS = 8, int LANES = 32>
+__global__ void __launch_bounds__(32 * WARPS, heat_min_ctas<T, ORDER, ROWS, WARPS>())
+heat_batch_kernel(const HeatBatchInst<T>* __restrict__ inst, int n_inst, int64_t total_units, int slot,
+                  const int* active) {
+  if (active && *active == 0) return;
+  heat_batch_prologue<T, ORDER, TMA>();
+  heat_batch_share<T, ORDER, TMA, STAGE, ROWS, WARPS, LANES>(inst, n_inst, 0, total_units, blockIdx.x, gridDim.x,
+                                                           slot);
+}
+
+// Batched stage over instances of two tile widths (FP32 O2, TMA loads, 4 rows per thread, 4
+// warps, one-dimensional blocks of 128 threads): instances [0, n_wide) in 128-wide tiles (rows
+// of 32 lanes), [n_wide, n_inst) in 64-wide tiles (rows of 16 lanes), each member in the width
+// that leaves fewer lanes idle on its rows. CTAs [0, ctas_wide) share the first group's units
+// [0, units_wide), the others the second group's. Both tiles hold the same number of nodes and
+// take the same ring (same shared memory), so a unit costs the same in either group.
+template <int STAGE>
+__global__ void __launch_bounds__(128, heat_min_ctas<float, 2, 4, 4>())
+heat_batch_mixed_kernel(const HeatBatchInst<float>* __restrict__ inst, int n_wide, int n_inst, int64_t units_wide,
+                        int64_t total_units, int ctas_wide, int slot, const int* active) {
+  static_assert(HeatTile<float, 2, 3, 4, 4, 32>::SMEM == HeatTile<float, 2, 3, 4, 4, 16>::SMEM, "same ring");
+  if (active && *active == 0) return;
+  heat_batch_prologue<float, 2, true>();
+  if ((int)blockIdx.x < ctas_wide)
+    heat_batch_share<float, 2, true, STAGE, 4, 4, 32>(inst, n_wide, 0, units_wide, blockIdx.x, ctas_wide, slot);
+  else
+    heat_batch_share<float, 2, true, STAGE, 4, 4, 16>(inst + n_wide, n_inst - n_wide, units_wide,
+                                                      total_units - units_wide, blockIdx.x - ctas_wide,
+                                                      gridDim.x - ctas_wide, slot);
 }
 
 }  // namespace adv

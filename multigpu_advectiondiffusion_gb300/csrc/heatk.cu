@@ -477,30 +477,32 @@ adv_status adv_heatk_forward(const adv_heatk_desc* d, const void* k, void* u, in
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const size_t one = array_bytes(*d);
   const size_t nb = (size_t)d->nx * d->ny * d->nz * (d->dtype == ADV_F32 ? 4 : 8);
-  char* a = static_cast<char*>(u);
-  char* b = static_cast<char*>(work);
-  // With checkpoints, the last interval runs from its checkpoint through work's slots (the states
-  // u^{n0+1} .. u^{nsteps-1}, where adv_heatk_backward would recompute them) into u.
+  char* const ub = static_cast<char*>(u);
+  char* const wb = static_cast<char*>(work);
+  char* const cb = static_cast<char*>(ckpt);
+  // A step whose result is a checkpoint writes it into its slot (only u^0 is copied), so storing
+  // checkpoints costs no traffic beyond the steps themselves; with interval 1 every state is kept
+  // and the backward run recomputes nothing. The last interval runs from its checkpoint through
+  // work's slots (the states u^{n0+1} .. u^{nsteps-1}, where adv_heatk_backward would recompute
+  // them) into u.
   const int64_t m = (nsteps + interval - 1) / interval;
   const int64_t n_last = ckpt && nsteps > 0 ? (m - 1) * interval : nsteps;
+  const char* src = ub;
+  if (ckpt && nsteps > 0) ADV_CUDA_TRY(cudaMemcpyAsync(cb, ub, nb, cudaMemcpyDeviceToDevice, s));
   for (int64_t n = 0; n < n_last; ++n) {
-    if (ckpt && n % interval == 0)
-      ADV_CUDA_TRY(cudaMemcpyAsync(static_cast<char*>(ckpt) + (n / interval) * one, a, nb, cudaMemcpyDeviceToDevice, s));
-    if ((st = heatk_step_launch(*d, k, a, b, s)) != ADV_OK) return st;
-    std::swap(a, b);
+    char* dst = ckpt && (n + 1) % interval == 0 ? cb + ((n + 1) / interval) * one : (src == ub ? wb : ub);
+    if ((st = heatk_step_launch(*d, k, src, dst, s)) != ADV_OK) return st;
+    src = dst;
   }
   if (n_last < nsteps) {
-    char* c = static_cast<char*>(ckpt) + (m - 1) * one;
-    ADV_CUDA_TRY(cudaMemcpyAsync(c, a, nb, cudaMemcpyDeviceToDevice, s));
-    const char* src = c;
-    char* states = static_cast<char*>(work);
+    src = cb + (m - 1) * one;  // u^{n_last}: the copy of u^0 or the step that wrote it there
     for (int64_t n = n_last; n < nsteps; ++n) {
-      char* dst = n + 1 < nsteps ? states + (n - n_last) * one : static_cast<char*>(u);
+      char* dst = n + 1 < nsteps ? wb + (n - n_last) * one : ub;
       if ((st = heatk_step_launch(*d, k, src, dst, s)) != ADV_OK) return st;
       src = dst;
     }
-  } else if (a != static_cast<char*>(u)) {
-    ADV_CUDA_TRY(cudaMemcpyAsync(u, a, nb, cudaMemcpyDeviceToDevice, s));
+  } else if (src != ub) {
+    ADV_CUDA_TRY(cudaMemcpyAsync(ub, src, nb, cudaMemcpyDeviceToDevice, s));
   }
   return ADV_OK;
 }

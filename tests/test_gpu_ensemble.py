@@ -3,8 +3,9 @@
 Every member of an ensemble must end bit for bit where adv_heat_run / adv_burgers_run would take
 it on its own (same stage kernels' arithmetic, same per-member dt and Lax-Friedrichs constants,
 same stop test), whether the run goes through the ensemble's CUDA graph or through direct
-launches, with uneven member sizes, with members whose rows TMA cannot describe (the whole batch
-then takes the cp.async path), and with heat and Burgers members running concurrently.
+launches, with uneven member sizes, with FP32 heat members in tiles of two widths in one launch,
+with members whose rows TMA cannot describe (the whole batch then takes the cp.async path), and
+with heat and Burgers members running concurrently.
 """
 import ctypes as C
 
@@ -46,13 +47,17 @@ def _burgers_state(cfg, dtype, seed, cuda):
 HEAT_SETS = {
     "aligned": [(64, 48, 40), (96, 96, 96), (36, 20, 70), (128, 64, 33), (8, 8, 9)],
     "unaligned": [(64, 48, 40), (37, 29, 31), (96, 40, 17)],  # nx = 37: 148-byte rows
+    # FP32 members in 128-wide tiles (nx 128, 96) and 64-wide tiles (nx 160, 64, 192, 40): one
+    # launch runs both widths (heat_batch_mixed_kernel), the table reordered by width
+    "widths": [(160, 24, 20), (64, 40, 17), (128, 33, 12), (192, 20, 9), (40, 16, 30), (96, 20, 11)],
+    "narrow": [(64, 40, 17), (40, 16, 30), (192, 20, 9)],  # 64-wide tiles only
 }
 
 
 @pytest.mark.parametrize("direct", [False, True], ids=["graph", "direct"])
 @pytest.mark.parametrize("scheme,steps", [(N.ADV_EULER, 7), (N.ADV_EULER, 6), (N.ADV_SSPRK3, 4)],
                          ids=["euler-odd", "euler-even", "rk3"])
-@pytest.mark.parametrize("sizes", ["aligned", "unaligned"])
+@pytest.mark.parametrize("sizes", ["aligned", "unaligned", "widths", "narrow"])
 @pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f32", "f64"])
 def test_heat_ensemble_matches_per_member_runs(cuda, native, dtype, sizes, scheme, steps, direct):
     rng = np.random.default_rng(5)
