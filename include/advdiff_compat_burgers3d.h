@@ -2,7 +2,11 @@
  * advdiff_compat_burgers3d.h -- the reference's 3D Burgers launch wrappers (REAL = double),
  * exported by libadvdiff_compat_burgers3d.so so SingleGPU/Burgers3d_WENO5/main.cpp links
  * unchanged. Define ADV_COMPAT_PITCHED for SingleGPU/Burgers3d_WENO5_PitchedMem's signatures
- * (libadvdiff_compat_burgers3d_pitched.so).
+ * (libadvdiff_compat_burgers3d_pitched.so). libadvdiff_compat_burgers3d_sharedmem.so has the same
+ * pitched signatures for SingleGPU/Burgers3d_WENO5_SharedMem (Burgers.h:79-83), its Call_Adv_*
+ * being that program's sweeps (adv_ref_burgers_sweep_all: every node, zero beyond the grid,
+ * reciprocal weight normalisation; kernels.cu:212-405, 552-568); its Call_Diff_ and Call_sspRK are
+ * the baseline's (the kernels are the same, kernels.cu:453-543).
  *
  *   CopyToConstantMemory <- Burgers.h:72 (kernels.cu:535-540): viscous constants C/(12 h^2)
  *   Call_Adv_x           <- Burgers.h:73 (kernels.cu:542-546): Lu  = -dF/dx (WENO5-Z, local LF)

@@ -3,7 +3,9 @@
  * names and signatures (REAL = double) by libadvdiff_compat_heat3d.so, so the reference's
  * SingleGPU/Diffusion3d_baselineCode/main.cpp links against this library unchanged.
  * Define ADV_COMPAT_PITCHED for the pitched signatures of SingleGPU/Diffusion3d_PitchedMem
- * (libadvdiff_compat_heat3d_pitched.so).
+ * (libadvdiff_compat_heat3d_pitched.so), ADV_COMPAT_BLOCKING for SingleGPU/Diffusion3d_Blocking
+ * (libadvdiff_compat_heat3d_blocking.so: the same pitched signatures, acoustics3d.h:58-60; its
+ * Call_Lu3d writes i, j in [3, n-4] and k in [3, nz-3], kernels.cu:37-88 and 167-171).
  *
  *   CopyToConstantMemory <- acoustics3d.h:57 (kernels.cu:147-152)
  *   Call_Lu3d            <- acoustics3d.h:58 (kernels.cu:154-158): O4 Laplacian, nodes 2..n-3
@@ -21,7 +23,7 @@
 extern "C" {
 #endif
 void CopyToConstantMemory(double kx, double ky, double kz);
-#ifndef ADV_COMPAT_PITCHED
+#if !defined(ADV_COMPAT_PITCHED) && !defined(ADV_COMPAT_BLOCKING)
 void Call_Lu3d(dim3 numBlocks, dim3 threadsPerBlock, cudaStream_t aStream, unsigned int nx, unsigned int ny,
                unsigned int nz, double* u, double* Lu);
 void Call_RK3d(dim3 numBlocks, dim3 threadsPerBlock, cudaStream_t aStream, unsigned int step, unsigned int nx,

@@ -144,6 +144,8 @@ SIGNATURES = [
     ("adv_ref_rk", _I, [_I, _I, _I, _I64, _I, _I, _I, _I, _D, _VP, _VP, _VP, _VP]),
     ("adv_ref_burgers_sweep", _I, [_I, _I, _I, _I64, _I, _I, _I, _D, _VP, _VP, _VP]),
     ("adv_ref_burgers_viscous", _I, [_I, _I64, _I, _I, _I, _D, _D, _D, _I, _VP, _VP, _VP]),
+    ("adv_ref_laplace_box", _I, [_I, _I, _I, _VP, _I, _I, _I64, _I, _I, _I, _D, _D, _D, _VP, _VP, _VP]),
+    ("adv_ref_burgers_sweep_all", _I, [_I, _I, _I, _I64, _I, _I, _I, _D, _VP, _VP, _VP]),
 ]
 
 

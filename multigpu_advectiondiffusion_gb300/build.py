@@ -42,6 +42,9 @@ COMPAT = {
     "libadvdiff_compat_heat2d_pitched.so": ("compat_heat2d.cpp", ["-DADV_COMPAT_PITCHED"]),
     "libadvdiff_compat_heat3d_pitched.so": ("compat_heat3d.cpp", ["-DADV_COMPAT_PITCHED"]),
     "libadvdiff_compat_burgers3d_pitched.so": ("compat_burgers3d.cpp", ["-DADV_COMPAT_PITCHED"]),
+    "libadvdiff_compat_heat3d_blocking.so": ("compat_heat3d.cpp", ["-DADV_COMPAT_BLOCKING"]),
+    "libadvdiff_compat_burgers3d_sharedmem.so": ("compat_burgers3d.cpp",
+                                                 ["-DADV_COMPAT_PITCHED", "-DADV_COMPAT_SHAREDMEM"]),
 }
 DRIVERS = {"heat2d": "drivers/heat2d_main.cpp", "heat3d": "drivers/heat3d_main.cpp",
            "burgers3d": "drivers/burgers3d_main.cpp", "burgers2d": "drivers/burgers2d_main.cpp"}

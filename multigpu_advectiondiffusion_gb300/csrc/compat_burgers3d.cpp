@@ -1,5 +1,6 @@
 // compat_burgers3d.cpp -- the reference's Burgers wrapper names over the reference-semantics
-// operators (include/advdiff_compat_burgers3d.h). ADV_COMPAT_PITCHED selects the pitched variant.
+// operators (include/advdiff_compat_burgers3d.h). ADV_COMPAT_PITCHED selects the pitched variant;
+// with ADV_COMPAT_SHAREDMEM as well, the shared-memory program's sweeps.
 #include "../../include/advdiff_compat_burgers3d.h"
 
 #include <atomic>
@@ -20,6 +21,12 @@ std::atomic<int> g_bug_b2{1};
 #define PITCH_VALUE pitch
 #endif
 
+#ifdef ADV_COMPAT_SHAREDMEM
+#define SWEEP adv_ref_burgers_sweep_all
+#else
+#define SWEEP adv_ref_burgers_sweep
+#endif
+
 extern "C" {
 
 void CopyToConstantMemory(double kx, double ky, double kz) {
@@ -30,15 +37,15 @@ void CopyToConstantMemory(double kx, double ky, double kz) {
 
 void Call_Adv_x(dim3, dim3, cudaStream_t s, PITCH_PARAM unsigned int Nx, unsigned int Ny, unsigned int Nz, double dx,
                 double* u, double* Lu) {
-  adv_compat::note(adv_ref_burgers_sweep(ADV_F64, 0, ADV_WENO5_Z, PITCH_VALUE, Nx, Ny, Nz, dx, u, Lu, s), "Call_Adv_x");
+  adv_compat::note(SWEEP(ADV_F64, 0, ADV_WENO5_Z, PITCH_VALUE, Nx, Ny, Nz, dx, u, Lu, s), "Call_Adv_x");
 }
 void Call_Adv_y(dim3, dim3, cudaStream_t s, PITCH_PARAM unsigned int Nx, unsigned int Ny, unsigned int Nz, double dy,
                 double* v, double* Lv) {
-  adv_compat::note(adv_ref_burgers_sweep(ADV_F64, 1, ADV_WENO5_Z, PITCH_VALUE, Nx, Ny, Nz, dy, v, Lv, s), "Call_Adv_y");
+  adv_compat::note(SWEEP(ADV_F64, 1, ADV_WENO5_Z, PITCH_VALUE, Nx, Ny, Nz, dy, v, Lv, s), "Call_Adv_y");
 }
 void Call_Adv_z(dim3, dim3, cudaStream_t s, PITCH_PARAM unsigned int Nx, unsigned int Ny, unsigned int Nz, double dz,
                 double* w, double* Lw) {
-  adv_compat::note(adv_ref_burgers_sweep(ADV_F64, 2, ADV_WENO5_Z, PITCH_VALUE, Nx, Ny, Nz, dz, w, Lw, s), "Call_Adv_z");
+  adv_compat::note(SWEEP(ADV_F64, 2, ADV_WENO5_Z, PITCH_VALUE, Nx, Ny, Nz, dz, w, Lw, s), "Call_Adv_z");
 }
 void Call_Diff_(dim3, dim3, cudaStream_t s, PITCH_PARAM unsigned int Nx, unsigned int Ny, unsigned int Nz, double* q,
                 double* Lq) {

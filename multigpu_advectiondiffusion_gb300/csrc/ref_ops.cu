@@ -27,15 +27,22 @@ struct Grid3 {
   __device__ __forceinline__ int64_t at(int i, int j, int k) const { return i + pitch * j + pitch * ny * (int64_t)k; }
 };
 
+// Nodes a Laplacian writes: i in [i0, i1), j in [j0, j1), k in [k0, k1).
+struct Box3 {
+  int i0, i1, j0, j1, k0, k1;
+};
+
+// west_first: the O4 operand order of the 2D kernel (west/south/bottom neighbours first), which
+// SG/Diffusion3d_Blocking/kernels.cu:66-68 and 78-80 also use in 3D; otherwise 3D takes the
+// baseline's east-first order.
 template <class T>
-__global__ void ref_laplace_kernel(Grid3 g, int ndim, int order, int lo, int zero_outside, T kx, T ky, T kz,
-                                   const T* __restrict__ u, T* __restrict__ Lu) {
+__global__ void ref_laplace_kernel(Grid3 g, int ndim, int order, Box3 b, int zero_outside, int west_first, T kx, T ky,
+                                   T kz, const T* __restrict__ u, T* __restrict__ Lu) {
   for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < g.count(); f += (int64_t)gridDim.x * blockDim.x) {
     int i, j, k;
     g.ijk(f, i, j, k);
     const int64_t o = g.at(i, j, k);
-    bool in = i >= lo && i < g.nx - lo && j >= lo && j < g.ny - lo;
-    if (ndim == 3) in = in && k >= lo && k < g.nz - lo;
+    const bool in = i >= b.i0 && i < b.i1 && j >= b.j0 && j < b.j1 && k >= b.k0 && k < b.k1;
     if (!in) {
       if (zero_outside) Lu[o] = T(0);
       continue;
@@ -44,7 +51,12 @@ __global__ void ref_laplace_kernel(Grid3 g, int ndim, int order, int lo, int zer
     const T c = u[o];
     T L;
     if (order == 4) {
-      if (ndim == 3) {  // east first (Diffusion3d_baselineCode/kernels.cu:95-97)
+      if (ndim == 3 && west_first) {
+        const T Sx = sub_rn(add_rn(sub_rn(add_rn(-u[o - 2], mul_rn(T(16), u[o - 1])), mul_rn(T(30), c)), mul_rn(T(16), u[o + 1])), u[o + 2]);
+        const T Sy = sub_rn(add_rn(sub_rn(add_rn(-u[o - 2 * sy], mul_rn(T(16), u[o - sy])), mul_rn(T(30), c)), mul_rn(T(16), u[o + sy])), u[o + 2 * sy]);
+        const T Sz = sub_rn(add_rn(sub_rn(add_rn(-u[o - 2 * sz], mul_rn(T(16), u[o - sz])), mul_rn(T(30), c)), mul_rn(T(16), u[o + sz])), u[o + 2 * sz]);
+        L = add_rn(add_rn(mul_rn(kx, Sx), mul_rn(ky, Sy)), mul_rn(kz, Sz));
+      } else if (ndim == 3) {  // east first (Diffusion3d_baselineCode/kernels.cu:95-97)
         const T Sx = sub_rn(add_rn(sub_rn(add_rn(-u[o + 2], mul_rn(T(16), u[o + 1])), mul_rn(T(30), c)), mul_rn(T(16), u[o - 1])), u[o - 2]);
         const T Sy = sub_rn(add_rn(sub_rn(add_rn(-u[o + 2 * sy], mul_rn(T(16), u[o + sy])), mul_rn(T(30), c)), mul_rn(T(16), u[o - sy])), u[o - 2 * sy]);
         const T Sz = sub_rn(add_rn(sub_rn(add_rn(-u[o + 2 * sz], mul_rn(T(16), u[o + sz])), mul_rn(T(30), c)), mul_rn(T(16), u[o - sz])), u[o - 2 * sz]);
@@ -128,6 +140,46 @@ __global__ void __launch_bounds__(256) ref_sweep_kernel(Grid3 g, int axis, T h, 
   }
 }
 
+// The shared-memory program's sweeps (Compute_dF / dG / dH,
+// SG/Burgers3d_WENO5_SharedMem/kernels.cu:212-405): every node of every line, u taken as 0 beyond
+// both ends of the line, face a-1/2 from nodes a-3 .. a+2 (the same local Lax-Friedrichs split),
+// the weights normalised by a reciprocal (RECIP form of weno_face_ref). One thread per line walks
+// a upwards with a sliding window of six split values; each face is reconstructed once.
+template <class T, bool Z>
+__global__ void __launch_bounds__(256) ref_sweep_all_kernel(Grid3 g, int axis, T h, const T* __restrict__ u,
+                                                            T* __restrict__ Lu) {
+  const int na = axis == 0 ? g.nx : axis == 1 ? g.ny : g.nz;
+  const int nb = axis == 0 ? g.ny : g.nx, nc = axis == 2 ? g.ny : g.nz;
+  const int64_t s = axis == 0 ? 1 : axis == 1 ? g.pitch : g.pitch * g.ny;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < (int64_t)nb * nc;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int b = (int)(t % nb), c = (int)(t / nb);
+    const int i = axis == 0 ? 0 : b, j = axis == 0 ? b : (axis == 1 ? 0 : c), k = axis == 2 ? 0 : c;
+    const int64_t o0 = g.at(i, j, k);  // node a = 0 of this line
+    auto split = [&](int a, T& p, T& m) {
+      const T v = a >= 0 && a < na ? u[o0 + (int64_t)a * s] : T(0);
+      lf_split<T>(v, fabs(v), p, m);
+    };
+    T fp[6], fm[6];  // split values of nodes a-3 .. a+2 (face a-1/2)
+#pragma unroll
+    for (int q = 0; q < 6; ++q) split(q - 3, fp[q], fm[q]);
+    T f_left = weno_face_ref<Z, T, true>(fp[0], fp[1], fp[2], fp[3], fp[4], fm[1], fm[2], fm[3], fm[4], fm[5]);
+    for (int a = 0; a < na; ++a) {
+#pragma unroll
+      for (int q = 0; q < 5; ++q) {
+        fp[q] = fp[q + 1];
+        fm[q] = fm[q + 1];
+      }
+      split(a + 3, fp[5], fm[5]);  // window: nodes a-2 .. a+3 (face a+1/2)
+      const T f_right = weno_face_ref<Z, T, true>(fp[0], fp[1], fp[2], fp[3], fp[4], fm[1], fm[2], fm[3], fm[4], fm[5]);
+      const int64_t o = o0 + (int64_t)a * s;
+      if (axis == 0) Lu[o] = div_rn(-sub_rn(f_right, f_left), h);
+      else Lu[o] = sub_rn(Lu[o], div_rn(sub_rn(f_right, f_left), h));
+      f_left = f_right;
+    }
+  }
+}
+
 template <class T>
 __global__ void ref_viscous_kernel(Grid3 g, T kx, T ky, T kz, int bug_b2, const T* __restrict__ u, T* __restrict__ Lu) {
   for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < g.count(); f += (int64_t)gridDim.x * blockDim.x) {
@@ -166,6 +218,23 @@ using namespace adv;
 
 extern "C" {
 
+static adv_status ref_laplace_launch(int dtype, int ndim, int order, Box3 b, int zero_outside, int west_first,
+                                     int64_t pitch, int nx, int ny, int nz, double kx, double ky, double kz,
+                                     const void* u, void* Lu, void* stream) {
+  Grid3 g{nx, ny, nz, pitch};
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const dim3 grid = flat_grid((int64_t)nx * ny * nz);
+  if (dtype == ADV_F64)
+    ref_laplace_kernel<double><<<grid, 256, 0, s>>>(g, ndim, order, b, zero_outside, west_first, kx, ky, kz,
+                                                    (const double*)u, (double*)Lu);
+  else
+    ref_laplace_kernel<float><<<grid, 256, 0, s>>>(g, ndim, order, b, zero_outside, west_first, (float)kx, (float)ky,
+                                                   (float)kz, (const float*)u, (float*)Lu);
+  ADV_CUDA_TRY(cudaGetLastError());
+  count_launches(1);
+  return ADV_OK;
+}
+
 adv_status adv_ref_laplace(int dtype, int ndim, int order, int lo, int zero_outside, int64_t pitch, int nx, int ny, int nz,
                            double kx, double ky, double kz, const void* u, void* Lu, void* stream) {
   ADV_NVTX_RANGE("adv_ref_laplace");
@@ -174,17 +243,27 @@ adv_status adv_ref_laplace(int dtype, int ndim, int order, int lo, int zero_outs
   if (st != ADV_OK) return st;
   if ((ndim != 2 && ndim != 3) || (order != 2 && order != 4) || lo < order / 2)
     return set_error(ADV_ERR_INVALID_ARG, "ref_laplace: bad ndim/order/lo");
-  Grid3 g{nx, ny, nz, pitch};
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const dim3 grid = flat_grid((int64_t)nx * ny * nz);
-  if (dtype == ADV_F64)
-    ref_laplace_kernel<double><<<grid, 256, 0, s>>>(g, ndim, order, lo, zero_outside, kx, ky, kz, (const double*)u, (double*)Lu);
-  else
-    ref_laplace_kernel<float><<<grid, 256, 0, s>>>(g, ndim, order, lo, zero_outside, (float)kx, (float)ky, (float)kz,
-                                                   (const float*)u, (float*)Lu);
-  ADV_CUDA_TRY(cudaGetLastError());
-  count_launches(1);
-  return ADV_OK;
+  const Box3 b{lo, nx - lo, lo, ny - lo, ndim == 3 ? lo : 0, ndim == 3 ? nz - lo : 1};
+  return ref_laplace_launch(dtype, ndim, order, b, zero_outside, 0, pitch, nx, ny, nz, kx, ky, kz, u, Lu, stream);
+}
+
+adv_status adv_ref_laplace_box(int dtype, int ndim, int order, const int32_t* box, int zero_outside, int west_first,
+                               int64_t pitch, int nx, int ny, int nz, double kx, double ky, double kz, const void* u,
+                               void* Lu, void* stream) {
+  ADV_NVTX_RANGE("adv_ref_laplace_box");
+  if (ndim == 2) nz = 1;
+  adv_status st = check_grid(dtype, pitch, nx, ny, nz, u, Lu);
+  if (st != ADV_OK) return st;
+  if ((ndim != 2 && ndim != 3) || (order != 2 && order != 4) || !box || (west_first != 0 && west_first != 1))
+    return set_error(ADV_ERR_INVALID_ARG, "ref_laplace_box: bad ndim/order/box/west_first");
+  const int r = order / 2;
+  Box3 b{box[0], box[1], box[2], box[3], ndim == 3 ? box[4] : 0, ndim == 3 ? box[5] : 1};
+  // every stencil read stays on the grid: [i0, i1) within [r, nx - r), and so on
+  if (b.i0 < r || b.i1 > nx - r || b.j0 < r || b.j1 > ny - r || (ndim == 3 && (b.k0 < r || b.k1 > nz - r)))
+    return set_error(ADV_ERR_INVALID_ARG, "ref_laplace_box: box reaches past the stencil's margin");
+  // 2D has one operand order (west first); west_first only selects the 3D one
+  return ref_laplace_launch(dtype, ndim, order, b, zero_outside, west_first, pitch, nx, ny, nz, kx, ky, kz, u, Lu,
+                            stream);
 }
 
 adv_status adv_ref_rk(int dtype, int ndim, int lo, int64_t pitch, int nx, int ny, int nz, int step, double dt, void* u,
@@ -225,6 +304,30 @@ adv_status adv_ref_burgers_sweep(int dtype, int axis, int weno, int64_t pitch, i
   } else {
     if (z) ref_sweep_kernel<float, true><<<grid, 256, 0, s>>>(g, axis, (float)h, (const float*)u, (float*)Lu);
     else ref_sweep_kernel<float, false><<<grid, 256, 0, s>>>(g, axis, (float)h, (const float*)u, (float*)Lu);
+  }
+  ADV_CUDA_TRY(cudaGetLastError());
+  count_launches(1);
+  return ADV_OK;
+}
+
+adv_status adv_ref_burgers_sweep_all(int dtype, int axis, int weno, int64_t pitch, int nx, int ny, int nz, double h,
+                                     const void* u, void* Lu, void* stream) {
+  ADV_NVTX_RANGE("adv_ref_burgers_sweep_all");
+  adv_status st = check_grid(dtype, pitch, nx, ny, nz, u, Lu);
+  if (st != ADV_OK) return st;
+  if (axis < 0 || axis > 2 || (weno != ADV_WENO5_JS && weno != ADV_WENO5_Z) || !(h != 0.0))
+    return set_error(ADV_ERR_INVALID_ARG, "ref_burgers_sweep_all: bad arguments");
+  Grid3 g{nx, ny, nz, pitch};
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int nb = axis == 0 ? ny : nx, nc = axis == 2 ? ny : nz;
+  const dim3 grid = flat_grid((int64_t)nb * nc);  // one thread per line
+  const bool z = weno == ADV_WENO5_Z;
+  if (dtype == ADV_F64) {
+    if (z) ref_sweep_all_kernel<double, true><<<grid, 256, 0, s>>>(g, axis, h, (const double*)u, (double*)Lu);
+    else ref_sweep_all_kernel<double, false><<<grid, 256, 0, s>>>(g, axis, h, (const double*)u, (double*)Lu);
+  } else {
+    if (z) ref_sweep_all_kernel<float, true><<<grid, 256, 0, s>>>(g, axis, (float)h, (const float*)u, (float*)Lu);
+    else ref_sweep_all_kernel<float, false><<<grid, 256, 0, s>>>(g, axis, (float)h, (const float*)u, (float*)Lu);
   }
   ADV_CUDA_TRY(cudaGetLastError());
   count_launches(1);

@@ -187,7 +187,9 @@ __device__ __forceinline__ void lf_split_fast64(double u, double a, double& fp, 
 
 // ---------------------------------------------------------- reference literal form
 // Operand order of kernels.cu:142-192 / :92-140 (and of the CPU oracle), correctly rounded.
-template <bool Z, class T>
+// RECIP: the normalisation of SingleGPU/Burgers3d_WENO5_SharedMem/kernels.cu:51-198, which takes
+// alphasum = 1/(a0 + a1 + a2) and multiplies by (1/6)*alphasum instead of dividing by 6*alphasum.
+template <bool Z, class T, bool RECIP = false>
 __device__ __forceinline__ T weno_face_ref(T vmm, T vm, T v, T vp, T vpp, T umm, T um, T u, T up, T upp) {
   const T c1312 = T(13. / 12.), c14 = T(1. / 4.), eps = T(1e-6);
   auto beta = [&](T a, T b, T c, T d, T e, T& B0, T& B1, T& B2) {
@@ -220,7 +222,10 @@ __device__ __forceinline__ T weno_face_ref(T vmm, T vm, T v, T vp, T vpp, T umm,
   const T q0m = add_rn(sub_rn(mul_rn(T(2), vmm), mul_rn(T(7), vm)), mul_rn(T(11), v));
   const T q1m = add_rn(add_rn(-vm, mul_rn(T(5), v)), mul_rn(T(2), vp));
   const T q2m = sub_rn(add_rn(mul_rn(T(2), v), mul_rn(T(5), vp)), vpp);
-  const T fm = div_rn(add_rn(add_rn(mul_rn(a0, q0m), mul_rn(a1, q1m)), mul_rn(a2, q2m)), mul_rn(T(6), asum));
+  auto normalise = [&](T num, T sum) {
+    return RECIP ? mul_rn(num, mul_rn(T(1. / 6.), div_rn(T(1), sum))) : div_rn(num, mul_rn(T(6), sum));
+  };
+  const T fm = normalise(add_rn(add_rn(mul_rn(a0, q0m), mul_rn(a1, q1m)), mul_rn(a2, q2m)), asum);
 
   beta(umm, um, u, up, upp, B0, B1, B2);
   weights(B0, B1, B2, T(3. / 10.), T(6. / 10.), T(1. / 10.), a0, a1, a2);
@@ -228,7 +233,7 @@ __device__ __forceinline__ T weno_face_ref(T vmm, T vm, T v, T vp, T vpp, T umm,
   const T q0p = add_rn(add_rn(-umm, mul_rn(T(5), um)), mul_rn(T(2), u));
   const T q1p = sub_rn(add_rn(mul_rn(T(2), um), mul_rn(T(5), u)), up);
   const T q2p = add_rn(sub_rn(mul_rn(T(11), u), mul_rn(T(7), up)), mul_rn(T(2), upp));
-  const T fp = div_rn(add_rn(add_rn(mul_rn(a0, q0p), mul_rn(a1, q1p)), mul_rn(a2, q2p)), mul_rn(T(6), asum));
+  const T fp = normalise(add_rn(add_rn(mul_rn(a0, q0p), mul_rn(a1, q1p)), mul_rn(a2, q2p)), asum);
   return add_rn(fm, fp);
 }
 

@@ -224,6 +224,41 @@ void heat_run(const HeatCfg& c, int time, int64_t nsteps, T* u) {
   }
 }
 
+// The z-blocked heat program's loop (SingleGPU/Diffusion3d_Blocking/main.cpp:101-123): Lu zeroed
+// once; per SSP-RK3 stage the O4 Laplacian on i, j in [3, n-4] and k in
+// [3, nz-3] (kernels.cu:37-88 with kstart 3, kstop nz-2, wrappers :167-171), then the stage update
+// in place on every index in [2, n-3] (kernels.cu:93-126). Nodes of the update range outside the
+// Laplacian's keep Lu = 0.
+template <class T>
+void heat_blocking_run(int64_t nx, int64_t ny, int64_t nz, T kx, T ky, T kz, T dt, int64_t iters, T* u) {
+  const int64_t sz = nx * ny, n = sz * nz;
+  std::vector<T> uo(n), Lu(n, (T)0);
+  for (int64_t it = 0; it < iters; ++it) {
+    std::memcpy(uo.data(), u, n * sizeof(T));
+    for (int stage = 1; stage <= 3; ++stage) {
+#pragma omp parallel for collapse(2) schedule(static)
+      for (int64_t k = 3; k < nz - 2; ++k)
+        for (int64_t j = 3; j < ny - 3; ++j)
+          for (int64_t i = 3; i < nx - 3; ++i) {
+            const int64_t o = i + nx * j + sz * k;
+            const T c = u[o];
+            // west/south/bottom first (kernels.cu:66-68, 78-80), unlike the baseline's 3D kernel
+            T Sx = -u[o - 2] + (T)16 * u[o - 1] - (T)30 * c + (T)16 * u[o + 1] - u[o + 2];
+            T Sy = -u[o - 2 * nx] + (T)16 * u[o - nx] - (T)30 * c + (T)16 * u[o + nx] - u[o + 2 * nx];
+            T Sz = -u[o - 2 * sz] + (T)16 * u[o - sz] - (T)30 * c + (T)16 * u[o + sz] - u[o + 2 * sz];
+            Lu[o] = kx * Sx + ky * Sy + kz * Sz;
+          }
+#pragma omp parallel for collapse(2) schedule(static)
+      for (int64_t k = 2; k < nz - 2; ++k)
+        for (int64_t j = 2; j < ny - 2; ++j)
+          for (int64_t i = 2; i < nx - 2; ++i) {
+            const int64_t o = i + nx * j + sz * k;
+            u[o] = stage_combine<T>(stage, uo[o], u[o], dt, Lu[o]);
+          }
+    }
+  }
+}
+
 // ------------------------------------------------------------------------------------------
 // Burgers. Flux f = u^2/2 (SingleGPU/Burgers3d_WENO5/kernels.cu:37-40), Lax-Friedrichs split
 // f+- = (f +- a u)/2 (kernels.cu:224-238; a = |u| local, or a = max|u| global as in
@@ -232,8 +267,10 @@ void heat_run(const HeatCfg& c, int time, int64_t nsteps, T* u) {
 // WENO5-JS as kernels.cu:92-140 (= MultiGPU/Burgers3d_Baseline/Kernels.cu:112-222).
 // The divisions of the smoothness-indicator weights run in type D.
 // ------------------------------------------------------------------------------------------
+// recip: the shared-memory program's normalisation (SingleGPU/Burgers3d_WENO5_SharedMem/
+// kernels.cu:119-129, 143-146): alphasum = 1/(a0+a1+a2), the weighted sum times (1/6)*alphasum.
 template <class T, class D>
-inline T weno_face(int z, T vmm, T vm, T v, T vp, T vpp, T umm, T um, T u, T up, T upp) {
+inline T weno_face(int z, T vmm, T vm, T v, T vp, T vpp, T umm, T um, T u, T up, T upp, int recip = 0) {
   const T c1312 = (T)(13. / 12.), c14 = (T)(1. / 4.);
   const D eps = (D)1e-6;
   T B0 = c1312 * (vmm - (T)2 * vm + v) * (vmm - (T)2 * vm + v) + c14 * (vmm - (T)4 * vm + (T)3 * v) * (vmm - (T)4 * vm + (T)3 * v);
@@ -251,8 +288,10 @@ inline T weno_face(int z, T vmm, T vm, T v, T vp, T vpp, T umm, T um, T u, T up,
     a2 = (D)(3. / 10.) / ((eps + (D)B2) * (eps + (D)B2));
   }
   D asum = a0 + a1 + a2;
-  D fm = (a0 * (D)((T)2 * vmm - (T)7 * vm + (T)11 * v) + a1 * (D)(-vm + (T)5 * v + (T)2 * vp) +
-          a2 * (D)((T)2 * v + (T)5 * vp - vpp)) / ((D)6 * asum);
+  auto normalise = [&](D num, D sum) { return recip ? num * ((D)(1. / 6.) * ((D)1 / sum)) : num / ((D)6 * sum); };
+  D fm = normalise(a0 * (D)((T)2 * vmm - (T)7 * vm + (T)11 * v) + a1 * (D)(-vm + (T)5 * v + (T)2 * vp) +
+                       a2 * (D)((T)2 * v + (T)5 * vp - vpp),
+                   asum);
 
   B0 = c1312 * (umm - (T)2 * um + u) * (umm - (T)2 * um + u) + c14 * (umm - (T)4 * um + (T)3 * u) * (umm - (T)4 * um + (T)3 * u);
   B1 = c1312 * (um - (T)2 * u + up) * (um - (T)2 * u + up) + c14 * (um - up) * (um - up);
@@ -268,8 +307,9 @@ inline T weno_face(int z, T vmm, T vm, T v, T vp, T vpp, T umm, T um, T u, T up,
     a2 = (D)(1. / 10.) / ((eps + (D)B2) * (eps + (D)B2));
   }
   asum = a0 + a1 + a2;
-  D fp = (a0 * (D)(-umm + (T)5 * um + (T)2 * u) + a1 * (D)((T)2 * um + (T)5 * u - up) +
-          a2 * (D)((T)11 * u - (T)7 * up + (T)2 * upp)) / ((D)6 * asum);
+  D fp = normalise(a0 * (D)(-umm + (T)5 * um + (T)2 * u) + a1 * (D)((T)2 * um + (T)5 * u - up) +
+                       a2 * (D)((T)11 * u - (T)7 * up + (T)2 * upp),
+                   asum);
   return (T)fm + (T)fp;
 }
 
@@ -281,6 +321,7 @@ struct BurgersCfg {
   int bug_b2;     // reproduce the doubled viscous slabs 16..18 of the reference
   double dx, dy, dz;
   double kx, ky, kz;  // viscous O4 coefficients C/(12 h^2); 0 disables the term
+  int recip = 0;      // 1: the shared-memory program's weight normalisation (weno_face)
 };
 
 template <class T>
@@ -296,7 +337,37 @@ template <class T, class D, class G>
 inline T face_flux(const BurgersCfg& c, T a_glob, G get) {
   T fp[6], fm[6];
   for (int q = 0; q < 6; ++q) lf_split<T>(get(q - 2), a_glob, c.lf_global, &fp[q], &fm[q]);
-  return weno_face<T, D>(c.weno_z, fp[0], fp[1], fp[2], fp[3], fp[4], fm[1], fm[2], fm[3], fm[4], fm[5]);
+  return weno_face<T, D>(c.weno_z, fp[0], fp[1], fp[2], fp[3], fp[4], fm[1], fm[2], fm[3], fm[4], fm[5], c.recip);
+}
+
+// The shared-memory program's directional sweep (SingleGPU/Burgers3d_WENO5_SharedMem/
+// kernels.cu:212-405) on every node of every line along `axis`: u = 0 beyond both ends of a line
+// (its Dirichlet fill, kernels.cu:247-259), F(a-1/2) from nodes a-3 .. a+2 with the local split
+// and the reciprocal normalisation; x assigns Lu = -(F(a+1/2) - F(a-1/2))/h, y and z subtract
+// (F(a+1/2) - F(a-1/2))/h. The reference defines Lu only for a <= n-4 (its tiles leave the
+// shared-memory cells past the grid unloaded); the zero extension is used for the last three.
+template <class T>
+void sweep_all(int axis, int weno_z, int64_t nx, int64_t ny, int64_t nz, T h, const T* u, T* Lu) {
+  const int64_t na = axis == 0 ? nx : axis == 1 ? ny : nz;
+  const int64_t nb = axis == 0 ? ny : nx, nc = axis == 2 ? ny : nz;
+  const int64_t s = axis == 0 ? 1 : axis == 1 ? nx : nx * ny;
+  BurgersCfg c{};
+  c.weno_z = weno_z;
+  c.recip = 1;
+#pragma omp parallel for schedule(static)
+  for (int64_t t = 0; t < nb * nc; ++t) {
+    const int64_t b = t % nb, cc = t / nb;
+    const int64_t i = axis == 0 ? 0 : b, j = axis == 0 ? b : (axis == 1 ? 0 : cc), k = axis == 2 ? 0 : cc;
+    const int64_t o0 = i + nx * j + nx * ny * k;
+    auto get = [&](int64_t a) -> T { return a >= 0 && a < na ? u[o0 + a * s] : (T)0; };
+    for (int64_t a = 0; a < na; ++a) {
+      const T fr = face_flux<T, T>(c, (T)0, [&](int q) { return get(a + q); });
+      const T fl = face_flux<T, T>(c, (T)0, [&](int q) { return get(a - 1 + q); });
+      const int64_t o = o0 + a * s;
+      if (axis == 0) Lu[o] = -(fr - fl) / h;
+      else Lu[o] = Lu[o] - (fr - fl) / h;
+    }
+  }
 }
 
 // Right-hand side Lu at every updated cell (others untouched). Accumulation order follows
@@ -1161,6 +1232,24 @@ int64_t orc_burgers_run_f32(BURG_ARGS, int div64, float* u, double tEnd, double 
                             double C, int64_t max_steps, double* t_out) {
   BURG_CFG if (div64) return burgers_run<float, double>(c, u, tEnd, CFL, dt_rule, C, max_steps, t_out);
   return burgers_run<float, float>(c, u, tEnd, CFL, dt_rule, C, max_steps, t_out);
+}
+
+// The shared-memory program's loop: the baseline loop with its weight normalisation (the interior
+// update depends on no node past the grid, so the zero fill plays no part there).
+int64_t orc_burgers_run_recip_f64(BURG_ARGS, double* u, double tEnd, double CFL, int dt_rule, double C,
+                                  int64_t max_steps, double* t_out) {
+  BURG_CFG c.recip = 1;
+  return burgers_run<double, double>(c, u, tEnd, CFL, dt_rule, C, max_steps, t_out);
+}
+void orc_burgers_sweep_all_f64(int axis, int weno_z, int nx, int ny, int nz, double h, const double* u, double* Lu) {
+  sweep_all<double>(axis, weno_z, nx, ny, nz, h, u, Lu);
+}
+void orc_burgers_sweep_all_f32(int axis, int weno_z, int nx, int ny, int nz, double h, const float* u, float* Lu) {
+  sweep_all<float>(axis, weno_z, nx, ny, nz, (float)h, u, Lu);
+}
+void orc_heat_blocking_run_f64(int nx, int ny, int nz, double kx, double ky, double kz, double dt, int64_t iters,
+                               double* u) {
+  heat_blocking_run<double>(nx, ny, nz, kx, ky, kz, dt, iters, u);
 }
 
 // Reference Burgers dt loop alone (no field update): number of steps and final t

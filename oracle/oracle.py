@@ -64,6 +64,10 @@ def lib() -> C.CDLL:
             "orc_burgers_run_f64": (_I64, _BURG + [C.c_void_p, _D, _D, _I, _D, _I64, _PD]),
             "orc_burgers_run_f32": (_I64, _BURG + [_I, C.c_void_p, _D, _D, _I, _D, _I64, _PD]),
             "orc_burgers_ref_steps": (_I64, [_D, _D, _D, _D, _D, _I, _I, _I, _D, _PD]),
+            "orc_burgers_run_recip_f64": (_I64, _BURG + [C.c_void_p, _D, _D, _I, _D, _I64, _PD]),
+            "orc_burgers_sweep_all_f64": (None, [_I, _I, _I, _I, _I, _D, C.c_void_p, C.c_void_p]),
+            "orc_burgers_sweep_all_f32": (None, [_I, _I, _I, _I, _I, _D, C.c_void_p, C.c_void_p]),
+            "orc_heat_blocking_run_f64": (None, [_I, _I, _I, _D, _D, _D, _D, _I64, C.c_void_p]),
             "orc_max_abs_f64": (_D, [C.c_void_p, _I64]),
             "orc_burgers_step_adjoint_f64": (None, _BURG + [C.c_void_p] * 3 + [_D, C.c_void_p]),
             "orc_burgers_step_adjoint_f32": (None, _BURG + [C.c_void_p] * 3 + [_D, C.c_void_p]),
@@ -218,15 +222,38 @@ def burgers_rhs(cfg, u, alpha):
     return Lu
 
 
-def burgers_run(cfg, u, tEnd, cfl, dt_rule, C_visc=0.0, max_steps=1 << 40, div64=True):
+def burgers_run(cfg, u, tEnd, cfl, dt_rule, C_visc=0.0, max_steps=1 << 40, div64=True, recip=False):
+    """recip: the shared-memory reference program's weight normalisation (FP64 only)."""
     u = np.ascontiguousarray(u).copy()
     t = C.c_double()
-    if u.dtype == np.float64:
+    if recip:
+        assert u.dtype == np.float64
+        it = lib().orc_burgers_run_recip_f64(*_burg_args(cfg), _p(u), tEnd, cfl, dt_rule, C_visc, max_steps,
+                                             C.byref(t))
+    elif u.dtype == np.float64:
         it = lib().orc_burgers_run_f64(*_burg_args(cfg), _p(u), tEnd, cfl, dt_rule, C_visc, max_steps, C.byref(t))
     else:
         it = lib().orc_burgers_run_f32(*_burg_args(cfg), int(div64), _p(u), tEnd, cfl, dt_rule, C_visc, max_steps,
                                        C.byref(t))
     return u, t.value, it
+
+
+def burgers_sweep_all(axis: int, weno_z: bool, u: np.ndarray, h: float, Lu: np.ndarray) -> np.ndarray:
+    """The shared-memory reference program's sweep along `axis` on a (nz, ny, nx) array: returns
+    Lu after it (x assigns, y and z subtract; Lu is not modified in place)."""
+    u = np.ascontiguousarray(u)
+    out = np.ascontiguousarray(Lu).copy()
+    nz, ny, nx = u.shape
+    f = lib().orc_burgers_sweep_all_f64 if u.dtype == np.float64 else lib().orc_burgers_sweep_all_f32
+    f(axis, int(weno_z), nx, ny, nz, h, _p(u), _p(out))
+    return out
+
+
+def heat_blocking_run(nx, ny, nz, kx, ky, kz, dt, iters, u: np.ndarray) -> np.ndarray:
+    """The z-blocked reference heat program's loop (FP64), iters time steps from u."""
+    u = np.ascontiguousarray(u, dtype=np.float64).copy()
+    lib().orc_heat_blocking_run_f64(nx, ny, nz, kx, ky, kz, dt, iters, _p(u))
+    return u
 
 
 def burgers_ref_steps(tEnd, cfl, L, W, H, nx, ny, nz, Cv=1e-5):

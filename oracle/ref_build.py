@@ -10,10 +10,15 @@ Sources (the reference checkout, read-only):
   SingleGPU/Diffusion2d/kernels.cu               -> heat2d       (Compute_Laplace2d, Compute_RK)
   SingleGPU/Burgers3d_WENO5/kernels.cu           -> burgers3d    (Compute_dF/dG/dH, Compute_Laplace_Async,
                                                                   Compute_RK)
+  SingleGPU/Diffusion3d_Blocking/kernels.cu      -> heat3d_blocking (Compute_Laplace3d_Async, Compute_RK)
+(SingleGPU/Burgers3d_WENO5_SharedMem/kernels.cu is not built: its sweeps call __syncthreads
+inside `if (I < nx)`, kernels.cu:235-270, which CUDA leaves undefined when a block straddles
+the grid's end, as every one of its x tiles does. Its programs still link against the
+compatibility library, whose kernels take no such barrier.)
 Each is built twice: `<name>.cubin` with nvcc's default flags (FMA contraction on: the reference's
 own build, used for timing) and `<name>_nofma.cubin` with -fmad=false (every operation rounded as
 written: comparable bit for bit with the FP64 oracle and the library's FP64 path). REAL is double
-in all three (USE_FLOAT false in the reference headers).
+in all of them (USE_FLOAT false in the reference headers).
 
 The same programs' host tools (SingleGPU/<program>/tools.cpp: initial conditions, result.bin)
 are compiled with g++ together with oracle/ref_tools_shim.cpp into host libraries
@@ -45,6 +50,7 @@ UNITS = {
     "heat3d": "SingleGPU/Diffusion3d_baselineCode/kernels.cu",
     "heat2d": "SingleGPU/Diffusion2d/kernels.cu",
     "burgers3d": "SingleGPU/Burgers3d_WENO5/kernels.cu",
+    "heat3d_blocking": "SingleGPU/Diffusion3d_Blocking/kernels.cu",
 }
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 TOOLS = {
@@ -61,6 +67,8 @@ MAINS = {  # reference program -> the compatibility library that replaces its ke
     "heat2d_pitched": ("SingleGPU/Diffusion2d_PitchedMem", "advdiff_compat_heat2d_pitched"),
     "burgers3d": ("SingleGPU/Burgers3d_WENO5", "advdiff_compat_burgers3d"),
     "burgers3d_pitched": ("SingleGPU/Burgers3d_WENO5_PitchedMem", "advdiff_compat_burgers3d_pitched"),
+    "heat3d_blocking": ("SingleGPU/Diffusion3d_Blocking", "advdiff_compat_heat3d_blocking"),
+    "burgers3d_sharedmem": ("SingleGPU/Burgers3d_WENO5_SharedMem", "advdiff_compat_burgers3d_sharedmem"),
 }
 LIBDIR = HERE.parent / "multigpu_advectiondiffusion_gb300" / "_lib"
 

@@ -12,6 +12,9 @@ launch geometry in the order of the reference's host loops:
   heat2d_run   SingleGPU/Diffusion2d/main.cpp:97-125.
   burgers3d_run SingleGPU/Burgers3d_WENO5/main.cpp:88-150 (dt = min(CFL dx, diffusive bound),
                trimmed to tEnd; per RK stage Compute_dF, dG, dH, Compute_Laplace_Async, Compute_RK).
+  heat3d_blocking_run SingleGPU/Diffusion3d_Blocking/main.cpp:86-123 (Lu zeroed once; per RK
+               stage Compute_Laplace3d_Async over 16-plane z blocks from kstart 3 to kstop nz-2,
+               then Compute_RK).
 
 Launch safety, checked by reading the kernels: Compute_Laplace2d writes Lu on every thread that
 fails its interior test (SingleGPU/Diffusion2d/kernels.cu:86-87), including threads of partial
@@ -20,7 +23,10 @@ Compute_Laplace_Async starts its first slab at max(3, blockIdx.z*16) without tes
 kstop (SingleGPU/Burgers3d_WENO5/kernels.cu:458-471), which reads past the array when
 nz mod 16 is 1 or 2, so burgers3d_run rejects those nz; Compute_dF/dG take x- and y-extents
 from swapped grids (main.cpp:101,105), so burgers3d_run requires nx == ny == nz and equal
-block sizes. Every state array is FP64 (the reference's REAL).
+block sizes. The blocked heat kernel likewise starts each z block at max(3, 16*blockIdx.z)
+without the kstop test (SingleGPU/Diffusion3d_Blocking/kernels.cu:57-68), reading two planes past
+that plane, so heat3d_blocking_run rejects nz mod 16 of 1 or 2 (the last block's first plane is
+then nz-2 or nz-1). Every state array is FP64 (the reference's REAL).
 """
 from __future__ import annotations
 
@@ -144,6 +150,32 @@ def heat3d_run(mod: RefModule, u, nx: int, ny: int, nz: int, kx: float, ky: floa
         for st in stages:
             mod.launch(lap, grid, block, [up, lp, *dims], s)
             mod.launch("Compute_RK", grid, block, [up, uop, lp, C.c_uint(st), *dims, C.c_double(dt)], s)
+
+
+def heat3d_blocking_run(mod: RefModule, u, nx: int, ny: int, nz: int, kx: float, ky: float, kz: float, dt: float,
+                        iters: int) -> None:
+    """iters time steps in place on the dense FP64 CUDA tensor u (pitch = nx), with the blocked
+    program's launch geometry: Laplacian blocks (32, 4, 1) over (nx/32, ny/4, nz/16), RK blocks
+    (32, 4, 4) over (nx/32, ny/4, nz/4) (main.cpp:88-98)."""
+    import torch
+    assert u.dtype == torch.float64 and u.numel() == nx * ny * nz
+    if nz % 16 in (1, 2) or min(nx, ny, nz) < 7:
+        raise ValueError("the blocked Laplacian's last z block would read past the array")
+    s = _stream()
+    uo = torch.empty_like(u)
+    Lu = torch.zeros_like(u)
+    for n, v in (("d_kx", kx), ("d_ky", ky), ("d_kz", kz)):
+        mod.set_const(n, v)
+    g2, b2 = (_div(nx, 32), _div(ny, 4), _div(nz, 16)), (32, 4, 1)
+    g3, b3 = (_div(nx, 32), _div(ny, 4), _div(nz, 4)), (32, 4, 4)
+    up, uop, lp = C.c_void_p(u.data_ptr()), C.c_void_p(uo.data_ptr()), C.c_void_p(Lu.data_ptr())
+    dims = [C.c_uint(nx), C.c_uint(nx), C.c_uint(ny), C.c_uint(nz)]  # pitch, nx, ny, nz
+    for _ in range(iters):
+        _copy(uo, u, s)
+        for st in (1, 2, 3):
+            mod.launch("Compute_Laplace3d_Async", g2, b2, [up, lp, *dims, C.c_uint(3), C.c_uint(nz - 2), C.c_uint(16)],
+                       s)
+            mod.launch("Compute_RK", g3, b3, [up, uop, lp, C.c_uint(st), *dims, C.c_double(dt)], s)
 
 
 def heat2d_run(mod: RefModule, u, nx: int, ny: int, kx: float, ky: float, dt: float, iters: int,

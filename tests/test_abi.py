@@ -49,6 +49,43 @@ def test_compat_exports_reference_names(native, lib, header, names, pitched):
     assert _declared(ROOT / "include" / header) <= exp
 
 
+@pytest.mark.parametrize("lib,header,names", [
+    ("libadvdiff_compat_heat3d_blocking.so", "advdiff_compat_heat3d.h",
+     {"CopyToConstantMemory", "Call_Lu3d", "Call_RK3d"}),
+    ("libadvdiff_compat_burgers3d_sharedmem.so", "advdiff_compat_burgers3d.h",
+     {"CopyToConstantMemory", "Call_Adv_x", "Call_Adv_y", "Call_Adv_z", "Call_Diff_", "Call_sspRK"}),
+])
+def test_compat_variant_libraries_export_reference_names(native, lib, header, names):
+    """The z-blocked heat and shared-memory Burgers programs' libraries (pitched signatures)."""
+    so = N.LIBDIR / lib
+    C.CDLL(str(so))
+    exp = _exports(so)
+    assert names | {"adv_compat_last_status"} <= exp
+    assert _declared(ROOT / "include" / header) <= exp
+
+
+def test_ref_variant_ops_reject_bad_arguments_without_gpu(native):
+    buf = C.c_void_p(64)
+    box = (C.c_int32 * 6)(3, 9, 3, 9, 3, 10)
+    # k1 = nz - 1 would read a plane past the grid (the O4 stencil needs k + 2 < nz)
+    bad = (C.c_int32 * 6)(3, 9, 3, 9, 3, 11)
+    assert native.adv_ref_laplace_box(N.ADV_F64, 3, 4, bad, 0, 1, 12, 12, 12, 12, 1.0, 1.0, 1.0, buf, buf,
+                                      None) == N.ADV_ERR_INVALID_ARG
+    assert b"margin" in native.adv_last_error_string()
+    assert native.adv_ref_laplace_box(N.ADV_F64, 3, 4, None, 0, 1, 12, 12, 12, 12, 1.0, 1.0, 1.0, buf, buf,
+                                      None) == N.ADV_ERR_INVALID_ARG
+    assert native.adv_ref_laplace_box(N.ADV_F64, 3, 3, box, 0, 1, 12, 12, 12, 12, 1.0, 1.0, 1.0, buf, buf,
+                                      None) == N.ADV_ERR_INVALID_ARG
+    assert native.adv_ref_laplace_box(N.ADV_F64, 3, 4, box, 0, 2, 12, 12, 12, 12, 1.0, 1.0, 1.0, buf, buf,
+                                      None) == N.ADV_ERR_INVALID_ARG
+    assert native.adv_ref_burgers_sweep_all(N.ADV_F64, 3, N.ADV_WENO5_Z, 12, 12, 12, 12, 0.1, buf, buf,
+                                            None) == N.ADV_ERR_INVALID_ARG
+    assert native.adv_ref_burgers_sweep_all(N.ADV_F64, 0, N.ADV_WENO5_Z, 12, 12, 12, 12, 0.0, buf, buf,
+                                            None) == N.ADV_ERR_INVALID_ARG
+    assert native.adv_ref_burgers_sweep_all(N.ADV_F64, 0, N.ADV_WENO5_Z, 8, 12, 12, 12, 0.1, buf, buf,
+                                            None) == N.ADV_ERR_INVALID_ARG  # pitch < nx
+
+
 def test_abi_version_and_strings(native):
     assert native.adv_abi_version() == 2
     assert native.adv_status_string(N.ADV_ERR_TIMEOUT) == b"ADV_ERR_TIMEOUT"

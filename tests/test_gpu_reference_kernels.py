@@ -103,3 +103,38 @@ def test_burgers3d_loop_equals_reference_kernels(cuda, native, mods, n, tEnd):
     torch.cuda.synchronize()
     assert (t, it) == (t_ref, it_ref)
     assert torch.equal(u, ref)
+
+
+@pytest.mark.parametrize("shape,iters", [((41, 37, 35), 4), ((64, 64, 48), 3)])
+def test_heat3d_blocking_equals_reference_kernels(cuda, oracle, mods, shape, iters):
+    """SingleGPU/Diffusion3d_Blocking's own kernels (its blocked Laplacian over 16-plane z blocks,
+    its launch geometry) against the compatibility library's Call_Lu3d / Call_RK3d and the
+    oracle's restatement: bit for bit. nz avoids the sizes where the reference's last z block
+    would read past the array (nz mod 16 of 1 or 2)."""
+    import ctypes as C
+    import torch
+    mod = _mod(mods, "heat3d_blocking")
+    nx, ny, nz = shape
+    cfg = HeatConfig.reference_3d(1.0, 10, 10, 10, *shape)
+    u = _rand(cfg.numel, 3, cuda)
+    u0 = u.cpu().numpy()
+    ref = u.clone()
+    ref_gpu.heat3d_blocking_run(mod, ref, nx, ny, nz, cfg.kx, cfg.ky, cfg.kz, cfg.dt, iters)
+    lib = C.CDLL(str(N.LIBDIR / "libadvdiff_compat_heat3d_blocking.so"))
+
+    class Dim3(C.Structure):
+        _fields_ = [("x", C.c_uint), ("y", C.c_uint), ("z", C.c_uint)]
+    uo, Lu = torch.empty_like(u), torch.zeros_like(u)
+    lib.CopyToConstantMemory(C.c_double(cfg.kx), C.c_double(cfg.ky), C.c_double(cfg.kz))
+    dd = [C.c_uint(nx), C.c_uint(nx), C.c_uint(ny), C.c_uint(nz)]
+    pu, puo, pL = (C.c_void_p(x.data_ptr()) for x in (u, uo, Lu))
+    for _ in range(iters):
+        uo.copy_(u)
+        for st in (1, 2, 3):
+            lib.Call_Lu3d(Dim3(1, 1, 1), Dim3(32, 4, 1), None, *dd, pu, pL)
+            lib.Call_RK3d(Dim3(1, 1, 1), Dim3(32, 4, 4), None, C.c_uint(st), *dd, C.c_double(cfg.dt), pu, puo, pL)
+    torch.cuda.synchronize()
+    assert lib.adv_compat_last_status() == 0
+    assert torch.equal(u, ref)
+    want = oracle.heat_blocking_run(nx, ny, nz, cfg.kx, cfg.ky, cfg.kz, cfg.dt, iters, u0)
+    np.testing.assert_array_equal(ref.cpu().numpy(), want)

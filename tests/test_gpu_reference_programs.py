@@ -10,7 +10,10 @@ the reference's own command line on small grids:
   * Burgers 3D, dense and pitched (SingleGPU/Burgers3d_WENO5/main.cpp:127-161): the printed step
     count and final time equal the oracle's dt loop (its header sets WRITE to 0, so the program
     writes no field; the field itself is compared through the same extern "C" names in
-    tests/test_gpu_compat.py).
+    tests/test_gpu_compat.py);
+  * the z-blocked heat program (SingleGPU/Diffusion3d_Blocking/main.cpp:101-144): result.bin
+    equals the oracle's restatement of its loop; the shared-memory Burgers program
+    (SingleGPU/Burgers3d_WENO5_SharedMem/main.cpp:136-178): step count and final time.
 """
 import re
 import subprocess
@@ -82,5 +85,30 @@ def test_reference_burgers3d_program(cuda, oracle, tmp_path, name, n, tEnd):
     u0 = oracle.ic_burgers_ref(n, n, n, cfg.dx, cfg.dy, cfg.dz)
     _, t_w, it_w = oracle.burgers_run(cfg, u0, tEnd, cfl, 0, C_visc=1e-5, max_steps=1 << 20)
     assert int(float(m.group(2))) == it_w
+    assert float(m.group(3)) == pytest.approx(t_w, rel=1e-5)
+    assert "Burgers-3D GPU-WENO5" in out
+
+
+@pytest.mark.parametrize("dims,iters", [((33, 33, 33), 20), ((41, 37, 35), 7)])
+def test_reference_heat3d_blocking_program(cuda, oracle, tmp_path, dims, iters):
+    nx, ny, nz = dims
+    C, L = 1.0, 10
+    out = _run("heat3d_blocking", [C, L, L, L, nx, ny, nz, iters], tmp_path)
+    cfg = HeatConfig.reference_3d(C, L, L, L, nx, ny, nz)
+    u0 = oracle.ic_heat_ref(3, nx, ny, nz, L / (nx - 1), L / (ny - 1), L / (nz - 1))
+    want = oracle.heat_blocking_run(nx, ny, nz, cfg.kx, cfg.ky, cfg.kz, cfg.dt, iters, u0).astype(np.float32)
+    got = np.fromfile(tmp_path / "result.bin", dtype=np.float32)
+    np.testing.assert_array_equal(got, want)
+    assert int(_field("Iterations", out)) == iters
+
+
+@pytest.mark.parametrize("n,tEnd", [(24, 0.02), (40, 0.05)])
+def test_reference_burgers3d_sharedmem_program(cuda, oracle, tmp_path, n, tEnd):
+    cfl, L = 0.3, 2.0
+    out = _run("burgers3d_sharedmem", [tEnd, cfl, L, L, L, n, n, n], tmp_path)
+    m = re.search(r"dt: (\S+), iterations: (\S+), final time: (\S+)", out)
+    assert m, out[-1500:]
+    it_w, t_w = oracle.burgers_ref_steps(tEnd, cfl, L, L, L, n, n, n)
+    assert int(float(m.group(2).rstrip(","))) == it_w
     assert float(m.group(3)) == pytest.approx(t_w, rel=1e-5)
     assert "Burgers-3D GPU-WENO5" in out

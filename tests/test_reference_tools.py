@@ -86,6 +86,9 @@ def test_result_bin_equals_the_reference_writer(native, tmp_path, monkeypatch, n
      {"CopyToConstantMemory", "Call_Adv_x", "Call_Adv_y", "Call_Adv_z", "Call_Diff_", "Call_sspRK"}),
     ("burgers3d_pitched", "advdiff_compat_burgers3d_pitched",
      {"CopyToConstantMemory", "Call_Adv_x", "Call_Adv_y", "Call_Adv_z", "Call_Diff_", "Call_sspRK"}),
+    ("heat3d_blocking", "advdiff_compat_heat3d_blocking", {"CopyToConstantMemory", "Call_Lu3d", "Call_RK3d"}),
+    ("burgers3d_sharedmem", "advdiff_compat_burgers3d_sharedmem",
+     {"CopyToConstantMemory", "Call_Adv_x", "Call_Adv_y", "Call_Adv_z", "Call_Diff_", "Call_sspRK"}),
 ])
 def test_reference_main_links_against_the_compat_library(native, name, lib, wrappers):
     """The reference program's own main.cpp + tools.cpp, unmodified and without its kernels.cu,
