@@ -284,14 +284,15 @@ BURGERS_FLOPS_PER_CELL_STAGE = 451.4
 
 ENSEMBLE_SEED = 2024
 ENSEMBLE_STEPS = 500
-# WENO weight division of the ensemble's Burgers members: in FP64 (whose quotient, rounded to the FP32
-# state, is also the IEEE FP32 division's bit for bit: tests/test_gpu_burgers.py)
-ENSEMBLE_DIV = "f64"
+# WENO weight division of the ensemble's Burgers members: IEEE FP32, whose quotient is the FP64
+# division's rounded to the FP32 state bit for bit (double rounding is innocuous for 53 >= 2*24+2
+# bits; tests/test_gpu_burgers.py compares the two), without the FP64 pipe
+ENSEMBLE_DIV = "f32"
 
 
 def ensemble_workload() -> str:
     return (f"ensemble 64 heat (n in 64..192, o2 euler r=1/8) + 32 burgers (n in 96..160, weno5-z global-lf "
-            f"periodic cfl 0.4, {ENSEMBLE_DIV} div) x {ENSEMBLE_STEPS} steps, one graph")
+            f"periodic cfl 0.4, {DIV_LABEL[ENSEMBLE_DIV]} div) x {ENSEMBLE_STEPS} steps, one graph")
 
 
 def ensemble_members():
@@ -946,9 +947,13 @@ def compat_program_rates(n: int = 256) -> dict | None:
     return out or None
 
 
+DIV_LABEL = {"f32": "f32 (ieee: the f64 division's quotient rounded to f32, bit for bit)", "f64": "f64",
+             "fast": "fast (reciprocal, <= 2 ulp)"}
+
+
 def burgers_workload(args) -> str:
     return (f"burgers3d 256^3 f32 weno5-{args.weno} global-lf periodic cfl 0.4 x 20 steps, "
-            f"div {args.div}")
+            f"div {DIV_LABEL[args.div]}")
 
 
 def burgers_config(args, world: int) -> dict:
@@ -972,9 +977,10 @@ def main():
     ap.add_argument("--workload", default="heat3d",
                     choices=["heat3d", "heat2d", "burgers3d", "weno7", "ensemble", "adjoint"])
     ap.add_argument("--cpu-budget", type=float, default=10.0, help="seconds of CPU-baseline work")
-    ap.add_argument("--div", default="f64", choices=["fast", "f32", "f64"],
-                    help="Burgers WENO weight division (FP32 state): f64 = computed in FP64; f32 = IEEE FP32, "
-                         "equal bit for bit to the FP64 division rounded to the state; fast = reciprocal-based")
+    ap.add_argument("--div", default="f32", choices=["fast", "f32", "f64"],
+                    help="Burgers WENO weight division (FP32 state): f32 = IEEE FP32, equal bit for bit to the "
+                         "FP64 division rounded to the state (the default); f64 = the FP64 instruction itself; "
+                         "fast = reciprocal-based")
     ap.add_argument("--weno", default="z", choices=["z", "js"], help="Burgers WENO5 flavour")
     ap.add_argument("--no-tune", action="store_true", help="skip the launch-shape autotuner")
     args = ap.parse_args()
