@@ -93,6 +93,11 @@ def _peaks() -> tuple[float, str]:
     return 6800.0, "fallback"
 
 
+TRAFFIC_NOTE = ("dram__bytes_read.sum + dram__bytes_write.sum of one ncu-captured launch (profiles/traffic.json); "
+                "writes still dirty in L2 when that launch ends are not counted, so it can sit below the "
+                "algorithmic bytes even though every node is written once per launch")
+
+
 def _traffic(workload: str):
     """DRAM bytes per launch of the dominant kernel from the committed ncu summary, or None."""
     p = ROOT / "profiles" / "traffic.json"
@@ -465,7 +470,7 @@ def bench_ensemble(args, world, rank, dev, stream, flush, lib):
                          "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                          "traffic": _traffic("ensemble"), "algorithmic_bytes_per_launch": bytes_per_launch,
                          "avg_launch_us": launch_ms * 1e3},
-            "cpu_baseline": None,
+            "cpu_baseline": cpu_baseline_sample(args, world) if world == 1 else None,
             "e2e": {"value": replica_throughput(work * args.steps, ems, world), "unit": "Gcell-updates/s",
                     "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
             "gpu_launches": int(launched),
@@ -620,7 +625,7 @@ def bench_adjoint(args, world, rank, dev, lib):
                                       f"{dt * float(u0.abs().max()) / bc.dx:.3f} at t = 0), SSP-RK3; the C3 forward "
                                       "uses global LF, whose max|u| constant the adjoint does not differentiate"),
             "roofline": None,
-            "cpu_baseline": None,
+            "cpu_baseline": cpu_baseline_sample(args, world) if world == 1 else None,
             "e2e": None,
             "gpu_launches": int(launched),
             "clocks": clk.summary(),
@@ -700,33 +705,11 @@ def reference_sg_gpu(workload: str, warmup: int) -> dict | None:
     return out
 
 
-def run_reference_arm(args, world, rank):
-    """--impl reference: the path's CPU implementation on the host cores, for the same workload,
-    metric and config as this library's line. The reference has no CPU code for the path, so this is
-    its scheme restated (the tuned CPU loop for heat, the oracle otherwise), with the inputs from
-    the oracle's generators; the library itself is not loaded. Each benchmark step is a bounded
-    sample of the workload; ms_per_step is its measured wall time."""
-    from oracle import oracle
-    if rank != 0:
-        return
-    threads = os.cpu_count() or 1
-    oracle.set_threads(threads)
-    if args.workload in ("heat3d", "heat2d"):
-        cfg, nsteps = heat_case(args.workload)
-        u0 = heat_initial(args.workload, source="oracle")
-        budget = 4.0
-        for _ in range(args.warmup):
-            cpu_heat_rate(cfg, u0, nsteps, 0.2)
-        rates, samples, secs = [], [], []
-        for _ in range(args.steps):
-            r, st, dt = cpu_heat_rate(cfg, u0, nsteps, budget)
-            rates.append(r)
-            samples.append(st)
-            secs.append(dt)
-        sample = (f"{cfg.nx}^{cfg.ndim} FP32 O2 Euler, {int(np.median(samples))} of the {nsteps} time steps per "
-                  "step (tuned CPU loop, oracle/cpu_baseline.cpp, OpenMP)")
-        config = heat_config(args.workload, world)
-    elif args.workload == "burgers3d":
+def cpu_reference_sample(args, world: int, oracle):
+    """A bounded sample of a non-heat workload run by the oracle's restatement on the host cores
+    (test infrastructure: the reference has no CPU code for the path): per-step rates, seconds,
+    a description of the sample and the workload's config."""
+    if args.workload == "burgers3d":
         from multigpu_advectiondiffusion_gb300.solvers import BurgersConfig
         n = 256
         cfg = BurgersConfig.periodic(n, weno=args.weno, div=args.div)
@@ -796,6 +779,50 @@ def run_reference_arm(args, world, rank):
                 secs.append(dt)
         sample = "2 heat instances x 4 Euler steps + 1 Burgers instance x 1 SSP-RK3 step of the ensemble"
         config = ensemble_config(world)
+    return rates, secs, sample, config
+
+
+def cpu_baseline_sample(args, world: int) -> dict:
+    """cpu_baseline of a GPU line for a non-heat workload: the oracle on a bounded sample (one
+    warm-up, two timed samples), all host threads."""
+    from oracle import oracle
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    a = argparse.Namespace(**vars(args))
+    a.warmup, a.steps = 1, 2
+    rates, _, sample, _ = cpu_reference_sample(a, world, oracle)
+    return {"value": float(np.median(rates)), "unit": "Gcell-updates/s", "cores": threads, "kind": "port",
+            "sample": sample, "cpu_model": cpu_model()}
+
+
+def run_reference_arm(args, world, rank):
+    """--impl reference: the path's CPU implementation on the host cores, for the same workload,
+    metric and config as this library's line. The reference has no CPU code for the path, so this is
+    its scheme restated (the tuned CPU loop for heat, the oracle otherwise), with the inputs from
+    the oracle's generators; the library itself is not loaded. Each benchmark step is a bounded
+    sample of the workload; ms_per_step is its measured wall time."""
+    from oracle import oracle
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    if args.workload in ("heat3d", "heat2d"):
+        cfg, nsteps = heat_case(args.workload)
+        u0 = heat_initial(args.workload, source="oracle")
+        budget = 4.0
+        for _ in range(args.warmup):
+            cpu_heat_rate(cfg, u0, nsteps, 0.2)
+        rates, samples, secs = [], [], []
+        for _ in range(args.steps):
+            r, st, dt = cpu_heat_rate(cfg, u0, nsteps, budget)
+            rates.append(r)
+            samples.append(st)
+            secs.append(dt)
+        sample = (f"{cfg.nx}^{cfg.ndim} FP32 O2 Euler, {int(np.median(samples))} of the {nsteps} time steps per "
+                  "step (tuned CPU loop, oracle/cpu_baseline.cpp, OpenMP)")
+        config = heat_config(args.workload, world)
+    else:
+        rates, secs, sample, config = cpu_reference_sample(args, world, oracle)
     value = float(np.median(rates))
     line = {"impl": "reference", "metric": "Gcell-updates/s/RK-stage", "value": value, "unit": "Gcell-updates/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(secs)) * 1e3,
@@ -895,7 +922,7 @@ def bench_weno7(args, world, rank, dev, stream, flush, lib):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (the prototype's Gaussian initial state)", "config": weno7_config(world),
-            "roofline": None, "cpu_baseline": None,
+            "roofline": None, "cpu_baseline": cpu_baseline_sample(args, world) if world == 1 else None,
             "e2e": {"value": replica_throughput(work * args.steps, ems, world), "unit": "Gcell-updates/s",
                     "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
             "gpu_launches": int(launched), "clocks": clk.summary(),
@@ -1139,6 +1166,7 @@ def main():
         heat_run(cfg, u64, inner, stream=sh)
         torch.cuda.synchronize()
         extra["rel_l2_vs_fp64"] = (torch.linalg.vector_norm(u32.double() - u64) / torch.linalg.vector_norm(u64)).item()
+        extra["rel_linf_vs_fp64"] = ((u32.double() - u64).abs().max() / u64.abs().max()).item()
         u64_ref = u64.clone()
         ws64 = heat_workspace(cfg, u64)
         for _ in range(2):
@@ -1195,6 +1223,7 @@ def main():
         u64 = u0.double()
         t64, it64 = burgers_run(c64, u64, 0.5, 0.4, N.ADV_DT_MAXU, stream=sh)
         extra["rel_l2_vs_fp64"] = (torch.linalg.vector_norm(u32.double() - u64) / torch.linalg.vector_norm(u64)).item()
+        extra["rel_linf_vs_fp64"] = ((u32.double() - u64).abs().max() / u64.abs().max()).item()
         extra["rel_l2_vs_fp64_after"] = f"the run to t = 0.5: {it32} FP32 steps, {it64} FP64 steps"
         del u32
         # FP64 state, same problem: the reference's operand order (bit-exact with the oracle) and
@@ -1211,8 +1240,8 @@ def main():
 
     # ---- CPU baseline (the tuned CPU loop on the host cores, rank 0, N = 1 only)
     cpu = None
-    if rank == 0 and world == 1 and heat:
-        cpu = cpu_baseline_heat(cfg, u0_np, inner, args.cpu_budget)
+    if rank == 0 and world == 1:
+        cpu = cpu_baseline_heat(cfg, u0_np, inner, args.cpu_budget) if heat else cpu_baseline_sample(args, world)
 
     if rank == 0:
         line = {
@@ -1226,6 +1255,7 @@ def main():
                              if tuned else "default"),
             "roofline": {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind, "traffic": _traffic(args.workload),
+                         "traffic_note": TRAFFIC_NOTE,
                          "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_us": launch_ms * 1e3,
                          "launches_per_step": launches_per_step},
             "cpu_baseline": cpu,
