@@ -198,16 +198,10 @@ __device__ __forceinline__ BurgersPipe burgers_segment(const CUtensorMap* tmap, 
     return fj * TL::SW + TL::PADX + c;  // row of y0+fj-3
   };
   const int fbx0 = xbase(tid), fbx1 = xbase(tid + TL::NT), fby0 = ybase(tid), fby1 = ybase(tid + TL::NT);
-  // The 48 left over: FP64 one face each in lanes of warps 0 (x) and 1 (y); FP32 as 24 pairs of
-  // neighbouring faces in lanes 0..23 of warp 0 (8 x pairs, then 16 y pairs: one paired
-  // reconstruction with a run-time stride, one warp instead of two).
+  // (Reconstructing the 48 as 24 pairs in one warp, with a run-time stride, measured 2% slower:
+  // one warp then carries three paired reconstructions while the others wait at the barrier.)
   const bool left_x = tid < 16, left_y = tid >= 32 && tid < 64;
   const int fbl = left_x ? xbase(2 * TL::NT + tid) : ybase(2 * TL::NT + (left_y ? tid - 32 : 0));
-  const bool lp = tid < 24, lpx = tid < 8;
-  const int lg = 2 * TL::NT + 2 * (lpx ? tid : (lp ? tid - 8 : 0));  // first face of the pair
-  const int lb = lpx ? xbase(lg) : ybase(lg);  // its stencil base; the pair's second face is at +1
-  const int lst = lpx ? 1 : TL::SW;
-  const int lo = lpx ? lg : TL::NXF + lg;
   // Per-thread columns: (lane, warp) and (lane, warp + 8).
   const int cx = lane;
   const int cy0 = warp, cy1 = warp + 8;
@@ -413,18 +407,8 @@ __device__ __forceinline__ BurgersPipe burgers_segment(const CUtensorMap* tmap, 
           fxS[TL::NXF + tid] = face1(fby0, YS{});
           fxS[TL::NXF + tid + TL::NT] = face1(fby1, YS{});
         }
-        if constexpr (sizeof(T) == 4) {
-          if (lp) {
-            auto P = [&](int k) { return make_float2(fpS[lb + k * lst], fpS[lb + 1 + k * lst]); };
-            auto M = [&](int k) { return make_float2(fmS[lb + k * lst], fmS[lb + 1 + k * lst]); };
-            const float2 fl = Face<T, Z, D>::f2(P(0), P(1), P(2), P(3), P(4), M(1), M(2), M(3), M(4), M(5));
-            fxS[lo] = fl.x;
-            fxS[lo + 1] = fl.y;
-          }
-        } else {
-          if (left_x) fxS[2 * TL::NT + tid] = face1(fbl, X1{});
-          else if (left_y) fxS[TL::NXF + 2 * TL::NT + (tid - 32)] = face1(fbl, YS{});
-        }
+        if (left_x) fxS[2 * TL::NT + tid] = face1(fbl, X1{});
+        else if (left_y) fxS[TL::NXF + 2 * TL::NT + (tid - 32)] = face1(fbl, YS{});
         __syncthreads();
       }
       // ---- RHS, stage combine, store, max|u_out|
