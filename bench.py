@@ -1068,7 +1068,8 @@ def main():
         tuned = None if args.no_tune else autotune_heat(cfg, u, stream=sh)
         config = heat_config(args.workload, world)
         kernel = ("heat_stage_kernel<float,2,3,TMA,stage 1,4 rows,4 warps>" if cfg.ndim == 3
-                  else "heat_stage_kernel<float,2,2,TMA,stage 1>")
+                  else "heat2d_multi_kernel<float,2,FMA> (up to 8 forward-Euler steps per launch, one read and "
+                       "one write of the state per launch)")
     else:
         n = 256
         cfg = BurgersConfig.periodic(n, weno=args.weno, div=args.div)

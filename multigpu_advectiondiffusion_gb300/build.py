@@ -32,7 +32,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompil
 
 LIB_UNITS = ["api.cu", "api_device.cu", "heat_kernels.cu", "heat_f32.cu", "heat_f64.cu", "heat2_f32.cu", "burgers_f32.cu", "burgers_f64.cu",
              "ref_ops.cu", "noalloc.cu", "heat_batch.cu", "burgers_batch_f32.cu", "burgers_batch_f64.cu", "ensemble.cu",
-             "heatk.cu", "burgers_adjoint.cu", "autotune.cu", "weno7.cu",
+             "heatk.cu", "burgers_adjoint.cu", "autotune.cu", "weno7.cu", "heat2d_multi.cu",
              "formats.cpp"]
 # library -> (source, extra defines)
 COMPAT = {

@@ -93,6 +93,9 @@ adv_status heat_prepare(const adv_heat_desc& d, const void* u_in, HeatLaunch* L,
 // Lanes per row of the 4-row FP32 tile for rows of nx nodes: 16 (64-wide tiles) where 128-wide
 // tiles leave clearly more lanes idle, else 32.
 int heat_row_lanes(int nx);
+// 2D forward Euler, up to heat2d_multi_steps() steps per launch (heat2d_multi.cu); in != out.
+int heat2d_multi_steps();
+adv_status heat2d_multi_launch(const adv_heat_desc& d, const void* in, void* out, int steps, cudaStream_t s);
 adv_status heat_launch(const adv_heat_desc& d, const HeatLaunch& L, int stage, const void* u_in,
                        const void* u_n, void* u_out, cudaStream_t s);
 adv_status heat_validate(const adv_heat_desc* d);

@@ -390,6 +390,43 @@ adv_status adv_heat_run(const adv_heat_desc* d, int time_scheme, int64_t nsteps,
       if ((st = heat_launch(*d, La, 1, u, u, w1, s)) != ADV_OK) return st;
       ADV_CUDA_TRY(cudaMemcpyAsync(u, w1, n * es, cudaMemcpyDeviceToDevice, s));
     }
+  } else if (time_scheme == ADV_EULER && d->ndim == 2 && d->dtype == ADV_F32 && nsteps >= 2) {
+    // 2D FP32: K steps per launch (overlapped temporal tiling in shared memory, heat2d_multi.cu;
+    // 512^2 x 1000 steps: 145 vs 102 Gcell-updates/s with one step per launch),
+    // ping-pong u -> w1 -> u; a chunk of 2*C launches is captured once and replayed, the
+    // remaining full launch and a shorter last one run directly.
+    const int K = heat2d_multi_steps();
+    const int64_t full = nsteps / K;
+    const int rem = (int)(nsteps % K);
+    const int64_t pairs = full / 2;
+    const int64_t C = std::min<int64_t>(pairs, 32);
+    auto chunk = [&](cudaStream_t cs) -> adv_status {
+      for (int64_t i = 0; i < C; ++i) {
+        adv_status r = heat2d_multi_launch(*d, u, w1, K, cs);
+        if (r != ADV_OK) return r;
+        r = heat2d_multi_launch(*d, w1, u, K, cs);
+        if (r != ADV_OK) return r;
+      }
+      return ADV_OK;
+    };
+    if (C > 0) {
+      const std::string key = graph_key("heat2d-multi", *d, u, workspace, C);
+      if ((st = replay(key, s, pairs / C, chunk, 2 * C)) != ADV_OK) return st;
+      for (int64_t i = 0; i < pairs % C; ++i) {
+        if ((st = heat2d_multi_launch(*d, u, w1, K, s)) != ADV_OK) return st;
+        if ((st = heat2d_multi_launch(*d, w1, u, K, s)) != ADV_OK) return st;
+      }
+    }
+    bool in_w1 = false;
+    if (full % 2) {
+      if ((st = heat2d_multi_launch(*d, u, w1, K, s)) != ADV_OK) return st;
+      in_w1 = true;
+    }
+    if (rem) {
+      if ((st = heat2d_multi_launch(*d, in_w1 ? w1 : u, in_w1 ? u : w1, rem, s)) != ADV_OK) return st;
+      in_w1 = !in_w1;
+    }
+    if (in_w1) ADV_CUDA_TRY(cudaMemcpyAsync(u, w1, n * es, cudaMemcpyDeviceToDevice, s));
   } else if (time_scheme == ADV_EULER) {
     HeatLaunch La, Lb;
     if ((st = heat_prepare(*d, u, &La)) != ADV_OK) return st;
