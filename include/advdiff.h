@@ -44,7 +44,8 @@ typedef enum adv_status {
   ADV_ERR_NONFINITE = 4,   /* a NaN/Inf was seen in the state (max|u| reduction) */
   ADV_ERR_CFL = 5,         /* dt rule produced a non-positive or non-finite step */
   ADV_ERR_UNSUPPORTED = 6, /* valid request this library does not implement */
-  ADV_ERR_ALLOC = 7        /* host or device allocation failed */
+  ADV_ERR_ALLOC = 7,       /* host or device allocation failed */
+  ADV_ERR_BOUNDS = 8       /* checked build only: a memory index out of range (status word) */
 } adv_status;
 
 typedef enum adv_dtype { ADV_F32 = 0, ADV_F64 = 1 } adv_dtype;
@@ -140,6 +141,12 @@ adv_status adv_heat_run_noalloc(const adv_heat_desc* d, int time_scheme, int64_t
  * which prints and exits the process (SingleGPU/Burgers3d_WENO5/main.cpp:13-24). Called while
  * `stream` is being captured it returns ADV_ERR_UNSUPPORTED and touches nothing. */
 adv_status adv_device_status(void* stream);
+
+/* 1 in the bounds-checked build of the library (libadvdiff_checked.so: every global-memory index of
+ * the stage kernels and the reference operators, and the dynamic shared-memory indices, tested
+ * before use; a failed test skips the access and records ADV_ERR_BOUNDS for adv_device_status),
+ * 0 in the normal build. No counterpart in the reference. */
+int adv_bounds_checked(void);
 
 /* For tests of the failure path only: one adv_heat_stage launch in which the shared-memory copy
  * of z plane `plane` is never issued, and the waits for planes give up after wait_limit_ns

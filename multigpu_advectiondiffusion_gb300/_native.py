@@ -12,7 +12,7 @@ from pathlib import Path
 LIBDIR = Path(__file__).resolve().parent / "_lib"
 
 ADV_OK, ADV_ERR_INVALID_ARG, ADV_ERR_CUDA, ADV_ERR_TIMEOUT = 0, 1, 2, 3
-ADV_ERR_NONFINITE, ADV_ERR_CFL, ADV_ERR_UNSUPPORTED, ADV_ERR_ALLOC = 4, 5, 6, 7
+ADV_ERR_NONFINITE, ADV_ERR_CFL, ADV_ERR_UNSUPPORTED, ADV_ERR_ALLOC, ADV_ERR_BOUNDS = 4, 5, 6, 7, 8
 ADV_F32, ADV_F64 = 0, 1
 ADV_EULER, ADV_SSPRK3 = 0, 1
 ADV_WENO5_JS, ADV_WENO5_Z = 0, 1
@@ -88,6 +88,7 @@ SIGNATURES = [
     ("adv_heat_run", _I, [C.POINTER(HeatDesc), _I, _I64, _VP, _VP, _VP]),
     ("adv_heat_run_noalloc", _I, [C.POINTER(HeatDesc), _I, _I64, _VP, _VP]),
     ("adv_device_status", _I, [_VP]),
+    ("adv_bounds_checked", _I, []),
     ("adv_test_heat_stage_withheld", _I, [C.POINTER(HeatDesc), _I, _VP, _VP, _VP, _I, C.c_uint64, _VP]),
     ("adv_burgers_stage", _I, [C.POINTER(BurgersDesc), _I, _VP, _VP, _VP, _D, _D, _VP, _VP]),
     ("adv_burgers_workspace_bytes", _I, [C.POINTER(BurgersDesc), C.POINTER(C.c_size_t)]),
@@ -158,8 +159,10 @@ class AdvError(RuntimeError):
 _lib = None
 
 
-def lib_path(name: str = "libadvdiff.so") -> Path:
-    return LIBDIR / name
+def lib_path(name: str | None = None) -> Path:
+    """The native library: libadvdiff.so, or the build named by ADVDIFF_LIBRARY (e.g.
+    libadvdiff_checked.so, the bounds-checked build the tests run against)."""
+    return LIBDIR / (name or os.environ.get("ADVDIFF_LIBRARY", "libadvdiff.so"))
 
 
 def load() -> C.CDLL:

@@ -3,6 +3,7 @@
 Outputs (all git-ignored) go to ``multigpu_advectiondiffusion_gb300/_lib``:
 
 * ``libadvdiff.so``                -- the native C ABI of include/advdiff.h (+ advdiff_ref_ops.h)
+* ``libadvdiff_checked.so``        -- the same with ADV_BOUNDS_CHECK (memory indices tested; for tests)
 * ``libadvdiff_compat_heat2d.so``  -- the reference's 2D heat extern "C" names
 * ``libadvdiff_compat_heat3d.so``  -- the reference's 3D heat extern "C" names
 * ``libadvdiff_compat_burgers3d.so`` -- the reference's Burgers extern "C" names
@@ -94,6 +95,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
 
     with cf.ThreadPoolExecutor(jobs) as ex:
         objs = list(ex.map(compile_unit, [CSRC / u for u in LIB_UNITS]))
+        checked_objs = list(ex.map(lambda u: compile_unit(CSRC / u, ["-DADV_BOUNDS_CHECK"], ".checked"), LIB_UNITS))
         compat_objs = dict(zip(COMPAT, ex.map(lambda kv: compile_unit(CSRC / kv[1][0], kv[1][1], "." + kv[0]),
                                               COMPAT.items())))
         driver_objs = dict(zip(DRIVERS, ex.map(compile_unit, [CSRC / s for s in DRIVERS.values()])))
@@ -101,6 +103,12 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
     lib = OUT / "libadvdiff.so"
     if _stale(lib, objs, 0.0):
         _run([nv, *ARCH, "-shared", "-cudart", "shared", "-o", str(lib), *map(str, objs)])
+    # the bounds-checked build (ADV_BOUNDS_CHECK: every global index of the stage kernels and the
+    # reference operators tested before use), for the tests; internal references bind to itself
+    checked = OUT / "libadvdiff_checked.so"
+    if _stale(checked, checked_objs, 0.0):
+        _run([nv, *ARCH, "-shared", "-cudart", "shared", "-Xlinker", "-Bsymbolic", "-o", str(checked),
+              *map(str, checked_objs)])
     rpath = ["-Xlinker", "-rpath,$ORIGIN"]
     for name, obj in compat_objs.items():
         target = OUT / name

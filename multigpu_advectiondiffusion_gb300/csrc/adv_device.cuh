@@ -27,6 +27,21 @@ __device__ __forceinline__ void raise_status(int* status, int code) {
   if (status) atomicCAS(status, 0, code);
 }
 
+// Bounds checking, compiled into the checked build of the library only (-DADV_BOUNDS_CHECK,
+// libadvdiff_checked.so): ADV_IN_RANGE(i, n, status) is true when 0 <= i < n; otherwise it records
+// ADV_ERR_BOUNDS in the device status word and is false, and the caller skips the access (no trap,
+// no fault). In the normal build it is the constant true and the checks vanish.
+#ifdef ADV_BOUNDS_CHECK
+__device__ __forceinline__ bool adv_in_range(long long i, long long n, int* status) {
+  if (i >= 0 && i < n) return true;
+  raise_status(status, 8 /* ADV_ERR_BOUNDS */);
+  return false;
+}
+#define ADV_IN_RANGE(i, n, status) ::adv::adv_in_range((long long)(i), (long long)(n), (status))
+#else
+#define ADV_IN_RANGE(i, n, status) true
+#endif
+
 // ------------------------------------------------------------------------- mbarrier
 __device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");

@@ -270,6 +270,14 @@ const char* adv_last_error_string(void) { return g_last_error.c_str(); }
 int adv_abi_version(void) { return ADV_ABI_VERSION; }
 int64_t adv_kernel_launch_count(void) { return g_launches.load(); }
 
+int adv_bounds_checked(void) {
+#ifdef ADV_BOUNDS_CHECK
+  return 1;
+#else
+  return 0;
+#endif
+}
+
 const char* adv_status_string(adv_status s) {
   switch (s) {
     case ADV_OK: return "ADV_OK";
@@ -280,6 +288,7 @@ const char* adv_status_string(adv_status s) {
     case ADV_ERR_CFL: return "ADV_ERR_CFL";
     case ADV_ERR_UNSUPPORTED: return "ADV_ERR_UNSUPPORTED";
     case ADV_ERR_ALLOC: return "ADV_ERR_ALLOC";
+    case ADV_ERR_BOUNDS: return "ADV_ERR_BOUNDS";
   }
   return "ADV_ERR_UNKNOWN";
 }

@@ -198,6 +198,13 @@ __device__ __forceinline__ BurgersPipe burgers_segment(const CUtensorMap* tmap, 
     return fj * TL::SW + TL::PADX + c;  // row of y0+fj-3
   };
   const int fbx0 = xbase(tid), fbx1 = xbase(tid + TL::NT), fby0 = ybase(tid), fby1 = ybase(tid + TL::NT);
+#ifdef ADV_BOUNDS_CHECK
+  // every face slot's stencil (base .. base + 5 strides) inside the staged plane (CTA-uniform
+  // decision, before any copy of this segment is issued)
+  if (__syncthreads_or(!ADV_IN_RANGE(fbx1 + 5, TL::PLANE, p.status) ||
+                       !ADV_IN_RANGE(fby1 + 5 * TL::SW, TL::PLANE, p.status)))
+    return BurgersPipe{-1, -1, 0u};
+#endif
   // (Reconstructing the 48 as 24 pairs in one warp, with a run-time stride, measured 2% slower:
   // one warp then carries three paired reconstructions while the others wait at the barrier.)
   const bool left_x = tid < 16, left_y = tid >= 32 && tid < 64;
@@ -240,7 +247,7 @@ __device__ __forceinline__ BurgersPipe burgers_segment(const CUtensorMap* tmap, 
         if (per) { gx = wrapi(gx, nx); gy = wrapi(gy, ny); }
         const bool ok = zok && gx >= 0 && gx < nx && gy >= 0 && gy < ny;
         const T* src = ok ? p.uin + (size_t)z * sxy + (size_t)gy * nx + gx : p.uin;
-        cp_async_zfill<sizeof(T)>(dst + e, src, ok);
+        cp_async_zfill<sizeof(T)>(dst + e, src, ok && ADV_IN_RANGE(src - p.uin, sxy * nz, p.status));
       }
       cp_async_commit();
     }
@@ -273,7 +280,10 @@ __device__ __forceinline__ BurgersPipe burgers_segment(const CUtensorMap* tmap, 
           const int r = e / TL::SW, c = e - r * TL::SW;
           const int gx = x0 - TL::PADX + c, gy = y0 - TL::R + r;
           if (gx < 0 || gx >= nx || gy < 0 || gy >= ny)
-            plq[e] = p.uin[(size_t)z * sxy + (size_t)wrapi(gy, ny) * nx + wrapi(gx, nx)];
+          {
+            const size_t gi = (size_t)z * sxy + (size_t)wrapi(gy, ny) * nx + wrapi(gx, nx);
+            if (ADV_IN_RANGE(gi, sxy * nz, p.status)) plq[e] = p.uin[gi];
+          }
         }
       }
     } else {
@@ -449,11 +459,15 @@ __device__ __forceinline__ BurgersPipe burgers_segment(const CUtensorMap* tmap, 
           }
           T un;
           if (p.un_is_uin) un = uo;
-          else un = p.un[(size_t)k * sxy + (size_t)y * nx + x];
+          else {
+            const size_t gi = (size_t)k * sxy + (size_t)y * nx + x;
+            un = ADV_IN_RANGE(gi, sxy * nz, p.status) ? p.un[gi] : T(0);
+          }
           res = stage_combine<T>(p.stage, un, uo, dt, L);
         }
         if (inside) {
-          p.out[(size_t)k * sxy + (size_t)y * nx + x] = res;
+          if (ADV_IN_RANGE((size_t)k * sxy + (size_t)y * nx + x, sxy * nz, p.status))
+            p.out[(size_t)k * sxy + (size_t)y * nx + x] = res;
           const K kk = abs_key(res);
           kmax = kk > kmax ? kk : kmax;
         }

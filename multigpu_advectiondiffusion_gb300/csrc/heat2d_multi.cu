@@ -14,6 +14,7 @@
 // the same neighbour values, so the result equals K single steps bit for bit.
 #include <algorithm>
 
+#include "adv_device.cuh"
 #include "adv_internal.h"
 #include "heat_stage.cuh"
 
@@ -31,6 +32,7 @@ struct Heat2MultiParams {
   T* out;
   int nx, ny, frozen, zero_boundary, steps;
   T kx, ky, dt;
+  int* status;  // device status word (bounds-checked build)
 };
 
 template <class T, int ORDER, bool FAST>
@@ -48,7 +50,10 @@ __global__ void __launch_bounds__(512) heat2d_multi_kernel(const __grid_constant
     const int gy = y0 + j;
     for (int i = threadIdx.x; i < EX; i += M::TX) {
       const int gx = x0 + i;
-      bufA[j * EX + i] = (gx >= 0 && gx < nx && gy >= 0 && gy < ny) ? p.in[(size_t)gy * nx + gx] : T(0);
+      const size_t gi = (size_t)gy * nx + gx;
+      bufA[j * EX + i] = (gx >= 0 && gx < nx && gy >= 0 && gy < ny && ADV_IN_RANGE(gi, (size_t)nx * ny, p.status))
+                             ? p.in[gi]
+                             : T(0);
     }
   }
   __syncthreads();
@@ -92,7 +97,8 @@ __global__ void __launch_bounds__(512) heat2d_multi_kernel(const __grid_constant
     if (gy >= ny) break;
     for (int i = threadIdx.x; i < M::BX; i += M::TX) {
       const int gx = x0 + H + i;
-      if (gx < nx) p.out[(size_t)gy * nx + gx] = src[(j + H) * EX + i + H];
+      if (gx < nx && ADV_IN_RANGE((size_t)gy * nx + gx, (size_t)nx * ny, p.status))
+        p.out[(size_t)gy * nx + gx] = src[(j + H) * EX + i + H];
     }
   }
 }
@@ -124,6 +130,7 @@ adv_status launch_t(const adv_heat_desc& d, const void* in, void* out, int steps
   p.kx = (T)d.kx;
   p.ky = (T)d.ky;
   p.dt = (T)d.dt;
+  p.status = device_status_ptr();
   const dim3 grid((unsigned)((d.nx + Heat2Multi::BX - 1) / Heat2Multi::BX),
                   (unsigned)((d.ny + Heat2Multi::BY - 1) / Heat2Multi::BY));
   heat2d_multi_kernel<T, ORDER, FAST><<<grid, dim3(Heat2Multi::TX, Heat2Multi::TY), smem, s>>>(p);

@@ -231,7 +231,7 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
         const int gx = x0 - C::PADX + c, gy = y0 - R + r;
         const bool ok = zok && gx >= 0 && gx < nx && gy >= 0 && gy < ny;
         const T* src = ok ? p.uin + (size_t)z * sxy + (size_t)gy * nx + gx : p.uin;
-        cp_async_zfill<sizeof(T)>(dst + e, src, ok);
+        cp_async_zfill<sizeof(T)>(dst + e, src, ok && ADV_IN_RANGE(src - p.uin, sxy * nz, p.status));
       }
       cp_async_commit();
     }
@@ -309,6 +309,7 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
     }
     parity ^= 1u << s_wait;
     const int s_cent = s_wait >= RZ ? s_wait - RZ : s_wait - RZ + C::NS;
+    if (!ADV_IN_RANGE(s_wait, C::NS, p.status) || !ADV_IN_RANGE(s_cent, C::NS, p.status)) ok = false;
     const T* plq = ring + s_wait * C::SLOT_ELEMS + (RY * ty + R) * SW + C::PADX + tx * VX;
     s_wait = s_wait + 1 == C::NS ? 0 : s_wait + 1;
     const bool warp_abort = __any_sync(0xffffffffu, !ok);  // shuffles below need all lanes
@@ -384,8 +385,10 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
             if (STAGE != 1) {
               const size_t off = (size_t)(q - 2 * RZ) * sxy + (size_t)r * nx + e;
               const T* src = p.un + (obase - p.out) + off;
-              const bool i0 = warp_inside || ((inside >> (r * VX + e)) & 1u);
-              const bool i1 = warp_inside || ((inside >> (r * VX + e + 1)) & 1u);
+              const bool i0 = (warp_inside || ((inside >> (r * VX + e)) & 1u)) &&
+                              ADV_IN_RANGE(src - p.un, sxy * nz, p.status);
+              const bool i1 = (warp_inside || ((inside >> (r * VX + e + 1)) & 1u)) &&
+                              ADV_IN_RANGE(src - p.un + 1, sxy * nz, p.status);
               un = make_float2(i0 ? src[0] : T(0), i1 ? src[1] : T(0));
             }
             const float2 v = combine<float2, true>(stage, un, c, dt2, L);
@@ -406,7 +409,10 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
           T un = c;
           if (STAGE != 1) {
             const size_t off = (size_t)(q - 2 * RZ) * sxy + (size_t)r * nx + e;
-            un = (warp_inside || ((inside >> (r * VX + e)) & 1u)) ? p.un[(obase - p.out) + off] : T(0);
+            un = ((warp_inside || ((inside >> (r * VX + e)) & 1u)) &&
+                  ADV_IN_RANGE((obase - p.out) + off, sxy * nz, p.status))
+                     ? p.un[(obase - p.out) + off]
+                     : T(0);
           }
           res[r][e] = combine<T, FAST>(stage, un, c, dt, L);
         }
@@ -452,7 +458,8 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
           V v;
 #pragma unroll
           for (int e = 0; e < VX; ++e) reinterpret_cast<T*>(&v)[e] = res[r][e];
-          *reinterpret_cast<V*>(dst0 + (size_t)r * nx) = v;
+          if (ADV_IN_RANGE(dst0 + (size_t)r * nx - p.out + VX - 1, sxy * nz, p.status))
+            *reinterpret_cast<V*>(dst0 + (size_t)r * nx) = v;
         }
       } else
 #pragma unroll
@@ -463,11 +470,11 @@ __device__ __forceinline__ HeatPipe heat_segment(const CUtensorMap* tmap, const 
           V v;
 #pragma unroll
           for (int e = 0; e < VX; ++e) reinterpret_cast<T*>(&v)[e] = res[r][e];
-          *reinterpret_cast<V*>(dst) = v;
+          if (ADV_IN_RANGE(dst - p.out + VX - 1, sxy * nz, p.status)) *reinterpret_cast<V*>(dst) = v;
         } else {
 #pragma unroll
           for (int e = 0; e < VX; ++e)
-            if (xb + e < nx) dst[e] = res[r][e];
+            if (xb + e < nx && ADV_IN_RANGE(dst + e - p.out, sxy * nz, p.status)) dst[e] = res[r][e];
         }
       }
     }

@@ -7,6 +7,7 @@
 #include <algorithm>
 
 #include "../../include/advdiff_ref_ops.h"
+#include "adv_device.cuh"
 #include "adv_internal.h"
 #include "nvtx_range.h"
 #include "adv_math.cuh"
@@ -25,6 +26,8 @@ struct Grid3 {
     k = (int)(r / ny);
   }
   __device__ __forceinline__ int64_t at(int i, int j, int k) const { return i + pitch * j + pitch * ny * (int64_t)k; }
+  __device__ __forceinline__ int64_t total() const { return pitch * ny * (int64_t)nz; }  // elements addressed
+  int* st;  // device status word (bounds-checked build)
 };
 
 // Nodes a Laplacian writes: i in [i0, i1), j in [j0, j1), k in [k0, k1).
@@ -44,10 +47,12 @@ __global__ void ref_laplace_kernel(Grid3 g, int ndim, int order, Box3 b, int zer
     const int64_t o = g.at(i, j, k);
     const bool in = i >= b.i0 && i < b.i1 && j >= b.j0 && j < b.j1 && k >= b.k0 && k < b.k1;
     if (!in) {
-      if (zero_outside) Lu[o] = T(0);
+      if (zero_outside && ADV_IN_RANGE(o, g.total(), g.st)) Lu[o] = T(0);
       continue;
     }
     const int64_t sy = g.pitch, sz = g.pitch * g.ny;
+    const int64_t span = (int64_t)(order / 2) * (ndim == 3 ? sz : sy);  // the stencil's farthest reach
+    if (!ADV_IN_RANGE(o - span, g.total(), g.st) || !ADV_IN_RANGE(o + span, g.total(), g.st)) continue;
     const T c = u[o];
     T L;
     if (order == 4) {
@@ -89,6 +94,7 @@ __global__ void ref_rk_kernel(Grid3 g, int ndim, int lo, int step, T dt, T* __re
     if (ndim == 3) in = in && k >= lo && k < g.nz - lo;
     if (!in || step < 1 || step > 3) continue;
     const int64_t o = g.at(i, j, k);
+    if (!ADV_IN_RANGE(o, g.total(), g.st)) continue;
     u[o] = stage_combine<T>(step, uo[o], u[o], dt, Lu[o]);
   }
 }
@@ -117,15 +123,17 @@ __global__ void __launch_bounds__(256) ref_sweep_kernel(Grid3 g, int axis, T h, 
     T fp[6], fm[6];                    // split values of nodes a-2 .. a+3
 #pragma unroll
     for (int q = 0; q < 6; ++q) {
-      const T v = u[o0 + q * s];
+      const T v = ADV_IN_RANGE(o0 + q * s, g.total(), g.st) ? u[o0 + q * s] : T(0);
       lf_split<T>(v, fabs(v), fp[q], fm[q]);
     }
     T fu_old = T(0);
     for (int a = 2; a <= na - 4; ++a) {
       const T fu = weno_face_ref<Z, T>(fp[0], fp[1], fp[2], fp[3], fp[4], fm[1], fm[2], fm[3], fm[4], fm[5]);
       const int64_t o = o0 + (int64_t)a * s;
-      if (axis == 0) Lu[o] = div_rn(-sub_rn(fu, fu_old), h);
-      else Lu[o] = sub_rn(Lu[o], div_rn(sub_rn(fu, fu_old), h));
+      if (ADV_IN_RANGE(o, g.total(), g.st)) {
+        if (axis == 0) Lu[o] = div_rn(-sub_rn(fu, fu_old), h);
+        else Lu[o] = sub_rn(Lu[o], div_rn(sub_rn(fu, fu_old), h));
+      }
       fu_old = fu;
 #pragma unroll
       for (int q = 0; q < 5; ++q) {
@@ -133,7 +141,8 @@ __global__ void __launch_bounds__(256) ref_sweep_kernel(Grid3 g, int axis, T h, 
         fm[q] = fm[q + 1];
       }
       if (a + 4 < na) {
-        const T v = u[o0 + (int64_t)(a + 4) * s];
+        const int64_t oa = o0 + (int64_t)(a + 4) * s;
+        const T v = ADV_IN_RANGE(oa, g.total(), g.st) ? u[oa] : T(0);
         lf_split<T>(v, fabs(v), fp[5], fm[5]);
       }
     }
@@ -157,7 +166,7 @@ __global__ void __launch_bounds__(256) ref_sweep_all_kernel(Grid3 g, int axis, T
     const int i = axis == 0 ? 0 : b, j = axis == 0 ? b : (axis == 1 ? 0 : c), k = axis == 2 ? 0 : c;
     const int64_t o0 = g.at(i, j, k);  // node a = 0 of this line
     auto split = [&](int a, T& p, T& m) {
-      const T v = a >= 0 && a < na ? u[o0 + (int64_t)a * s] : T(0);
+      const T v = a >= 0 && a < na && ADV_IN_RANGE(o0 + (int64_t)a * s, g.total(), g.st) ? u[o0 + (int64_t)a * s] : T(0);
       lf_split<T>(v, fabs(v), p, m);
     };
     T fp[6], fm[6];  // split values of nodes a-3 .. a+2 (face a-1/2)
@@ -173,8 +182,10 @@ __global__ void __launch_bounds__(256) ref_sweep_all_kernel(Grid3 g, int axis, T
       split(a + 3, fp[5], fm[5]);  // window: nodes a-2 .. a+3 (face a+1/2)
       const T f_right = weno_face_ref<Z, T, true>(fp[0], fp[1], fp[2], fp[3], fp[4], fm[1], fm[2], fm[3], fm[4], fm[5]);
       const int64_t o = o0 + (int64_t)a * s;
-      if (axis == 0) Lu[o] = div_rn(-sub_rn(f_right, f_left), h);
-      else Lu[o] = sub_rn(Lu[o], div_rn(sub_rn(f_right, f_left), h));
+      if (ADV_IN_RANGE(o, g.total(), g.st)) {
+        if (axis == 0) Lu[o] = div_rn(-sub_rn(f_right, f_left), h);
+        else Lu[o] = sub_rn(Lu[o], div_rn(sub_rn(f_right, f_left), h));
+      }
       f_left = f_right;
     }
   }
@@ -187,6 +198,7 @@ __global__ void ref_viscous_kernel(Grid3 g, T kx, T ky, T kz, int bug_b2, const 
     g.ijk(f, i, j, k);
     if (i < 3 || i > g.nx - 4 || j < 3 || j > g.ny - 4 || k < 3 || k > g.nz - 3) continue;
     const int64_t o = g.at(i, j, k), sy = g.pitch, sz = g.pitch * g.ny;
+    if (!ADV_IN_RANGE(o - 2 * sz, g.total(), g.st) || !ADV_IN_RANGE(o + 2 * sz, g.total(), g.st)) continue;
     const T c = u[o];
     const T vx = sub_rn(add_rn(sub_rn(add_rn(-u[o - 2], mul_rn(T(16), u[o - 1])), mul_rn(T(30), c)), mul_rn(T(16), u[o + 1])), u[o + 2]);
     const T vy = sub_rn(add_rn(sub_rn(add_rn(-u[o - 2 * sy], mul_rn(T(16), u[o - sy])), mul_rn(T(30), c)), mul_rn(T(16), u[o + sy])), u[o + 2 * sy]);
@@ -221,7 +233,7 @@ extern "C" {
 static adv_status ref_laplace_launch(int dtype, int ndim, int order, Box3 b, int zero_outside, int west_first,
                                      int64_t pitch, int nx, int ny, int nz, double kx, double ky, double kz,
                                      const void* u, void* Lu, void* stream) {
-  Grid3 g{nx, ny, nz, pitch};
+  Grid3 g{nx, ny, nz, pitch, device_status_ptr()};
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const dim3 grid = flat_grid((int64_t)nx * ny * nz);
   if (dtype == ADV_F64)
@@ -274,7 +286,7 @@ adv_status adv_ref_rk(int dtype, int ndim, int lo, int64_t pitch, int nx, int ny
   if (st != ADV_OK) return st;
   if (!Lu || (ndim != 2 && ndim != 3) || lo < 0 || step < 1 || step > 3)
     return set_error(ADV_ERR_INVALID_ARG, "ref_rk: bad arguments");
-  Grid3 g{nx, ny, nz, pitch};
+  Grid3 g{nx, ny, nz, pitch, device_status_ptr()};
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const dim3 grid = flat_grid((int64_t)nx * ny * nz);
   if (dtype == ADV_F64)
@@ -293,7 +305,7 @@ adv_status adv_ref_burgers_sweep(int dtype, int axis, int weno, int64_t pitch, i
   if (st != ADV_OK) return st;
   if (axis < 0 || axis > 2 || (weno != ADV_WENO5_JS && weno != ADV_WENO5_Z) || !(h != 0.0))
     return set_error(ADV_ERR_INVALID_ARG, "ref_burgers_sweep: bad arguments");
-  Grid3 g{nx, ny, nz, pitch};
+  Grid3 g{nx, ny, nz, pitch, device_status_ptr()};
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const int nb = axis == 0 ? ny : nx, nc = axis == 2 ? ny : nz;
   const dim3 grid = flat_grid((int64_t)std::max(nb - 6, 1) * std::max(nc - 6, 1));  // one thread per line
@@ -317,7 +329,7 @@ adv_status adv_ref_burgers_sweep_all(int dtype, int axis, int weno, int64_t pitc
   if (st != ADV_OK) return st;
   if (axis < 0 || axis > 2 || (weno != ADV_WENO5_JS && weno != ADV_WENO5_Z) || !(h != 0.0))
     return set_error(ADV_ERR_INVALID_ARG, "ref_burgers_sweep_all: bad arguments");
-  Grid3 g{nx, ny, nz, pitch};
+  Grid3 g{nx, ny, nz, pitch, device_status_ptr()};
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const int nb = axis == 0 ? ny : nx, nc = axis == 2 ? ny : nz;
   const dim3 grid = flat_grid((int64_t)nb * nc);  // one thread per line
@@ -339,7 +351,7 @@ adv_status adv_ref_burgers_viscous(int dtype, int64_t pitch, int nx, int ny, int
   ADV_NVTX_RANGE("adv_ref_burgers_viscous");
   adv_status st = check_grid(dtype, pitch, nx, ny, nz, u, Lu);
   if (st != ADV_OK) return st;
-  Grid3 g{nx, ny, nz, pitch};
+  Grid3 g{nx, ny, nz, pitch, device_status_ptr()};
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const dim3 grid = flat_grid((int64_t)nx * ny * nz);
   if (dtype == ADV_F64)

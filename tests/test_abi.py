@@ -330,3 +330,16 @@ def test_ctypes_structures_match_the_c_layout(tmp_path):
     assert r.returncode == 0, r.stderr
     got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
     assert got == want
+
+
+def test_checked_build_exports_the_same_symbols_and_says_so(native):
+    """libadvdiff_checked.so (ADV_BOUNDS_CHECK) exports every declared symbol; adv_bounds_checked()
+    is 1 there and 0 in the normal build (callable without a GPU)."""
+    so = N.LIBDIR / "libadvdiff_checked.so"
+    exp = _exports(so)
+    for h in ("advdiff.h", "advdiff_ref_ops.h"):
+        assert _declared(ROOT / "include" / h) <= exp
+    checked = C.CDLL(str(so))
+    assert checked.adv_bounds_checked() == 1
+    assert native.adv_bounds_checked() == 0
+    assert native.adv_status_string(N.ADV_ERR_BOUNDS) == b"ADV_ERR_BOUNDS"
