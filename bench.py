@@ -855,6 +855,12 @@ def weno7_config(world: int) -> dict:
             "l2": "per stage 4 sweeps of 64 MiB arrays > 126 MiB L2; 252 MiB L2 flush between GPU steps"}
 
 
+# FP32 flops per cell-stage of the WENO7 right-hand side, counted from the ncu instruction mix of
+# adv_weno7_rhs at 256^3 (FFMA 495 x 2 + FADD 401 + FMUL 558 per cell; no paired instructions:
+# the prototype's operations are each rounded as written; profiles/weno7_rhs_weno7_256_f32_ncu.md)
+WENO7_FLOPS_PER_CELL_STAGE = 1949.0
+
+
 def bench_weno7(args, world, rank, dev, stream, flush, lib):
     """The WENO7 prototype solver at 256^3 FP32: one benchmark step = 10 LSRK(5,4) time steps (50
     stages) through adv_weno7_run; rel-L2 of a 0.05-time-unit run against the same run in FP64."""
@@ -898,6 +904,22 @@ def bench_weno7(args, world, rank, dev, stream, flush, lib):
     ms_max = max_over_ranks(ms, dev)
     work = cfg.numel * 5 * S
     value = replica_throughput(work * args.steps, ms_max, world)
+    # rooflines of one LSRK stage (the L2 flushes' own time subtracted): HBM with the 2N-storage
+    # stage's algorithmic 16 B per cell (read u and r, write u and r), and the FP32 CUDA-core rate
+    fl = timed(lambda: None, args.steps)
+    stage_s = max(ms - fl, 1e-9) * 1e-3 / (args.steps * 5 * S)
+    peak, peak_kind = _peaks()
+    achieved = 16 * cfg.numel / stage_s / 1e9
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    fp32_peak = sms * 128 * 2 * 2070.0 * 1e6 / 1e12
+    flops = WENO7_FLOPS_PER_CELL_STAGE * cfg.numel / stage_s / 1e12
+    roofline = {"bound": "hbm", "kernel": "weno7_face_kernel + weno7_residual_kernel (3 axes per stage)",
+                "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                "traffic": None, "algorithmic_bytes_per_launch": 16 * cfg.numel, "avg_launch_us": stage_s * 1e6,
+                "launch": "one LSRK stage (six kernels)"}
+    roofline_alu = {"bound": "fp32", "achieved": flops, "peak": fp32_peak, "unit": "TFLOP/s",
+                    "frac": flops / fp32_peak, "flops_per_cell_stage": WENO7_FLOPS_PER_CELL_STAGE,
+                    "peak_source": f"nominal: {sms} SMs x 128 FP32 lanes x 2 flop x 2070 MHz"}
     # accuracy: FP32 vs FP64 over a short run from the initial state
     a32 = u0.clone()
     a64 = torch.from_numpy(u0n).to(dev)
@@ -922,7 +944,8 @@ def bench_weno7(args, world, rank, dev, stream, flush, lib):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (the prototype's Gaussian initial state)", "config": weno7_config(world),
-            "roofline": None, "cpu_baseline": cpu_baseline_sample(args, world) if world == 1 else None,
+            "roofline": roofline, "roofline_alu": roofline_alu,
+            "cpu_baseline": cpu_baseline_sample(args, world) if world == 1 else None,
             "e2e": {"value": replica_throughput(work * args.steps, ems, world), "unit": "Gcell-updates/s",
                     "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
             "gpu_launches": int(launched), "clocks": clk.summary(),
