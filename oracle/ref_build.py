@@ -27,13 +27,13 @@ are compiled with g++ together with oracle/ref_tools_shim.cpp into host librarie
 Drop-in programs: each program's own main.cpp + tools.cpp (dense and pitched variants) are linked,
 unmodified and without their kernels.cu, against the GB300 compatibility library that replaces it
 (`refmain_<name>`, once multigpu_advectiondiffusion_gb300/_lib is built). They are linked from
-copies staged under oracle/_ref/src/ (git-ignored), so a GPU host of another architecture links
+copies staged under oracle/_ref/src/ (git-ignored), so a host of another architecture links
 them too (build_mains). The CPU tests check that every symbol resolves; the GPU tests run them.
 
     python oracle/ref_build.py [--src DIR]
 
-DIR defaults to $ADV_REFERENCE_DIR, else /root/reference (where this build's container mounts the
-reference checkout; the GPU hosts have none and use the prebuilt outputs).
+DIR defaults to $ADV_REFERENCE_DIR, else /root/reference (the usual mount point of the reference
+checkout; machines without a checkout use the outputs built beside it).
 """
 from __future__ import annotations
 

@@ -68,7 +68,7 @@ def _reference_line(workload: str) -> dict:
 
 def test_reference_arm_prints_one_contract_line_without_loading_the_library():
     """`bench.py --impl reference` (the tuned CPU loop on the host cores) prints one JSON line with
-    the fields the driver reads, a measured ms_per_step, the GPU arm's config, and never maps
+    the contract's fields, a measured ms_per_step, the GPU arm's config, and never maps
     libadvdiff.so (its inputs come from the oracle's generators); it needs no GPU."""
     line = _reference_line("heat3d")
     assert line["impl"] == "reference" and line["metric"] == "Gcell-updates/s/RK-stage"
@@ -84,7 +84,7 @@ def test_reference_arm_prints_one_contract_line_without_loading_the_library():
 
 def test_reference_arm_heat2d_samples_the_plain_method():
     """C1 (2D 512^2, 1000 steps, the plain method): up to the whole solve per step within the CPU
-    budget (all 1000 steps on an idle host of the GPU machine's size)."""
+    budget (all 1000 steps on an idle 16-core host)."""
     line = _reference_line("heat2d")
     assert line["config"] == bench.heat_config("heat2d", 1)
     assert "of the 1000 time steps" in line["cpu_baseline"]["sample"]
