@@ -529,9 +529,12 @@ def adjoint_setup():
 
 def bench_adjoint(args, world, rank, dev, lib):
     import torch
-    from multigpu_advectiondiffusion_gb300.solvers import burgers_run_fixed, default_interval, heatk_run
+    from multigpu_advectiondiffusion_gb300.solvers import auto_interval, burgers_run_fixed, default_interval, heatk_run
     bc, u0n, utn, dt, hc, kn, k2n, h0n = adjoint_setup()
     u0 = torch.from_numpy(u0n.astype(np.float32)).to(dev)
+    # checkpoint spacing the library's wrappers choose by default: the whole run kept when it fits
+    # in half the free HBM (here: every stage input, no recompute), else sqrt(N)
+    iv_b = auto_interval(ADJ_STEPS, 3, u0)
     with torch.no_grad():
         target = burgers_run_fixed(bc, torch.from_numpy(utn.astype(np.float32)).to(dev), dt, ADJ_STEPS, ADJ_INTERVAL)
 
@@ -544,9 +547,9 @@ def bench_adjoint(args, world, rank, dev, lib):
         torch.cuda.synchronize()
         return a.elapsed_time(b), r
 
-    def grad_burgers(u, tgt):
+    def grad_burgers(u, tgt, interval=iv_b):
         uu = u.clone().requires_grad_(True)
-        tf, uT = ev(lambda: burgers_run_fixed(bc, uu, dt, ADJ_STEPS, ADJ_INTERVAL))
+        tf, uT = ev(lambda: burgers_run_fixed(bc, uu, dt, ADJ_STEPS, interval))
         loss = 0.5 * ((uT - tgt) ** 2).sum()
         tb, _ = ev(loss.backward)
         return tf, tb, uu.grad, float(loss.detach())
@@ -569,10 +572,14 @@ def bench_adjoint(args, world, rank, dev, lib):
         launched = lib.adv_kernel_launch_count() - launches0
     tf, tb = float(np.median(tfs)), float(np.median(tbs))
     cells = ADJ_N ** 3 * 3 * ADJ_STEPS
+    # sqrt(N) checkpoints (every ADJ_INTERVAL steps): the backward run recomputes every interval
+    sq = [grad_burgers(u0, target, ADJ_INTERVAL) for _ in range(3)]
+    tf_s, tb_s = float(np.median([r[0] for r in sq])), float(np.median([r[1] for r in sq]))
+    assert torch.equal(sq[0][2], g32), "the gradient depends on the checkpoint spacing"
     # FP64 adjoint and central differences of the FP64 forward along 16 seeded directions
     u64 = u0.double()
     t64 = target.double()
-    _, _, g64, _ = grad_burgers(u64, t64)
+    _, _, g64, _ = grad_burgers(u64, t64, ADJ_INTERVAL)
     rel64 = (torch.linalg.vector_norm(g32.double() - g64) / torch.linalg.vector_norm(g64)).item()
 
     def J64(u):
@@ -609,9 +616,15 @@ def bench_adjoint(args, world, rank, dev, lib):
             grad_heat(interval)
         hts = [grad_heat(interval) for _ in range(3)]
         return float(np.median([h[0] for h in hts])), float(np.median([h[1] for h in hts]))
-    tfh, tbh = median_grad()
-    # every state kept (interval 1: 200 states of 192^3 FP32, 5.7 GB of HBM): no recompute
-    tfh1, tbh1 = median_grad(1)
+    iv_h = auto_interval(HEATK_STEPS, 1, h0)
+    tfh, tbh = median_grad(iv_h)
+    tfh_s, tbh_s = median_grad(default_interval(HEATK_STEPS))
+
+    def kept(iv, nsteps, arrays, one_b=0):
+        if iv >= nsteps:
+            return (f"whole run kept ({arrays} arrays, {arrays * one_b / 1e9:.1f} GB of HBM; the default when it "
+                    f"fits in half the free memory): no recompute")
+        return f"every {iv} steps (sqrt N; the default when the whole run does not fit)"
     t_grad = max_over_ranks(tf + tb, dev)
     if rank == 0:
         line = {
@@ -632,14 +645,17 @@ def bench_adjoint(args, world, rank, dev, lib):
             "burgers": {"forward_ms": tf, "backward_ms": tb, "backward_over_forward": tb / tf,
                         "forward_value": cells / (tf * 1e-3) / 1e9, "grad_fp32_vs_fp64_rel_l2": rel64,
                         "fd_rel_err_max_16_dirs": max(fd_err), "fd_rel_err_median": float(np.median(fd_err)),
-                        "fd": "central differences of the FP64 forward run, step 1e-8, 16 seeded directions"},
+                        "fd": "central differences of the FP64 forward run, step 1e-8, 16 seeded directions",
+                        "checkpoints": kept(iv_b, ADJ_STEPS, 3 * min(iv_b, ADJ_STEPS) + 3, ADJ_N ** 3 * 4)},
+            "burgers_sqrt_n": {"forward_ms": tf_s, "backward_ms": tb_s, "backward_over_forward": tb_s / tf_s,
+                               "checkpoints": kept(ADJ_INTERVAL, ADJ_STEPS, 0),
+                               "gradient": "bit-identical to the kept run's"},
             "heat_k": {"forward_ms": tfh, "backward_ms": tbh, "backward_over_forward": tbh / tfh,
                        "forward_value": HEATK_N ** 3 * HEATK_STEPS / (tfh * 1e-3) / 1e9,
-                       "checkpoints": f"every {default_interval(HEATK_STEPS)} steps (sqrt N)"},
-            "heat_k_every_state": {"forward_ms": tfh1, "backward_ms": tbh1, "backward_over_forward": tbh1 / tfh1,
-                                   "forward_value": HEATK_N ** 3 * HEATK_STEPS / (tfh1 * 1e-3) / 1e9,
-                                   "checkpoints": "every step (interval 1): no recompute",
-                                   "checkpoint_bytes": HEATK_STEPS * HEATK_N ** 3 * 4},
+                       "checkpoints": kept(iv_h, HEATK_STEPS, min(iv_h, HEATK_STEPS) + 1, HEATK_N ** 3 * 4)},
+            "heat_k_sqrt_n": {"forward_ms": tfh_s, "backward_ms": tbh_s, "backward_over_forward": tbh_s / tfh_s,
+                              "forward_value": HEATK_N ** 3 * HEATK_STEPS / (tfh_s * 1e-3) / 1e9,
+                              "checkpoints": kept(default_interval(HEATK_STEPS), HEATK_STEPS, 0)},
         }
         print(json.dumps(line), flush=True)
 
@@ -1014,7 +1030,8 @@ def burgers_config(args, world: int) -> dict:
 
 def adjoint_config(world: int) -> dict:
     return {"workload": f"adjoint burgers3d {ADJ_N}^3 f32 weno5-z local-lf periodic, {ADJ_STEPS} steps to t={ADJ_T}, "
-                        f"checkpoints every {ADJ_INTERVAL}; heat k(x) {HEATK_N}^3 f32 {HEATK_STEPS} steps",
+                        f"checkpoints by the default policy (the whole run kept in HBM when it fits; every "
+                        f"{ADJ_INTERVAL} steps reported beside); heat k(x) {HEATK_N}^3 f32 {HEATK_STEPS} steps",
             "parallelism": f"replicas{world}"}
 
 

@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define ADV_ABI_VERSION 2
+#define ADV_ABI_VERSION 3
 
 typedef enum adv_status {
   ADV_OK = 0,
@@ -290,13 +290,18 @@ adv_status adv_burgers_adjoint_step(const adv_burgers_desc* d, const void* u_n, 
 /* ckpt: ceil(nsteps/interval) arrays; work: 3*interval + 2 arrays (enough for both runs). */
 adv_status adv_burgers_checkpoint_bytes(const adv_burgers_desc* d, int64_t nsteps, int64_t interval,
                                         size_t* ckpt_bytes, size_t* work_bytes);
-/* nsteps fixed-dt steps in place on u; ckpt may be NULL. */
+/* nsteps fixed-dt steps in place on u; ckpt may be NULL. With checkpoints, the run also leaves
+ * the stage inputs of its last checkpoint interval in work, where adv_burgers_backward would
+ * recompute them (interval >= nsteps: every stage input of the run, 3*nsteps - 1 arrays). */
 adv_status adv_burgers_forward(const adv_burgers_desc* d, void* u, double dt, int64_t nsteps,
                                int64_t interval, void* ckpt, void* work, void* stream);
-/* lam: in dJ/du at step nsteps, out dJ/du at step 0. */
+/* lam: in dJ/du at step nsteps, out dJ/du at step 0. flags: ADV_BURGERS_LAST_INTERVAL_IN_WORK
+ * when work still holds what adv_burgers_forward left there (the same nsteps, interval, dt and
+ * ckpt, nothing written to work since): the last interval is then not recomputed. */
+#define ADV_BURGERS_LAST_INTERVAL_IN_WORK 1
 adv_status adv_burgers_backward(const adv_burgers_desc* d, double dt, int64_t nsteps,
                                 int64_t interval, const void* ckpt, void* lam, void* work,
-                                void* stream);
+                                int flags, void* stream);
 
 /* ------------------------------------------------------------------ batched ensembles
  * Many independent 3D problems of uneven size and coefficients advanced together. No counterpart

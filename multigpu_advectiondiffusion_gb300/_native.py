@@ -22,6 +22,7 @@ ADV_DIV_F32, ADV_DIV_F64, ADV_DIV_FAST = 0, 1, 2
 ADV_DT_FIXED, ADV_DT_MAXU = 0, 1
 ADV_ENSEMBLE_DIRECT = 1
 ADV_HEATK_LAST_INTERVAL_IN_WORK = 1
+ADV_BURGERS_LAST_INTERVAL_IN_WORK = 1
 
 
 class HeatDesc(C.Structure):
@@ -107,7 +108,7 @@ SIGNATURES = [
     ("adv_burgers_checkpoint_bytes", _I, [C.POINTER(BurgersDesc), _I64, _I64, C.POINTER(C.c_size_t),
                                           C.POINTER(C.c_size_t)]),
     ("adv_burgers_forward", _I, [C.POINTER(BurgersDesc), _VP, _D, _I64, _I64, _VP, _VP, _VP]),
-    ("adv_burgers_backward", _I, [C.POINTER(BurgersDesc), _D, _I64, _I64, _VP, _VP, _VP, _VP]),
+    ("adv_burgers_backward", _I, [C.POINTER(BurgersDesc), _D, _I64, _I64, _VP, _VP, _VP, _I, _VP]),
     ("adv_ensemble_create", _I, [C.POINTER(HeatMember), _I, _I, C.POINTER(BurgersMember), _I,
                                  C.POINTER(_VP)]),
     ("adv_ensemble_run", _I, [_VP, _I64, _I, _VP]),

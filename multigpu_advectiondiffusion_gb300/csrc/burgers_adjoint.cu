@@ -568,23 +568,39 @@ adv_status adv_burgers_forward(const adv_burgers_desc* d, void* u, double dt, in
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const size_t one = one_array(*d);
   const size_t nb = (size_t)d->nx * d->ny * d->nz * (d->dtype == ADV_F32 ? 4 : 8);
-  char* w1 = static_cast<char*>(work);
-  char* w2 = w1 + one;
+  char* const ub = static_cast<char*>(u);
+  char* const states = static_cast<char*>(work);
+  // Steps before the last checkpoint interval run in place on u through two stage arrays. The
+  // last interval (with checkpoints) writes its stage inputs where adv_burgers_backward would
+  // recompute them -- step r of the interval: u1 at 3r, u2 at 3r + 1, its result u^{n+1} at
+  // 3r + 2 -- and its last step writes u; with interval >= nsteps the whole run is kept and the
+  // backward run recomputes nothing.
+  const int64_t m = (nsteps + interval - 1) / interval;
+  const int64_t n_last = ckpt && nsteps > 0 ? (m - 1) * interval : nsteps;
   for (int64_t n = 0; n < nsteps; ++n) {
     if (ckpt && n % interval == 0)
       ADV_CUDA_TRY(cudaMemcpyAsync(static_cast<char*>(ckpt) + (n / interval) * one, u, nb, cudaMemcpyDeviceToDevice, s));
-    if ((st = forward_step(*d, u, w1, w2, u, dt, s)) != ADV_OK) return st;
+    if (n < n_last) {
+      st = forward_step(*d, ub, states, states + one, ub, dt, s);
+    } else {
+      const int64_t r = n - n_last;
+      const char* un = r == 0 ? ub : states + (3 * r - 1) * one;
+      char* next = n + 1 < nsteps ? states + (3 * r + 2) * one : ub;
+      st = forward_step(*d, un, states + 3 * r * one, states + (3 * r + 1) * one, next, dt, s);
+    }
+    if (st != ADV_OK) return st;
   }
   return ADV_OK;
 }
 
 adv_status adv_burgers_backward(const adv_burgers_desc* d, double dt, int64_t nsteps, int64_t interval,
-                                const void* ckpt, void* lam, void* work, void* stream) {
+                                const void* ckpt, void* lam, void* work, int flags, void* stream) {
   ADV_NVTX_RANGE("adv_burgers_backward");
   adv_status st = adjoint_validate(d);
   if (st != ADV_OK) return st;
   if (!ckpt || !lam || !work) return set_error(ADV_ERR_INVALID_ARG, "burgers adjoint: null buffer");
   if (nsteps < 0 || interval < 1 || !(dt > 0)) return set_error(ADV_ERR_INVALID_ARG, "burgers adjoint: bad nsteps/interval/dt");
+  if (flags & ~ADV_BURGERS_LAST_INTERVAL_IN_WORK) return set_error(ADV_ERR_INVALID_ARG, "burgers adjoint: unknown flags");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const size_t one = one_array(*d);
   char* states = static_cast<char*>(work);             // 3 interval - 1 arrays
@@ -598,7 +614,8 @@ adv_status adv_burgers_backward(const adv_burgers_desc* d, double dt, int64_t ns
     auto un = [&](int64_t r) -> const char* { return r == 0 ? base : states + (3 * r - 1) * one; };
     auto u1 = [&](int64_t r) { return states + (3 * r) * one; };
     auto u2 = [&](int64_t r) { return states + (3 * r + 1) * one; };
-    for (int64_t r = 0; r < n1 - n0; ++r) {
+    const bool kept = seg == m - 1 && (flags & ADV_BURGERS_LAST_INTERVAL_IN_WORK);
+    for (int64_t r = 0; !kept && r < n1 - n0; ++r) {
       char* next = r + 1 < n1 - n0 ? states + (3 * (r + 1) - 1) * one : nullptr;
       if (next) {
         if ((st = forward_step(*d, un(r), u1(r), u2(r), next, dt, s)) != ADV_OK) return st;

@@ -358,12 +358,34 @@ def default_interval(nsteps: int) -> int:
     return max(1, math.ceil(math.sqrt(max(nsteps, 1))))
 
 
+def checkpoint_interval(nsteps: int, arrays_per_step: int, array_bytes: int, free_bytes: int) -> int:
+    """Checkpoint spacing of a differentiable run. The whole run is kept (interval = nsteps: the
+    forward run leaves every state or stage input in its work buffer and the backward run
+    recomputes nothing) when its arrays_per_step * nsteps arrays fit in half of free_bytes (the
+    device's free memory); otherwise sqrt(N) spacing."""
+    nsteps = max(int(nsteps), 1)
+    if arrays_per_step * nsteps * array_bytes <= free_bytes // 2:
+        return nsteps
+    return default_interval(nsteps)
+
+
+def auto_interval(nsteps: int, arrays_per_step: int, like, need_grad: bool = True) -> int:
+    """checkpoint_interval for a run on like's device; sqrt(N) when no gradient will be taken
+    (the kept run would only cost memory)."""
+    if not need_grad:
+        return default_interval(nsteps)
+    import torch
+    free, _ = torch.cuda.mem_get_info(like.device)
+    one = (like.numel() * like.element_size() + 255) // 256 * 256
+    return checkpoint_interval(nsteps, arrays_per_step, one, free)
+
+
 def _autograd():
     import torch
 
     class HeatKRun(torch.autograd.Function):
         """u(T) = heat-with-k(x) forward run from (k, u0); backward by the hand-written adjoint
-        (adv_heatk_backward) over sqrt(N) checkpoints. For gradient checks."""
+        (adv_heatk_backward) over checkpoints every `interval` steps."""
 
         @staticmethod
         def forward(ctx, k, u0, cfg, nsteps, interval):
@@ -398,7 +420,7 @@ def _burgers_autograd():
 
     class BurgersRun(torch.autograd.Function):
         """u(T) of nsteps fixed-dt SSP-RK3 steps (periodic, local LF) from u0; backward by the
-        hand-written adjoint (adv_burgers_backward) over sqrt(N) checkpoints. For gradient checks."""
+        hand-written adjoint (adv_burgers_backward) over checkpoints every `interval` steps."""
 
         @staticmethod
         def forward(ctx, u0, cfg, dt, nsteps, interval):
@@ -419,8 +441,10 @@ def _burgers_autograd():
         def backward(ctx, grad_u):
             lam = grad_u.detach().clone().contiguous()
             d = ctx.cfg.desc(_fields(ctx.cfg.numel, lam))
+            # the forward run left its last interval's stage inputs in ctx.work, untouched since
             N.check(N.load().adv_burgers_backward(C.byref(d), float(ctx.dt), int(ctx.nsteps), int(ctx.interval),
                                                   _ptr(ctx.ckpt), _ptr(lam), _ptr(ctx.work),
+                                                  N.ADV_BURGERS_LAST_INTERVAL_IN_WORK,
                                                   N.stream_handle(torch.cuda.current_stream())),
                     "adv_burgers_backward")
             return lam, None, None, None, None
@@ -432,11 +456,16 @@ _BurgersRun = None
 
 
 def burgers_run_fixed(cfg: BurgersConfig, u0, dt: float, nsteps: int, interval: int | None = None):
-    """Differentiable (w.r.t. u0) run of nsteps fixed-dt steps; returns u(T)."""
+    """Differentiable (w.r.t. u0) run of nsteps fixed-dt steps; returns u(T). interval None: the
+    whole run kept when its 3 stage inputs per step fit in half the free device memory (the
+    backward run then recomputes nothing), else sqrt(N) checkpoints."""
+    import torch
     global _BurgersRun
     if _BurgersRun is None:
         _BurgersRun = _burgers_autograd()
-    return _BurgersRun.apply(u0, cfg, float(dt), int(nsteps), int(interval or default_interval(nsteps)))
+    if not interval:
+        interval = auto_interval(nsteps, 3, u0, torch.is_grad_enabled() and u0.requires_grad)
+    return _BurgersRun.apply(u0, cfg, float(dt), int(nsteps), int(interval))
 
 
 def burgers_adjoint_step(cfg: BurgersConfig, u_n, u1, u2, dt: float, lam, work=None, stream=None):
@@ -456,11 +485,17 @@ _HeatKRun = None
 
 
 def heatk_run(cfg: HeatKConfig, k, u0, nsteps: int, interval: int | None = None):
-    """Differentiable (w.r.t. k and u0) forward run of nsteps steps; returns u(T)."""
+    """Differentiable (w.r.t. k and u0) forward run of nsteps steps; returns u(T). interval None:
+    the whole run kept when its states fit in half the free device memory (the backward run then
+    recomputes nothing), else sqrt(N) checkpoints."""
+    import torch
     global _HeatKRun
     if _HeatKRun is None:
         _HeatKRun = _autograd()
-    return _HeatKRun.apply(k, u0, cfg, int(nsteps), int(interval or default_interval(nsteps)))
+    if not interval:
+        need = torch.is_grad_enabled() and (k.requires_grad or u0.requires_grad)
+        interval = auto_interval(nsteps, 1, u0, need)
+    return _HeatKRun.apply(k, u0, cfg, int(nsteps), int(interval))
 
 
 class Ensemble:

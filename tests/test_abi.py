@@ -87,7 +87,7 @@ def test_ref_variant_ops_reject_bad_arguments_without_gpu(native):
 
 
 def test_abi_version_and_strings(native):
-    assert native.adv_abi_version() == 2
+    assert native.adv_abi_version() == 3
     assert native.adv_status_string(N.ADV_ERR_TIMEOUT) == b"ADV_ERR_TIMEOUT"
 
 

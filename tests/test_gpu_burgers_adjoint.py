@@ -58,9 +58,10 @@ def test_adjoint_step_matches_oracle(cuda, native, oracle, weno, shape):
         assert _rel(got, want) < tol, (dtype, _rel(got, want))
 
 
-@pytest.mark.parametrize("interval", [1, 3, 7])
+@pytest.mark.parametrize("interval", [1, 3, 7, 10, None])
 @pytest.mark.parametrize("weno", ["z", "js"])
 def test_checkpointed_gradient_matches_oracle(cuda, native, oracle, weno, interval):
+    """interval None: the wrapper's choice (here the whole run kept, nothing recomputed)."""
     import torch
     shape = (24, 20, 18)
     cfg = _cfg(shape, weno)
@@ -76,6 +77,45 @@ def test_checkpointed_gradient_matches_oracle(cuda, native, oracle, weno, interv
     torch.cuda.synchronize()
     assert abs(loss.item() - J) <= 1e-12 * J
     assert _rel(uu.grad.cpu().numpy(), g) < 1e-11
+
+
+@pytest.mark.parametrize("steps,interval", [(10, 4), (12, 4), (7, 7), (5, 9), (9, 1), (1, 3)])
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_backward_with_and_without_the_kept_interval(cuda, native, dtype, steps, interval):
+    """adv_burgers_forward leaves its last interval's stage inputs in work; the backward run that
+    takes them (ADV_BURGERS_LAST_INTERVAL_IN_WORK) and the one that recomputes them (flags 0) give
+    the same bits, for last intervals of every length, and the forward's result is the plain
+    run's (no checkpoints)."""
+    import torch
+    shape = (24, 20, 18)
+    cfg = _cfg(shape, "z")
+    u0 = _state(cfg, 5).astype(dtype)
+    target = _state(cfg, 6).astype(dtype)
+    dt = 0.3 * cfg.dx / np.abs(u0).max()
+    code = N.ADV_F32 if dtype == np.float32 else N.ADV_F64
+    d = cfg.desc(code)
+    cb, wb = N.C.c_size_t(0), N.C.c_size_t(0)
+    assert native.adv_burgers_checkpoint_bytes(N.C.byref(d), steps, interval, N.C.byref(cb), N.C.byref(wb)) == N.ADV_OK
+    plain = _t(u0, cuda)
+    w2 = torch.empty(2 * plain.numel() + 256, dtype=plain.dtype, device=cuda)
+    assert native.adv_burgers_forward(N.C.byref(d), plain.data_ptr(), dt, steps, interval, None, w2.data_ptr(),
+                                      None) == N.ADV_OK
+    res = []
+    for flags in (N.ADV_BURGERS_LAST_INTERVAL_IN_WORK, 0):
+        u = _t(u0, cuda)
+        ckpt = torch.empty(cb.value, dtype=torch.uint8, device=cuda)
+        work = torch.empty(wb.value, dtype=torch.uint8, device=cuda)
+        assert native.adv_burgers_forward(N.C.byref(d), u.data_ptr(), dt, steps, interval, ckpt.data_ptr(),
+                                          work.data_ptr(), None) == N.ADV_OK
+        assert torch.equal(u, plain)
+        lam = u - _t(target, cuda)
+        assert native.adv_burgers_backward(N.C.byref(d), dt, steps, interval, ckpt.data_ptr(), lam.data_ptr(),
+                                           work.data_ptr(), flags, None) == N.ADV_OK
+        torch.cuda.synchronize()
+        res.append(lam.cpu().numpy())
+    assert np.array_equal(res[0], res[1])
+    assert native.adv_burgers_backward(N.C.byref(d), dt, steps, interval, ckpt.data_ptr(), lam.data_ptr(),
+                                       work.data_ptr(), 2, None) == N.ADV_ERR_INVALID_ARG
 
 
 @pytest.mark.parametrize("weno", ["z", "js"])

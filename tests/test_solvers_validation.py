@@ -135,3 +135,14 @@ def test_valid_calls_reach_the_native_library(monkeypatch):
         assert want in names, want
     stage = dict(fake.calls)["adv_burgers_stage"]
     assert stage[2:5] == (0x10000, 0x10000, 0x10000) and stage[7] == 0x10000  # fields and the key
+
+
+def test_checkpoint_interval_keeps_the_run_when_it_fits():
+    """The differentiable runs keep every state (interval = nsteps: no recompute in the backward
+    run) when the kept arrays fit in half the free memory, else space checkpoints sqrt(N) apart."""
+    one = 8 << 20                                  # one 128^3 FP32 array
+    assert S.checkpoint_interval(400, 3, one, 1200 * one * 2) == 400      # exactly half the free memory
+    assert S.checkpoint_interval(400, 3, one, 1200 * one * 2 - 1) == 20   # one byte short: sqrt(400)
+    assert S.checkpoint_interval(200, 1, one, 10 * one) == S.default_interval(200) == 15
+    assert S.checkpoint_interval(0, 1, one, 1 << 40) == 1
+    assert S.default_interval(1) == 1 and S.default_interval(10) == 4
