@@ -60,11 +60,12 @@ __device__ __forceinline__ float weno_side_fast(float a, float b, float c, float
   const float q1 = fmaf(-0.25f, s1, fmaf(r12, t1, c));
   const float q2 = fmaf(-0.25f, s2, fmaf(r12, t2, c));
   float w0, w1, w2;
-  if (Z) {  // alpha_k = d_k (1 + tau/b_k), times 10 b0 b1 b2
+  if (Z) {  // alpha_k = d_k (1 + tau/b_k), times 10 b0 b1 b2: d_k (P + tau P/b_k), P = b0 b1 b2
     const float tau = fabsf(b0 - b2);
-    w0 = (b0 + tau) * (b1 * b2);
-    w1 = (6.f * (b1 + tau)) * (b0 * b2);
-    w2 = (3.f * (b2 + tau)) * (b0 * b1);
+    const float p12 = b1 * b2, P = b0 * p12;
+    w0 = fmaf(tau, p12, P);
+    w1 = 6.f * fmaf(tau, b0 * b2, P);
+    w2 = 3.f * fmaf(tau, b0 * b1, P);
   } else {  // alpha_k = d_k / b_k^2, times 10 (b0 b1 b2)^2
     const float p12 = b1 * b2, p02 = b0 * b2, p01 = b0 * b1;
     w0 = p12 * p12;
@@ -119,9 +120,10 @@ __device__ __forceinline__ float2 weno_side_fast2(float2 a, float2 b, float2 c, 
   if (Z) {
     const float2 dd = sub2(b0, b2);
     const float2 tau = make_float2(fabsf(dd.x), fabsf(dd.y));
-    w0 = mul2(add2(b0, tau), mul2(b1, b2));
-    w1 = mul2(mul2(f2(6.f), add2(b1, tau)), mul2(b0, b2));
-    w2 = mul2(mul2(f2(3.f), add2(b2, tau)), mul2(b0, b1));
+    const float2 p12 = mul2(b1, b2), P = mul2(b0, p12);
+    w0 = fma2(tau, p12, P);
+    w1 = mul2(f2(6.f), fma2(tau, mul2(b0, b2), P));
+    w2 = mul2(f2(3.f), fma2(tau, mul2(b0, b1), P));
   } else {
     const float2 p12 = mul2(b1, b2), p02 = mul2(b0, b2), p01 = mul2(b0, b1);
     w0 = mul2(p12, p12);
