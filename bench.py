@@ -877,9 +877,11 @@ def weno7_config(world: int) -> dict:
 
 
 # FP32 flops per cell-stage of the WENO7 right-hand side, counted from the ncu instruction mix of
-# adv_weno7_rhs at 256^3 (FFMA 495 x 2 + FADD 401 + FMUL 558 per cell; no paired instructions:
-# the prototype's operations are each rounded as written; profiles/weno7_rhs_weno7_256_f32_ncu.md)
-WENO7_FLOPS_PER_CELL_STAGE = 1949.0
+# adv_weno7_rhs at 256^3 (FP32 state: the tiled face kernels with paired instructions and
+# reciprocal-based weights). Per cell: FFMA2 153 x 4 + FADD2 21 x 2 + FMUL2 96 x 2 + FFMA 22.3 x 2
+# + FADD 11.0 + FMUL 50.6 = 952.25. (The prototype's own operand order, which the FP64 state
+# keeps, counted 1949: FFMA 495 x 2 + FADD 401 + FMUL 558.)
+WENO7_FLOPS_PER_CELL_STAGE = 952.25
 
 
 def bench_weno7(args, world, rank, dev, stream, flush, lib):
@@ -934,7 +936,7 @@ def bench_weno7(args, world, rank, dev, stream, flush, lib):
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
     fp32_peak = sms * 128 * 2 * 2070.0 * 1e6 / 1e12
     flops = WENO7_FLOPS_PER_CELL_STAGE * cfg.numel / stage_s / 1e12
-    roofline = {"bound": "hbm", "kernel": "weno7_face_kernel + weno7_residual_kernel (3 axes per stage)",
+    roofline = {"bound": "hbm", "kernel": "weno7_face_fast_kernel + weno7_residual_kernel (3 axes per stage)",
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                 "traffic": None, "algorithmic_bytes_per_launch": 16 * cfg.numel, "avg_launch_us": stage_s * 1e6,
                 "launch": "one LSRK stage (six kernels)"}
@@ -1232,8 +1234,8 @@ def main():
             lambda: [heat_run(cfg_c, u64c, inner, ws64, stream=sh) for _ in range(3)]) / 1e9
     else:
         # ALU roofline: the stage is compute-bound. FP32 flops per cell-stage from the ncu
-        # instruction mix of the stage kernel (FFMA2 = 4, FADD2/FMUL2/FFMA = 2, FADD/FMUL = 1;
-        # profiles/burgers_stage_burgers3d_256_f32_ncu.md); peak = nominal FP32 CUDA-core rate.
+        # instruction mix of the stage kernel (FFMA2 = 4, FADD2/FMUL2/FFMA = 2, FADD/FMUL = 1);
+        # peak = nominal FP32 CUDA-core rate.
         sm_mhz = 2070.0
         try:
             sm_mhz = float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text()).get("sm_max_mhz", sm_mhz))

@@ -14,9 +14,10 @@
 //   * time: dt = CFL dx / max|u| trimmed to land on tEnd, the five-stage fourth-order 2N-storage
 //     Runge-Kutta scheme of Carpenter & Kennedy (NASA TM-109112, 1994): r = A_s r + dt R(u),
 //     u = u - B_s r.
-// Every operation is evaluated in the prototypes' operand order with correctly rounded
-// intrinsics (no contraction), so the FP64 results are those of the prototypes -- and of the CPU
-// oracle that restates them -- bit for bit; the FP32 state runs the same operations in FP32.
+// For the FP64 state every operation is evaluated in the prototypes' operand order with correctly
+// rounded intrinsics (no contraction), so its results are those of the prototypes -- and of the
+// CPU oracle that restates them -- bit for bit; the FP32 state's faces take a faster form of the
+// same scheme (the FP32 face kernels below).
 //
 // Kernels. Per stage and axis: a face kernel (one thread per face i+1/2, the two split parts'
 // reconstructions hp and hn into two face arrays) and a residual kernel (one thread per node,
@@ -29,11 +30,13 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <type_traits>
 
 #include "adv_device.cuh"
 #include "adv_internal.h"
 #include "adv_math.cuh"
 #include "nvtx_range.h"
+#include "weno.cuh"
 
 namespace adv {
 namespace {
@@ -141,10 +144,157 @@ __global__ void __launch_bounds__(256) weno7_face_kernel(const T* __restrict__ u
   }
 }
 
+// ------------------------------------------------------------------ FP32 face kernels
+// The FP32 state takes a form written for speed rather than the prototype's operand order (the
+// FP64 state keeps that order, bit for bit):
+//  * a tile of faces stages the split parts (f+, f-) of its cells in shared memory once --
+//    64-bit pairs, one load per stencil cell -- instead of every face re-reading and re-splitting
+//    its eight cells;
+//  * both split parts of a face are reconstructed together in paired FP32 instructions (lane x
+//    the part moving towards +x on cells i-3..i+3, lane y the other on cells i-2..i+4: the
+//    smoothness indicators use the same coefficients on both);
+//  * the prototype's weights d_k / (eps + beta_k)^2, normalised, are evaluated from
+//    r_k = e_min / e_k (e_k = eps + beta_k, e_min the smallest): alpha_k = d_k r_k^2 lies in
+//    (0, d_k] and the largest is at least d_min, so no product overflows, underflows or leaves a
+//    zero sum, and the face value sum_k alpha_k q_k / (12 sum_k alpha_k) takes one division; the
+//    quotients use the reciprocal-based division (at most 2 ulp each).
+// Tiles: AX = 0, 32 faces along x by 8 rows (one face per thread); AX = 1, 2, 32 x positions by
+// 32 faces along the line (four faces per thread). Cells past a line's ends are its end values
+// (clamped), as in the prototype.
+namespace w7f {
+constexpr int TX = 32;  // x positions (AX = 0: faces) per tile
+constexpr int TR = 8;   // rows per tile, AX = 0
+constexpr int TL = 32;  // faces along the line per tile, AX = 1, 2
+}  // namespace w7f
+
+template <int K>
+__device__ __forceinline__ float2 w7_beta2(const float2* x) {  // x: the candidate's cells 0..3
+  constexpr W7B B = kBeta[K];
+  auto c = [](double v) { return f2((float)v); };
+  const float2 a = fma2(c(B.k[1]), x[3], mul2(c(B.k[0]), x[2]));
+  const float2 b = fma2(c(B.k[5]), x[3], fma2(c(B.k[4]), x[B.d], fma2(c(B.k[3]), x[B.c], mul2(c(B.k[2]), x[B.b]))));
+  const float2 t = fma2(c(B.k[9]), x[3], fma2(c(B.k[8]), x[B.t], mul2(c(B.k[7]), x[B.s])));
+  return fma2(x[0], b, fma2(x[1], t, fma2(mul2(c(B.k[6]), x[3]), x[3], mul2(x[2], a))));
+}
+
+template <int K>
+__device__ __forceinline__ float2 w7_cand2(const float2* x) {  // 12 x candidate K, per lane
+  auto c = [](int j) { return make_float2((float)kPolyP[K][j], (float)kPolyM[K][j]); };
+  return fma2(c(3), x[3], fma2(c(2), x[2], fma2(c(1), x[1], mul2(c(0), x[0]))));
+}
+
+// x[j] = (f+, f-) of cells i-3+j, j = 0..7. Returns (hn, hp): the +x part on cells i-3..i+3, the
+// -x part on cells i-2..i+4.
+__device__ __forceinline__ float2 w7_face2(const float2 (&c)[8]) {
+  float2 x[7];
+#pragma unroll
+  for (int j = 0; j < 7; ++j) x[j] = make_float2(c[j].x, c[j + 1].y);
+  const float2 eps = f2(1e-6f);
+  const float2 e0 = add2(w7_beta2<0>(x + 0), eps), e1 = add2(w7_beta2<1>(x + 1), eps);
+  const float2 e2 = add2(w7_beta2<2>(x + 2), eps), e3 = add2(w7_beta2<3>(x + 3), eps);
+  const float2 em = make_float2(fminf(fminf(e0.x, e1.x), fminf(e2.x, e3.x)), fminf(fminf(e0.y, e1.y), fminf(e2.y, e3.y)));
+  auto alpha = [&](float2 e, int k) {
+    const float2 r = make_float2(__fdividef(em.x, e.x), __fdividef(em.y, e.y));
+    return mul2(mul2(make_float2((float)kLinP[k], (float)kLinM[k]), r), r);
+  };
+  const float2 a0 = alpha(e0, 0), a1 = alpha(e1, 1), a2 = alpha(e2, 2), a3 = alpha(e3, 3);
+  const float2 num = fma2(a3, w7_cand2<3>(x + 3), fma2(a2, w7_cand2<2>(x + 2), fma2(a1, w7_cand2<1>(x + 1),
+                                                                                   mul2(a0, w7_cand2<0>(x + 0)))));
+  const float2 den = mul2(f2(12.f), add2(add2(a0, a1), add2(a2, a3)));
+  return make_float2(__fdividef(num.x, den.x), __fdividef(num.y, den.y));
+}
+
+// (f+, f-) of one node value: f = u^2/2 split with a = |u|.
+__device__ __forceinline__ float2 w7_split_fast(float v) {
+  const float f = 0.5f * v * v, av = fabsf(v) * v;
+  return make_float2(0.5f * (f + av), 0.5f * (f - av));
+}
+
+template <int AX>
+__global__ void __launch_bounds__(256) weno7_face_fast_kernel(const float* __restrict__ u, float* __restrict__ hp,
+                                                              float* __restrict__ hn, W7Geom g) {
+  using namespace w7f;
+  constexpr int ROWS = AX == 0 ? TR : TL + 7;  // shared rows: y rows (AX 0) or line cells
+  constexpr int COLS = AX == 0 ? TX + 8 : TX;  // shared columns: x cells (AX 0; 39 used) or x
+  __shared__ float2 fs[ROWS][COLS];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int nx = g.nx, ny = g.ny, nz = g.nz;
+  const int x0 = blockIdx.x * TX;
+  // line position of the tile's first face and the fixed coordinate(s)
+  const int l0 = AX == 0 ? x0 : blockIdx.y * TL;
+  const int N = AX == 0 ? nx : AX == 1 ? ny : nz;
+  const int64_t sxy = (int64_t)nx * ny;
+  auto at = [&](int x, int y, int z) { return (int64_t)z * sxy + (int64_t)y * nx + x; };
+  for (int e = threadIdx.x; e < ROWS * COLS; e += 256) {
+    const int r = e / COLS, c = e - r * COLS;
+    float2 v = make_float2(0.f, 0.f);
+    if (AX == 0) {
+      const int y = blockIdx.y * TR + r, z = blockIdx.z;
+      const int x = min(max(x0 + c - 3, 0), nx - 1);
+      if (c < TX + 7 && y < ny) v = w7_split_fast(u[at(x, y, z)]);
+    } else {
+      const int x = x0 + c, l = min(max(l0 + r - 3, 0), N - 1);
+      if (x < nx) v = w7_split_fast(AX == 1 ? u[at(x, l, blockIdx.z)] : u[at(x, blockIdx.z, l)]);
+    }
+    fs[r][c] = v;
+  }
+  __syncthreads();
+  if (AX == 0) {
+    const int x = x0 + tx, y = blockIdx.y * TR + ty;
+    if (x < nx && y < ny) {
+      float2 c[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) c[j] = fs[ty][tx + j];
+      const float2 h = w7_face2(c);
+      const int64_t o = at(x, y, blockIdx.z);
+      hn[o] = h.x;
+      hp[o] = h.y;
+    }
+  } else {
+    const int x = x0 + tx;
+    if (x < nx) {
+#pragma unroll
+      for (int j = 0; j < TL / 8; ++j) {
+        const int t = ty + 8 * j, l = l0 + t;
+        if (l < N) {
+          float2 c[8];
+#pragma unroll
+          for (int m = 0; m < 8; ++m) c[m] = fs[t + m][tx];
+          const float2 h = w7_face2(c);
+          const int64_t o = AX == 1 ? at(x, l, blockIdx.z) : at(x, blockIdx.z, l);
+          hn[o] = h.x;
+          hp[o] = h.y;
+        }
+      }
+    }
+  }
+}
+
+// Face launch of axis AX: the tiled FP32 kernel where its grid fits, else the generic kernel.
+template <class T, int AX>
+void weno7_face_launch(const T* u, T* hp, T* hn, const W7Geom& g, int grid, cudaStream_t s) {
+  if constexpr (std::is_same<T, float>::value) {
+    using namespace w7f;
+    const int64_t gx = (g.nx + TX - 1) / TX;
+    const int64_t gy = AX == 0 ? (g.ny + TR - 1) / TR : AX == 1 ? (g.ny + TL - 1) / TL : (g.nz + TL - 1) / TL;
+    const int64_t gz = AX == 2 ? g.ny : g.nz;
+    if (gx <= 0x7fffffff && gy <= 65535 && gz <= 65535) {
+      weno7_face_fast_kernel<AX><<<dim3((unsigned)gx, (unsigned)gy, (unsigned)gz), 256, 0, s>>>(u, hp, hn, g);
+      return;
+    }
+  }
+  weno7_face_kernel<T, AX><<<grid, 256, 0, s>>>(u, hp, hn, g);
+}
+
 // Residual kernel of axis AX: res_i = (((hp_i + hn_i) - hp_{i-1}) - hn_{i-1}) / h (0 for the face
 // left of node 0), accumulated into acc (FIRST: acc = res). LAST: then the Runge-Kutta update
 // r = A r + dt acc, u = u - B r in place, and (REDUCE) max|u_new| into *maxkey.
-template <class T, int AX, bool FIRST, bool LAST>
+constexpr int kW7ResZ = 16;  // z planes per thread of the tiled residual kernel
+
+// TILED: a 3D grid of 32 x 8 (x, y) tiles, each thread walking kW7ResZ z planes of its column,
+// so a node's line position comes from its coordinates; otherwise a grid-stride loop over the
+// flat index (whose line position takes an integer division).
+template <class T, int AX, bool FIRST, bool LAST, bool TILED>
 __global__ void __launch_bounds__(256) weno7_residual_kernel(const T* __restrict__ hp, const T* __restrict__ hn,
                                                              T* __restrict__ acc, T* __restrict__ r, T* __restrict__ u,
                                                              W7Geom g, T h, int stage, const double* dt_dev,
@@ -155,8 +305,23 @@ __global__ void __launch_bounds__(256) weno7_residual_kernel(const T* __restrict
   const T A = T(kA[stage]), B = T(kB[stage]);
   const T dt = LAST ? T(*dt_dev) : T(0);
   K kmax = 0;
-  for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < g.n; o += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = AX == 0 ? o % g.nx : AX == 1 ? (o / g.nx) % g.ny : o / ((int64_t)g.nx * g.ny);
+  int64_t o, o_end, o_step;
+  int64_t i = 0;
+  if (TILED) {
+    const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
+    const int z0 = blockIdx.z * kW7ResZ, z1 = min(g.nz, z0 + kW7ResZ);
+    const bool in = x < g.nx && y < g.ny;
+    o_step = (int64_t)g.nx * g.ny;
+    o = (int64_t)z0 * o_step + (int64_t)y * g.nx + x;
+    o_end = in ? o + (int64_t)(z1 - z0) * o_step : o;
+    i = AX == 0 ? x : AX == 1 ? y : z0;
+  } else {
+    o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    o_end = g.n;
+    o_step = (int64_t)gridDim.x * blockDim.x;
+  }
+  for (; o < o_end; o += o_step, i += (TILED && AX == 2) ? 1 : 0) {
+    if (!TILED) i = AX == 0 ? o % g.nx : AX == 1 ? (o / g.nx) % g.ny : o / ((int64_t)g.nx * g.ny);
     const T hp0 = i > 0 ? hp[o - stride] : T(0), hn0 = i > 0 ? hn[o - stride] : T(0);
     const T res = div_rn(sub_rn(sub_rn(add_rn(hp[o], hn[o]), hp0), hn0), h);
     const T L = FIRST ? res : add_rn(acc[o], res);
@@ -177,6 +342,20 @@ __global__ void __launch_bounds__(256) weno7_residual_kernel(const T* __restrict
     kmax = warp_max(kmax);
     if ((threadIdx.x & 31) == 0 && kmax) atomicMax(maxkey, kmax);
   }
+}
+
+// Residual launch of axis AX: the tiled kernel where its grid fits, else the grid-stride one.
+template <class T, int AX, bool FIRST, bool LAST>
+void weno7_residual_launch(const T* hp, const T* hn, T* acc, T* r, T* u, const W7Geom& g, T h, int stage,
+                           const double* dt_dev, typename KeyOf<T>::type* maxkey, const int* active, int grid,
+                           cudaStream_t s) {
+  const int64_t gx = (g.nx + 31) / 32, gy = (g.ny + 7) / 8, gz = (g.nz + kW7ResZ - 1) / kW7ResZ;
+  if (gx <= 0x7fffffff && gy <= 65535 && gz <= 65535)
+    weno7_residual_kernel<T, AX, FIRST, LAST, true><<<dim3((unsigned)gx, (unsigned)gy, (unsigned)gz), 256, 0, s>>>(
+        hp, hn, acc, r, u, g, h, stage, dt_dev, maxkey, active);
+  else
+    weno7_residual_kernel<T, AX, FIRST, LAST, false><<<grid, 256, 0, s>>>(hp, hn, acc, r, u, g, h, stage, dt_dev,
+                                                                          maxkey, active);
 }
 
 adv_status weno7_validate(const adv_weno7_desc* d) {
@@ -228,16 +407,16 @@ adv_status weno7_stage_t(const adv_weno7_desc& d, T* u, const W7Work& w, int sta
   T* r = reinterpret_cast<T*>(w.r);
   K* mk = static_cast<K*>(maxkey);
   const T hx = T(d.dx), hy = T(d.dy), hz = T(d.dz);
-  weno7_face_kernel<T, 0><<<grid, 256, 0, s>>>(u, hp, hn, g);
-  weno7_residual_kernel<T, 0, true, false><<<grid, 256, 0, s>>>(hp, hn, acc, r, u, g, hx, stage, dt_dev, mk, active);
-  weno7_face_kernel<T, 1><<<grid, 256, 0, s>>>(u, hp, hn, g);
+  weno7_face_launch<T, 0>(u, hp, hn, g, grid, s);
+  weno7_residual_launch<T, 0, true, false>(hp, hn, acc, r, u, g, hx, stage, dt_dev, mk, active, grid, s);
+  weno7_face_launch<T, 1>(u, hp, hn, g, grid, s);
   if (nd == 2) {
-    weno7_residual_kernel<T, 1, false, true><<<grid, 256, 0, s>>>(hp, hn, acc, r, u, g, hy, stage, dt_dev, mk, active);
+    weno7_residual_launch<T, 1, false, true>(hp, hn, acc, r, u, g, hy, stage, dt_dev, mk, active, grid, s);
   } else {
-    weno7_residual_kernel<T, 1, false, false><<<grid, 256, 0, s>>>(hp, hn, acc, r, u, g, hy, stage, dt_dev, mk,
-                                                                   active);
-    weno7_face_kernel<T, 2><<<grid, 256, 0, s>>>(u, hp, hn, g);
-    weno7_residual_kernel<T, 2, false, true><<<grid, 256, 0, s>>>(hp, hn, acc, r, u, g, hz, stage, dt_dev, mk, active);
+    weno7_residual_launch<T, 1, false, false>(hp, hn, acc, r, u, g, hy, stage, dt_dev, mk,
+                                                                   active, grid, s);
+    weno7_face_launch<T, 2>(u, hp, hn, g, grid, s);
+    weno7_residual_launch<T, 2, false, true>(hp, hn, acc, r, u, g, hz, stage, dt_dev, mk, active, grid, s);
   }
   ADV_CUDA_TRY(cudaGetLastError());
   if (count) count_launches(2 * nd);
@@ -260,16 +439,16 @@ adv_status weno7_rhs_t(const adv_weno7_desc& d, const T* u, T* L, const W7Work& 
   const int nd = weno7_ndim(d);
   T* hp = reinterpret_cast<T*>(w.hp);
   T* hn = reinterpret_cast<T*>(w.hn);
-  weno7_face_kernel<T, 0><<<grid, 256, 0, s>>>(u, hp, hn, g);
-  weno7_residual_kernel<T, 0, true, false><<<grid, 256, 0, s>>>(hp, hn, L, nullptr, nullptr, g, T(d.dx), 0, nullptr,
-                                                                 nullptr, nullptr);
-  weno7_face_kernel<T, 1><<<grid, 256, 0, s>>>(u, hp, hn, g);
-  weno7_residual_kernel<T, 1, false, false><<<grid, 256, 0, s>>>(hp, hn, L, nullptr, nullptr, g, T(d.dy), 0, nullptr,
-                                                                 nullptr, nullptr);
+  weno7_face_launch<T, 0>(u, hp, hn, g, grid, s);
+  weno7_residual_launch<T, 0, true, false>(hp, hn, L, nullptr, nullptr, g, T(d.dx), 0, nullptr,
+                                                                 nullptr, nullptr, grid, s);
+  weno7_face_launch<T, 1>(u, hp, hn, g, grid, s);
+  weno7_residual_launch<T, 1, false, false>(hp, hn, L, nullptr, nullptr, g, T(d.dy), 0, nullptr,
+                                                                 nullptr, nullptr, grid, s);
   if (nd == 3) {
-    weno7_face_kernel<T, 2><<<grid, 256, 0, s>>>(u, hp, hn, g);
-    weno7_residual_kernel<T, 2, false, false><<<grid, 256, 0, s>>>(hp, hn, L, nullptr, nullptr, g, T(d.dz), 0,
-                                                                   nullptr, nullptr, nullptr);
+    weno7_face_launch<T, 2>(u, hp, hn, g, grid, s);
+    weno7_residual_launch<T, 2, false, false>(hp, hn, L, nullptr, nullptr, g, T(d.dz), 0,
+                                                                   nullptr, nullptr, nullptr, grid, s);
   }
   ADV_CUDA_TRY(cudaGetLastError());
   count_launches(2 * nd);

@@ -4,7 +4,8 @@ FP64 is held bit for bit against the reference's own MATLAB prototypes -- the ou
 Matlab_Prototipes/InviscidBurgersNd/WENO7resAdv_{X,Y,Z}.m and the solver loops of
 LFWENO7FDM{2,3}d.m, run through tests/golden/matlab_subset.py into
 tests/golden/matlab_burgers_prototypes.npz -- and against the CPU oracle's restatement of them on
-other grids; FP32 to a stated relative L2 bound against FP64.
+other grids; FP32 (a form of its own, written for speed) to stated relative L2 bounds against
+FP64.
 """
 from pathlib import Path
 
@@ -81,6 +82,29 @@ def test_weno7_rhs_and_run_equal_the_oracle(cuda, oracle, shape):
     t, it = weno7_run(cfg, a, 0.05, 0.4)
     assert (it, t) == (itw, tw)
     np.testing.assert_array_equal(a.cpu().numpy().reshape(u0.shape), uw)
+
+
+@pytest.mark.parametrize("shape", [(11, 17, 13), (40, 9, 6), (64, 48), (33, 5), (70, 35, 37), (300, 3), (5, 70, 40)])
+def test_weno7_fp32_rhs_within_bound_of_fp64(cuda, oracle, shape):
+    """The FP32 state's tiled face kernels (split parts staged once per tile, both parts of a face
+    in paired instructions, weights from r_k = e_min / e_k): ragged tiles along every axis, lines
+    shorter than the stencil, several tiles per line; relative L2 error of the summed residuals
+    against the FP64 oracle <= 5e-6 (a float32 emulation of the form on the host measured 2e-7)."""
+    import torch
+    rng = np.random.default_rng(sum(shape) + 1)
+    u0 = rng.standard_normal(shape[::-1]) * 0.5 + 0.3
+    h = [2.0 / (n - 1) for n in shape]
+    want = oracle.proto_residual(7, 0, u0, h[0])
+    for ax in range(1, len(shape)):
+        want = want + oracle.proto_residual(7, ax, u0, h[ax])
+    cfg = _cfg(u0, h)
+    a = _t(u0.astype(np.float32).ravel(), cuda)
+    L = torch.full_like(a, float("nan"))
+    weno7_rhs(cfg, a, L)
+    got = L.cpu().numpy().astype(np.float64).reshape(u0.shape)
+    assert np.isfinite(got).all()
+    rel = np.linalg.norm(got - want) / np.linalg.norm(want)
+    assert rel <= 5e-6, rel
 
 
 def test_weno7_fp32_run_within_bound_of_fp64(cuda, oracle):
