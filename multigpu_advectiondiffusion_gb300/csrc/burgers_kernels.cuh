@@ -133,6 +133,17 @@ __device__ __forceinline__ int* burgers_abort_flag() {
   __shared__ int flag;
   return &flag;
 }
+// A periodic edge tile's patch list: the staged plane's elements that lie outside the domain
+// (slot index) and the in-plane offset of the wrapped node each takes.
+struct BurgersPatch {
+  int n;
+  uint16_t slot[BurgersTile::PLANE];
+  int64_t src[BurgersTile::PLANE];
+};
+__device__ __forceinline__ BurgersPatch* burgers_patch() {
+  __shared__ BurgersPatch patch;
+  return &patch;
+}
 
 template <class T>
 __device__ __forceinline__ void burgers_cta_init(const CUtensorMap* tmap, bool tma) {
@@ -229,6 +240,24 @@ __device__ __forceinline__ BurgersPipe burgers_segment(const CUtensorMap* tmap, 
   // and their difference is exactly zero; no z layer is frozen.
   const bool twod = nz == 1;
   auto plane_z = [&](int q) { return per || twod ? wrapi(p0 + q, nz) : p0 + q; };
+  // Periodic edge tile: the TMA box zero-fills what lies outside the domain. The elements to
+  // patch with their wrapped neighbours are listed once per segment (CTA-uniform branch), so a
+  // plane's patch is one load and one store per listed element.
+  BurgersPatch* patch = burgers_patch();
+  if (edge) {
+    if (tid == 0) patch->n = 0;
+    __syncthreads();
+    for (int e = tid; e < TL::PLANE; e += TL::NT) {
+      const int r = e / TL::SW, c = e - r * TL::SW;
+      const int gx = x0 - TL::PADX + c, gy = y0 - TL::R + r;
+      if (gx < 0 || gx >= nx || gy < 0 || gy >= ny) {
+        const int k = atomicAdd(&patch->n, 1);
+        patch->slot[k] = (uint16_t)e;
+        patch->src[k] = (int64_t)wrapi(gy, ny) * nx + wrapi(gx, nx);
+      }
+    }
+    __syncthreads();
+  }
   auto issue = [&](int q) {
     T* dst = ring + s_issue * SM::SLOT_ELEMS;
     const int z = plane_z(q);
@@ -273,17 +302,13 @@ __device__ __forceinline__ BurgersPipe burgers_segment(const CUtensorMap* tmap, 
     if (p.tma) {
       if (!mbar_wait_bounded(&bars[s_wait], (parity >> s_wait) & 1u, p.status)) *abort_flag = 1;  // every lane waits (converged)
       if (edge) {
-        // Periodic edge tile: the TMA box zero-filled what lies outside the domain; fill it with
-        // the wrapped neighbours. Written here, read only after the next barrier.
-        const int z = plane_z(q);
-        for (int e = tid; e < TL::PLANE; e += TL::NT) {
-          const int r = e / TL::SW, c = e - r * TL::SW;
-          const int gx = x0 - TL::PADX + c, gy = y0 - TL::R + r;
-          if (gx < 0 || gx >= nx || gy < 0 || gy >= ny)
-          {
-            const size_t gi = (size_t)z * sxy + (size_t)wrapi(gy, ny) * nx + wrapi(gx, nx);
-            if (ADV_IN_RANGE(gi, sxy * nz, p.status)) plq[e] = p.uin[gi];
-          }
+        // the listed elements of plane q take their wrapped neighbours; written here, read only
+        // after the next barrier
+        const size_t zo = (size_t)plane_z(q) * sxy;
+        for (int k = tid; k < patch->n; k += TL::NT) {
+          const size_t gi = zo + (size_t)patch->src[k];
+          const int e = patch->slot[k];
+          if (ADV_IN_RANGE(gi, sxy * nz, p.status) && ADV_IN_RANGE(e, TL::PLANE, p.status)) plq[e] = p.uin[gi];
         }
       }
     } else {
@@ -493,15 +518,18 @@ __device__ __forceinline__ BurgersPipe burgers_segment(const CUtensorMap* tmap, 
 }
 
 // Minimum resident CTAs per SM the compiler must allow for (it caps registers accordingly).
-// FP32 inviscid: asking for 2 lets the compiler pick its own schedule, which lands at 78-80
-// registers -- still three CTAs (24 warps) per SM -- and measured 3-4% faster than the schedule
-// it picks under a 3-CTA bound (76 registers); the grid follows the occupancy it reports. FP32
-// viscous: 3 (under a 2-CTA bound it takes 86-90 registers and only two CTAs fit). FP64: 2.
-template <class T, bool VISC>
-constexpr int burgers_min_ctas() { return sizeof(T) == 4 && VISC ? 3 : 2; }
+// FP32 inviscid with the IEEE or FP64 weight division: asking for 2 lets the compiler pick its
+// own schedule, which lands at 78-80 registers -- still three CTAs (24 warps) per SM -- and
+// measured 3-4% faster than the schedule it picks under a 3-CTA bound (76 registers); the grid
+// follows the occupancy it reports. FP32 with the reciprocal division and FP32 viscous: 3 (under
+// a 2-CTA bound they take 86-90 registers and only two CTAs fit). FP64: 2.
+template <class T, bool VISC, class D>
+constexpr int burgers_min_ctas() {
+  return sizeof(T) == 4 && (VISC || std::is_same<D, FastDiv>::value) ? 3 : 2;
+}
 
 template <class T, bool Z, class D, bool VISC>
-__global__ void __launch_bounds__(256, burgers_min_ctas<T, VISC>())
+__global__ void __launch_bounds__(256, burgers_min_ctas<T, VISC, D>())
 burgers_stage_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ BurgersParams<T> p) {
   using TL = BurgersTile;
   if (p.active && *p.active == 0) return;
