@@ -72,7 +72,10 @@ template <> __device__ __forceinline__ float absv<float>(float x) { return fabsf
 __device__ __forceinline__ float rcp(float x) { return __frcp_rn(x); }
 __device__ __forceinline__ double rcp(double x) { return 1.0 / x; }
 
+// Periodic index. Inside the domain (every element of an interior tile) it is the index itself,
+// without the integer division of the general case.
 __device__ __forceinline__ int wrap(int i, int n) {
+  if (i >= 0 && i < n) return i;
   i %= n;
   return i < 0 ? i + n : i;
 }
