@@ -239,7 +239,17 @@ __device__ __forceinline__ BurgersPipe burgers_segment(const CUtensorMap* tmap, 
   // 2D (nz == 1): every streamed plane is the one plane, so the z faces of each column are equal
   // and their difference is exactly zero; no z layer is frozen.
   const bool twod = nz == 1;
-  auto plane_z = [&](int q) { return per || twod ? wrapi(p0 + q, nz) : p0 + q; };
+  // Periodic plane index: within one period of the domain (the usual case) a conditional add or
+  // subtract, not the integer division of wrapi (5% of the stage at 256^3).
+  auto plane_z = [&](int q) {
+    int z = p0 + q;
+    if (per || twod) {
+      if (z < 0) z += nz;
+      else if (z >= nz) z -= nz;
+      if ((unsigned)z >= (unsigned)nz) z = wrapi(z, nz);
+    }
+    return z;
+  };
   // Periodic edge tile: the TMA box zero-fills what lies outside the domain. The elements to
   // patch with their wrapped neighbours are listed once per segment (CTA-uniform branch), so a
   // plane's patch is one load and one store per listed element.
