@@ -140,6 +140,7 @@ struct BurgersPatch {
   uint16_t slot[BurgersTile::PLANE];
   int64_t src[BurgersTile::PLANE];
 };
+static_assert(BurgersTile::PLANE <= 65535, "patch slots are 16-bit");
 __device__ __forceinline__ BurgersPatch* burgers_patch() {
   __shared__ BurgersPatch patch;
   return &patch;
