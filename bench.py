@@ -285,12 +285,11 @@ def cpu_baseline_heat(cfg, u0, nsteps: int, budget_s: float) -> dict:
 
 
 # FP32 flops per cell-stage of the fused WENO5-Z stage, counting an FFMA2 as 4 flops, an FADD2,
-# FMUL2 or FFMA as 2 and an FADD or FMUL as 1: 451.4 from the ncu instruction mix of the
-# reciprocal-division form at 256^3 (stage 1), plus 6.2 for the WENO-Z weights written as
-# d_k (P + tau P / b_k) (one more flop per face side: 2 x 1.047 x 2 for the x and y faces with
-# the tile's extra faces, 2 for z). The division counts as the reciprocal form's two operations
+# FMUL2 or FFMA as 2 and an FADD or FMUL as 1, from the ncu instruction mix of the
+# reciprocal-division form at 256^3 (stage 1): FFMA2 81.2, FADD2 18.5, FMUL2 37.3, FFMA 6.6,
+# FADD 5.3, FMUL 10.1 per cell = 465.0. The division counts as the reciprocal form's operations
 # whichever division is run.
-BURGERS_FLOPS_PER_CELL_STAGE = 457.6
+BURGERS_FLOPS_PER_CELL_STAGE = 465.0
 
 ENSEMBLE_SEED = 2024
 ENSEMBLE_STEPS = 500
